@@ -1,0 +1,212 @@
+/*
+ * padenti_gb300.h -- C ABI of the GB300-native Padenti hot path.
+ *
+ * libpadenti_gb300.so runs Padenti's per-depth random-forest training pass
+ * (candidate evaluation + class histograms, best split, pixel reassignment)
+ * and forest prediction as sm_103a CUDA kernels.  The reference is a
+ * header-only C++ template library with no FFI of its own; these entry points
+ * are what its C++ classes bind in the header-only facade under
+ * include/padenti/ (cuda_tree_trainer.hpp, cuda_classifier.hpp), and what the
+ * Python package padenti_gb300 binds with ctypes.
+ *
+ * Conventions:
+ *   - Every function returns PD_OK (0) or a negative PD_ERR_* code; the
+ *     message of the last failure on the calling thread is pd_last_error().
+ *   - Pointers are host pointers unless the name says _device.
+ *   - One context = one GPU = one CUDA stream.  Calls on one context must be
+ *     serialised by the caller; separate contexts may be used from separate
+ *     threads.
+ *   - The template parameters of the reference classes
+ *     <ImgType, nChannels, FeatType, FeatDim, nClasses> are the pd_config
+ *     given at context creation.
+ */
+#ifndef PADENTI_GB300_H
+#define PADENTI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PD_OK 0
+#define PD_ERR_INVALID (-1)      /* bad argument or inconsistent sizes */
+#define PD_ERR_CUDA (-2)         /* CUDA runtime error (message has the call) */
+#define PD_ERR_NOMEM (-3)        /* device or host allocation failed */
+#define PD_ERR_UNSUPPORTED (-4)  /* configuration outside the built kernels */
+#define PD_ERR_STATE (-5)        /* call out of order (e.g. no dataset uploaded) */
+
+#define PD_IMG_U8 1
+#define PD_IMG_U16 2
+
+#define PD_FEAT_I16 1
+#define PD_FEAT_I32 2
+
+/* Built-in feature plugins.  The reference compiles a user OpenCL C
+ * computeFeature() into its kernels (kernels/hist_update.cl:33,
+ * kernels/predict.cl:32); here a plugin is a CUDA device functor compiled into
+ * the kernels.
+ *   DEPTH_DIFF2  uint16 x1, int32, D=4 (ux,uy,vx,vy):
+ *                I(x+u/d(x)) - I(x+v/d(x)); out-of-image or zero probes = 10000.
+ *   DEPTH_DIFF1  uint16 x1, int16, D=2: the reference test/feature.cl:29-64,
+ *                D(x) - D(x + round(u*500/D(x))).
+ *   CHANNEL_DIFF uint8 x3, int32, D=6 (c1,c2,ux,uy,vx,vy):
+ *                I_c1(x+u) - I_c2(x+v), channels clamped to [0,2], outside = 0. */
+#define PD_PLUGIN_DEPTH_DIFF2 1
+#define PD_PLUGIN_DEPTH_DIFF1 2
+#define PD_PLUGIN_CHANNEL_DIFF 3
+
+#define PD_MAX_FEAT_DIM 8
+#define PD_MAX_CLASSES 64
+#define PD_MAX_THRESHOLDS 256
+#define PD_MAX_TREES 64
+
+typedef struct pd_ctx pd_ctx;
+
+/* The reference's class template parameters. */
+typedef struct {
+  int32_t plugin;       /* PD_PLUGIN_* */
+  int32_t img_type;     /* PD_IMG_* (ImgType) */
+  int32_t n_channels;   /* nChannels */
+  int32_t feat_type;    /* PD_FEAT_* (FeatType) */
+  int32_t feat_dim;     /* FeatDim */
+  int32_t n_classes;    /* nClasses */
+} pd_config;
+
+/* TreeTrainerParameters (tree_trainer.hpp:35-51).  Bounds are given as int32
+ * and converted to FeatType. */
+typedef struct {
+  uint32_t n_features;
+  uint32_t n_thresholds;
+  int32_t feat_low[PD_MAX_FEAT_DIM];
+  int32_t feat_up[PD_MAX_FEAT_DIM];
+  int32_t thr_low;
+  int32_t thr_up;
+  uint32_t per_leaf_samples_thr;
+} pd_train_params;
+
+/* A TrainingSet (training_set.hpp:39-112) flattened into host arrays.
+ * Images are interleaved row-major [H][W][C]; labels are one byte per pixel
+ * with 0 = unlabelled and class k stored as k+1 (training_set_image.hpp:29-33);
+ * samples are pixel indices y*W+x (training_set_image.hpp:38-110). */
+typedef struct {
+  uint32_t n_images;
+  const void *pixels;        /* all images concatenated */
+  const uint64_t *pix_off;   /* byte offset of image i in pixels */
+  const uint32_t *width;
+  const uint32_t *height;
+  const uint8_t *labels;     /* all label images concatenated */
+  const uint64_t *lab_off;   /* offset of image i in labels (pixels) */
+  const uint32_t *samples;   /* all sample lists concatenated */
+  const uint64_t *samp_off;  /* n_images+1 offsets into samples */
+} pd_dataset_desc;
+
+/* Counters and CUDA-event times of the last pd_train_tree call. */
+typedef struct {
+  uint64_t evals;            /* (sample, candidate) evaluations, each with T comparisons */
+  uint64_t nodes_trained;
+  uint64_t nodes_split;
+  uint64_t hist_launches;
+  uint64_t split_rechecked;  /* candidates rechecked in FP64 */
+  double ms_candidates;
+  double ms_hist;
+  double ms_split;
+  double ms_reassign;
+  double ms_total;           /* wall time of the call */
+} pd_train_stats;
+
+const char *pd_last_error(void);
+int pd_version(void);
+
+/* Context ------------------------------------------------------------------ */
+int pd_ctx_create(const pd_config *cfg, int device, pd_ctx **out);
+int pd_ctx_destroy(pd_ctx *ctx);
+/* Device memory the training pass may use for histograms (default 8 GiB);
+ * frontiers whose histograms exceed it are processed in slices, as the
+ * reference does with its 20 GiB host cap (cl_tree_trainer_impl.hpp:47-50). */
+int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
+/* Synchronises the context's stream. */
+int pd_ctx_sync(pd_ctx *ctx);
+/* The CUDA stream (cudaStream_t) the context launches on. */
+void *pd_ctx_stream(pd_ctx *ctx);
+
+/* TrainingSet upload (replaces the per-image streaming of
+ * cl_tree_trainer_impl_traverse_ts.hpp:127-358): the whole set is kept in HBM. */
+int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds);
+int pd_dataset_info(pd_ctx *ctx, uint64_t *n_samples, uint32_t *n_images);
+
+/* Training: CLTreeTrainer::train (cl_tree_trainer_impl.hpp:203-255).
+ * Levels start_depth..end_depth-1 are split (start_depth must be 1, as in the
+ * reference).  The tree SoA arrays (2^end_depth - 1 nodes; features/thresholds
+ * of FeatType) are read and written in place, as the reference mutates Tree&.
+ * root_prior (nClasses floats) becomes the root posterior. */
+int pd_train_tree(pd_ctx *ctx, const pd_train_params *params, uint32_t tree_id,
+                  uint32_t start_depth, uint32_t end_depth, const float *root_prior,
+                  int32_t *left_child, void *features, void *thresholds, float *posteriors);
+int pd_train_get_stats(pd_ctx *ctx, pd_train_stats *out);
+/* Node of every sample after the last pd_train_tree call (n_samples int32). */
+int pd_train_sample_nodes(pd_ctx *ctx, int32_t *out);
+
+/* Stage entry points of one depth, for drop-in use and parity testing. ---- */
+/* Candidate table (kernels/hist_update.cl:62-114,127-184): features
+ * [n_nodes][F][D] and thresholds [n_nodes][F][T], FeatType. */
+int pd_candidates(pd_ctx *ctx, const pd_train_params *params, uint32_t tree_id,
+                  const int32_t *nodes, uint32_t n_nodes, void *features_out, void *thresholds_out);
+/* Class histograms hist[n][l][t][f] = #samples of node nodes[n] with label l
+ * whose response to candidate f is <= threshold t (kernels/hist_update.cl:36-187
+ * + cl_tree_trainer_impl_traverse_ts.hpp:462-704).  sample_node holds the
+ * current node of every uploaded sample. */
+int pd_hist(pd_ctx *ctx, const pd_train_params *params, uint32_t tree_id,
+            const int32_t *sample_node, const int32_t *nodes, uint32_t n_nodes, uint32_t *hist_out);
+/* Best split of each node from its histogram and class totals
+ * (kernels/learn_best_feature.cl:22-111 + learn_best_featthr.hpp:101-112).
+ * Ties go to the lowest t*F+f; out_t/out_f are -1 for an empty node. */
+int pd_split(pd_ctx *ctx, const pd_train_params *params, const uint32_t *hist,
+             const uint32_t *class_tot, uint32_t n_nodes, int32_t *out_t, int32_t *out_f,
+             double *out_gain);
+/* Exact per-integer log2 table used by the split: out[n] = log2(n), out[0]=0. */
+int pd_log2_table(pd_ctx *ctx, uint32_t n, double *out);
+
+/* Classifier (cl_classifier_impl.hpp) ---------------------------------------- */
+int pd_forest_clear(pd_ctx *ctx);
+/* CLClassifier::operator<< (cl_classifier_impl.hpp:146-195). */
+int pd_forest_add_tree(pd_ctx *ctx, uint32_t depth, const int32_t *left_child,
+                       const void *features, const void *thresholds, const float *posteriors);
+int pd_forest_size(pd_ctx *ctx, uint32_t *n_trees);
+/* CLClassifier::predict(image, posterior, mask) (cl_classifier_impl.hpp:356-557):
+ * out is planar [nClasses][H][W] floats; mask may be NULL (all pixels);
+ * masked-out pixels are 0. */
+int pd_predict_posterior(pd_ctx *ctx, const void *image, uint32_t width, uint32_t height,
+                         const uint8_t *mask, float *out);
+/* CLClassifier::predict(treeID, image, prediction, mask) (:200-341): leaf node
+ * id per pixel; masked-out pixels are 0. */
+int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, uint32_t width,
+                    uint32_t height, const uint8_t *mask, int32_t *out);
+/* Batched posterior prediction of n same-size images already in device
+ * memory: images n*H*W*C, masks n*H*W (or NULL), out n*K*H*W. */
+int pd_predict_posterior_device(pd_ctx *ctx, uint32_t n_images, const void *images_device,
+                                uint32_t width, uint32_t height, const uint8_t *masks_device,
+                                float *out_device);
+
+/* Synthetic data (seeded, bit-identical on every host) ------------------------ */
+/* Depth maps: background plane U(3000,4000) mm + N(0,5^2) noise, ellipses at
+ * U(800,2500) mm.  parts=0: 3 classes (bg, left half, right half of each
+ * ellipse); parts=1: 9 classes (bg + 8 angular sectors).  Samples: with
+ * replacement, (1000-bg_permille)/1000 among object pixels, the rest among
+ * background, sorted.  Buffers: pixels n*W*H uint16, labels n*W*H, samples
+ * n*samples_per_image. */
+int pd_synth_depth(uint64_t seed, uint32_t first_image, uint32_t n_images, uint32_t width,
+                   uint32_t height, uint32_t min_ellipses, uint32_t max_ellipses,
+                   uint32_t parts, uint32_t samples_per_image, uint32_t bg_permille,
+                   uint16_t *pixels, uint8_t *labels, uint32_t *samples);
+/* RGB Voronoi images: 8-20 cells, classes 0..n_classes-1 with a seeded palette,
+ * uniform texture noise +-20 per channel; samples uniform over all pixels. */
+int pd_synth_rgb(uint64_t seed, uint32_t first_image, uint32_t n_images, uint32_t width,
+                 uint32_t height, uint32_t n_classes, uint32_t samples_per_image,
+                 uint8_t *pixels, uint8_t *labels, uint32_t *samples);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

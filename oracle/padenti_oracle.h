@@ -1,0 +1,141 @@
+/*
+ * padenti_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C CPU restatement of Padenti's random-forest training and
+ * prediction hot path.  It is the checker for the CUDA library in
+ * padenti_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline (and its reference arm) may load it.  Nothing in the product
+ * links, calls or falls back to it.
+ *
+ * Parity status:
+ *   - MD5 counter RNG (candidate and threshold generation) is pinned against
+ *     RFC-1321 known answers (Python hashlib) and against the reference's own
+ *     src/padenti/prng.hpp compiled from its source (oracle/ref_shim).
+ *   - The split rule is cross-checked against the reference's own
+ *     learnBestFeature kernel (kernels/learn_best_feature.cl) compiled as C
+ *     from its source (oracle/ref_shim) on the same histograms.
+ *   - The single-offset depth plugin is checked against the reference's own
+ *     test/feature.cl compiled as C (oracle/ref_shim).
+ *   - Everything else (histogram accumulation, finalize, traversal, forest
+ *     posterior) is "parity unpinned": the reference needs OpenCL, Boost and
+ *     OpenCV, none of which exist here, and its tests hold no golden vectors.
+ *     The restatement follows the reference line by line; the cited
+ *     file:line of each function names what it follows.
+ */
+#ifndef PADENTI_ORACLE_H
+#define PADENTI_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { OR_FEAT_I16 = 1, OR_FEAT_I32 = 2 };
+enum { OR_IMG_U8 = 1, OR_IMG_U16 = 2 };
+/* Built-in feature plugins (same numbering as the CUDA library). */
+enum {
+  OR_PLUGIN_DEPTH_DIFF2 = 1,   /* I(x+u/d) - I(x+v/d), int32, D=4 */
+  OR_PLUGIN_DEPTH_DIFF1 = 2,   /* test/feature.cl: D(x) - D(x+round(u*500/D(x))), int16, D=2 */
+  OR_PLUGIN_CHANNEL_DIFF = 3   /* I_c1(x+u) - I_c2(x+v), RGB u8, int32, D=6 */
+};
+
+#define OR_MAX_FEAT_DIM 8
+
+typedef struct {
+  int32_t plugin;
+  int32_t feat_type;          /* OR_FEAT_* */
+  int32_t feat_dim;           /* D */
+  int32_t n_classes;          /* K */
+  uint32_t n_features;        /* F */
+  uint32_t n_thresholds;      /* T */
+  int32_t feat_low[OR_MAX_FEAT_DIM];
+  int32_t feat_up[OR_MAX_FEAT_DIM];
+  int32_t thr_low;
+  int32_t thr_up;
+  uint32_t per_leaf_samples_thr;
+} or_params;
+
+/* A training set flattened into host arrays (images interleaved row-major). */
+typedef struct {
+  uint32_t n_images;
+  uint32_t n_channels;
+  uint32_t img_type;            /* OR_IMG_* */
+  const uint8_t *pixels;        /* all images, concatenated */
+  const uint64_t *pix_off;      /* byte offset of each image */
+  const uint32_t *width;
+  const uint32_t *height;
+  const uint8_t *labels;        /* per-pixel labels, 0 = unlabelled, class k = k+1 */
+  const uint64_t *lab_off;      /* label offset (pixels) of each image */
+  const uint32_t *samples;      /* sampled pixel indices y*W+x, per image, concatenated */
+  const uint64_t *samp_off;     /* n_images+1 offsets into samples */
+} or_dataset;
+
+typedef struct {
+  uint64_t evals;               /* (sample, candidate) feature evaluations */
+  uint64_t nodes_trained;       /* frontier nodes processed */
+  uint64_t nodes_split;
+  double seconds_hist;
+  double seconds_split;
+} or_stats;
+
+/* a1: one MD5 compression of the 16-byte little-endian block (s0..s3). */
+void or_md5(const uint32_t in[4], uint32_t out[4]);
+
+/* a2+a3: candidate f of node `node` of tree `tree_id`. */
+void or_candidate(const or_params *p, uint32_t tree_id, uint32_t node, uint32_t f,
+                  int32_t *feat_out /*[D]*/, int32_t *thr_out /*[T]*/);
+
+/* a4: built-in plugin response at pixel (x,y) of one image. */
+int32_t or_feature(int32_t plugin, int32_t feat_type, const void *img, uint32_t w, uint32_t h,
+                   uint32_t n_channels, int32_t x, int32_t y, const int32_t *feat);
+
+/* Per-integer log2 table used by the exact gain: out[n] = log2(n), out[0] = 0. */
+void or_log2_table(uint32_t n, double *out);
+
+/* a5+a6: histograms hist[i][l][t][f] for frontier nodes nodes[i], given each
+ * sample's current node.  reference_cost=1 regenerates the candidate with MD5
+ * per (sample, candidate) exactly as the reference kernel does. */
+int or_hist(const or_params *p, const or_dataset *ds, uint32_t tree_id,
+            const int32_t *sample_node, const int32_t *nodes, uint32_t n_nodes,
+            uint32_t *hist, int reference_cost, int n_threads);
+
+/* a7: exact best split per node.  out_t/out_f/out_gain receive the winner. */
+int or_split(const or_params *p, const uint32_t *hist, const uint32_t *class_tot,
+             uint32_t n_nodes, const double *log2_table, uint64_t table_len,
+             int32_t *out_t, int32_t *out_f, double *out_gain,
+             float *out_gain32_max /* nullable: FP32 reference-formula max gain */,
+             double *out_max_abs_err /* nullable: max |gain32 - gain64| seen */);
+
+/* Training-set priors: mean of per-image priors over labelled samples. */
+void or_priors(const or_dataset *ds, uint32_t n_classes, float *out_priors);
+
+/* a9..a12: train one tree of depth end_depth (levels 1..end_depth-1 are split).
+ * Tree arrays have 2^end_depth - 1 nodes and must be initialised by the caller
+ * as a fresh reference Tree (left_child -2, zeros).  sample_leaf (nullable)
+ * receives each sample's node after training. */
+int or_train_tree(const or_params *p, const or_dataset *ds, uint32_t tree_id, uint32_t end_depth,
+                  const float *root_prior, int32_t *left_child, int32_t *features,
+                  int32_t *thresholds, float *posteriors, int32_t *sample_leaf,
+                  int reference_cost, int n_threads, or_stats *stats);
+
+/* a11: forest posterior, planar [K][H][W]; masked-out pixels are 0.
+ * Trees are given as concatenated SoA arrays; tree t has 2^depth[t]-1 nodes
+ * starting at node_off[t]. */
+int or_predict_posterior(const or_params *p, const void *img, uint32_t w, uint32_t h,
+                         uint32_t n_channels, const uint8_t *mask, uint32_t n_trees,
+                         const uint32_t *depth, const uint64_t *node_off,
+                         const int32_t *left_child, const int32_t *features,
+                         const int32_t *thresholds, const float *posteriors,
+                         float *out, int n_threads);
+
+/* Leaf-ID prediction of one tree (unmasked pixels get 0). */
+int or_predict_leaf(const or_params *p, const void *img, uint32_t w, uint32_t h,
+                    uint32_t n_channels, const uint8_t *mask, uint32_t depth,
+                    const int32_t *left_child, const int32_t *features,
+                    const int32_t *thresholds, int32_t *out, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,410 @@
+"""padenti_gb300 -- GB300-native training and prediction hot path of Padenti.
+
+Python mirror of the reference's C++ API (src/padenti/): ``TrainingSetImage`` /
+``TrainingSet`` (training_set*.hpp), ``Tree`` with its XML file layout
+(tree.hpp, tree_impl.hpp), ``TreeTrainerParameters`` and ``TreeTrainer``
+(tree_trainer.hpp, cl_tree_trainer.hpp) and ``Classifier``
+(classifier.hpp, cl_classifier.hpp).  The reference's class template
+parameters <ImgType, nChannels, FeatType, FeatDim, nClasses> are a
+``ForestConfig``.  All compute runs in libpadenti_gb300.so (sm_103a CUDA
+kernels behind the C ABI of include/padenti_gb300.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import xml.etree.ElementTree as ET
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+from ._native import PadentiError, check, lib
+
+__all__ = [
+    "ForestConfig", "TreeTrainerParameters", "TrainingSetImage", "TrainingSet", "Tree", "TreeTrainer",
+    "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS",
+]
+
+FEAT_DTYPE = {N.PD_FEAT_I16: np.int16, N.PD_FEAT_I32: np.int32}
+IMG_DTYPE = {N.PD_IMG_U8: np.uint8, N.PD_IMG_U16: np.uint16}
+
+# Built-in feature plugins and the template parameters they are compiled for.
+PLUGINS = {
+    "depth_diff2": dict(plugin=N.PD_PLUGIN_DEPTH_DIFF2, img_type=N.PD_IMG_U16, n_channels=1,
+                        feat_type=N.PD_FEAT_I32, feat_dim=4),
+    "depth_diff1": dict(plugin=N.PD_PLUGIN_DEPTH_DIFF1, img_type=N.PD_IMG_U16, n_channels=1,
+                        feat_type=N.PD_FEAT_I16, feat_dim=2),
+    "channel_diff": dict(plugin=N.PD_PLUGIN_CHANNEL_DIFF, img_type=N.PD_IMG_U8, n_channels=3,
+                         feat_type=N.PD_FEAT_I32, feat_dim=6),
+}
+
+
+def _ptr(a: np.ndarray | None) -> int | None:
+    return None if a is None else a.ctypes.data
+
+
+@dataclass(frozen=True)
+class ForestConfig:
+    """<ImgType, nChannels, FeatType, FeatDim, nClasses> for one plugin."""
+
+    plugin: str
+    n_classes: int
+
+    def __post_init__(self):
+        if self.plugin not in PLUGINS:
+            raise ValueError(f"unknown plugin {self.plugin!r}; built-in: {sorted(PLUGINS)}")
+
+    @property
+    def spec(self) -> dict:
+        return PLUGINS[self.plugin]
+
+    @property
+    def img_dtype(self):
+        return IMG_DTYPE[self.spec["img_type"]]
+
+    @property
+    def feat_dtype(self):
+        return FEAT_DTYPE[self.spec["feat_type"]]
+
+    @property
+    def n_channels(self) -> int:
+        return self.spec["n_channels"]
+
+    @property
+    def feat_dim(self) -> int:
+        return self.spec["feat_dim"]
+
+    def c(self) -> N.Config:
+        s = self.spec
+        return N.Config(s["plugin"], s["img_type"], s["n_channels"], s["feat_type"], s["feat_dim"], self.n_classes)
+
+
+@dataclass
+class TreeTrainerParameters:
+    """tree_trainer.hpp:35-51 (computeFRange and randomThrSampling are unused there too)."""
+
+    n_features: int
+    n_thresholds: int
+    feat_low_bounds: list
+    feat_up_bounds: list
+    thr_low_bound: int
+    thr_up_bound: int
+    per_leaf_samples_thr: int = 0
+
+    def c(self) -> N.TrainParams:
+        p = N.TrainParams()
+        p.n_features = self.n_features
+        p.n_thresholds = self.n_thresholds
+        for i, v in enumerate(self.feat_low_bounds):
+            p.feat_low[i] = int(v)
+        for i, v in enumerate(self.feat_up_bounds):
+            p.feat_up[i] = int(v)
+        p.thr_low = int(self.thr_low_bound)
+        p.thr_up = int(self.thr_up_bound)
+        p.per_leaf_samples_thr = int(self.per_leaf_samples_thr)
+        return p
+
+
+class TrainingSetImage:
+    """training_set_image.hpp: pixels, labels (0 = unlabelled, class k stored as k+1) and
+    sampled pixel indices.  Priors over labelled samples (training_set_image_impl.hpp:38-52)."""
+
+    def __init__(self, data: np.ndarray, labels: np.ndarray, n_classes: int, samples: np.ndarray):
+        self.data = np.ascontiguousarray(data)
+        self.labels = np.ascontiguousarray(labels, dtype=np.uint8)
+        self.samples = np.ascontiguousarray(samples, dtype=np.uint32)
+        self.height, self.width = self.labels.shape
+        self.n_classes = n_classes
+        lab = self.labels.reshape(-1)[self.samples]
+        lab = lab[lab != 0]
+        cnt = np.bincount(lab.astype(np.int64) - 1, minlength=n_classes)[:n_classes].astype(np.uint32)
+        tot = np.float32(len(lab))
+        self.priors = (cnt.astype(np.float32) / tot).astype(np.float32)
+
+
+class TrainingSet:
+    """training_set.hpp.  ``TrainingSet(n_classes, images)`` sets the priors to the mean of the
+    per-image priors (training_set_impl.hpp:116-133); ``ts << image`` updates them incrementally
+    as the reference's operator<< does (training_set_impl.hpp:157-170)."""
+
+    def __init__(self, n_classes: int, images: list | None = None):
+        self.n_classes = n_classes
+        self.images: list[TrainingSetImage] = []
+        self.priors = np.zeros(n_classes, np.float32)
+        self._version = 0
+        if images:
+            self.images = list(images)
+            acc = np.zeros(n_classes, np.float64)
+            for im in self.images:
+                acc += im.priors.astype(np.float64)
+            self.priors = (acc / len(self.images)).astype(np.float32)
+
+    def __lshift__(self, image: TrainingSetImage) -> "TrainingSet":
+        n = len(self.images)
+        pc = self.priors.astype(np.float64)
+        self.priors = (pc * n / (n + 1) + image.priors.astype(np.float64) / (n + 1)).astype(np.float32)
+        self.images.append(image)
+        self._version += 1
+        return self
+
+    @property
+    def n_samples(self) -> int:
+        return int(sum(len(im.samples) for im in self.images))
+
+    def flat(self) -> dict:
+        """Concatenated host arrays in the layout of pd_dataset_desc."""
+        n = len(self.images)
+        pix = [np.ascontiguousarray(im.data).reshape(-1).view(np.uint8) for im in self.images]
+        pix_off = np.zeros(n, np.uint64)
+        lab_off = np.zeros(n, np.uint64)
+        samp_off = np.zeros(n + 1, np.uint64)
+        o = lo = 0
+        for i, im in enumerate(self.images):
+            pix_off[i], lab_off[i] = o, lo
+            o += pix[i].nbytes
+            lo += im.labels.size
+            samp_off[i + 1] = samp_off[i] + len(im.samples)
+        return dict(
+            pixels=np.concatenate(pix) if n else np.zeros(1, np.uint8),
+            pix_off=pix_off,
+            width=np.array([im.width for im in self.images], np.uint32),
+            height=np.array([im.height for im in self.images], np.uint32),
+            labels=np.concatenate([im.labels.reshape(-1) for im in self.images]),
+            lab_off=lab_off,
+            samples=np.concatenate([im.samples for im in self.images]).astype(np.uint32),
+            samp_off=samp_off,
+        )
+
+    @staticmethod
+    def desc(flat: dict) -> N.DatasetDesc:
+        d = N.DatasetDesc()
+        d.n_images = len(flat["width"])
+        for k in ("pixels", "pix_off", "width", "height", "labels", "lab_off", "samples", "samp_off"):
+            setattr(d, k, flat[k].ctypes.data)
+        return d
+
+
+class Tree:
+    """tree.hpp: complete binary heap of 2^depth-1 nodes as SoA arrays.  left_child is -2 for an
+    absent node, -1 for a leaf, 2i+1 for a split node."""
+
+    def __init__(self, config: ForestConfig, tree_id: int = 0, depth: int = 0):
+        self.config = config
+        self.id = tree_id
+        self.depth = depth
+        self._init()
+
+    def _init(self):
+        n = (1 << self.depth) - 1 if self.depth else 0
+        self.left_child = np.full(n, -2, np.int32)
+        self.features = np.zeros((n, self.config.feat_dim), self.config.feat_dtype)
+        self.thresholds = np.zeros(n, self.config.feat_dtype)
+        self.posteriors = np.zeros((n, self.config.n_classes), np.float32)
+
+    @property
+    def n_nodes(self) -> int:
+        return len(self.left_child)
+
+    # -- XML layout of tree_impl.hpp:103-234 (Boost.PropertyTree, no indentation) --
+    def to_xml(self, idx: int = -1) -> str:
+        tid = self.id if idx == -1 else idx
+        out = [f"<Trees><TreeNumber>1</TreeNumber><MaxDepth>{self.depth}</MaxDepth><Tree{tid}>"]
+        K = self.config.n_classes
+        for i in range(self.n_nodes):
+            c = int(self.left_child[i])
+            if c == -2:
+                continue
+            out.append(f"<Node{i}><LeftChild>{c}</LeftChild>")
+            if c != -1:
+                vals = " ".join(str(int(v)) for v in self.features[i])
+                out.append(f"<SplitParameters>{vals} {int(self.thresholds[i])}</SplitParameters>")
+            hist = " ".join("%g" % float(self.posteriors[i, l]) for l in range(K))
+            out.append(f"<Histogram>{hist}</Histogram></Node{i}>")
+        out.append(f"</Tree{tid}></Trees>")
+        return '<?xml version="1.0" encoding="utf-8"?>\n' + "".join(out)
+
+    def save(self, path: str, idx: int = -1) -> None:
+        with open(path, "w") as fh:
+            fh.write(self.to_xml(idx))
+
+    def load(self, path: str, idx: int = -1) -> None:
+        root = ET.parse(path).getroot()
+        if idx != -1:
+            self.id = idx
+        depth = int(root.findtext("MaxDepth"))
+        if not self.depth or self.depth != depth:
+            self.depth = depth
+        self._init()
+        t = root.find(f"Tree{self.id}")
+        if t is None:
+            return
+        K, D = self.config.n_classes, self.config.feat_dim
+        for node in t:
+            i = int(node.tag[4:])
+            c = int(node.findtext("LeftChild"))
+            self.left_child[i] = c
+            h = node.findtext("Histogram")
+            if h is not None:
+                self.posteriors[i] = np.array(h.split()[:K], np.float32)
+            if c >= 0:
+                v = node.findtext("SplitParameters").split()
+                self.features[i] = np.array([int(x) for x in v[:D]], self.config.feat_dtype)
+                self.thresholds[i] = int(v[D])
+
+
+class _Ctx:
+    def __init__(self, config: ForestConfig, device: int = 0):
+        self.config = config
+        h = C.c_void_p()
+        check(lib().pd_ctx_create(C.byref(config.c()), device, C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            lib().pd_ctx_destroy(h)
+            self.h = None
+
+
+class TreeTrainer(_Ctx):
+    """CLTreeTrainer (cl_tree_trainer.hpp:115-120) on one GB300."""
+
+    def __init__(self, config: ForestConfig, device: int = 0, hist_budget: int | None = None):
+        super().__init__(config, device)
+        self._uploaded = None
+        if hist_budget:
+            check(lib().pd_ctx_set_hist_budget(self.h, hist_budget))
+
+    def upload(self, ts: TrainingSet) -> None:
+        key = (id(ts), ts._version, len(ts.images))
+        if self._uploaded == key:
+            return
+        flat = ts.flat()
+        check(lib().pd_dataset_upload(self.h, C.byref(TrainingSet.desc(flat))))
+        self._uploaded = key
+
+    def train(self, tree: Tree, ts: TrainingSet, params: TreeTrainerParameters, start_depth: int = 1,
+              end_depth: int | None = None) -> None:
+        end_depth = tree.depth if end_depth is None else end_depth
+        if end_depth > tree.depth:
+            raise ValueError("end_depth exceeds the tree depth")
+        self.upload(ts)
+        n = (1 << end_depth) - 1
+        lc = np.ascontiguousarray(tree.left_child[:n])
+        ft = np.ascontiguousarray(tree.features[:n])
+        th = np.ascontiguousarray(tree.thresholds[:n])
+        po = np.ascontiguousarray(tree.posteriors[:n])
+        prior = np.ascontiguousarray(ts.priors, np.float32)
+        check(lib().pd_train_tree(self.h, C.byref(params.c()), tree.id, start_depth, end_depth, _ptr(prior),
+                                  _ptr(lc), _ptr(ft), _ptr(th), _ptr(po)))
+        tree.left_child[:n], tree.features[:n], tree.thresholds[:n], tree.posteriors[:n] = lc, ft, th, po
+
+    def stats(self) -> dict:
+        s = N.TrainStats()
+        check(lib().pd_train_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def sample_nodes(self, n_samples: int) -> np.ndarray:
+        out = np.zeros(n_samples, np.int32)
+        check(lib().pd_train_sample_nodes(self.h, _ptr(out)))
+        return out
+
+    # -- stage entry points of one depth --
+    def candidates(self, params: TreeTrainerParameters, tree_id: int, nodes) -> tuple[np.ndarray, np.ndarray]:
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        F, T, D = params.n_features, params.n_thresholds, self.config.feat_dim
+        feat = np.zeros((len(nodes), F, D), self.config.feat_dtype)
+        thr = np.zeros((len(nodes), F, T), self.config.feat_dtype)
+        check(lib().pd_candidates(self.h, C.byref(params.c()), tree_id, _ptr(nodes), len(nodes), _ptr(feat),
+                                  _ptr(thr)))
+        return feat, thr
+
+    def hist(self, params: TreeTrainerParameters, tree_id: int, sample_node, nodes) -> np.ndarray:
+        nodes = np.ascontiguousarray(nodes, np.int32)
+        sample_node = np.ascontiguousarray(sample_node, np.int32)
+        K, T, F = self.config.n_classes, params.n_thresholds, params.n_features
+        out = np.zeros((len(nodes), K, T, F), np.uint32)
+        check(lib().pd_hist(self.h, C.byref(params.c()), tree_id, _ptr(sample_node), _ptr(nodes), len(nodes),
+                            _ptr(out)))
+        return out
+
+    def split(self, params: TreeTrainerParameters, hist: np.ndarray, class_tot: np.ndarray):
+        hist = np.ascontiguousarray(hist, np.uint32)
+        class_tot = np.ascontiguousarray(class_tot, np.uint32)
+        n = hist.shape[0]
+        t = np.zeros(n, np.int32)
+        f = np.zeros(n, np.int32)
+        g = np.zeros(n, np.float64)
+        check(lib().pd_split(self.h, C.byref(params.c()), _ptr(hist), _ptr(class_tot), n, _ptr(t), _ptr(f), _ptr(g)))
+        return t, f, g
+
+    def log2_table(self, n: int) -> np.ndarray:
+        out = np.zeros(n, np.float64)
+        check(lib().pd_log2_table(self.h, n, _ptr(out)))
+        return out
+
+
+class Classifier(_Ctx):
+    """CLClassifier (cl_classifier.hpp:81-94): a forest and per-pixel prediction."""
+
+    def __init__(self, config: ForestConfig, device: int = 0):
+        super().__init__(config, device)
+        self.trees: list[Tree] = []
+
+    def __lshift__(self, tree: Tree) -> "Classifier":
+        check(lib().pd_forest_add_tree(self.h, tree.depth, _ptr(np.ascontiguousarray(tree.left_child)),
+                                       _ptr(np.ascontiguousarray(tree.features)),
+                                       _ptr(np.ascontiguousarray(tree.thresholds)),
+                                       _ptr(np.ascontiguousarray(tree.posteriors))))
+        self.trees.append(tree)
+        return self
+
+    def clear(self) -> None:
+        check(lib().pd_forest_clear(self.h))
+        self.trees = []
+
+    def predict(self, image: np.ndarray, mask: np.ndarray | None = None) -> np.ndarray:
+        """Posterior [nClasses][H][W] (cl_classifier_impl.hpp:356-557); masked-out pixels are 0."""
+        image = np.ascontiguousarray(image, self.config.img_dtype)
+        H, W = image.shape[:2]
+        out = np.zeros((self.config.n_classes, H, W), np.float32)
+        m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+        check(lib().pd_predict_posterior(self.h, _ptr(image), W, H, _ptr(m), _ptr(out)))
+        return out
+
+    def predict_leaf(self, tree: int, image: np.ndarray, mask: np.ndarray | None = None) -> np.ndarray:
+        """Leaf node id per pixel (cl_classifier_impl.hpp:200-341); masked-out pixels are 0."""
+        image = np.ascontiguousarray(image, self.config.img_dtype)
+        H, W = image.shape[:2]
+        out = np.zeros((H, W), np.int32)
+        m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+        check(lib().pd_predict_leaf(self.h, tree, _ptr(image), W, H, _ptr(m), _ptr(out)))
+        return out
+
+
+def synth_depth(seed: int, n_images: int, width: int, height: int, *, first_image: int = 0, min_ellipses: int = 1,
+                max_ellipses: int = 3, parts: int = 0, samples_per_image: int = 500, bg_permille: int = 100):
+    """Seeded synthetic depth maps (uint16 mm), labels and sorted sample lists."""
+    px = np.zeros((n_images, height, width), np.uint16)
+    lb = np.zeros((n_images, height, width), np.uint8)
+    sm = np.zeros((n_images, samples_per_image), np.uint32)
+    check(lib().pd_synth_depth(seed, first_image, n_images, width, height, min_ellipses, max_ellipses, parts,
+                               samples_per_image, bg_permille, _ptr(px), _ptr(lb), _ptr(sm)))
+    return px, lb, sm
+
+
+def synth_rgb(seed: int, n_images: int, width: int, height: int, *, first_image: int = 0, n_classes: int = 21,
+              samples_per_image: int = 2000):
+    """Seeded synthetic RGB Voronoi images (uint8 HxWx3), labels and sorted sample lists."""
+    px = np.zeros((n_images, height, width, 3), np.uint8)
+    lb = np.zeros((n_images, height, width), np.uint8)
+    sm = np.zeros((n_images, samples_per_image), np.uint32)
+    check(lib().pd_synth_rgb(seed, first_image, n_images, width, height, n_classes, samples_per_image, _ptr(px),
+                             _ptr(lb), _ptr(sm)))
+    return px, lb, sm
+
+
+def training_set(n_classes: int, pixels: np.ndarray, labels: np.ndarray, samples: np.ndarray) -> TrainingSet:
+    """TrainingSet from stacked arrays (priors = mean of per-image priors)."""
+    return TrainingSet(n_classes, [TrainingSetImage(pixels[i], labels[i], n_classes, samples[i])
+                                   for i in range(len(pixels))])

@@ -1,0 +1,127 @@
+"""ctypes binding of libpadenti_gb300.so (the C ABI in include/padenti_gb300.h).
+
+The library is built in-tree by padenti_gb300.build.  Nothing here falls back to
+another implementation: if the library is missing or fails to load, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+LIB_PATH = pathlib.Path(__file__).resolve().parent / "_build" / "libpadenti_gb300.so"
+
+PD_OK = 0
+PD_IMG_U8, PD_IMG_U16 = 1, 2
+PD_FEAT_I16, PD_FEAT_I32 = 1, 2
+PD_PLUGIN_DEPTH_DIFF2, PD_PLUGIN_DEPTH_DIFF1, PD_PLUGIN_CHANNEL_DIFF = 1, 2, 3
+PD_MAX_FEAT_DIM = 8
+
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "unsupported", -5: "bad state"}
+
+
+class Config(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("plugin", "img_type", "n_channels", "feat_type", "feat_dim", "n_classes")]
+
+
+class TrainParams(C.Structure):
+    _fields_ = [
+        ("n_features", C.c_uint32),
+        ("n_thresholds", C.c_uint32),
+        ("feat_low", C.c_int32 * PD_MAX_FEAT_DIM),
+        ("feat_up", C.c_int32 * PD_MAX_FEAT_DIM),
+        ("thr_low", C.c_int32),
+        ("thr_up", C.c_int32),
+        ("per_leaf_samples_thr", C.c_uint32),
+    ]
+
+
+class DatasetDesc(C.Structure):
+    _fields_ = [
+        ("n_images", C.c_uint32),
+        ("pixels", C.c_void_p),
+        ("pix_off", C.c_void_p),
+        ("width", C.c_void_p),
+        ("height", C.c_void_p),
+        ("labels", C.c_void_p),
+        ("lab_off", C.c_void_p),
+        ("samples", C.c_void_p),
+        ("samp_off", C.c_void_p),
+    ]
+
+
+class TrainStats(C.Structure):
+    _fields_ = [
+        ("evals", C.c_uint64),
+        ("nodes_trained", C.c_uint64),
+        ("nodes_split", C.c_uint64),
+        ("hist_launches", C.c_uint64),
+        ("split_rechecked", C.c_uint64),
+        ("ms_candidates", C.c_double),
+        ("ms_hist", C.c_double),
+        ("ms_split", C.c_double),
+        ("ms_reassign", C.c_double),
+        ("ms_total", C.c_double),
+    ]
+
+
+# name -> (restype, argtypes)
+_P = C.c_void_p
+_SIGS = {
+    "pd_last_error": (C.c_char_p, []),
+    "pd_version": (C.c_int, []),
+    "pd_ctx_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(_P)]),
+    "pd_ctx_destroy": (C.c_int, [_P]),
+    "pd_ctx_set_hist_budget": (C.c_int, [_P, C.c_uint64]),
+    "pd_ctx_sync": (C.c_int, [_P]),
+    "pd_ctx_stream": (_P, [_P]),
+    "pd_dataset_upload": (C.c_int, [_P, C.POINTER(DatasetDesc)]),
+    "pd_dataset_info": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
+    "pd_train_tree": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]),
+    "pd_train_get_stats": (C.c_int, [_P, C.POINTER(TrainStats)]),
+    "pd_train_sample_nodes": (C.c_int, [_P, _P]),
+    "pd_candidates": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, _P, C.c_uint32, _P, _P]),
+    "pd_hist": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, _P, _P, C.c_uint32, _P]),
+    "pd_split": (C.c_int, [_P, C.POINTER(TrainParams), _P, _P, C.c_uint32, _P, _P, _P]),
+    "pd_log2_table": (C.c_int, [_P, C.c_uint32, _P]),
+    "pd_forest_clear": (C.c_int, [_P]),
+    "pd_forest_add_tree": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P]),
+    "pd_forest_size": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "pd_predict_posterior": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P, _P]),
+    "pd_predict_leaf": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
+    "pd_predict_posterior_device": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
+    "pd_synth_depth": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                                 C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]),
+    "pd_synth_rgb": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
+                               C.c_uint32, _P, _P, _P]),
+}
+
+EXPORTED = tuple(_SIGS)
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded native library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m padenti_gb300.build`")
+        l = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+class PadentiError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+def check(rc: int) -> None:
+    if rc != PD_OK:
+        msg = lib().pd_last_error()
+        raise PadentiError(rc, msg.decode() if msg else "")

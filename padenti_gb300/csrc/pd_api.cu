@@ -1,0 +1,172 @@
+// Context, error reporting and training-set upload of libpadenti_gb300.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pd_ctx.cuh"
+#include "pd_plugins.cuh"
+
+namespace pd {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+const char *last_error() { return g_last_error.c_str(); }
+
+// Checks a pd_config against the plugin's compiled types.
+static int check_config(const pd_config *c) {
+  PD_CHECK(c, PD_ERR_INVALID, "null config");
+  PD_CHECK(c->n_classes >= 1 && c->n_classes <= PD_MAX_CLASSES, PD_ERR_UNSUPPORTED, "nClasses %d outside [1,%d]",
+           c->n_classes, PD_MAX_CLASSES);
+  return dispatch_plugin(c->plugin, [&]<class P>() {
+    const int img = sizeof(typename P::img_t) == 1 ? PD_IMG_U8 : PD_IMG_U16;
+    const int ft = sizeof(typename P::feat_t) == 2 ? PD_FEAT_I16 : PD_FEAT_I32;
+    PD_CHECK(c->img_type == img && c->n_channels == P::kChannels && c->feat_type == ft &&
+                 c->feat_dim == P::kFeatDim,
+             PD_ERR_INVALID,
+             "plugin %d needs img_type %d, %d channel(s), feat_type %d, FeatDim %d (got %d, %d, %d, %d)", c->plugin,
+             img, P::kChannels, ft, P::kFeatDim, c->img_type, c->n_channels, c->feat_type, c->feat_dim);
+    return PD_OK;
+  });
+}
+
+}  // namespace pd
+
+using namespace pd;
+
+extern "C" const char *pd_last_error(void) { return last_error(); }
+extern "C" int pd_version(void) { return 10000; }
+
+extern "C" int pd_ctx_create(const pd_config *cfg, int device, pd_ctx **out) {
+  PD_CHECK(out, PD_ERR_INVALID, "null output");
+  *out = nullptr;
+  PD_TRY(check_config(cfg));
+  int n = 0;
+  PD_CUDA(cudaGetDeviceCount(&n));
+  PD_CHECK(device >= 0 && device < n, PD_ERR_INVALID, "device %d not present (%d devices)", device, n);
+  PD_CUDA(cudaSetDevice(device));
+  pd_ctx *c = new pd_ctx();
+  c->cfg = *cfg;
+  c->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return set_error(PD_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  for (auto &ev : c->ev) cudaEventCreate(&ev);
+  *out = c;
+  return PD_OK;
+}
+
+extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
+  if (!ctx) return PD_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  DevBuf *bufs[] = {&ctx->pixels, &ctx->img_off, &ctx->img_wh, &ctx->s_xy, &ctx->s_img, &ctx->s_label,
+                    &ctx->log2_tab, &ctx->snode, &ctx->act[0], &ctx->act[1], &ctx->act_slot[0],
+                    &ctx->act_slot[1], &ctx->flags, &ctx->scan_blocks, &ctx->slot_adj, &ctx->scatter_err,
+                    &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->hist, &ctx->g32, &ctx->items,
+                    &ctx->zero_slots, &ctx->split_out, &ctx->split_cl, &ctx->recheck, &ctx->t_lc,
+                    &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
+                    &ctx->f_post, &ctx->f_meta, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
+  for (DevBuf *b : bufs) b->release();
+  for (auto &ev : ctx->ev)
+    if (ev) cudaEventDestroy(ev);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return PD_OK;
+}
+
+extern "C" int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes) {
+  PD_CHECK(ctx, PD_ERR_INVALID, "null context");
+  PD_CHECK(bytes >= (1ull << 20), PD_ERR_INVALID, "histogram budget below 1 MiB");
+  ctx->hist_budget = bytes;
+  return PD_OK;
+}
+
+extern "C" int pd_ctx_sync(pd_ctx *ctx) {
+  PD_CHECK(ctx, PD_ERR_INVALID, "null context");
+  PD_CUDA(cudaStreamSynchronize(ctx->stream));
+  return PD_OK;
+}
+
+extern "C" void *pd_ctx_stream(pd_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
+  PD_CHECK(ctx && ds, PD_ERR_INVALID, "null argument");
+  PD_CHECK(ds->n_images >= 1, PD_ERR_INVALID, "empty training set");
+  PD_CHECK(ds->pixels && ds->pix_off && ds->width && ds->height && ds->labels && ds->lab_off && ds->samples &&
+               ds->samp_off,
+           PD_ERR_INVALID, "null dataset array");
+  PD_CUDA(cudaSetDevice(ctx->device));
+  const uint32_t n = ds->n_images;
+  const size_t px = img_size(ctx->cfg.img_type) * ctx->cfg.n_channels;
+  const uint64_t S = ds->samp_off[n];
+  PD_CHECK(S < (1ull << 31), PD_ERR_UNSUPPORTED, "%llu samples (max 2^31-1)", (unsigned long long)S);
+  uint64_t bytes = 0;
+  std::vector<uint64_t> off(n);
+  std::vector<uint32_t> wh(n);
+  for (uint32_t i = 0; i < n; i++) {
+    PD_CHECK(ds->width[i] >= 1 && ds->height[i] >= 1 && ds->width[i] < 65536 && ds->height[i] < 65536,
+             PD_ERR_UNSUPPORTED, "image %u is %ux%u (sides must be in [1,65535])", i, ds->width[i], ds->height[i]);
+    PD_CHECK(ds->samp_off[i + 1] >= ds->samp_off[i], PD_ERR_INVALID, "sample offsets not monotone at image %u", i);
+    off[i] = ds->pix_off[i];
+    wh[i] = ds->width[i] | (ds->height[i] << 16);
+    bytes = std::max<uint64_t>(bytes, ds->pix_off[i] + (uint64_t)ds->width[i] * ds->height[i] * px);
+  }
+  std::vector<uint32_t> xy(S), im(S);
+  std::vector<uint8_t> lab(S);
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t w = ds->width[i], h = ds->height[i];
+    for (uint64_t k = ds->samp_off[i]; k < ds->samp_off[i + 1]; k++) {
+      const uint32_t p = ds->samples[k];
+      PD_CHECK((uint64_t)p < (uint64_t)w * h, PD_ERR_INVALID, "sample %llu of image %u outside the image", (unsigned long long)k, i);
+      const uint8_t l = ds->labels[ds->lab_off[i] + p];
+      PD_CHECK(l >= 1 && l <= ctx->cfg.n_classes, PD_ERR_INVALID,
+               "sample %llu of image %u has label %u (sampled pixels need a label in [1,%d])",
+               (unsigned long long)k, i, l, ctx->cfg.n_classes);
+      xy[k] = (p % w) | ((p / w) << 16);
+      im[k] = i;
+      lab[k] = (uint8_t)(l - 1);
+    }
+  }
+  cudaStream_t st = ctx->stream;
+  PD_TRY(ctx->pixels.ensure(bytes));
+  PD_TRY(ctx->img_off.ensure(n * 8));
+  PD_TRY(ctx->img_wh.ensure(n * 4));
+  PD_TRY(ctx->s_xy.ensure(S * 4 + 4));
+  PD_TRY(ctx->s_img.ensure(S * 4 + 4));
+  PD_TRY(ctx->s_label.ensure(S + 4));
+  PD_CUDA(cudaMemcpyAsync(ctx->pixels.ptr, ds->pixels, bytes, cudaMemcpyHostToDevice, st));
+  PD_CUDA(cudaMemcpyAsync(ctx->img_off.ptr, off.data(), n * 8, cudaMemcpyHostToDevice, st));
+  PD_CUDA(cudaMemcpyAsync(ctx->img_wh.ptr, wh.data(), n * 4, cudaMemcpyHostToDevice, st));
+  if (S) {
+    PD_CUDA(cudaMemcpyAsync(ctx->s_xy.ptr, xy.data(), S * 4, cudaMemcpyHostToDevice, st));
+    PD_CUDA(cudaMemcpyAsync(ctx->s_img.ptr, im.data(), S * 4, cudaMemcpyHostToDevice, st));
+    PD_CUDA(cudaMemcpyAsync(ctx->s_label.ptr, lab.data(), S, cudaMemcpyHostToDevice, st));
+  }
+  PD_CUDA(cudaStreamSynchronize(st));
+  ctx->h_label.swap(lab);
+  ctx->n_images = n;
+  ctx->n_samples = S;
+  ctx->have_dataset = true;
+  PD_TRY(ensure_log2_table(ctx, S + 2));
+  PD_CUDA(cudaStreamSynchronize(st));
+  return PD_OK;
+}
+
+extern "C" int pd_dataset_info(pd_ctx *ctx, uint64_t *n_samples, uint32_t *n_images) {
+  PD_CHECK(ctx, PD_ERR_INVALID, "null context");
+  if (n_samples) *n_samples = ctx->n_samples;
+  if (n_images) *n_images = ctx->n_images;
+  return PD_OK;
+}

@@ -1,0 +1,60 @@
+// Internal state of a pd_ctx: the device-resident training set, the training
+// scratch buffers and the forest.
+#pragma once
+
+#include <vector>
+
+#include "pd_common.cuh"
+
+struct pd_ctx {
+  pd_config cfg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t hist_budget = 8ull << 30;
+  uint32_t chunk = 4096;  // samples per histogram work item
+
+  // ---- training set in HBM (cl_tree_trainer_impl_init.hpp:99-154 streams it
+  // image by image; here it stays resident) ----
+  bool have_dataset = false;
+  uint32_t n_images = 0;
+  uint64_t n_samples = 0;
+  pd::DevBuf pixels;    // concatenated images
+  pd::DevBuf img_off;   // uint64 byte offsets
+  pd::DevBuf img_wh;    // uint32 w | h << 16
+  pd::DevBuf s_xy;      // uint32 x | y << 16 per sample
+  pd::DevBuf s_img;     // uint32 image per sample
+  pd::DevBuf s_label;   // uint8 class (0..K-1) per sample
+  std::vector<uint8_t> h_label;  // host copy of the sample classes
+  pd::DevBuf log2_tab;  // double log2(n), n < log2_len
+  uint64_t log2_len = 0;
+
+  // ---- training scratch ----
+  pd::DevBuf snode;                  // int32 node per sample
+  pd::DevBuf act[2], act_slot[2];    // active samples sorted by frontier slot
+  pd::DevBuf flags;                  // uint8 per active sample
+  pd::DevBuf scan_blocks;            // uint64 per scan block
+  pd::DevBuf slot_adj;               // int64 [4] per slot: adjL, adjR, kL, kR
+  pd::DevBuf scatter_err;            // uint32 error counter
+  pd::DevBuf cand_feat, cand_thr, cand_perm;
+  pd::DevBuf hist, g32;
+  pd::DevBuf items, zero_slots;
+  pd::DevBuf split_out, split_cl, recheck;
+  pd::DevBuf t_lc, t_feat, t_thr, t_post;  // device copy of the tree being trained
+  pd_train_stats stats{};
+
+  // ---- forest (CLClassifier) ----
+  std::vector<uint32_t> tree_depth;
+  std::vector<uint64_t> tree_off;
+  std::vector<int32_t> h_lc;
+  std::vector<uint8_t> h_feat, h_thr;  // FeatType bytes
+  std::vector<float> h_post;
+  bool forest_dirty = true;
+  pd::DevBuf f_lc, f_feat, f_thr, f_post, f_meta;
+  pd::DevBuf p_img, p_mask, p_out;     // staging for host-buffer prediction
+
+  cudaEvent_t ev[8] = {};
+};
+
+namespace pd {
+int ensure_log2_table(pd_ctx *ctx, uint64_t n);
+}

@@ -1,0 +1,259 @@
+// Forest container and prediction: CLClassifier (cl_classifier_impl.hpp).
+// The reference launches `predict` (depth-1) times per tree with an image copy
+// between levels, then `computePosterior`, reads the [K][H][W] buffer back and
+// sums on the host (cl_classifier_impl.hpp:478-552).  Here one kernel walks the
+// whole forest per pixel, keeps the leaf ids of all trees, sums the leaf
+// posteriors in tree order and divides by the tree count, writing the planar
+// posterior once, coalesced.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "pd_ctx.cuh"
+#include "pd_plugins.cuh"
+
+namespace pd {
+
+struct TreeMeta {
+  unsigned long long off;  // first node of the tree in the forest arrays
+  uint32_t depth, pad;
+};
+
+constexpr int kPredX = 32, kPredY = 8, kPredThreads = kPredX * kPredY;
+
+template <class P>
+PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
+                  const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+                  uint32_t depth) {
+  using FeatT = typename P::feat_t;
+  constexpr int D = P::kFeatDim;
+  int32_t node = 0;
+  for (uint32_t d = 1; d < depth; d++) {
+    const int32_t c = ldg(lc + node);
+    if (c < 0) break;  // leaf (-1); an untrained root (-2) also stops
+    FeatT fv[D];
+#pragma unroll
+    for (int k = 0; k < D; k++) fv[k] = ldg(feat + (size_t)node * D + k);
+    const FeatT r = P::eval(prep, fv);
+    node = c + (r <= ldg(thr + node) ? 0 : 1);
+  }
+  return node;
+}
+
+// grid (ceil(W/32), ceil(H/8), n_images); dynamic smem n_trees*256 int32.
+template <class P>
+__global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
+    const uint8_t *__restrict__ images, uint64_t img_bytes, uint32_t W, uint32_t H,
+    const uint8_t *__restrict__ masks, float *__restrict__ out, const int32_t *__restrict__ lc,
+    const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+    const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K) {
+  using ImgT = typename P::img_t;
+  constexpr int D = P::kFeatDim;
+  extern __shared__ int32_t leaf_s[];
+  const uint32_t tid = threadIdx.y * kPredX + threadIdx.x;
+  const uint32_t x = blockIdx.x * kPredX + threadIdx.x, y = blockIdx.y * kPredY + threadIdx.y, z = blockIdx.z;
+  if (x >= W || y >= H) return;
+  const size_t P_ = (size_t)W * H, pix = (size_t)y * W + x;
+  float *o = out + (size_t)z * K * P_ + pix;
+  if (masks && !masks[(size_t)z * P_ + pix]) {
+    for (uint32_t l = 0; l < K; l++) o[l * P_] = 0.0f;
+    return;
+  }
+  ImageRef<ImgT> im;
+  im.data = reinterpret_cast<const ImgT *>(images + (size_t)z * img_bytes);
+  im.w = (int32_t)W;
+  im.h = (int32_t)H;
+  const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
+  for (uint32_t t = 0; t < n_trees; t++) {
+    const size_t off = meta[t].off;
+    leaf_s[t * kPredThreads + tid] = walk<P>(prep, lc + off, feat + off * D, thr + off, meta[t].depth);
+  }
+  const float nt = (float)n_trees;
+  for (uint32_t l = 0; l < K; l++) {
+    float acc = 0.0f;
+    for (uint32_t t = 0; t < n_trees; t++)
+      acc = acc + ldg(post + (meta[t].off + (size_t)leaf_s[t * kPredThreads + tid]) * K + l);
+    o[l * P_] = fdiv(acc, nt);
+  }
+}
+
+template <class P>
+__global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__restrict__ image, uint32_t W,
+                                                               uint32_t H, const uint8_t *__restrict__ mask,
+                                                               int32_t *__restrict__ out,
+                                                               const int32_t *__restrict__ lc,
+                                                               const typename P::feat_t *__restrict__ feat,
+                                                               const typename P::feat_t *__restrict__ thr,
+                                                               uint32_t depth) {
+  using ImgT = typename P::img_t;
+  const uint32_t x = blockIdx.x * kPredX + threadIdx.x, y = blockIdx.y * kPredY + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const size_t pix = (size_t)y * W + x;
+  if (mask && !mask[pix]) {
+    out[pix] = 0;
+    return;
+  }
+  ImageRef<ImgT> im;
+  im.data = reinterpret_cast<const ImgT *>(image);
+  im.w = (int32_t)W;
+  im.h = (int32_t)H;
+  out[pix] = walk<P>(P::prepare(im, (int32_t)x, (int32_t)y), lc, feat, thr, depth);
+}
+
+static int upload_forest(pd_ctx *ctx) {
+  if (!ctx->forest_dirty) return PD_OK;
+  const size_t fs = feat_size(ctx->cfg.feat_type);
+  const size_t nodes = ctx->h_lc.size();
+  const uint32_t nt = (uint32_t)ctx->tree_depth.size();
+  std::vector<TreeMeta> meta(nt);
+  for (uint32_t t = 0; t < nt; t++) {
+    meta[t].off = ctx->tree_off[t];
+    meta[t].depth = ctx->tree_depth[t];
+    meta[t].pad = 0;
+  }
+  PD_TRY(ctx->f_lc.ensure(nodes * 4 + 4));
+  PD_TRY(ctx->f_feat.ensure(ctx->h_feat.size() + 4));
+  PD_TRY(ctx->f_thr.ensure(ctx->h_thr.size() + 4));
+  PD_TRY(ctx->f_post.ensure(ctx->h_post.size() * 4 + 4));
+  PD_TRY(ctx->f_meta.ensure(nt * sizeof(TreeMeta) + 16));
+  cudaStream_t st = ctx->stream;
+  if (nodes) {
+    PD_CUDA(cudaMemcpyAsync(ctx->f_lc.ptr, ctx->h_lc.data(), nodes * 4, cudaMemcpyHostToDevice, st));
+    PD_CUDA(cudaMemcpyAsync(ctx->f_feat.ptr, ctx->h_feat.data(), ctx->h_feat.size(), cudaMemcpyHostToDevice, st));
+    PD_CUDA(cudaMemcpyAsync(ctx->f_thr.ptr, ctx->h_thr.data(), ctx->h_thr.size(), cudaMemcpyHostToDevice, st));
+    PD_CUDA(cudaMemcpyAsync(ctx->f_post.ptr, ctx->h_post.data(), ctx->h_post.size() * 4, cudaMemcpyHostToDevice, st));
+    PD_CUDA(cudaMemcpyAsync(ctx->f_meta.ptr, meta.data(), nt * sizeof(TreeMeta), cudaMemcpyHostToDevice, st));
+  }
+  (void)fs;
+  ctx->forest_dirty = false;
+  return PD_OK;
+}
+
+template <class P>
+static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_t W, uint32_t H,
+                            const uint8_t *masks, float *out) {
+  using FeatT = typename P::feat_t;
+  const uint32_t nt = (uint32_t)ctx->tree_depth.size();
+  const size_t smem = (size_t)nt * kPredThreads * 4;
+  PD_CUDA(cudaFuncSetAttribute(k_predict_posterior<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((W + kPredX - 1) / kPredX, (H + kPredY - 1) / kPredY, n);
+  const uint64_t img_bytes = (uint64_t)W * H * P::kChannels * sizeof(typename P::img_t);
+  k_predict_posterior<P><<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
+      static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_lc.as<int32_t>(),
+      ctx->f_feat.as<FeatT>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(), ctx->f_meta.as<TreeMeta>(), nt,
+      (uint32_t)ctx->cfg.n_classes);
+  PD_CUDA(cudaGetLastError());
+  return PD_OK;
+}
+
+}  // namespace pd
+
+using namespace pd;
+
+extern "C" int pd_forest_clear(pd_ctx *ctx) {
+  PD_CHECK(ctx, PD_ERR_INVALID, "null context");
+  ctx->tree_depth.clear();
+  ctx->tree_off.clear();
+  ctx->h_lc.clear();
+  ctx->h_feat.clear();
+  ctx->h_thr.clear();
+  ctx->h_post.clear();
+  ctx->forest_dirty = true;
+  return PD_OK;
+}
+
+extern "C" int pd_forest_add_tree(pd_ctx *ctx, uint32_t depth, const int32_t *left_child, const void *features,
+                                  const void *thresholds, const float *posteriors) {
+  PD_CHECK(ctx && left_child && features && thresholds && posteriors, PD_ERR_INVALID, "null argument");
+  PD_CHECK(depth >= 1 && depth <= 24, PD_ERR_UNSUPPORTED, "tree depth %u outside [1,24]", depth);
+  PD_CHECK(ctx->tree_depth.size() < PD_MAX_TREES, PD_ERR_UNSUPPORTED, "forest already holds %d trees", PD_MAX_TREES);
+  const uint64_t nodes = (1ull << depth) - 1ull;
+  const size_t fs = feat_size(ctx->cfg.feat_type), D = ctx->cfg.feat_dim, K = ctx->cfg.n_classes;
+  // Every split node must point to an existing child pair.
+  for (uint64_t i = 0; i < nodes; i++) {
+    const int32_t c = left_child[i];
+    PD_CHECK(c == -1 || c == -2 || (c >= 1 && (uint64_t)c + 1 < nodes), PD_ERR_INVALID,
+             "node %llu has left child %d outside the tree", (unsigned long long)i, c);
+  }
+  ctx->tree_off.push_back(ctx->h_lc.size());
+  ctx->tree_depth.push_back(depth);
+  ctx->h_lc.insert(ctx->h_lc.end(), left_child, left_child + nodes);
+  const uint8_t *fb = static_cast<const uint8_t *>(features), *tb = static_cast<const uint8_t *>(thresholds);
+  ctx->h_feat.insert(ctx->h_feat.end(), fb, fb + nodes * D * fs);
+  ctx->h_thr.insert(ctx->h_thr.end(), tb, tb + nodes * fs);
+  ctx->h_post.insert(ctx->h_post.end(), posteriors, posteriors + nodes * K);
+  ctx->forest_dirty = true;
+  return PD_OK;
+}
+
+extern "C" int pd_forest_size(pd_ctx *ctx, uint32_t *n_trees) {
+  PD_CHECK(ctx && n_trees, PD_ERR_INVALID, "null argument");
+  *n_trees = (uint32_t)ctx->tree_depth.size();
+  return PD_OK;
+}
+
+extern "C" int pd_predict_posterior_device(pd_ctx *ctx, uint32_t n_images, const void *images_device, uint32_t width,
+                                           uint32_t height, const uint8_t *masks_device, float *out_device) {
+  PD_CHECK(ctx && images_device && out_device, PD_ERR_INVALID, "null argument");
+  PD_CHECK(!ctx->tree_depth.empty(), PD_ERR_STATE, "empty forest");
+  PD_CHECK(width >= 1 && height >= 1 && n_images >= 1 && n_images <= 65535, PD_ERR_INVALID, "bad image batch");
+  PD_CUDA(cudaSetDevice(ctx->device));
+  PD_TRY(upload_forest(ctx));
+  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
+    return launch_posterior<P>(ctx, n_images, images_device, width, height, masks_device, out_device);
+  });
+}
+
+extern "C" int pd_predict_posterior(pd_ctx *ctx, const void *image, uint32_t width, uint32_t height,
+                                    const uint8_t *mask, float *out) {
+  PD_CHECK(ctx && image && out, PD_ERR_INVALID, "null argument");
+  PD_CHECK(!ctx->tree_depth.empty(), PD_ERR_STATE, "empty forest");
+  PD_CHECK(width >= 1 && height >= 1, PD_ERR_INVALID, "empty image");
+  PD_CUDA(cudaSetDevice(ctx->device));
+  const size_t P_ = (size_t)width * height;
+  const size_t ib = P_ * ctx->cfg.n_channels * img_size(ctx->cfg.img_type);
+  const size_t ob = P_ * ctx->cfg.n_classes * 4;
+  PD_TRY(ctx->p_img.ensure(ib));
+  PD_TRY(ctx->p_out.ensure(ob));
+  if (mask) PD_TRY(ctx->p_mask.ensure(P_));
+  cudaStream_t st = ctx->stream;
+  PD_CUDA(cudaMemcpyAsync(ctx->p_img.ptr, image, ib, cudaMemcpyHostToDevice, st));
+  if (mask) PD_CUDA(cudaMemcpyAsync(ctx->p_mask.ptr, mask, P_, cudaMemcpyHostToDevice, st));
+  PD_TRY(pd_predict_posterior_device(ctx, 1, ctx->p_img.ptr, width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
+                                     ctx->p_out.as<float>()));
+  PD_CUDA(cudaMemcpyAsync(out, ctx->p_out.ptr, ob, cudaMemcpyDeviceToHost, st));
+  PD_CUDA(cudaStreamSynchronize(st));
+  return PD_OK;
+}
+
+extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, uint32_t width, uint32_t height,
+                               const uint8_t *mask, int32_t *out) {
+  PD_CHECK(ctx && image && out, PD_ERR_INVALID, "null argument");
+  PD_CHECK(tree < ctx->tree_depth.size(), PD_ERR_INVALID, "tree %u not in the forest", tree);
+  PD_CHECK(width >= 1 && height >= 1, PD_ERR_INVALID, "empty image");
+  PD_CUDA(cudaSetDevice(ctx->device));
+  PD_TRY(upload_forest(ctx));
+  const size_t P_ = (size_t)width * height;
+  const size_t ib = P_ * ctx->cfg.n_channels * img_size(ctx->cfg.img_type);
+  PD_TRY(ctx->p_img.ensure(ib));
+  PD_TRY(ctx->p_out.ensure(P_ * 4));
+  if (mask) PD_TRY(ctx->p_mask.ensure(P_));
+  cudaStream_t st = ctx->stream;
+  PD_CUDA(cudaMemcpyAsync(ctx->p_img.ptr, image, ib, cudaMemcpyHostToDevice, st));
+  if (mask) PD_CUDA(cudaMemcpyAsync(ctx->p_mask.ptr, mask, P_, cudaMemcpyHostToDevice, st));
+  const size_t off = ctx->tree_off[tree];
+  const uint32_t depth = ctx->tree_depth[tree];
+  PD_TRY(dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
+    using FeatT = typename P::feat_t;
+    dim3 grid((width + kPredX - 1) / kPredX, (height + kPredY - 1) / kPredY, 1);
+    k_predict_leaf<P><<<grid, dim3(kPredX, kPredY), 0, st>>>(
+        ctx->p_img.as<uint8_t>(), width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
+        ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_feat.as<FeatT>() + off * P::kFeatDim,
+        ctx->f_thr.as<FeatT>() + off, depth);
+    PD_CUDA(cudaGetLastError());
+    return PD_OK;
+  }));
+  PD_CUDA(cudaMemcpyAsync(out, ctx->p_out.ptr, P_ * 4, cudaMemcpyDeviceToHost, st));
+  PD_CUDA(cudaStreamSynchronize(st));
+  return PD_OK;
+}

@@ -1,0 +1,602 @@
+// Device kernels of one training depth: candidate table, class histograms,
+// best split with FP64 recheck, reassignment and the stable regrouping of the
+// active samples by frontier slot.
+#pragma once
+
+#include <cfloat>
+
+#include "pd_log2.cuh"
+#include "pd_plugins.cuh"
+#include "pd_rng.cuh"
+
+namespace pd {
+
+constexpr int kTile = 32;          // candidates per histogram tile (one per lane)
+constexpr int kHistThreads = 256;  // 8 warps, each on its own samples
+constexpr int kSplitThreads = 256;
+constexpr int kScanItems = 4096;   // active samples per scan block (256 threads x 16)
+constexpr float kRecheckDelta = 5e-4f;  // FP32 gain window rechecked in FP64
+
+struct CandBounds {
+  int32_t low[PD_MAX_FEAT_DIM];
+  int32_t up[PD_MAX_FEAT_DIM];
+  int32_t thr_lo, thr_hi;
+};
+
+// One histogram work item: candidates [tile*32, tile*32+32) of frontier slot
+// `slot` over the active samples act[begin, end).  multi=1 when other work
+// items add into the same histogram rows.
+struct WorkItem {
+  uint32_t slot, tile, begin, end, multi, pad0, pad1, pad2;
+};
+
+struct DevSet {
+  const uint8_t *pixels;
+  const uint64_t *img_off;
+  const uint32_t *img_wh;
+  const uint32_t *s_xy;
+  const uint32_t *s_img;
+  const uint8_t *s_label;
+};
+
+template <typename T>
+PD_D T max_of() {
+  return (T)(sizeof(T) == 2 ? 32767 : 2147483647);
+}
+
+// ------------------------------------------------------ candidate table ----
+// Thread per (slot, candidate).  Thresholds are written sorted ascending with
+// their original index, so a response needs one binary search instead of T
+// comparisons and the split can prefix-sum the counts back.
+template <typename FeatT>
+__global__ void __launch_bounds__(128) k_candidates(const int32_t *__restrict__ nodes, uint32_t n_nodes,
+                                                    uint32_t tree, uint32_t F, uint32_t T, int D,
+                                                    CandBounds b, FeatT *__restrict__ feat,
+                                                    FeatT *__restrict__ thr_sorted,
+                                                    uint8_t *__restrict__ perm) {
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (uint64_t)n_nodes * F) return;
+  const uint32_t n = (uint32_t)(idx / F), f = (uint32_t)(idx % F);
+  const uint32_t node = (uint32_t)nodes[n];
+  FeatT fv[PD_MAX_FEAT_DIM];
+  candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
+  for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + f] = fv[d];
+
+  FeatT v[PD_MAX_THRESHOLDS];
+  uint8_t id[PD_MAX_THRESHOLDS];
+  uint32_t seed[4] = {tree, node, f, 1u}, st[4] = {0u, 0u, 0u, 0u};
+  for (uint32_t t = 0; t < T; t++) {
+    if ((t & 3u) == 0) {
+      md5_block(seed, st);
+      seed[0] = st[0];
+      seed[1] = st[1];
+      seed[2] = st[2];
+      seed[3] = st[3];
+    }
+    const FeatT x = draw<FeatT>(st[t & 3u], b.thr_lo, b.thr_hi);
+    // stable insertion
+    uint32_t j = t;
+    while (j > 0 && v[j - 1] > x) {
+      v[j] = v[j - 1];
+      id[j] = id[j - 1];
+      j--;
+    }
+    v[j] = x;
+    id[j] = (uint8_t)t;
+  }
+  for (uint32_t j = 0; j < T; j++) {
+    thr_sorted[((size_t)n * T + j) * F + f] = v[j];
+    perm[((size_t)n * T + j) * F + f] = id[j];
+  }
+}
+
+// ------------------------------------------------------------ histogram ----
+// Each CTA owns one (slot, 32-candidate tile, sample chunk).  Lane = candidate,
+// warp = sample stream.  Per evaluation: the plugin response, a branch-free
+// lower_bound over the 32 sorted threshold columns in shared memory, and one
+// conflict-free shared atomic into bin [label][rank][lane] (rank = number of
+// thresholds below the response; rank T counts for no threshold and is
+// dropped).  The tile histogram then goes to global memory in rank space.
+template <class P>
+__global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t *__restrict__ act,
+                                                       const WorkItem *__restrict__ items,
+                                                       const typename P::feat_t *__restrict__ cand_feat,
+                                                       const typename P::feat_t *__restrict__ cand_thr,
+                                                       uint32_t *__restrict__ hist, uint32_t F,
+                                                       uint32_t T, uint32_t K, uint32_t search_top) {
+  using FeatT = typename P::feat_t;
+  using ImgT = typename P::img_t;
+  constexpr int D = P::kFeatDim;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);
+  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * kTile);
+
+  const WorkItem w = items[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t f0 = w.tile * kTile;
+  const uint32_t f = f0 + lane;
+  const bool valid = f < F;
+
+  for (uint32_t j = threadIdx.x; j < T * kTile; j += blockDim.x) {
+    const uint32_t ff = f0 + (j & 31);
+    sh_thr[j] = ff < F ? cand_thr[((size_t)w.slot * T + (j >> 5)) * F + ff] : max_of<FeatT>();
+  }
+  for (uint32_t j = threadIdx.x; j < K * T * kTile; j += blockDim.x) sh_hist[j] = 0u;
+  FeatT fv[D];
+#pragma unroll
+  for (int d = 0; d < D; d++) fv[d] = valid ? cand_feat[((size_t)w.slot * D + d) * F + f] : (FeatT)0;
+  __syncthreads();
+
+  const unsigned full = 0xffffffffu;
+  for (uint32_t base = w.begin + warp * 32; base < w.end; base += kHistThreads) {
+    const uint32_t n_here = min(32u, w.end - base);
+    uint32_t my_xy = 0, my_wh = 0, my_lab = 0;
+    uint64_t my_off = 0;
+    if ((uint32_t)lane < n_here) {
+      const uint32_t s = act[base + lane];
+      my_xy = ds.s_xy[s];
+      my_lab = ds.s_label[s];
+      const uint32_t im = ds.s_img[s];
+      my_off = ds.img_off[im];
+      my_wh = ds.img_wh[im];
+    }
+    for (uint32_t i = 0; i < n_here; i++) {
+      const uint32_t xy = __shfl_sync(full, my_xy, i);
+      const uint32_t wh = __shfl_sync(full, my_wh, i);
+      const uint32_t lab = __shfl_sync(full, my_lab, i);
+      const uint64_t off = __shfl_sync(full, my_off, i);
+      ImageRef<ImgT> im;
+      im.data = reinterpret_cast<const ImgT *>(ds.pixels + off);
+      im.w = (int32_t)(wh & 0xffffu);
+      im.h = (int32_t)(wh >> 16);
+      const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16));
+      const FeatT r = P::eval(prep, fv);
+      uint32_t pos = 0;
+      for (uint32_t step = search_top; step > 0; step >>= 1) {
+        const uint32_t q = pos + step;
+        if (q <= T && sh_thr[(q - 1) * kTile + lane] < r) pos = q;
+      }
+      if (valid && pos < T) atomicAdd(&sh_hist[(lab * T + pos) * kTile + lane], 1u);
+    }
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < K * T * kTile; j += blockDim.x) {
+    const uint32_t ff = f0 + (j & 31);
+    if (ff >= F) continue;
+    const uint32_t v = sh_hist[j];
+    uint32_t *dst = hist + ((size_t)w.slot * K * T + (j >> 5)) * F + ff;
+    if (w.multi) {
+      if (v) atomicAdd(dst, v);
+    } else {
+      *dst = v;
+    }
+  }
+}
+
+__global__ void k_zero_slots(uint32_t *__restrict__ hist, const uint32_t *__restrict__ slots, uint32_t n,
+                             uint64_t per_slot) {
+  const uint64_t total = (uint64_t)n * per_slot;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = i / per_slot;
+    hist[(uint64_t)slots[s] * per_slot + (i - s * per_slot)] = 0u;
+  }
+}
+
+// Rank-space counts -> the reference layout hist[n][l][t][f] (number of
+// samples with response <= threshold t).
+__global__ void k_hist_to_ref(const uint32_t *__restrict__ rank_hist, const uint8_t *__restrict__ perm,
+                              uint32_t *__restrict__ out, uint32_t n_nodes, uint32_t K, uint32_t T,
+                              uint32_t F) {
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (uint64_t)n_nodes * K * F) return;
+  const uint32_t f = (uint32_t)(idx % F);
+  const uint64_t nl = idx / F;
+  const uint32_t n = (uint32_t)(nl / K);
+  uint32_t c = 0;
+  for (uint32_t j = 0; j < T; j++) {
+    c += rank_hist[(nl * T + j) * F + f];
+    out[(nl * T + perm[((size_t)n * T + j) * F + f]) * F + f] = c;
+  }
+}
+
+// ---------------------------------------------------------------- split ----
+struct SplitOut {
+  int32_t t, f, j, pad;
+  double gain;
+};
+
+// Reference-formula FP32 entropy (kernels/learn_best_feature.cl:75-93) with the
+// p <= 1e-6 cutoff as the integer test 1e6*c <= n; fast intrinsics, error well
+// inside kRecheckDelta/2.
+template <int KM>
+PD_D float ent32(const uint32_t *c, uint32_t K, uint32_t n) {
+  if (n == 0) return 0.0f;
+  const float inv = __frcp_rn((float)n);
+  float s = 0.0f;
+#pragma unroll
+  for (int l = 0; l < KM; l++) {
+    if ((uint32_t)l < K) {
+      const uint32_t cl = c[l];
+      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
+        const float p = (float)cl * inv;
+        s -= p * __log2f(p);
+      }
+    }
+  }
+  return s;
+}
+template <int KM>
+PD_D float ent32_right(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n) {
+  if (n == 0) return 0.0f;
+  const float inv = __frcp_rn((float)n);
+  float s = 0.0f;
+#pragma unroll
+  for (int l = 0; l < KM; l++) {
+    if ((uint32_t)l < K) {
+      const uint32_t cl = tot[l] - c[l];
+      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
+        const float p = (float)cl * inv;
+        s -= p * __log2f(p);
+      }
+    }
+  }
+  return s;
+}
+// Exact entropy: sum over classes of (c/n)(log2 n - log2 c), one IEEE double
+// operation at a time with the shared log2 table.
+template <int KM, bool RIGHT>
+PD_D double ent64(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n, const double *L) {
+  double s = 0.0;
+  if (n == 0) return s;
+  const double ln = L[n];
+#pragma unroll
+  for (int l = 0; l < KM; l++) {
+    if ((uint32_t)l < K) {
+      const uint32_t cl = RIGHT ? tot[l] - c[l] : c[l];
+      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
+        const double p = ddiv((double)cl, (double)n);
+        const double lg = dsub(ln, L[cl]);
+        s = dadd(s, dmul(p, lg));
+      }
+    }
+  }
+  return s;
+}
+
+struct SplitArgs {
+  const uint32_t *hist;       // [slots][K][T][F]: rank space, or cumulative when CUM
+  const uint8_t *perm;        // [slots][T][F] original threshold of sorted position (null: identity)
+  const uint32_t *class_tot;  // [slots][K]
+  float *g32;                 // scratch [slots][T][F]
+  const double *L;
+  uint64_t L_len;
+  uint32_t F, T, K;
+  float delta;
+  SplitOut *out;
+  uint32_t *out_cl;           // [slots][K] left class counts of the winner
+  unsigned long long *rechecked;
+};
+
+// One CTA per node.  Pass 1: every (t,f) gain in FP32, kept in scratch, and the
+// node maximum.  Pass 2: candidates within delta of it are re-evaluated with
+// the exact FP64 gain; the largest exact gain wins, ties to the lowest t*F+f
+// (the first-max rule of learn_best_feature.cl:96-101 + std::max_element).
+template <int KM, bool CUM>
+__global__ void __launch_bounds__(kSplitThreads) k_split(SplitArgs a) {
+  const uint32_t slot = blockIdx.x;
+  const uint32_t F = a.F, T = a.T, K = a.K;
+  __shared__ uint32_t tot[KM];
+  __shared__ float red_f[kSplitThreads / 32];
+  __shared__ double red_g[kSplitThreads / 32];
+  __shared__ long long red_i[kSplitThreads / 32];
+  __shared__ float s_gmax;
+  for (uint32_t l = threadIdx.x; l < KM; l += blockDim.x) tot[l] = l < K ? a.class_tot[(size_t)slot * K + l] : 0u;
+  __syncthreads();
+  uint32_t N = 0;
+#pragma unroll
+  for (int l = 0; l < KM; l++) N += tot[l];
+  if (N == 0 || (uint64_t)N >= a.L_len) {
+    if (threadIdx.x == 0) {
+      a.out[slot].t = -1;
+      a.out[slot].f = -1;
+      a.out[slot].j = -1;
+      a.out[slot].gain = 0.0;
+    }
+    return;
+  }
+  const float hp32 = ent32<KM>(tot, K, N);
+  const uint32_t *H = a.hist + (size_t)slot * K * T * F;
+  float *G = a.g32 + (size_t)slot * T * F;
+
+  float lmax = -FLT_MAX;
+  for (uint32_t f = threadIdx.x; f < F; f += blockDim.x) {
+    uint32_t c[KM];
+#pragma unroll
+    for (int l = 0; l < KM; l++) c[l] = 0u;
+    for (uint32_t j = 0; j < T; j++) {
+      uint32_t nL = 0;
+#pragma unroll
+      for (int l = 0; l < KM; l++) {
+        if ((uint32_t)l < K) {
+          const uint32_t h = H[((size_t)l * T + j) * F + f];
+          c[l] = CUM ? h : c[l] + h;
+          nL += c[l];
+        }
+      }
+      const uint32_t nR = N - nL;
+      const float hl = ent32<KM>(c, K, nL);
+      const float hr = ent32_right<KM>(tot, c, K, nR);
+      const float invN = __frcp_rn((float)N);
+      const float g = hp32 - ((float)nL * invN * hl + (float)nR * invN * hr);
+      G[(size_t)j * F + f] = g;
+      lmax = fmaxf(lmax, g);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+  if ((threadIdx.x & 31) == 0) red_f[threadIdx.x >> 5] = lmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = red_f[0];
+    for (int i = 1; i < kSplitThreads / 32; i++) m = fmaxf(m, red_f[i]);
+    s_gmax = m;
+  }
+  __syncthreads();
+  const float cut = s_gmax - a.delta;
+  const double hp64 = ent64<KM, false>(tot, tot, K, N, a.L);
+
+  double best = -DBL_MAX;
+  long long best_idx = LLONG_MAX;  // t*F + f
+  int best_j = -1;
+  unsigned long long n_checked = 0;
+  for (uint32_t f = threadIdx.x; f < F; f += blockDim.x) {
+    int jmax = -1;
+    for (uint32_t j = 0; j < T; j++)
+      if (G[(size_t)j * F + f] >= cut) jmax = (int)j;
+    if (jmax < 0) continue;
+    uint32_t c[KM];
+#pragma unroll
+    for (int l = 0; l < KM; l++) c[l] = 0u;
+    for (int j = 0; j <= jmax; j++) {
+      uint32_t nL = 0;
+#pragma unroll
+      for (int l = 0; l < KM; l++) {
+        if ((uint32_t)l < K) {
+          const uint32_t h = H[((size_t)l * T + j) * F + f];
+          c[l] = CUM ? h : c[l] + h;
+          nL += c[l];
+        }
+      }
+      if (!(G[(size_t)j * F + f] >= cut)) continue;
+      n_checked++;
+      const uint32_t nR = N - nL;
+      const double hl = ent64<KM, false>(tot, c, K, nL, a.L);
+      const double hr = ent64<KM, true>(tot, c, K, nR, a.L);
+      const double wl = ddiv((double)nL, (double)N);
+      const double wr = ddiv((double)nR, (double)N);
+      const double g = dsub(hp64, dadd(dmul(wl, hl), dmul(wr, hr)));
+      const uint32_t t = a.perm ? a.perm[((size_t)slot * T + j) * F + f] : (uint32_t)j;
+      const long long idx = (long long)t * F + f;
+      if (g > best || (g == best && idx < best_idx)) {
+        best = g;
+        best_idx = idx;
+        best_j = j;
+      }
+    }
+  }
+  if (n_checked) atomicAdd(a.rechecked, n_checked);
+  // block arg-max: larger gain, then smaller index
+  for (int o = 16; o > 0; o >>= 1) {
+    const double og = __shfl_xor_sync(0xffffffffu, best, o);
+    const long long oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
+    const int oj = __shfl_xor_sync(0xffffffffu, best_j, o);
+    if (og > best || (og == best && oi < best_idx)) {
+      best = og;
+      best_idx = oi;
+      best_j = oj;
+    }
+  }
+  __shared__ int red_j[kSplitThreads / 32];
+  if ((threadIdx.x & 31) == 0) {
+    red_g[threadIdx.x >> 5] = best;
+    red_i[threadIdx.x >> 5] = best_idx;
+    red_j[threadIdx.x >> 5] = best_j;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < kSplitThreads / 32; i++) {
+      if (red_g[i] > red_g[0] || (red_g[i] == red_g[0] && red_i[i] < red_i[0])) {
+        red_g[0] = red_g[i];
+        red_i[0] = red_i[i];
+        red_j[0] = red_j[i];
+      }
+    }
+    SplitOut o;
+    o.pad = 0;
+    if (red_i[0] == LLONG_MAX) {
+      o.t = -1;
+      o.f = -1;
+      o.j = -1;
+      o.gain = 0.0;
+    } else {
+      o.t = (int32_t)(red_i[0] / F);
+      o.f = (int32_t)(red_i[0] % F);
+      o.j = red_j[0];
+      o.gain = red_g[0];
+      for (uint32_t l = 0; l < K; l++) {
+        uint32_t c = 0;
+        if (CUM) {
+          c = H[((size_t)l * T + o.j) * F + o.f];
+        } else {
+          for (int j = 0; j <= o.j; j++) c += H[((size_t)l * T + j) * F + o.f];
+        }
+        a.out_cl[(size_t)slot * K + l] = c;
+      }
+    }
+    a.out[slot] = o;
+  }
+}
+
+// ------------------------------------------------------------ reassign ----
+// kernels/predict.cl:36-85 as used by the trainer: a sample on a node that has
+// just been split moves to leftChild + (response > threshold).  flags: 1 = goes
+// to a left child that is on the next frontier, 2 = right child on the next
+// frontier, 0 = leaves the active set.
+struct SlotNext {
+  long long adj_l, adj_r;  // next position base (next offset of child - samples of earlier parents)
+  int32_t k_l, k_r;        // next frontier slot of each child or -1
+};
+
+template <class P>
+__global__ void k_reassign(DevSet ds, const uint32_t *__restrict__ act, const uint32_t *__restrict__ act_slot,
+                           uint32_t n_act, int32_t *__restrict__ snode, const int32_t *__restrict__ lc,
+                           const typename P::feat_t *__restrict__ feat,
+                           const typename P::feat_t *__restrict__ thr, const SlotNext *__restrict__ nxt,
+                           uint8_t *__restrict__ flags) {
+  using FeatT = typename P::feat_t;
+  using ImgT = typename P::img_t;
+  constexpr int D = P::kFeatDim;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_act) return;
+  const uint32_t s = act[i];
+  const int32_t n = snode[s];
+  const int32_t c = lc[n];
+  uint8_t flag = 0;
+  if (c >= 0) {
+    const uint32_t xy = ds.s_xy[s], im_i = ds.s_img[s];
+    const uint32_t wh = ds.img_wh[im_i];
+    ImageRef<ImgT> im;
+    im.data = reinterpret_cast<const ImgT *>(ds.pixels + ds.img_off[im_i]);
+    im.w = (int32_t)(wh & 0xffffu);
+    im.h = (int32_t)(wh >> 16);
+    FeatT fv[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) fv[d] = feat[(size_t)n * D + d];
+    const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16));
+    const FeatT r = P::eval(prep, fv);
+    const bool right = r > thr[n];
+    snode[s] = c + (right ? 1 : 0);
+    const SlotNext sn = nxt[act_slot[i]];
+    if (right) flag = sn.k_r >= 0 ? 2 : 0;
+    else flag = sn.k_l >= 0 ? 1 : 0;
+  }
+  flags[i] = flag;
+}
+
+// Per scan block: number of flags equal to 1 (low 32 bits) and 2 (high 32).
+__global__ void __launch_bounds__(256) k_scan_reduce(const uint8_t *__restrict__ flags, uint32_t n,
+                                                     unsigned long long *__restrict__ bsum) {
+  const uint32_t b0 = blockIdx.x * kScanItems;
+  unsigned long long acc = 0;
+  for (uint32_t i = b0 + threadIdx.x; i < min(n, b0 + kScanItems); i += blockDim.x) {
+    const uint8_t fl = flags[i];
+    acc += fl == 1 ? 1ull : (fl == 2 ? (1ull << 32) : 0ull);
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ unsigned long long red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long s = 0;
+    for (int i = 0; i < 8; i++) s += red[i];
+    bsum[blockIdx.x] = s;
+  }
+}
+
+// Exclusive scan of the block sums in one CTA (any count).
+__global__ void __launch_bounds__(1024) k_scan_blocks(unsigned long long *__restrict__ bsum, uint32_t nb,
+                                                      unsigned long long *__restrict__ total) {
+  const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
+  const uint32_t b = threadIdx.x * per, e = min(nb, b + per);
+  unsigned long long s = 0;
+  for (uint32_t i = b; i < e; i++) s += bsum[i];
+  __shared__ unsigned long long sh[1024];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t o = 1; o < blockDim.x; o <<= 1) {
+    const unsigned long long v = threadIdx.x >= o ? sh[threadIdx.x - o] : 0ull;
+    __syncthreads();
+    sh[threadIdx.x] += v;
+    __syncthreads();
+  }
+  unsigned long long run = sh[threadIdx.x] - s;
+  for (uint32_t i = b; i < e; i++) {
+    const unsigned long long v = bsum[i];
+    bsum[i] = run;
+    run += v;
+  }
+  if (threadIdx.x == blockDim.x - 1) *total = sh[threadIdx.x];
+}
+
+// Stable regrouping: sample i of parent slot p goes to
+// adj[p] + (number of earlier samples with the same flag).  Because parents are
+// in slot order and their children in the same order, this keeps every child's
+// samples in their previous (image-major) order.
+__global__ void __launch_bounds__(256) k_scatter(const uint8_t *__restrict__ flags, uint32_t n,
+                                                 const unsigned long long *__restrict__ bsum,
+                                                 const uint32_t *__restrict__ act,
+                                                 const uint32_t *__restrict__ act_slot,
+                                                 const SlotNext *__restrict__ nxt, uint32_t n_next,
+                                                 uint32_t *__restrict__ act_out,
+                                                 uint32_t *__restrict__ slot_out,
+                                                 uint32_t *__restrict__ err) {
+  constexpr int PER = kScanItems / 256;
+  const uint32_t b0 = blockIdx.x * kScanItems + threadIdx.x * PER;
+  uint8_t fl[PER];
+  unsigned long long mine = 0;
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const uint32_t i = b0 + k;
+    fl[k] = i < n ? flags[i] : 0;
+    mine += fl[k] == 1 ? 1ull : (fl[k] == 2 ? (1ull << 32) : 0ull);
+  }
+  // block exclusive scan of per-thread counts
+  __shared__ unsigned long long sh[256];
+  sh[threadIdx.x] = mine;
+  __syncthreads();
+  for (int o = 1; o < 256; o <<= 1) {
+    const unsigned long long v = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0ull;
+    __syncthreads();
+    sh[threadIdx.x] += v;
+    __syncthreads();
+  }
+  unsigned long long run = bsum[blockIdx.x] + sh[threadIdx.x] - mine;
+#pragma unroll
+  for (int k = 0; k < PER; k++) {
+    const uint32_t i = b0 + k;
+    if (fl[k] == 0) continue;
+    const SlotNext sn = nxt[act_slot[i]];
+    long long pos;
+    uint32_t kslot;
+    if (fl[k] == 1) {
+      pos = sn.adj_l + (long long)(run & 0xffffffffull);
+      kslot = (uint32_t)sn.k_l;
+      run += 1ull;
+    } else {
+      pos = sn.adj_r + (long long)(run >> 32);
+      kslot = (uint32_t)sn.k_r;
+      run += 1ull << 32;
+    }
+    if (pos < 0 || pos >= (long long)n_next) {
+      atomicAdd(err, 1u);
+      continue;
+    }
+    act_out[pos] = act[i];
+    slot_out[pos] = kslot;
+  }
+}
+
+__global__ void k_iota(uint32_t *__restrict__ a, uint32_t *__restrict__ slot, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    a[i] = i;
+    slot[i] = 0u;
+  }
+}
+
+__global__ void k_log2_table(double *__restrict__ out, uint64_t n, DD inv_ln2) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = dd_log2_u32((uint32_t)i, inv_ln2);
+}
+
+}  // namespace pd

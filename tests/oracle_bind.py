@@ -1,0 +1,203 @@
+"""ctypes binding of the CPU oracle (oracle/padenti_oracle.c) for the tests.
+
+Test infrastructure: loads oracle/_build/libpadenti_oracle.so, building it with
+``make -C oracle`` if it is missing.  The reference pieces compiled from the
+Padenti sources (oracle/_ref) are optional: ``ref()`` returns None when absent.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+import subprocess
+
+import numpy as np
+
+REPO = pathlib.Path(__file__).resolve().parent.parent
+ORACLE_SO = REPO / "oracle" / "_build" / "libpadenti_oracle.so"
+REF_DIR = REPO / "oracle" / "_ref"
+
+PLUGIN_IDS = {"depth_diff2": 1, "depth_diff1": 2, "channel_diff": 3}
+FEAT_IDS = {np.dtype(np.int16): 1, np.dtype(np.int32): 2}
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("plugin", C.c_int32), ("feat_type", C.c_int32), ("feat_dim", C.c_int32), ("n_classes", C.c_int32),
+        ("n_features", C.c_uint32), ("n_thresholds", C.c_uint32),
+        ("feat_low", C.c_int32 * 8), ("feat_up", C.c_int32 * 8),
+        ("thr_low", C.c_int32), ("thr_up", C.c_int32), ("per_leaf_samples_thr", C.c_uint32),
+    ]
+
+
+class Dataset(C.Structure):
+    _fields_ = [
+        ("n_images", C.c_uint32), ("n_channels", C.c_uint32), ("img_type", C.c_uint32),
+        ("pixels", C.c_void_p), ("pix_off", C.c_void_p), ("width", C.c_void_p), ("height", C.c_void_p),
+        ("labels", C.c_void_p), ("lab_off", C.c_void_p), ("samples", C.c_void_p), ("samp_off", C.c_void_p),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [("evals", C.c_uint64), ("nodes_trained", C.c_uint64), ("nodes_split", C.c_uint64),
+                ("seconds_hist", C.c_double), ("seconds_split", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not ORACLE_SO.exists():
+            subprocess.run(["make", "-C", str(REPO / "oracle"), "all"], check=True, capture_output=True)
+        _lib = C.CDLL(str(ORACLE_SO))
+        _lib.or_feature.restype = C.c_int32
+    return _lib
+
+
+def ref(name: str):
+    p = REF_DIR / f"libref_{name}.so"
+    return C.CDLL(str(p)) if p.exists() else None
+
+
+def P(a):
+    """Pointer argument (ctypes would pass a bare int as a 32-bit C int)."""
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+def params(config, tp) -> Params:
+    """Oracle parameters from a ForestConfig and TreeTrainerParameters."""
+    p = Params()
+    p.plugin = PLUGIN_IDS[config.plugin]
+    p.feat_type = FEAT_IDS[np.dtype(config.feat_dtype)]
+    p.feat_dim = config.feat_dim
+    p.n_classes = config.n_classes
+    p.n_features = tp.n_features
+    p.n_thresholds = tp.n_thresholds
+    for i, v in enumerate(tp.feat_low_bounds):
+        p.feat_low[i] = int(v)
+    for i, v in enumerate(tp.feat_up_bounds):
+        p.feat_up[i] = int(v)
+    p.thr_low = int(tp.thr_low_bound)
+    p.thr_up = int(tp.thr_up_bound)
+    p.per_leaf_samples_thr = int(tp.per_leaf_samples_thr)
+    return p
+
+
+class OracleSet:
+    """Keeps the flattened arrays of a TrainingSet alive for the oracle."""
+
+    def __init__(self, ts, config):
+        self.flat = ts.flat()
+        d = Dataset()
+        d.n_images = len(self.flat["width"])
+        d.n_channels = config.n_channels
+        d.img_type = 1 if np.dtype(config.img_dtype) == np.uint8 else 2
+        for k in ("pixels", "pix_off", "width", "height", "labels", "lab_off", "samples", "samp_off"):
+            setattr(d, k, self.flat[k].ctypes.data)
+        self.c = d
+        self.n_samples = int(self.flat["samp_off"][-1])
+
+
+def md5(words) -> tuple:
+    a = (C.c_uint32 * 4)(*words)
+    b = (C.c_uint32 * 4)()
+    lib().or_md5(a, b)
+    return tuple(b)
+
+
+def candidate(p: Params, tree: int, node: int, f: int):
+    feat = np.zeros(p.feat_dim, np.int32)
+    thr = np.zeros(p.n_thresholds, np.int32)
+    lib().or_candidate(C.byref(p), tree, node, f, P(feat), P(thr))
+    return feat, thr
+
+
+def log2_table(n: int) -> np.ndarray:
+    out = np.zeros(n, np.float64)
+    lib().or_log2_table(n, P(out))
+    return out
+
+
+def hist(p: Params, ds: OracleSet, tree: int, sample_node, nodes, reference_cost=False, threads=0):
+    nodes = np.ascontiguousarray(nodes, np.int32)
+    sample_node = np.ascontiguousarray(sample_node, np.int32)
+    out = np.zeros((len(nodes), p.n_classes, p.n_thresholds, p.n_features), np.uint32)
+    rc = lib().or_hist(C.byref(p), C.byref(ds.c), tree, P(sample_node), P(nodes), len(nodes), P(out),
+                       int(reference_cost), threads)
+    assert rc == 0
+    return out
+
+
+def split(p: Params, hist_, class_tot, table=None):
+    hist_ = np.ascontiguousarray(hist_, np.uint32)
+    class_tot = np.ascontiguousarray(class_tot, np.uint32)
+    n = hist_.shape[0]
+    if table is None:
+        table = log2_table(int(class_tot.sum(axis=1).max()) + 2)
+    t = np.zeros(n, np.int32)
+    f = np.zeros(n, np.int32)
+    g = np.zeros(n, np.float64)
+    g32 = np.zeros(n, np.float32)
+    err = C.c_double(0.0)
+    rc = lib().or_split(C.byref(p), P(hist_), P(class_tot), n, P(table), C.c_uint64(len(table)), P(t), P(f), P(g),
+                        P(g32), C.byref(err))
+    assert rc == 0
+    return t, f, g, g32, err.value
+
+
+def priors(ds: OracleSet, n_classes: int) -> np.ndarray:
+    out = np.zeros(n_classes, np.float32)
+    lib().or_priors(C.byref(ds.c), n_classes, P(out))
+    return out
+
+
+def train_tree(p: Params, ds: OracleSet, tree_id: int, depth: int, root_prior, reference_cost=False, threads=0):
+    n = (1 << depth) - 1
+    lc = np.full(n, -2, np.int32)
+    feats = np.zeros((n, p.feat_dim), np.int32)
+    thrs = np.zeros(n, np.int32)
+    posts = np.zeros((n, p.n_classes), np.float32)
+    leaf = np.zeros(ds.n_samples, np.int32)
+    st = Stats()
+    prior = np.ascontiguousarray(root_prior, np.float32)
+    rc = lib().or_train_tree(C.byref(p), C.byref(ds.c), tree_id, depth, P(prior), P(lc), P(feats), P(thrs),
+                             P(posts), P(leaf), int(reference_cost), threads, C.byref(st))
+    assert rc == 0
+    return dict(left_child=lc, features=feats, thresholds=thrs, posteriors=posts, sample_leaf=leaf,
+                evals=st.evals, nodes_split=st.nodes_split, seconds_hist=st.seconds_hist)
+
+
+def predict_posterior(p: Params, image, mask, trees, n_channels=1, threads=0):
+    """trees: list of (depth, left_child, features, thresholds, posteriors) with int32 features."""
+    H, W = image.shape[:2]
+    img = np.ascontiguousarray(image)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    depth = np.array([t[0] for t in trees], np.uint32)
+    off = np.zeros(len(trees), np.uint64)
+    acc = 0
+    for i, t in enumerate(trees):
+        off[i] = acc
+        acc += (1 << t[0]) - 1
+    lc = np.ascontiguousarray(np.concatenate([t[1] for t in trees]), np.int32)
+    ft = np.ascontiguousarray(np.concatenate([np.asarray(t[2], np.int32).reshape(-1) for t in trees]), np.int32)
+    th = np.ascontiguousarray(np.concatenate([np.asarray(t[3], np.int32) for t in trees]), np.int32)
+    po = np.ascontiguousarray(np.concatenate([np.asarray(t[4], np.float32).reshape(-1) for t in trees]), np.float32)
+    out = np.zeros((p.n_classes, H, W), np.float32)
+    rc = lib().or_predict_posterior(C.byref(p), P(img), W, H, n_channels, P(m), len(trees), P(depth), P(off), P(lc),
+                                    P(ft), P(th), P(po), P(out), threads)
+    assert rc == 0
+    return out
+
+
+def predict_leaf(p: Params, image, mask, depth, lc, feats, thrs, n_channels=1, threads=0):
+    H, W = image.shape[:2]
+    img = np.ascontiguousarray(image)
+    m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
+    out = np.zeros((H, W), np.int32)
+    rc = lib().or_predict_leaf(C.byref(p), P(img), W, H, n_channels, P(m), depth,
+                               P(np.ascontiguousarray(lc, np.int32)),
+                               P(np.ascontiguousarray(np.asarray(feats, np.int32).reshape(-1))),
+                               P(np.ascontiguousarray(np.asarray(thrs, np.int32))), P(out), threads)
+    assert rc == 0
+    return out

@@ -1,0 +1,204 @@
+"""Parity of the sm_103a kernels (through the C ABI) with the CPU oracle.
+
+Integer outputs (candidates, histograms, tree structure, leaf ids) must be
+bit-identical; the split gain is the exact FP64 value (bit-identical); tree
+posteriors and forest posteriors are IEEE float results of the same operation
+sequence and must be bit-identical too (tolerance 0).
+"""
+import numpy as np
+import pytest
+
+import oracle_bind as ob
+import padenti_gb300 as pg
+from cases import depth1_case, depth_case, rgb_case, sample_labels, tree_tuple
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_tree(cfg, ts, tp, tree_id, depth):
+    p = ob.params(cfg, tp)
+    ds = ob.OracleSet(ts, cfg)
+    return ob.train_tree(p, ds, tree_id, depth, ts.priors)
+
+
+def test_log2_table_bit_identical():
+    cfg, ts, tp, _ = depth_case(n_images=2)
+    tr = pg.TreeTrainer(cfg)
+    n = 300_000
+    g = tr.log2_table(n)
+    o = ob.log2_table(n)
+    assert np.array_equal(g.view(np.uint64), o.view(np.uint64))
+
+
+def test_candidates_match_oracle():
+    cfg, ts, tp, _ = depth_case(n_images=2, n_features=100, n_thresholds=50)
+    tr = pg.TreeTrainer(cfg)
+    nodes = np.array([0, 1, 2, 77, 4095, 123456], np.int32)
+    feat, thr = tr.candidates(tp, 7, nodes)
+    p = ob.params(cfg, tp)
+    for i, n in enumerate(nodes):
+        for f in range(tp.n_features):
+            of, ot = ob.candidate(p, 7, int(n), f)
+            assert np.array_equal(feat[i, f], of), (n, f)
+            assert np.array_equal(thr[i, f], ot), (n, f)
+
+
+def test_hist_root_bit_exact():
+    """8000 samples at the root: two sample chunks accumulate into the same rows."""
+    cfg, ts, tp, _ = depth_case(n_images=16)
+    tr = pg.TreeTrainer(cfg)
+    tr.upload(ts)
+    S = ts.n_samples
+    sample_node = np.zeros(S, np.int32)
+    g = tr.hist(tp, 0, sample_node, [0])
+    o = ob.hist(ob.params(cfg, tp), ob.OracleSet(ts, cfg), 0, sample_node, [0])
+    assert g.shape == o.shape
+    assert np.array_equal(g, o)
+    assert g.sum() > 0
+
+
+def test_hist_many_nodes_with_empty_and_ragged():
+    cfg, ts, tp, _ = depth_case(n_images=16, n_features=50, n_thresholds=17)
+    tr = pg.TreeTrainer(cfg)
+    tr.upload(ts)
+    rng = np.random.default_rng(1)
+    S = ts.n_samples
+    # uneven node sizes, one node absent from the samples, some samples on other nodes
+    sample_node = rng.choice([3, 4, 5, 6, 9, 10], size=S, p=[0.6, 0.25, 0.1, 0.03, 0.01, 0.01]).astype(np.int32)
+    nodes = [6, 3, 4, 5, 11]
+    g = tr.hist(tp, 2, sample_node, nodes)
+    o = ob.hist(ob.params(cfg, tp), ob.OracleSet(ts, cfg), 2, sample_node, nodes)
+    assert np.array_equal(g, o)
+    assert g[4].sum() == 0
+
+
+def test_split_matches_oracle_on_oracle_histograms():
+    cfg, ts, tp, _ = depth_case(n_images=16)
+    p = ob.params(cfg, tp)
+    ds = ob.OracleSet(ts, cfg)
+    rng = np.random.default_rng(2)
+    S = ts.n_samples
+    sample_node = rng.choice([3, 4, 5, 6], size=S, p=[0.7, 0.2, 0.09, 0.01]).astype(np.int32)
+    nodes = [3, 4, 5, 6]
+    h = ob.hist(p, ds, 0, sample_node, nodes)
+    labels = sample_labels(ts)
+    ctot = np.zeros((len(nodes), cfg.n_classes), np.uint32)
+    for i, n in enumerate(nodes):
+        ctot[i] = np.bincount(labels[sample_node == n], minlength=cfg.n_classes)
+    ot, of, og, _, err = ob.split(p, h, ctot)
+    tr = pg.TreeTrainer(cfg)
+    gt, gf, gg = tr.split(tp, h, ctot)
+    assert np.array_equal(gt, ot) and np.array_equal(gf, of)
+    assert np.array_equal(gg.view(np.uint64), og.view(np.uint64))
+    assert err < 5e-5
+
+
+def test_split_ties_pick_lowest_index():
+    cfg, ts, tp, _ = depth_case(n_images=1, n_features=8, n_thresholds=4)
+    # every candidate identical -> winner (t=0, f=0); then make (t=2,f=5) and (t=1,f=7) equal best
+    K, T, F = 3, 4, 8
+    ctot = np.array([[10, 10, 10]], np.uint32)
+    h = np.tile(np.array([5, 5, 5], np.uint32)[None, :, None, None], (1, 1, T, F))
+    tr = pg.TreeTrainer(cfg)
+    t, f, g = tr.split(tp, h, ctot)
+    assert (t[0], f[0]) == (0, 0)
+    h2 = h.copy()
+    h2[0, :, 2, 5] = [10, 0, 0]
+    h2[0, :, 1, 7] = [10, 0, 0]
+    t, f, g = tr.split(tp, h2, ctot)
+    assert (t[0], f[0]) == (1, 7)
+    p = ob.params(cfg, tp)
+    ot, of, og, _, _ = ob.split(p, h2, ctot)
+    assert (ot[0], of[0]) == (1, 7) and og[0] == g[0]
+
+
+def _assert_same_tree(g: pg.Tree, o: dict):
+    assert np.array_equal(g.left_child, o["left_child"])
+    assert np.array_equal(np.asarray(g.features, np.int32), o["features"])
+    assert np.array_equal(np.asarray(g.thresholds, np.int32), o["thresholds"])
+    assert np.array_equal(g.posteriors.view(np.uint32), o["posteriors"].view(np.uint32))
+
+
+def test_train_tree_config0_bit_exact():
+    """The full 64-image 160x120 configuration: F=200, T=20, depth 8, min 20 pixels per leaf."""
+    cfg, ts, tp, _ = depth_case(n_images=64, n_features=200, n_thresholds=20)
+    tr = pg.TreeTrainer(cfg)
+    tree = pg.Tree(cfg, 0, 8)
+    tr.train(tree, ts, tp, 1, 8)
+    o = _oracle_tree(cfg, ts, tp, 0, 8)
+    _assert_same_tree(tree, o)
+    assert np.array_equal(tr.sample_nodes(ts.n_samples), o["sample_leaf"])
+    st = tr.stats()
+    assert st["evals"] == o["evals"] and st["nodes_split"] == o["nodes_split"]
+    assert (tree.left_child >= 0).sum() > 20
+
+
+def test_train_tree_sliced_histograms_identical():
+    """A 1 MiB histogram budget forces many slices per depth; the tree must not change."""
+    cfg, ts, tp, _ = depth_case(n_images=16, n_features=96, n_thresholds=20)
+    a = pg.Tree(cfg, 4, 7)
+    b = pg.Tree(cfg, 4, 7)
+    pg.TreeTrainer(cfg).train(a, ts, tp)
+    pg.TreeTrainer(cfg, hist_budget=1 << 20).train(b, ts, tp)
+    assert np.array_equal(a.left_child, b.left_child)
+    assert np.array_equal(a.features, b.features) and np.array_equal(a.thresholds, b.thresholds)
+    _assert_same_tree(a, _oracle_tree(cfg, ts, tp, 4, 7))
+
+
+def test_train_tree_nine_classes_bit_exact():
+    cfg, ts, tp, _ = depth_case(n_images=12, width=320, height=240, n_features=64, n_thresholds=50, parts=1,
+                                samples=1000)
+    tree = pg.Tree(cfg, 1, 9)
+    pg.TreeTrainer(cfg).train(tree, ts, tp)
+    _assert_same_tree(tree, _oracle_tree(cfg, ts, tp, 1, 9))
+
+
+def test_train_tree_reference_plugin_int16():
+    cfg, ts, tp, _ = depth1_case()
+    tree = pg.Tree(cfg, 2, 7)
+    pg.TreeTrainer(cfg).train(tree, ts, tp)
+    _assert_same_tree(tree, _oracle_tree(cfg, ts, tp, 2, 7))
+
+
+def test_train_tree_rgb_channel_diff():
+    cfg, ts, tp, _ = rgb_case()
+    tree = pg.Tree(cfg, 0, 8)
+    pg.TreeTrainer(cfg).train(tree, ts, tp)
+    _assert_same_tree(tree, _oracle_tree(cfg, ts, tp, 0, 8))
+
+
+def test_predict_posterior_and_leaf_bit_exact():
+    cfg, ts, tp, (px, lb, sm) = depth_case(n_images=16, n_features=64)
+    tr = pg.TreeTrainer(cfg)
+    trees = []
+    for t in range(3):
+        tree = pg.Tree(cfg, t, 7)
+        tr.train(tree, ts, tp)
+        trees.append(tree)
+    clf = pg.Classifier(cfg)
+    for tree in trees:
+        clf << tree
+    tpx, tlb, _ = pg.synth_depth(0, 3, 160, 120, first_image=1000)
+    p = ob.params(cfg, tp)
+    for i in range(3):
+        mask = (tpx[i] < 3000).astype(np.uint8) if i == 1 else None
+        g = clf.predict(tpx[i], mask)
+        o = ob.predict_posterior(p, tpx[i], mask, [tree_tuple(t) for t in trees])
+        assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+        if mask is not None:
+            assert np.all(g[:, mask == 0] == 0)
+        for t, tree in enumerate(trees):
+            gl = clf.predict_leaf(t, tpx[i], mask)
+            ol = ob.predict_leaf(p, tpx[i], mask, tree.depth, tree.left_child, tree.features, tree.thresholds)
+            assert np.array_equal(gl, ol)
+
+
+def test_predict_rgb_bit_exact():
+    cfg, ts, tp, (px, lb, sm) = rgb_case()
+    tree = pg.Tree(cfg, 0, 8)
+    pg.TreeTrainer(cfg).train(tree, ts, tp)
+    clf = pg.Classifier(cfg)
+    clf << tree
+    g = clf.predict(px[0])
+    o = ob.predict_posterior(ob.params(cfg, tp), px[0], None, [tree_tuple(tree)], n_channels=3)
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
