@@ -109,8 +109,12 @@ typedef struct {
   uint64_t nodes_split;
   uint64_t hist_launches;
   uint64_t split_rechecked;  /* candidates rechecked in FP64 */
+  uint64_t kernel_launches;  /* kernels this library launched in the call */
+  uint64_t hist_bytes;       /* algorithmic HBM bytes of all histogram launches */
+  uint64_t h2d_bytes;        /* host->device bytes copied by the call */
+  uint64_t d2h_bytes;        /* device->host bytes copied by the call */
   double ms_candidates;
-  double ms_hist;
+  double ms_hist;            /* CUDA-event time of the histogram kernels alone */
   double ms_split;
   double ms_reassign;
   double ms_total;           /* wall time of the call */
@@ -130,6 +134,8 @@ int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
 int pd_ctx_sync(pd_ctx *ctx);
 /* The CUDA stream (cudaStream_t) the context launches on. */
 void *pd_ctx_stream(pd_ctx *ctx);
+/* Bytes copied host->device and device->host by this context since creation. */
+int pd_ctx_transfer_bytes(pd_ctx *ctx, uint64_t *h2d, uint64_t *d2h);
 
 /* TrainingSet upload (replaces the per-image streaming of
  * cl_tree_trainer_impl_traverse_ts.hpp:127-358): the whole set is kept in HBM. */

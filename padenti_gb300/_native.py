@@ -56,6 +56,10 @@ class TrainStats(C.Structure):
         ("nodes_split", C.c_uint64),
         ("hist_launches", C.c_uint64),
         ("split_rechecked", C.c_uint64),
+        ("kernel_launches", C.c_uint64),
+        ("hist_bytes", C.c_uint64),
+        ("h2d_bytes", C.c_uint64),
+        ("d2h_bytes", C.c_uint64),
         ("ms_candidates", C.c_double),
         ("ms_hist", C.c_double),
         ("ms_split", C.c_double),
@@ -74,6 +78,7 @@ _SIGS = {
     "pd_ctx_set_hist_budget": (C.c_int, [_P, C.c_uint64]),
     "pd_ctx_sync": (C.c_int, [_P]),
     "pd_ctx_stream": (_P, [_P]),
+    "pd_ctx_transfer_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "pd_dataset_upload": (C.c_int, [_P, C.POINTER(DatasetDesc)]),
     "pd_dataset_info": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
     "pd_train_tree": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]),

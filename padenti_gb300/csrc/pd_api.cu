@@ -101,6 +101,13 @@ extern "C" int pd_ctx_sync(pd_ctx *ctx) {
 
 extern "C" void *pd_ctx_stream(pd_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
+extern "C" int pd_ctx_transfer_bytes(pd_ctx *ctx, uint64_t *h2d_bytes, uint64_t *d2h_bytes) {
+  PD_CHECK(ctx, PD_ERR_INVALID, "null context");
+  if (h2d_bytes) *h2d_bytes = ctx->bytes_h2d;
+  if (d2h_bytes) *d2h_bytes = ctx->bytes_d2h;
+  return PD_OK;
+}
+
 extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   PD_CHECK(ctx && ds, PD_ERR_INVALID, "null argument");
   PD_CHECK(ds->n_images >= 1, PD_ERR_INVALID, "empty training set");
@@ -146,16 +153,17 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   PD_TRY(ctx->s_xy.ensure(S * 4 + 4));
   PD_TRY(ctx->s_img.ensure(S * 4 + 4));
   PD_TRY(ctx->s_label.ensure(S + 4));
-  PD_CUDA(cudaMemcpyAsync(ctx->pixels.ptr, ds->pixels, bytes, cudaMemcpyHostToDevice, st));
-  PD_CUDA(cudaMemcpyAsync(ctx->img_off.ptr, off.data(), n * 8, cudaMemcpyHostToDevice, st));
-  PD_CUDA(cudaMemcpyAsync(ctx->img_wh.ptr, wh.data(), n * 4, cudaMemcpyHostToDevice, st));
+  PD_CUDA(h2d(ctx, ctx->pixels.ptr, ds->pixels, bytes));
+  PD_CUDA(h2d(ctx, ctx->img_off.ptr, off.data(), n * 8));
+  PD_CUDA(h2d(ctx, ctx->img_wh.ptr, wh.data(), n * 4));
   if (S) {
-    PD_CUDA(cudaMemcpyAsync(ctx->s_xy.ptr, xy.data(), S * 4, cudaMemcpyHostToDevice, st));
-    PD_CUDA(cudaMemcpyAsync(ctx->s_img.ptr, im.data(), S * 4, cudaMemcpyHostToDevice, st));
-    PD_CUDA(cudaMemcpyAsync(ctx->s_label.ptr, lab.data(), S, cudaMemcpyHostToDevice, st));
+    PD_CUDA(h2d(ctx, ctx->s_xy.ptr, xy.data(), S * 4));
+    PD_CUDA(h2d(ctx, ctx->s_img.ptr, im.data(), S * 4));
+    PD_CUDA(h2d(ctx, ctx->s_label.ptr, lab.data(), S));
   }
   PD_CUDA(cudaStreamSynchronize(st));
   ctx->h_label.swap(lab);
+  ctx->pixels_bytes = bytes;
   ctx->n_images = n;
   ctx->n_samples = S;
   ctx->have_dataset = true;

@@ -11,7 +11,7 @@ struct pd_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   uint64_t hist_budget = 8ull << 30;
-  uint32_t chunk = 4096;  // samples per histogram work item
+  uint32_t chunk = 4096;  // samples per histogram work item (at most 65535)
 
   // ---- training set in HBM (cl_tree_trainer_impl_init.hpp:99-154 streams it
   // image by image; here it stays resident) ----
@@ -19,6 +19,7 @@ struct pd_ctx {
   uint32_t n_images = 0;
   uint64_t n_samples = 0;
   pd::DevBuf pixels;    // concatenated images
+  uint64_t pixels_bytes = 0;
   pd::DevBuf img_off;   // uint64 byte offsets
   pd::DevBuf img_wh;    // uint32 w | h << 16
   pd::DevBuf s_xy;      // uint32 x | y << 16 per sample
@@ -53,7 +54,20 @@ struct pd_ctx {
   pd::DevBuf p_img, p_mask, p_out;     // staging for host-buffer prediction
 
   cudaEvent_t ev[8] = {};
+  uint64_t bytes_h2d = 0, bytes_d2h = 0, launches = 0;
 };
+
+namespace pd {
+// Counted copies on the context stream.
+inline cudaError_t h2d(pd_ctx *c, void *dst, const void *src, size_t n) {
+  c->bytes_h2d += n;
+  return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, c->stream);
+}
+inline cudaError_t d2h(pd_ctx *c, void *dst, const void *src, size_t n) {
+  c->bytes_d2h += n;
+  return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, c->stream);
+}
+}  // namespace pd
 
 namespace pd {
 int ensure_log2_table(pd_ctx *ctx, uint64_t n);

@@ -27,9 +27,34 @@ PD_D T ldg(const T *p) {
 #endif
 }
 
+// (int)roundf((float)u / (float)d) -- round half away from zero of the
+// correctly rounded float quotient -- for an integer offset u and a depth
+// 1 <= d <= 65535, given rcp ~= 1/d.
+//
+// For |u| < 2^23 the float quotient lies within 2^-24 |u/d| < 1/(2d) of u/d,
+// and u/d is either a half-integer (then the quotient is exact) or at least
+// 1/(2d) away from every half-integer, so the float rounding never crosses a
+// rounding boundary: the result is the exact rational rounding
+// sign(u) * floor((2|u| + d) / (2d)).  That is computed here with an estimate
+// from rcp and one integer correction step (the estimate is within 1 for
+// |u| <= 2^21); larger |u| take the float path.
+PD_D int32_t round_div(int32_t u, int32_t d, float rcp) {
+  const int32_t a = u < 0 ? -u : u;
+  if (a > (1 << 21)) return (int32_t)roundf(fdiv((float)u, (float)d));
+#if defined(__CUDA_ARCH__)
+  int32_t q = __float2int_rz(__fmaf_rn((float)a, rcp, 0.5f));
+#else
+  int32_t q = (int32_t)((float)a * rcp + 0.5f);
+#endif
+  const int32_t r = 2 * a + d - 2 * d * q;  // (2a + d) - 2d*q, in [-2d, 4d)
+  q += (r >= 2 * d ? 1 : 0) - (r < 0 ? 1 : 0);
+  return u < 0 ? -q : q;
+}
+
 // I(x+u/d(x)) - I(x+v/d(x)); u,v in pixel*mm, d(x) the centre depth in mm.
 // Probes outside the image or on zero depth read 10000; a zero centre depth
-// scales as 10000.  Offsets are round-half-away of an IEEE float quotient.
+// scales as 10000.  Offsets are round-half-away of the IEEE float quotient
+// (round_div, bit-identical to roundf(u/d)).
 struct DepthDiff2 {
   using img_t = uint16_t;
   using feat_t = int32_t;
@@ -38,8 +63,8 @@ struct DepthDiff2 {
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF2;
   struct Prep {
     const uint16_t *im;
-    int32_t w, h, x, y;
-    float d;
+    int32_t w, h, x, y, d;
+    float rcp;
   };
   static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
     Prep p;
@@ -49,19 +74,20 @@ struct DepthDiff2 {
     p.x = x;
     p.y = y;
     const uint16_t c = ldg(im.data + (size_t)y * im.w + x);
-    p.d = (float)(c ? (int32_t)c : kBgDepth);
+    p.d = c ? (int32_t)c : kBgDepth;
+    p.rcp = 1.0f / (float)p.d;
     return p;
   }
   static PD_D int32_t probe(const Prep &p, int32_t x, int32_t y) {
-    if (x < 0 || y < 0 || x >= p.w || y >= p.h) return kBgDepth;
+    if ((uint32_t)x >= (uint32_t)p.w || (uint32_t)y >= (uint32_t)p.h) return kBgDepth;
     const uint16_t v = ldg(p.im + (size_t)y * p.w + x);
     return v ? (int32_t)v : kBgDepth;
   }
   static PD_D int32_t eval(const Prep &p, const int32_t *f) {
-    const int32_t x1 = p.x + (int32_t)roundf(fdiv((float)f[0], p.d));
-    const int32_t y1 = p.y + (int32_t)roundf(fdiv((float)f[1], p.d));
-    const int32_t x2 = p.x + (int32_t)roundf(fdiv((float)f[2], p.d));
-    const int32_t y2 = p.y + (int32_t)roundf(fdiv((float)f[3], p.d));
+    const int32_t x1 = p.x + round_div(f[0], p.d, p.rcp);
+    const int32_t y1 = p.y + round_div(f[1], p.d, p.rcp);
+    const int32_t x2 = p.x + round_div(f[2], p.d, p.rcp);
+    const int32_t y2 = p.y + round_div(f[3], p.d, p.rcp);
     return probe(p, x1, y1) - probe(p, x2, y2);
   }
 };

@@ -118,11 +118,11 @@ static int upload_forest(pd_ctx *ctx) {
   PD_TRY(ctx->f_meta.ensure(nt * sizeof(TreeMeta) + 16));
   cudaStream_t st = ctx->stream;
   if (nodes) {
-    PD_CUDA(cudaMemcpyAsync(ctx->f_lc.ptr, ctx->h_lc.data(), nodes * 4, cudaMemcpyHostToDevice, st));
-    PD_CUDA(cudaMemcpyAsync(ctx->f_feat.ptr, ctx->h_feat.data(), ctx->h_feat.size(), cudaMemcpyHostToDevice, st));
-    PD_CUDA(cudaMemcpyAsync(ctx->f_thr.ptr, ctx->h_thr.data(), ctx->h_thr.size(), cudaMemcpyHostToDevice, st));
-    PD_CUDA(cudaMemcpyAsync(ctx->f_post.ptr, ctx->h_post.data(), ctx->h_post.size() * 4, cudaMemcpyHostToDevice, st));
-    PD_CUDA(cudaMemcpyAsync(ctx->f_meta.ptr, meta.data(), nt * sizeof(TreeMeta), cudaMemcpyHostToDevice, st));
+    PD_CUDA(h2d(ctx, ctx->f_lc.ptr, ctx->h_lc.data(), nodes * 4));
+    PD_CUDA(h2d(ctx, ctx->f_feat.ptr, ctx->h_feat.data(), ctx->h_feat.size()));
+    PD_CUDA(h2d(ctx, ctx->f_thr.ptr, ctx->h_thr.data(), ctx->h_thr.size()));
+    PD_CUDA(h2d(ctx, ctx->f_post.ptr, ctx->h_post.data(), ctx->h_post.size() * 4));
+    PD_CUDA(h2d(ctx, ctx->f_meta.ptr, meta.data(), nt * sizeof(TreeMeta)));
   }
   (void)fs;
   ctx->forest_dirty = false;
@@ -143,6 +143,7 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
       ctx->f_feat.as<FeatT>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(), ctx->f_meta.as<TreeMeta>(), nt,
       (uint32_t)ctx->cfg.n_classes);
   PD_CUDA(cudaGetLastError());
+  ctx->launches++;
   return PD_OK;
 }
 
@@ -217,11 +218,11 @@ extern "C" int pd_predict_posterior(pd_ctx *ctx, const void *image, uint32_t wid
   PD_TRY(ctx->p_out.ensure(ob));
   if (mask) PD_TRY(ctx->p_mask.ensure(P_));
   cudaStream_t st = ctx->stream;
-  PD_CUDA(cudaMemcpyAsync(ctx->p_img.ptr, image, ib, cudaMemcpyHostToDevice, st));
-  if (mask) PD_CUDA(cudaMemcpyAsync(ctx->p_mask.ptr, mask, P_, cudaMemcpyHostToDevice, st));
+  PD_CUDA(h2d(ctx, ctx->p_img.ptr, image, ib));
+  if (mask) PD_CUDA(h2d(ctx, ctx->p_mask.ptr, mask, P_));
   PD_TRY(pd_predict_posterior_device(ctx, 1, ctx->p_img.ptr, width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
                                      ctx->p_out.as<float>()));
-  PD_CUDA(cudaMemcpyAsync(out, ctx->p_out.ptr, ob, cudaMemcpyDeviceToHost, st));
+  PD_CUDA(d2h(ctx, out, ctx->p_out.ptr, ob));
   PD_CUDA(cudaStreamSynchronize(st));
   return PD_OK;
 }
@@ -239,8 +240,8 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
   PD_TRY(ctx->p_out.ensure(P_ * 4));
   if (mask) PD_TRY(ctx->p_mask.ensure(P_));
   cudaStream_t st = ctx->stream;
-  PD_CUDA(cudaMemcpyAsync(ctx->p_img.ptr, image, ib, cudaMemcpyHostToDevice, st));
-  if (mask) PD_CUDA(cudaMemcpyAsync(ctx->p_mask.ptr, mask, P_, cudaMemcpyHostToDevice, st));
+  PD_CUDA(h2d(ctx, ctx->p_img.ptr, image, ib));
+  if (mask) PD_CUDA(h2d(ctx, ctx->p_mask.ptr, mask, P_));
   const size_t off = ctx->tree_off[tree];
   const uint32_t depth = ctx->tree_depth[tree];
   PD_TRY(dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
@@ -253,7 +254,7 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
     PD_CUDA(cudaGetLastError());
     return PD_OK;
   }));
-  PD_CUDA(cudaMemcpyAsync(out, ctx->p_out.ptr, P_ * 4, cudaMemcpyDeviceToHost, st));
+  PD_CUDA(d2h(ctx, out, ctx->p_out.ptr, P_ * 4));
   PD_CUDA(cudaStreamSynchronize(st));
   return PD_OK;
 }

@@ -14,10 +14,16 @@
 
 namespace pd {
 
-static uint32_t search_top(uint32_t T) {
+// Threshold rows padded to the next power of two above T, so the branch-free
+// search needs no bounds test.
+static uint32_t padded_rows(uint32_t T) {
   uint32_t p = 1;
   while (p < T + 1) p <<= 1;
-  return p >> 1;
+  return p;
+}
+
+static size_t hist_smem(const pd_ctx *ctx, uint32_t T) {
+  return (size_t)ctx->cfg.n_classes * T * 32 * 4 + (size_t)padded_rows(T) * kTileF * feat_size(ctx->cfg.feat_type);
 }
 
 static DevSet devset(const pd_ctx *ctx) {
@@ -59,8 +65,7 @@ static int check_params(const pd_ctx *ctx, const pd_train_params *p) {
   PD_CHECK(p->n_features >= 1 && p->n_thresholds >= 1, PD_ERR_INVALID, "n_features and n_thresholds must be >= 1");
   PD_CHECK(p->n_thresholds <= PD_MAX_THRESHOLDS, PD_ERR_UNSUPPORTED, "n_thresholds %u > %d",
            p->n_thresholds, PD_MAX_THRESHOLDS);
-  const size_t smem = (size_t)ctx->cfg.n_classes * p->n_thresholds * kTile * 4 +
-                      (size_t)p->n_thresholds * kTile * feat_size(ctx->cfg.feat_type);
+  const size_t smem = hist_smem(ctx, p->n_thresholds);
   PD_CHECK(smem <= 227 * 1024, PD_ERR_UNSUPPORTED,
            "nClasses*nThresholds too large for one shared-memory histogram tile (%zu bytes)", smem);
   return PD_OK;
@@ -98,6 +103,7 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
       d_nodes, n, tree, p->n_features, p->n_thresholds, P::kFeatDim, bounds(p, P::kFeatDim),
       ctx->cand_feat.as<FeatT>(), ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>());
   PD_CUDA(cudaGetLastError());
+  ctx->launches++;
   return PD_OK;
 }
 
@@ -105,10 +111,12 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
 // and launches the histogram kernel.
 template <class P>
 static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *off, uint32_t n,
-                       const uint32_t *d_act, uint64_t *n_items_out) {
+                       const uint32_t *d_act, uint64_t *n_items_out, cudaEvent_t ev_before = nullptr,
+                       cudaEvent_t ev_after = nullptr) {
   using FeatT = typename P::feat_t;
   const uint32_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
-  const uint32_t tiles = (F + kTile - 1) / kTile;
+  const uint32_t tiles = (F + kTileF - 1) / kTileF;
+  PD_CHECK(ctx->chunk >= 1 && ctx->chunk <= kMaxChunk, PD_ERR_INVALID, "chunk %u outside [1,%u]", ctx->chunk, kMaxChunk);
   std::vector<WorkItem> items;
   std::vector<uint32_t> zero;
   for (uint32_t i = 0; i < n; i++) {
@@ -140,26 +148,43 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   PD_TRY(ctx->zero_slots.ensure(std::max<size_t>(1, zero.size()) * 4));
   const uint64_t per_slot = (uint64_t)K * T * F;
   if (!zero.empty()) {
-    PD_CUDA(cudaMemcpyAsync(ctx->zero_slots.ptr, zero.data(), zero.size() * 4, cudaMemcpyHostToDevice,
-                            ctx->stream));
+    PD_CUDA(h2d(ctx, ctx->zero_slots.ptr, zero.data(), zero.size() * 4));
     k_zero_slots<<<1216, 256, 0, ctx->stream>>>(ctx->hist.as<uint32_t>(), ctx->zero_slots.as<uint32_t>(),
                                                 (uint32_t)zero.size(), per_slot);
     PD_CUDA(cudaGetLastError());
   }
-  if (items.empty()) return PD_OK;
-  PD_CUDA(cudaMemcpyAsync(ctx->items.ptr, items.data(), items.size() * sizeof(WorkItem),
-                          cudaMemcpyHostToDevice, ctx->stream));
-  const size_t smem = (size_t)K * T * kTile * 4 + (size_t)T * kTile * sizeof(FeatT);
+  if (!zero.empty()) ctx->launches++;
+  if (items.empty()) {
+    if (ev_before) PD_CUDA(cudaEventRecord(ev_before, ctx->stream));
+    if (ev_after) PD_CUDA(cudaEventRecord(ev_after, ctx->stream));
+    return PD_OK;
+  }
+  PD_CUDA(h2d(ctx, ctx->items.ptr, items.data(), items.size() * sizeof(WorkItem)));
+  const size_t smem = hist_smem(ctx, T);
   PD_CUDA(cudaFuncSetAttribute(k_hist<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (ev_before) PD_CUDA(cudaEventRecord(ev_before, ctx->stream));
   // The grid is the work list; the hardware scheduler keeps every SM full.
   for (uint64_t b = 0; b < items.size(); b += 0x7fffffffull) {
     const uint64_t cnt = std::min<uint64_t>(items.size() - b, 0x7fffffffull);
     k_hist<P><<<(unsigned)cnt, kHistThreads, smem, ctx->stream>>>(
         devset(ctx), d_act, ctx->items.as<WorkItem>() + b, ctx->cand_feat.as<FeatT>(),
-        ctx->cand_thr.as<FeatT>(), ctx->hist.as<uint32_t>(), F, T, K, search_top(T));
+        ctx->cand_thr.as<FeatT>(), ctx->hist.as<uint32_t>(), F, T, K, padded_rows(T));
     PD_CUDA(cudaGetLastError());
+    ctx->launches++;
   }
+  if (ev_after) PD_CUDA(cudaEventRecord(ev_after, ctx->stream));
   return PD_OK;
+}
+
+// Algorithmic HBM bytes of one histogram launch: the training-set images read
+// once, 9 bytes per active sample (index 4, packed x|y 4,
+// class 1), the candidate table of the slots read once and the K*T*F uint32
+// histogram of each slot written once.
+static uint64_t hist_algorithmic_bytes(const pd_ctx *ctx, const pd_train_params *p, uint64_t n_samples,
+                                       uint32_t n_slots, uint64_t image_bytes) {
+  const uint64_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
+  const uint64_t fs = feat_size(ctx->cfg.feat_type);
+  return image_bytes + 9ull * n_samples + (uint64_t)n_slots * (K * T * F * 4 + T * F * fs + ctx->cfg.feat_dim * F * fs);
 }
 
 template <bool CUM>
@@ -187,6 +212,7 @@ static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const
   else if (K <= 32) k_split<32, CUM><<<n, kSplitThreads, 0, ctx->stream>>>(a);
   else k_split<64, CUM><<<n, kSplitThreads, 0, ctx->stream>>>(a);
   PD_CUDA(cudaGetLastError());
+  ctx->launches++;
   return PD_OK;
 }
 
@@ -210,6 +236,8 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   cudaStream_t st = ctx->stream;
   pd_train_stats stats;
   memset(&stats, 0, sizeof(stats));
+  const uint64_t h2d0 = ctx->bytes_h2d, d2h0 = ctx->bytes_d2h, launches0 = ctx->launches;
+  const uint64_t image_bytes = ctx->pixels_bytes;
 
   PD_TRY(ensure_log2_table(ctx, S + 2));
   PD_TRY(ctx->t_lc.ensure(n_nodes * 4));
@@ -218,10 +246,10 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   PD_TRY(ctx->t_post.ensure(n_nodes * K * 4));
   memcpy(posts, root_prior, sizeof(float) * K);
   // The tree as the caller holds it goes to the device (init:33-50).
-  PD_CUDA(cudaMemcpyAsync(ctx->t_lc.ptr, lc, n_nodes * 4, cudaMemcpyHostToDevice, st));
-  PD_CUDA(cudaMemcpyAsync(ctx->t_feat.ptr, feats, n_nodes * D * sizeof(FeatT), cudaMemcpyHostToDevice, st));
-  PD_CUDA(cudaMemcpyAsync(ctx->t_thr.ptr, thrs, n_nodes * sizeof(FeatT), cudaMemcpyHostToDevice, st));
-  PD_CUDA(cudaMemcpyAsync(ctx->t_post.ptr, posts, n_nodes * K * 4, cudaMemcpyHostToDevice, st));
+  PD_CUDA(h2d(ctx, ctx->t_lc.ptr, lc, n_nodes * 4));
+  PD_CUDA(h2d(ctx, ctx->t_feat.ptr, feats, n_nodes * D * sizeof(FeatT)));
+  PD_CUDA(h2d(ctx, ctx->t_thr.ptr, thrs, n_nodes * sizeof(FeatT)));
+  PD_CUDA(h2d(ctx, ctx->t_post.ptr, posts, n_nodes * K * 4));
 
   PD_TRY(ctx->snode.ensure(S * 4 + 4));
   for (int b = 0; b < 2; b++) {
@@ -232,7 +260,10 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   PD_TRY(ctx->scan_blocks.ensure((S / kScanItems + 2) * 8 + 16));
   PD_TRY(ctx->scatter_err.ensure(16));
   PD_CUDA(cudaMemsetAsync(ctx->snode.ptr, 0, S * 4, st));
-  if (S) k_iota<<<(unsigned)((S + 255) / 256), 256, 0, st>>>(ctx->act[0].as<uint32_t>(), ctx->act_slot[0].as<uint32_t>(), (uint32_t)S);
+  if (S) {
+    k_iota<<<(unsigned)((S + 255) / 256), 256, 0, st>>>(ctx->act[0].as<uint32_t>(), ctx->act_slot[0].as<uint32_t>(), (uint32_t)S);
+    ctx->launches++;
+  }
   PD_CUDA(cudaGetLastError());
 
   std::vector<uint32_t> node_tot(n_nodes, 0u), class_tot(n_nodes * K, 0u);
@@ -267,29 +298,29 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       std::vector<uint32_t> ctot((size_t)ns * K);
       for (uint32_t i = 0; i < ns; i++)
         memcpy(&ctot[(size_t)i * K], &class_tot[(size_t)frontier[s0 + i] * K], K * 4);
-      PD_CUDA(cudaMemcpyAsync(d_nodes.ptr, &frontier[s0], (size_t)ns * 4, cudaMemcpyHostToDevice, st));
-      PD_CUDA(cudaMemcpyAsync(d_ctot.ptr, ctot.data(), (size_t)ns * K * 4, cudaMemcpyHostToDevice, st));
+      PD_CUDA(h2d(ctx, d_nodes.ptr, &frontier[s0], (size_t)ns * 4));
+      PD_CUDA(h2d(ctx, d_ctot.ptr, ctot.data(), (size_t)ns * K * 4));
       PD_CUDA(cudaMemsetAsync(ctx->recheck.ptr, 0, sizeof(unsigned long long), st));
       std::vector<uint64_t> off(cur_off.begin() + s0, cur_off.begin() + s0 + ns + 1);
       PD_CUDA(cudaEventRecord(ev[0], st));
       PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns));
       PD_CUDA(cudaEventRecord(ev[1], st));
       uint64_t n_items = 0;
-      PD_TRY(launch_hist<P>(ctx, p, off.data(), ns, ctx->act[cur].as<uint32_t>(), &n_items));
+      PD_TRY(launch_hist<P>(ctx, p, off.data(), ns, ctx->act[cur].as<uint32_t>(), &n_items, ev[6], ev[2]));
       stats.hist_launches++;
-      PD_CUDA(cudaEventRecord(ev[2], st));
+      stats.hist_bytes += hist_algorithmic_bytes(ctx, p, off.back() - off.front(), ns, image_bytes);
       PD_TRY(launch_split<false>(ctx, p, ns, ctx->hist.as<uint32_t>(), ctx->cand_perm.as<uint8_t>(),
                                  d_ctot.as<uint32_t>()));
       PD_CUDA(cudaEventRecord(ev[3], st));
       h_out.resize(ns);
       h_cl.resize((size_t)ns * K);
       unsigned long long rechecked = 0;
-      PD_CUDA(cudaMemcpyAsync(h_out.data(), ctx->split_out.ptr, ns * sizeof(SplitOut), cudaMemcpyDeviceToHost, st));
-      PD_CUDA(cudaMemcpyAsync(h_cl.data(), ctx->split_cl.ptr, (size_t)ns * K * 4, cudaMemcpyDeviceToHost, st));
-      PD_CUDA(cudaMemcpyAsync(&rechecked, ctx->recheck.ptr, 8, cudaMemcpyDeviceToHost, st));
+      PD_CUDA(d2h(ctx, h_out.data(), ctx->split_out.ptr, ns * sizeof(SplitOut)));
+      PD_CUDA(d2h(ctx, h_cl.data(), ctx->split_cl.ptr, (size_t)ns * K * 4));
+      PD_CUDA(d2h(ctx, &rechecked, ctx->recheck.ptr, 8));
       PD_CUDA(cudaStreamSynchronize(st));
       stats.ms_candidates += elapsed(ev[0], ev[1]);
-      stats.ms_hist += elapsed(ev[1], ev[2]);
+      stats.ms_hist += elapsed(ev[6], ev[2]);
       stats.ms_split += elapsed(ev[2], ev[3]);
       stats.split_rechecked += rechecked;
 
@@ -329,14 +360,12 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
     // device tree update for the frontier nodes and their children
     const uint64_t nmin = (uint64_t)frontier.front(), nmax = (uint64_t)frontier.back();
     const uint64_t cmax = std::min<uint64_t>(n_nodes - 1, 2 * nmax + 2);
-    PD_CUDA(cudaMemcpyAsync(ctx->t_lc.as<int32_t>() + nmin, lc + nmin, (cmax - nmin + 1) * 4, cudaMemcpyHostToDevice, st));
-    PD_CUDA(cudaMemcpyAsync(ctx->t_feat.as<FeatT>() + nmin * D, feats + nmin * D, (nmax - nmin + 1) * D * sizeof(FeatT),
-                            cudaMemcpyHostToDevice, st));
-    PD_CUDA(cudaMemcpyAsync(ctx->t_thr.as<FeatT>() + nmin, thrs + nmin, (nmax - nmin + 1) * sizeof(FeatT),
-                            cudaMemcpyHostToDevice, st));
+    PD_CUDA(h2d(ctx, ctx->t_lc.as<int32_t>() + nmin, lc + nmin, (cmax - nmin + 1) * 4));
+    PD_CUDA(h2d(ctx, ctx->t_feat.as<FeatT>() + nmin * D, feats + nmin * D, (nmax - nmin + 1) * D * sizeof(FeatT)));
+    PD_CUDA(h2d(ctx, ctx->t_thr.as<FeatT>() + nmin, thrs + nmin, (nmax - nmin + 1) * sizeof(FeatT)));
     if (2 * nmin + 1 < n_nodes)
-      PD_CUDA(cudaMemcpyAsync(ctx->t_post.as<float>() + (2 * nmin + 1) * K, posts + (2 * nmin + 1) * K,
-                              (cmax - (2 * nmin + 1) + 1) * K * 4, cudaMemcpyHostToDevice, st));
+      PD_CUDA(h2d(ctx, ctx->t_post.as<float>() + (2 * nmin + 1) * K, posts + (2 * nmin + 1) * K,
+                              (cmax - (2 * nmin + 1) + 1) * K * 4));
 
     // next frontier (init:333-365: leaf children with more than perLeafSamplesThr samples)
     std::vector<int32_t> next;
@@ -366,7 +395,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       }
     }
     PD_TRY(d_next.ensure((size_t)nf * sizeof(SlotNext)));
-    PD_CUDA(cudaMemcpyAsync(d_next.ptr, sn.data(), (size_t)nf * sizeof(SlotNext), cudaMemcpyHostToDevice, st));
+    PD_CUDA(h2d(ctx, d_next.ptr, sn.data(), (size_t)nf * sizeof(SlotNext)));
     PD_CUDA(cudaEventRecord(ev[4], st));
     if (n_act) {
       k_reassign<P><<<(unsigned)((n_act + 255) / 256), 256, 0, st>>>(
@@ -374,6 +403,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
           ctx->snode.as<int32_t>(), ctx->t_lc.as<int32_t>(), ctx->t_feat.as<FeatT>(), ctx->t_thr.as<FeatT>(),
           d_next.as<SlotNext>(), ctx->flags.as<uint8_t>());
       PD_CUDA(cudaGetLastError());
+      ctx->launches++;
     }
     const uint64_t n_next = next_off.back();
     if (!next.empty() && n_act) {
@@ -387,10 +417,11 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
                                     ctx->act[1 - cur].as<uint32_t>(), ctx->act_slot[1 - cur].as<uint32_t>(),
                                     ctx->scatter_err.as<uint32_t>());
       PD_CUDA(cudaGetLastError());
+      ctx->launches += 3;
       unsigned long long total = 0;
       uint32_t err = 0;
-      PD_CUDA(cudaMemcpyAsync(&total, bs + nb, 8, cudaMemcpyDeviceToHost, st));
-      PD_CUDA(cudaMemcpyAsync(&err, ctx->scatter_err.ptr, 4, cudaMemcpyDeviceToHost, st));
+      PD_CUDA(d2h(ctx, &total, bs + nb, 8));
+      PD_CUDA(d2h(ctx, &err, ctx->scatter_err.ptr, 4));
       PD_CUDA(cudaEventRecord(ev[5], st));
       PD_CUDA(cudaStreamSynchronize(st));
       const uint64_t got = (total & 0xffffffffull) + (total >> 32);
@@ -409,6 +440,9 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   }
   PD_CUDA(cudaStreamSynchronize(st));
   stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  stats.h2d_bytes = ctx->bytes_h2d - h2d0;
+  stats.d2h_bytes = ctx->bytes_d2h - d2h0;
+  stats.kernel_launches = ctx->launches - launches0;
   ctx->stats = stats;
   return PD_OK;
 }
@@ -444,7 +478,7 @@ extern "C" int pd_train_sample_nodes(pd_ctx *ctx, int32_t *out) {
   PD_CHECK(ctx && out, PD_ERR_INVALID, "null argument");
   PD_CHECK(ctx->have_dataset && ctx->snode.cap >= ctx->n_samples * 4, PD_ERR_STATE, "no training run");
   PD_CUDA(cudaSetDevice(ctx->device));
-  PD_CUDA(cudaMemcpyAsync(out, ctx->snode.ptr, ctx->n_samples * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  PD_CUDA(d2h(ctx, out, ctx->snode.ptr, ctx->n_samples * 4));
   PD_CUDA(cudaStreamSynchronize(ctx->stream));
   return PD_OK;
 }
@@ -462,13 +496,13 @@ extern "C" int pd_candidates(pd_ctx *ctx, const pd_train_params *params, uint32_
     PD_TRY(ensure_slice(ctx, params, n_nodes));
     DevBuf dn;
     PD_TRY(dn.ensure((size_t)n_nodes * 4));
-    PD_CUDA(cudaMemcpyAsync(dn.ptr, nodes, (size_t)n_nodes * 4, cudaMemcpyHostToDevice, ctx->stream));
+    PD_CUDA(h2d(ctx, dn.ptr, nodes, (size_t)n_nodes * 4));
     PD_TRY(launch_candidates<P>(ctx, params, tree_id, dn.as<int32_t>(), n_nodes));
     std::vector<FeatT> f((size_t)n_nodes * D * F), t((size_t)n_nodes * T * F);
     std::vector<uint8_t> perm((size_t)n_nodes * T * F);
-    PD_CUDA(cudaMemcpyAsync(f.data(), ctx->cand_feat.ptr, f.size() * sizeof(FeatT), cudaMemcpyDeviceToHost, ctx->stream));
-    PD_CUDA(cudaMemcpyAsync(t.data(), ctx->cand_thr.ptr, t.size() * sizeof(FeatT), cudaMemcpyDeviceToHost, ctx->stream));
-    PD_CUDA(cudaMemcpyAsync(perm.data(), ctx->cand_perm.ptr, perm.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    PD_CUDA(d2h(ctx, f.data(), ctx->cand_feat.ptr, f.size() * sizeof(FeatT)));
+    PD_CUDA(d2h(ctx, t.data(), ctx->cand_thr.ptr, t.size() * sizeof(FeatT)));
+    PD_CUDA(d2h(ctx, perm.data(), ctx->cand_perm.ptr, perm.size()));
     PD_CUDA(cudaStreamSynchronize(ctx->stream));
     dn.release();
     FeatT *fo = static_cast<FeatT *>(features_out), *to = static_cast<FeatT *>(thresholds_out);
@@ -516,9 +550,9 @@ extern "C" int pd_hist(pd_ctx *ctx, const pd_train_params *params, uint32_t tree
     PD_TRY(dn.ensure((size_t)n_nodes * 4));
     PD_TRY(da.ensure(act.size() * 4 + 4));
     PD_TRY(dref.ensure((size_t)n_nodes * K * T * F * 4 + 4));
-    PD_CUDA(cudaMemcpyAsync(dn.ptr, nodes, (size_t)n_nodes * 4, cudaMemcpyHostToDevice, ctx->stream));
+    PD_CUDA(h2d(ctx, dn.ptr, nodes, (size_t)n_nodes * 4));
     if (!act.empty())
-      PD_CUDA(cudaMemcpyAsync(da.ptr, act.data(), act.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+      PD_CUDA(h2d(ctx, da.ptr, act.data(), act.size() * 4));
     PD_TRY(launch_candidates<P>(ctx, params, tree_id, dn.as<int32_t>(), n_nodes));
     uint64_t n_items = 0;
     PD_TRY(launch_hist<P>(ctx, params, cnt.data(), n_nodes, da.as<uint32_t>(), &n_items));
@@ -528,7 +562,7 @@ extern "C" int pd_hist(pd_ctx *ctx, const pd_train_params *params, uint32_t tree
           ctx->hist.as<uint32_t>(), ctx->cand_perm.as<uint8_t>(), dref.as<uint32_t>(), n_nodes, K, T, F);
       PD_CUDA(cudaGetLastError());
     }
-    PD_CUDA(cudaMemcpyAsync(hist_out, dref.ptr, (size_t)n_nodes * K * T * F * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    PD_CUDA(d2h(ctx, hist_out, dref.ptr, (size_t)n_nodes * K * T * F * 4));
     PD_CUDA(cudaStreamSynchronize(ctx->stream));
     return PD_OK;
   });
@@ -551,12 +585,12 @@ extern "C" int pd_split(pd_ctx *ctx, const pd_train_params *params, const uint32
   DevBuf dh, dc;
   PD_TRY(dh.ensure((size_t)n_nodes * K * T * F * 4 + 4));
   PD_TRY(dc.ensure((size_t)n_nodes * K * 4 + 4));
-  PD_CUDA(cudaMemcpyAsync(dh.ptr, hist, (size_t)n_nodes * K * T * F * 4, cudaMemcpyHostToDevice, ctx->stream));
-  PD_CUDA(cudaMemcpyAsync(dc.ptr, class_tot, (size_t)n_nodes * K * 4, cudaMemcpyHostToDevice, ctx->stream));
+  PD_CUDA(h2d(ctx, dh.ptr, hist, (size_t)n_nodes * K * T * F * 4));
+  PD_CUDA(h2d(ctx, dc.ptr, class_tot, (size_t)n_nodes * K * 4));
   PD_CUDA(cudaMemsetAsync(ctx->recheck.ptr, 0, 8, ctx->stream));
   PD_TRY(launch_split<true>(ctx, params, n_nodes, dh.as<uint32_t>(), nullptr, dc.as<uint32_t>()));
   std::vector<SplitOut> o(n_nodes);
-  PD_CUDA(cudaMemcpyAsync(o.data(), ctx->split_out.ptr, n_nodes * sizeof(SplitOut), cudaMemcpyDeviceToHost, ctx->stream));
+  PD_CUDA(d2h(ctx, o.data(), ctx->split_out.ptr, n_nodes * sizeof(SplitOut)));
   PD_CUDA(cudaStreamSynchronize(ctx->stream));
   for (uint32_t i = 0; i < n_nodes; i++) {
     out_t[i] = o[i].t;
@@ -570,7 +604,7 @@ extern "C" int pd_log2_table(pd_ctx *ctx, uint32_t n, double *out) {
   PD_CHECK(ctx && out, PD_ERR_INVALID, "null argument");
   PD_CUDA(cudaSetDevice(ctx->device));
   PD_TRY(ensure_log2_table(ctx, n));
-  PD_CUDA(cudaMemcpyAsync(out, ctx->log2_tab.ptr, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  PD_CUDA(d2h(ctx, out, ctx->log2_tab.ptr, (size_t)n * 8));
   PD_CUDA(cudaStreamSynchronize(ctx->stream));
   return PD_OK;
 }

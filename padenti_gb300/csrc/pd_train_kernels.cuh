@@ -11,7 +11,6 @@
 
 namespace pd {
 
-constexpr int kTile = 32;          // candidates per histogram tile (one per lane)
 constexpr int kHistThreads = 256;  // 8 warps, each on its own samples
 constexpr int kSplitThreads = 256;
 constexpr int kScanItems = 4096;   // active samples per scan block (256 threads x 16)
@@ -23,8 +22,8 @@ struct CandBounds {
   int32_t thr_lo, thr_hi;
 };
 
-// One histogram work item: candidates [tile*32, tile*32+32) of frontier slot
-// `slot` over the active samples act[begin, end).  multi=1 when other work
+// One histogram work item: candidates [tile*64, tile*64+64) of frontier slot
+// `slot` over the active samples act[begin, end) (end - begin <= 65535).  multi=1 when other work
 // items add into the same histogram rows.
 struct WorkItem {
   uint32_t slot, tile, begin, end, multi, pad0, pad1, pad2;
@@ -91,42 +90,54 @@ __global__ void __launch_bounds__(128) k_candidates(const int32_t *__restrict__ 
 }
 
 // ------------------------------------------------------------ histogram ----
-// Each CTA owns one (slot, 32-candidate tile, sample chunk).  Lane = candidate,
-// warp = sample stream.  Per evaluation: the plugin response, a branch-free
-// lower_bound over the 32 sorted threshold columns in shared memory, and one
-// conflict-free shared atomic into bin [label][rank][lane] (rank = number of
-// thresholds below the response; rank T counts for no threshold and is
-// dropped).  The tile histogram then goes to global memory in rank space.
+// Each CTA owns one (slot, 64-candidate tile, sample chunk).  Lane l evaluates
+// candidates l and l+32 of the tile; each warp walks its own samples.  Per
+// evaluation: the plugin response, a branch-free lower_bound over the sorted
+// thresholds of the candidate (padded with +max to a power of two, column-major
+// in shared memory so every lane hits its own bank), and one shared atomic into
+// bin [label][rank] of a word that packs the two candidates of the lane as
+// 16-bit counters (rank = number of thresholds below the response; rank T counts
+// for no threshold and is dropped).  A chunk has at most 65535 samples, so a
+// 16-bit counter never carries.  The tile histogram then goes to global memory
+// in rank space as uint32.
+constexpr int kCandPerLane = 2;
+constexpr int kTileF = 32 * kCandPerLane;
+constexpr uint32_t kMaxChunk = 65535;
+
 template <class P>
 __global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t *__restrict__ act,
                                                        const WorkItem *__restrict__ items,
                                                        const typename P::feat_t *__restrict__ cand_feat,
                                                        const typename P::feat_t *__restrict__ cand_thr,
                                                        uint32_t *__restrict__ hist, uint32_t F,
-                                                       uint32_t T, uint32_t K, uint32_t search_top) {
+                                                       uint32_t T, uint32_t K, uint32_t TP) {
   using FeatT = typename P::feat_t;
   using ImgT = typename P::img_t;
   constexpr int D = P::kFeatDim;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);
-  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * kTile);
+  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);             // [K][T][32] packed
+  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32);  // [TP][64]
 
   const WorkItem w = items[blockIdx.x];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t f0 = w.tile * kTile;
-  const uint32_t f = f0 + lane;
-  const bool valid = f < F;
+  const uint32_t f0 = w.tile * kTileF;
+  const uint32_t fa = f0 + lane, fb = f0 + 32 + lane;
+  const bool va = fa < F, vb = fb < F;
 
-  for (uint32_t j = threadIdx.x; j < T * kTile; j += blockDim.x) {
-    const uint32_t ff = f0 + (j & 31);
-    sh_thr[j] = ff < F ? cand_thr[((size_t)w.slot * T + (j >> 5)) * F + ff] : max_of<FeatT>();
+  for (uint32_t j = threadIdx.x; j < TP * kTileF; j += blockDim.x) {
+    const uint32_t t = j / kTileF, ff = f0 + (j % kTileF);
+    sh_thr[j] = (t < T && ff < F) ? cand_thr[((size_t)w.slot * T + t) * F + ff] : max_of<FeatT>();
   }
-  for (uint32_t j = threadIdx.x; j < K * T * kTile; j += blockDim.x) sh_hist[j] = 0u;
-  FeatT fv[D];
+  for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) sh_hist[j] = 0u;
+  FeatT fva[D], fvb[D];
 #pragma unroll
-  for (int d = 0; d < D; d++) fv[d] = valid ? cand_feat[((size_t)w.slot * D + d) * F + f] : (FeatT)0;
+  for (int d = 0; d < D; d++) {
+    fva[d] = va ? cand_feat[((size_t)w.slot * D + d) * F + fa] : (FeatT)0;
+    fvb[d] = vb ? cand_feat[((size_t)w.slot * D + d) * F + fb] : (FeatT)0;
+  }
   __syncthreads();
 
+  const FeatT *ta = sh_thr + lane, *tb = sh_thr + 32 + lane;
   const unsigned full = 0xffffffffu;
   for (uint32_t base = w.begin + warp * 32; base < w.end; base += kHistThreads) {
     const uint32_t n_here = min(32u, w.end - base);
@@ -150,25 +161,36 @@ __global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t
       im.w = (int32_t)(wh & 0xffffu);
       im.h = (int32_t)(wh >> 16);
       const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16));
-      const FeatT r = P::eval(prep, fv);
-      uint32_t pos = 0;
-      for (uint32_t step = search_top; step > 0; step >>= 1) {
-        const uint32_t q = pos + step;
-        if (q <= T && sh_thr[(q - 1) * kTile + lane] < r) pos = q;
+      const FeatT ra = P::eval(prep, fva);
+      const FeatT rb = P::eval(prep, fvb);
+      uint32_t pa = 0, pb = 0;
+      for (uint32_t step = TP >> 1; step > 0; step >>= 1) {
+        pa += ta[(pa + step - 1) * kTileF] < ra ? step : 0u;
+        pb += tb[(pb + step - 1) * kTileF] < rb ? step : 0u;
       }
-      if (valid && pos < T) atomicAdd(&sh_hist[(lab * T + pos) * kTile + lane], 1u);
+      uint32_t *row = sh_hist + (size_t)lab * T * 32 + lane;
+      if (va && pa < T) atomicAdd(row + pa * 32, 1u);
+      if (vb && pb < T) atomicAdd(row + pb * 32, 0x10000u);
     }
   }
   __syncthreads();
-  for (uint32_t j = threadIdx.x; j < K * T * kTile; j += blockDim.x) {
-    const uint32_t ff = f0 + (j & 31);
-    if (ff >= F) continue;
+  for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) {
     const uint32_t v = sh_hist[j];
-    uint32_t *dst = hist + ((size_t)w.slot * K * T + (j >> 5)) * F + ff;
-    if (w.multi) {
-      if (v) atomicAdd(dst, v);
-    } else {
-      *dst = v;
+    const uint32_t l = j & 31;
+    uint32_t *dst = hist + ((size_t)w.slot * K * T + (j >> 5)) * F + f0 + l;
+    if (f0 + l < F) {
+      if (w.multi) {
+        if (v & 0xffffu) atomicAdd(dst, v & 0xffffu);
+      } else {
+        *dst = v & 0xffffu;
+      }
+    }
+    if (f0 + 32 + l < F) {
+      if (w.multi) {
+        if (v >> 16) atomicAdd(dst + 32, v >> 16);
+      } else {
+        dst[32] = v >> 16;
+      }
     }
   }
 }
