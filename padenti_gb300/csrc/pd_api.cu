@@ -63,6 +63,11 @@ extern "C" int pd_ctx_create(const pd_config *cfg, int device, pd_ctx **out) {
     return set_error(PD_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
   }
   for (auto &ev : c->ev) cudaEventCreate(&ev);
+  const int rc = init_tables(c);
+  if (rc != PD_OK) {
+    pd_ctx_destroy(c);
+    return rc;
+  }
   *out = c;
   return PD_OK;
 }
@@ -72,7 +77,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   DevBuf *bufs[] = {&ctx->pixels, &ctx->img_off, &ctx->img_wh, &ctx->s_xy, &ctx->s_img, &ctx->s_label,
-                    &ctx->log2_tab, &ctx->snode, &ctx->act[0], &ctx->act[1], &ctx->act_slot[0],
+                    &ctx->log2_tab, &ctx->magic_tab, &ctx->snode, &ctx->act[0], &ctx->act[1], &ctx->act_slot[0],
                     &ctx->act_slot[1], &ctx->flags, &ctx->scan_blocks, &ctx->slot_adj, &ctx->scatter_err,
                     &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->hist, &ctx->g32, &ctx->items,
                     &ctx->zero_slots, &ctx->split_out, &ctx->split_cl, &ctx->recheck, &ctx->t_lc,

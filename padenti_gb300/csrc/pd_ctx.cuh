@@ -27,6 +27,7 @@ struct pd_ctx {
   pd::DevBuf s_label;   // uint8 class (0..K-1) per sample
   std::vector<uint8_t> h_label;  // host copy of the sample classes
   pd::DevBuf log2_tab;  // double log2(n), n < log2_len
+  pd::DevBuf magic_tab; // uint32 RoundDiv multiplier by depth value (65536)
   uint64_t log2_len = 0;
 
   // ---- training scratch ----
@@ -71,4 +72,5 @@ inline cudaError_t d2h(pd_ctx *c, void *dst, const void *src, size_t n) {
 
 namespace pd {
 int ensure_log2_table(pd_ctx *ctx, uint64_t n);
+int init_tables(pd_ctx *ctx);
 }

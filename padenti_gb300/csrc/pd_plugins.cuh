@@ -14,8 +14,9 @@ constexpr int32_t kBgDepth = 10000;  // out-of-image / zero-depth reading
 
 template <typename ImgT>
 struct ImageRef {
-  const ImgT *data;  // interleaved [H][W][C]
+  const ImgT *data;        // interleaved [H][W][C]
   int32_t w, h;
+  const uint32_t *magic;   // RoundDiv multipliers by depth (65536 entries)
 };
 
 template <typename T>
@@ -27,34 +28,70 @@ PD_D T ldg(const T *p) {
 #endif
 }
 
-// (int)roundf((float)u / (float)d) -- round half away from zero of the
-// correctly rounded float quotient -- for an integer offset u and a depth
-// 1 <= d <= 65535, given rcp ~= 1/d.
+// Exact rounded quotients round_half_away(u / d) for integers u and d > 0.
 //
-// For |u| < 2^23 the float quotient lies within 2^-24 |u/d| < 1/(2d) of u/d,
-// and u/d is either a half-integer (then the quotient is exact) or at least
-// 1/(2d) away from every half-integer, so the float rounding never crosses a
-// rounding boundary: the result is the exact rational rounding
-// sign(u) * floor((2|u| + d) / (2d)).  That is computed here with an estimate
-// from rcp and one integer correction step (the estimate is within 1 for
-// |u| <= 2^21); larger |u| take the float path.
-PD_D int32_t round_div(int32_t u, int32_t d, float rcp) {
-  const int32_t a = u < 0 ? -u : u;
-  if (a > (1 << 21)) return (int32_t)roundf(fdiv((float)u, (float)d));
-#if defined(__CUDA_ARCH__)
-  int32_t q = __float2int_rz(__fmaf_rn((float)a, rcp, 0.5f));
-#else
-  int32_t q = (int32_t)((float)a * rcp + 0.5f);
-#endif
-  const int32_t r = 2 * a + d - 2 * d * q;  // (2a + d) - 2d*q, in [-2d, 4d)
-  q += (r >= 2 * d ? 1 : 0) - (r < 0 ? 1 : 0);
-  return u < 0 ? -q : q;
-}
+// The plugins compute an offset as (int)roundf((float)u / (float)d), the round
+// half away from zero of the correctly rounded float quotient.  For |u| < 2^23
+// that quotient lies within 2^-24 |u/d| < 1/(2d) of u/d, and u/d is either a
+// half-integer (then the quotient is exact) or at least 1/(2d) away from every
+// half-integer, so the float rounding never crosses a rounding boundary and the
+// result is the exact rational rounding
+//     sign(u) * floor((2|u| + d) / (2d)).
+// The floor is a division by the per-pixel invariant M = 2d, done as a
+// multiply-high by a magic number (Granlund & Montgomery, "Division by
+// invariant integers using multiplication", 1994): with s = floor(log2 M) and
+// m = floor(2^(31+s) / M) + 1 < 2^32, m*M - 2^(31+s) lies in (0, M] and M <=
+// 2^(8+s), so floor(N*m / 2^(31+s)) = floor(N/M) for every N < 2^23.  Offsets
+// with |u| > 2^21 (so that N >= 2^23 is possible) take the float path.
+struct RoundDiv {
+  uint32_t m, sh;  // multiplier and shift for M = 2d
+  int32_t d;
+  static PD_HD uint32_t multiplier(uint32_t d) {
+    const uint32_t M = 2u * d;
+    uint32_t s = 31;
+    while (!((M >> s) & 1u)) s--;
+    return (uint32_t)((1ull << (31 + s)) / M + 1ull);
+  }
+  // d in [1, 65535]; magic[d] = multiplier(d)
+  static PD_D RoundDiv make(int32_t d, const uint32_t *magic) {
+    RoundDiv r;
+    r.d = d;
+    r.m = ldg(magic + d);
+    r.sh = 31u - (uint32_t)__clz(d);  // floor(log2 2d) - 1 = floor(log2 d)
+    return r;
+  }
+  // n2 = 2|u| (|u| <= 2^21): floor((2|u| + d) / (2d))
+  PD_D uint32_t q(uint32_t n2) const { return __umulhi(n2 + (uint32_t)d, m) >> sh; }
+};
+
+// Per-candidate constants of an offset: 2|u| and the sign, or the raw u when
+// |u| > 2^21 (float path).
+struct OffsetConst {
+  uint32_t n2;  // 2|u|, or (uint32_t)u on the float path
+  int32_t sg;   // +1 / -1, or 0 on the float path
+  static PD_D OffsetConst make(int32_t u) {
+    OffsetConst o;
+    const int64_t a = u < 0 ? -(int64_t)u : (int64_t)u;
+    if (a > (1 << 21)) {
+      o.n2 = (uint32_t)u;
+      o.sg = 0;
+    } else {
+      o.n2 = (uint32_t)(2 * a);
+      o.sg = u < 0 ? -1 : 1;
+    }
+    return o;
+  }
+  // round_half_away(u / d), identical to (int)roundf((float)u / (float)d)
+  PD_D int32_t apply(const RoundDiv &r) const {
+    if (sg == 0) return (int32_t)roundf(fdiv((float)(int32_t)n2, (float)r.d));
+    return (int32_t)r.q(n2) * sg;
+  }
+};
 
 // I(x+u/d(x)) - I(x+v/d(x)); u,v in pixel*mm, d(x) the centre depth in mm.
 // Probes outside the image or on zero depth read 10000; a zero centre depth
-// scales as 10000.  Offsets are round-half-away of the IEEE float quotient
-// (round_div, bit-identical to roundf(u/d)).
+// scales as 10000.  Offsets are (int)roundf((float)u / (float)d), computed
+// exactly by OffsetConst::apply.
 struct DepthDiff2 {
   using img_t = uint16_t;
   using feat_t = int32_t;
@@ -63,8 +100,11 @@ struct DepthDiff2 {
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF2;
   struct Prep {
     const uint16_t *im;
-    int32_t w, h, x, y, d;
-    float rcp;
+    int32_t w, h, x, y;
+    RoundDiv div;
+  };
+  struct Cand {
+    OffsetConst o[4];
   };
   static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
     Prep p;
@@ -74,27 +114,35 @@ struct DepthDiff2 {
     p.x = x;
     p.y = y;
     const uint16_t c = ldg(im.data + (size_t)y * im.w + x);
-    p.d = c ? (int32_t)c : kBgDepth;
-    p.rcp = 1.0f / (float)p.d;
+    p.div = RoundDiv::make(c ? (int32_t)c : kBgDepth, im.magic);
     return p;
+  }
+  static PD_D Cand candidate(const int32_t *f) {
+    Cand c;
+#pragma unroll
+    for (int k = 0; k < 4; k++) c.o[k] = OffsetConst::make(f[k]);
+    return c;
   }
   static PD_D int32_t probe(const Prep &p, int32_t x, int32_t y) {
     if ((uint32_t)x >= (uint32_t)p.w || (uint32_t)y >= (uint32_t)p.h) return kBgDepth;
     const uint16_t v = ldg(p.im + (size_t)y * p.w + x);
     return v ? (int32_t)v : kBgDepth;
   }
-  static PD_D int32_t eval(const Prep &p, const int32_t *f) {
-    const int32_t x1 = p.x + round_div(f[0], p.d, p.rcp);
-    const int32_t y1 = p.y + round_div(f[1], p.d, p.rcp);
-    const int32_t x2 = p.x + round_div(f[2], p.d, p.rcp);
-    const int32_t y2 = p.y + round_div(f[3], p.d, p.rcp);
+  static PD_D int32_t eval(const Prep &p, const Cand &c) {
+    const int32_t x1 = p.x + c.o[0].apply(p.div);
+    const int32_t y1 = p.y + c.o[1].apply(p.div);
+    const int32_t x2 = p.x + c.o[2].apply(p.div);
+    const int32_t y2 = p.y + c.o[3].apply(p.div);
     return probe(p, x1, y1) - probe(p, x2, y2);
   }
+  static PD_D int32_t eval(const Prep &p, const int32_t *f) { return eval(p, candidate(f)); }
 };
 
 // The reference example plugin test/feature.cl:29-64 with feat_t = short:
 // D(x) - D(x + round(u*500/D(x))), out-of-image or zero probe = 10000.  A zero
 // centre depth (a division by zero in the reference) reads the probe as 10000.
+// (float)u*500 is exact for short u, so the offset is the exact rounded
+// quotient of 500u by D(x) (OffsetConst::apply) for a positive depth.
 struct DepthDiff1 {
   using img_t = uint16_t;
   using feat_t = int16_t;
@@ -105,6 +153,11 @@ struct DepthDiff1 {
     const uint16_t *im;
     int32_t w, h, x, y;
     int16_t depth;
+    RoundDiv div;
+  };
+  struct Cand {
+    OffsetConst o[2];
+    int16_t f[2];
   };
   static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
     Prep p;
@@ -114,20 +167,36 @@ struct DepthDiff1 {
     p.x = x;
     p.y = y;
     p.depth = (int16_t)ldg(im.data + (size_t)y * im.w + x);
+    p.div = RoundDiv::make(p.depth > 0 ? (int32_t)p.depth : 1, im.magic);
     return p;
   }
-  static PD_D int16_t eval(const Prep &p, const int16_t *f) {
+  static PD_D Cand candidate(const int16_t *f) {
+    Cand c;
+    c.o[0] = OffsetConst::make(500 * (int32_t)f[0]);
+    c.o[1] = OffsetConst::make(500 * (int32_t)f[1]);
+    c.f[0] = f[0];
+    c.f[1] = f[1];
+    return c;
+  }
+  static PD_D int16_t eval(const Prep &p, const Cand &c) {
     int32_t probe = kBgDepth;
     if (p.depth != 0) {
-      const float dd = (float)p.depth;
-      const int32_t ox = p.x + (int32_t)roundf(fdiv(fmul((float)f[0], 500.0f), dd));
-      const int32_t oy = p.y + (int32_t)roundf(fdiv(fmul((float)f[1], 500.0f), dd));
-      const bool out = ox < 0 || oy < 0 || ox >= p.w || oy >= p.h;
+      int32_t ox, oy;
+      if (p.depth > 0) {
+        ox = p.x + c.o[0].apply(p.div);
+        oy = p.y + c.o[1].apply(p.div);
+      } else {
+        const float dd = (float)p.depth;
+        ox = p.x + (int32_t)roundf(fdiv(fmul((float)c.f[0], 500.0f), dd));
+        oy = p.y + (int32_t)roundf(fdiv(fmul((float)c.f[1], 500.0f), dd));
+      }
+      const bool out = (uint32_t)ox >= (uint32_t)p.w || (uint32_t)oy >= (uint32_t)p.h;
       const int16_t v = out ? (int16_t)kBgDepth : (int16_t)ldg(p.im + (size_t)oy * p.w + ox);
       probe = v ? v : kBgDepth;
     }
     return (int16_t)((int32_t)p.depth - probe);
   }
+  static PD_D int16_t eval(const Prep &p, const int16_t *f) { return eval(p, candidate(f)); }
 };
 
 // I_c1(x+u) - I_c2(x+v) on an RGB uint8 image; channels clamped to [0,2]
@@ -142,6 +211,9 @@ struct ChannelDiff {
     const uint8_t *im;
     int32_t w, h, x, y;
   };
+  struct Cand {
+    int32_t c1, c2, ux, uy, vx, vy;
+  };
   static PD_D Prep prepare(const ImageRef<uint8_t> &im, int32_t x, int32_t y) {
     Prep p;
     p.im = im.data;
@@ -151,15 +223,24 @@ struct ChannelDiff {
     p.y = y;
     return p;
   }
+  static PD_D Cand candidate(const int32_t *f) {
+    Cand c;
+    c.c1 = f[0] < 0 ? 0 : (f[0] > 2 ? 2 : f[0]);
+    c.c2 = f[1] < 0 ? 0 : (f[1] > 2 ? 2 : f[1]);
+    c.ux = f[2];
+    c.uy = f[3];
+    c.vx = f[4];
+    c.vy = f[5];
+    return c;
+  }
   static PD_D int32_t read(const Prep &p, int32_t x, int32_t y, int32_t c) {
-    if (x < 0 || y < 0 || x >= p.w || y >= p.h) return 0;
+    if ((uint32_t)x >= (uint32_t)p.w || (uint32_t)y >= (uint32_t)p.h) return 0;
     return ldg(p.im + ((size_t)y * p.w + x) * 3 + c);
   }
-  static PD_D int32_t eval(const Prep &p, const int32_t *f) {
-    const int32_t c1 = f[0] < 0 ? 0 : (f[0] > 2 ? 2 : f[0]);
-    const int32_t c2 = f[1] < 0 ? 0 : (f[1] > 2 ? 2 : f[1]);
-    return read(p, p.x + f[2], p.y + f[3], c1) - read(p, p.x + f[4], p.y + f[5], c2);
+  static PD_D int32_t eval(const Prep &p, const Cand &c) {
+    return read(p, p.x + c.ux, p.y + c.uy, c.c1) - read(p, p.x + c.vx, p.y + c.vy, c.c2);
   }
+  static PD_D int32_t eval(const Prep &p, const int32_t *f) { return eval(p, candidate(f)); }
 };
 
 // Calls fn.template operator()<Plugin>() for the plugin id; returns

@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
     const uint8_t *__restrict__ images, uint64_t img_bytes, uint32_t W, uint32_t H,
     const uint8_t *__restrict__ masks, float *__restrict__ out, const int32_t *__restrict__ lc,
     const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
-    const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K) {
+    const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
+    const uint32_t *__restrict__ magic) {
   using ImgT = typename P::img_t;
   constexpr int D = P::kFeatDim;
   extern __shared__ int32_t leaf_s[];
@@ -63,6 +64,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
   im.data = reinterpret_cast<const ImgT *>(images + (size_t)z * img_bytes);
   im.w = (int32_t)W;
   im.h = (int32_t)H;
+  im.magic = magic;
   const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
   for (uint32_t t = 0; t < n_trees; t++) {
     const size_t off = meta[t].off;
@@ -84,7 +86,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__
                                                                const int32_t *__restrict__ lc,
                                                                const typename P::feat_t *__restrict__ feat,
                                                                const typename P::feat_t *__restrict__ thr,
-                                                               uint32_t depth) {
+                                                               uint32_t depth, const uint32_t *__restrict__ magic) {
   using ImgT = typename P::img_t;
   const uint32_t x = blockIdx.x * kPredX + threadIdx.x, y = blockIdx.y * kPredY + threadIdx.y;
   if (x >= W || y >= H) return;
@@ -97,6 +99,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__
   im.data = reinterpret_cast<const ImgT *>(image);
   im.w = (int32_t)W;
   im.h = (int32_t)H;
+  im.magic = magic;
   out[pix] = walk<P>(P::prepare(im, (int32_t)x, (int32_t)y), lc, feat, thr, depth);
 }
 
@@ -141,7 +144,7 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
   k_predict_posterior<P><<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
       static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_lc.as<int32_t>(),
       ctx->f_feat.as<FeatT>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(), ctx->f_meta.as<TreeMeta>(), nt,
-      (uint32_t)ctx->cfg.n_classes);
+      (uint32_t)ctx->cfg.n_classes, ctx->magic_tab.as<uint32_t>());
   PD_CUDA(cudaGetLastError());
   ctx->launches++;
   return PD_OK;
@@ -250,7 +253,7 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
     k_predict_leaf<P><<<grid, dim3(kPredX, kPredY), 0, st>>>(
         ctx->p_img.as<uint8_t>(), width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
         ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_feat.as<FeatT>() + off * P::kFeatDim,
-        ctx->f_thr.as<FeatT>() + off, depth);
+        ctx->f_thr.as<FeatT>() + off, depth, ctx->magic_tab.as<uint32_t>());
     PD_CUDA(cudaGetLastError());
     return PD_OK;
   }));

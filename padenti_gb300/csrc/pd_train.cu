@@ -28,6 +28,7 @@ static size_t hist_smem(const pd_ctx *ctx, uint32_t T) {
 
 static DevSet devset(const pd_ctx *ctx) {
   DevSet d;
+  d.magic = ctx->magic_tab.as<uint32_t>();
   d.pixels = ctx->pixels.as<uint8_t>();
   d.img_off = ctx->img_off.as<uint64_t>();
   d.img_wh = ctx->img_wh.as<uint32_t>();
@@ -45,6 +46,13 @@ int ensure_log2_table(pd_ctx *ctx, uint64_t n) {
   k_log2_table<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(ctx->log2_tab.as<double>(), n, inv);
   PD_CUDA(cudaGetLastError());
   ctx->log2_len = n;
+  return PD_OK;
+}
+
+int init_tables(pd_ctx *ctx) {
+  PD_TRY(ctx->magic_tab.ensure(65536 * 4));
+  k_magic_table<<<256, 256, 0, ctx->stream>>>(ctx->magic_tab.as<uint32_t>());
+  PD_CUDA(cudaGetLastError());
   return PD_OK;
 }
 
@@ -161,16 +169,31 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   }
   PD_CUDA(h2d(ctx, ctx->items.ptr, items.data(), items.size() * sizeof(WorkItem)));
   const size_t smem = hist_smem(ctx, T);
-  PD_CUDA(cudaFuncSetAttribute(k_hist<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (ev_before) PD_CUDA(cudaEventRecord(ev_before, ctx->stream));
-  // The grid is the work list; the hardware scheduler keeps every SM full.
-  for (uint64_t b = 0; b < items.size(); b += 0x7fffffffull) {
-    const uint64_t cnt = std::min<uint64_t>(items.size() - b, 0x7fffffffull);
-    k_hist<P><<<(unsigned)cnt, kHistThreads, smem, ctx->stream>>>(
-        devset(ctx), d_act, ctx->items.as<WorkItem>() + b, ctx->cand_feat.as<FeatT>(),
-        ctx->cand_thr.as<FeatT>(), ctx->hist.as<uint32_t>(), F, T, K, padded_rows(T));
-    PD_CUDA(cudaGetLastError());
-    ctx->launches++;
+  auto run = [&]<uint32_t TP>() -> int {
+    PD_CUDA(cudaFuncSetAttribute(k_hist<P, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (ev_before) PD_CUDA(cudaEventRecord(ev_before, ctx->stream));
+    // The grid is the work list; the hardware scheduler keeps every SM full.
+    for (uint64_t b = 0; b < items.size(); b += 0x7fffffffull) {
+      const uint64_t cnt = std::min<uint64_t>(items.size() - b, 0x7fffffffull);
+      k_hist<P, TP><<<(unsigned)cnt, kHistThreads, smem, ctx->stream>>>(
+          devset(ctx), d_act, ctx->items.as<WorkItem>() + b, ctx->cand_feat.as<FeatT>(),
+          ctx->cand_thr.as<FeatT>(), ctx->hist.as<uint32_t>(), F, T, K);
+      PD_CUDA(cudaGetLastError());
+      ctx->launches++;
+    }
+    return PD_OK;
+  };
+  switch (padded_rows(T)) {
+    case 2: PD_TRY(run.template operator()<2>()); break;
+    case 4: PD_TRY(run.template operator()<4>()); break;
+    case 8: PD_TRY(run.template operator()<8>()); break;
+    case 16: PD_TRY(run.template operator()<16>()); break;
+    case 32: PD_TRY(run.template operator()<32>()); break;
+    case 64: PD_TRY(run.template operator()<64>()); break;
+    case 128: PD_TRY(run.template operator()<128>()); break;
+    case 256: PD_TRY(run.template operator()<256>()); break;
+    case 512: PD_TRY(run.template operator()<512>()); break;
+    default: return set_error(PD_ERR_UNSUPPORTED, "n_thresholds %u", T);
   }
   if (ev_after) PD_CUDA(cudaEventRecord(ev_after, ctx->stream));
   return PD_OK;

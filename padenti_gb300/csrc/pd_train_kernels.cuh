@@ -30,6 +30,7 @@ struct WorkItem {
 };
 
 struct DevSet {
+  const uint32_t *magic;
   const uint8_t *pixels;
   const uint64_t *img_off;
   const uint32_t *img_wh;
@@ -104,13 +105,13 @@ constexpr int kCandPerLane = 2;
 constexpr int kTileF = 32 * kCandPerLane;
 constexpr uint32_t kMaxChunk = 65535;
 
-template <class P>
+template <class P, uint32_t TP>
 __global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t *__restrict__ act,
                                                        const WorkItem *__restrict__ items,
                                                        const typename P::feat_t *__restrict__ cand_feat,
                                                        const typename P::feat_t *__restrict__ cand_thr,
                                                        uint32_t *__restrict__ hist, uint32_t F,
-                                                       uint32_t T, uint32_t K, uint32_t TP) {
+                                                       uint32_t T, uint32_t K) {
   using FeatT = typename P::feat_t;
   using ImgT = typename P::img_t;
   constexpr int D = P::kFeatDim;
@@ -129,11 +130,16 @@ __global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t
     sh_thr[j] = (t < T && ff < F) ? cand_thr[((size_t)w.slot * T + t) * F + ff] : max_of<FeatT>();
   }
   for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) sh_hist[j] = 0u;
-  FeatT fva[D], fvb[D];
+  typename P::Cand ca, cb;
+  {
+    FeatT fva[D], fvb[D];
 #pragma unroll
-  for (int d = 0; d < D; d++) {
-    fva[d] = va ? cand_feat[((size_t)w.slot * D + d) * F + fa] : (FeatT)0;
-    fvb[d] = vb ? cand_feat[((size_t)w.slot * D + d) * F + fb] : (FeatT)0;
+    for (int d = 0; d < D; d++) {
+      fva[d] = va ? cand_feat[((size_t)w.slot * D + d) * F + fa] : (FeatT)0;
+      fvb[d] = vb ? cand_feat[((size_t)w.slot * D + d) * F + fb] : (FeatT)0;
+    }
+    ca = P::candidate(fva);
+    cb = P::candidate(fvb);
   }
   __syncthreads();
 
@@ -160,17 +166,21 @@ __global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t
       im.data = reinterpret_cast<const ImgT *>(ds.pixels + off);
       im.w = (int32_t)(wh & 0xffffu);
       im.h = (int32_t)(wh >> 16);
+      im.magic = ds.magic;
       const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16));
-      const FeatT ra = P::eval(prep, fva);
-      const FeatT rb = P::eval(prep, fvb);
-      uint32_t pa = 0, pb = 0;
+      const FeatT ra = P::eval(prep, ca);
+      const FeatT rb = P::eval(prep, cb);
+      // lower_bound over the padded sorted column: pa = #thresholds < ra
+      const FeatT *pa = ta, *pb = tb;
+#pragma unroll
       for (uint32_t step = TP >> 1; step > 0; step >>= 1) {
-        pa += ta[(pa + step - 1) * kTileF] < ra ? step : 0u;
-        pb += tb[(pb + step - 1) * kTileF] < rb ? step : 0u;
+        if (pa[(step - 1) * kTileF] < ra) pa += step * kTileF;
+        if (pb[(step - 1) * kTileF] < rb) pb += step * kTileF;
       }
+      const uint32_t ka = (uint32_t)(pa - ta) / kTileF, kb = (uint32_t)(pb - tb) / kTileF;
       uint32_t *row = sh_hist + (size_t)lab * T * 32 + lane;
-      if (va && pa < T) atomicAdd(row + pa * 32, 1u);
-      if (vb && pb < T) atomicAdd(row + pb * 32, 0x10000u);
+      if (va && ka < T) atomicAdd(row + ka * 32, 1u);
+      if (vb && kb < T) atomicAdd(row + kb * 32, 0x10000u);
     }
   }
   __syncthreads();
@@ -491,6 +501,7 @@ __global__ void k_reassign(DevSet ds, const uint32_t *__restrict__ act, const ui
     im.data = reinterpret_cast<const ImgT *>(ds.pixels + ds.img_off[im_i]);
     im.w = (int32_t)(wh & 0xffffu);
     im.h = (int32_t)(wh >> 16);
+    im.magic = ds.magic;
     FeatT fv[D];
 #pragma unroll
     for (int d = 0; d < D; d++) fv[d] = feat[(size_t)n * D + d];
@@ -614,6 +625,11 @@ __global__ void k_iota(uint32_t *__restrict__ a, uint32_t *__restrict__ slot, ui
     a[i] = i;
     slot[i] = 0u;
   }
+}
+
+__global__ void k_magic_table(uint32_t *__restrict__ out) {
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d < 65536u) out[d] = d ? RoundDiv::multiplier(d) : 0u;
 }
 
 __global__ void k_log2_table(double *__restrict__ out, uint64_t n, DD inv_ln2) {
