@@ -255,6 +255,8 @@ def run_ours(a):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     evals = hist_ms = hist_bytes = launches = hist_launches = 0
+    phases = dict(ms_candidates=0.0, ms_hist=0.0, ms_split=0.0, ms_reassign=0.0, ms_total=0.0, split_rechecked=0,
+                  nodes_split=0)
     trees = []
     with Clocks(local) as clk:
         e0.record(stream)
@@ -266,6 +268,8 @@ def run_ours(a):
             hist_bytes += st["hist_bytes"]
             launches += st["kernel_launches"]
             hist_launches += st["hist_launches"]
+            for k in phases:
+                phases[k] += st[k]
         e1.record(stream)
         barrier()
     ms = allmax(e0.elapsed_time(e1))
@@ -370,7 +374,7 @@ def run_ours(a):
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
                 roofline=roof, cpu_baseline=base, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
-                predict=pred, impl="ours")
+                predict=pred, phases_per_step={k: v / a.steps for k, v in phases.items()}, impl="ours")
     print(json.dumps(line), flush=True)
 
 

@@ -383,35 +383,33 @@ int or_hist(const or_params *p, const or_dataset *ds, uint32_t tree_id,
 /* ------------------------------------------------------------------------ */
 /* a7: best split.                                                          */
 /* kernels/learn_best_feature.cl:22-111 + learn_best_featthr.hpp:101-112.    */
-/* The reference gain H(parent) - (nL/N H(L) + nR/N H(R)) with Shannon       */
-/* entropies in log2 and probabilities <= 1e-6 dropped, evaluated exactly:   */
-/* -p log2 p = (c/n)(log2 n - log2 c) in IEEE double with a shared log2       */
-/* table; the cutoff p <= 1e-6 is the integer test 1e6*c <= n.  The first    */
-/* (t-major, f-minor) candidate with the largest gain wins.                  */
+/* The reference gain H(parent) - (nL/N H(L) + nR/N H(R)), Shannon entropies  */
+/* in log2 with probabilities <= 1e-6 dropped, evaluated exactly from the     */
+/* integer counts: n H(c, n) = S(c, n) = sum over classes of                  */
+/* c (log2 n - log2 c) in IEEE double with a shared log2 table (the cutoff    */
+/* p <= 1e-6 is the integer test 1e6*c <= n), so                              */
+/*     gain = S(tot, N)/N - (S(cL, nL) + S(cR, nR)) / N.                      */
+/* The first (t-major, f-minor) candidate with the largest gain wins.         */
 /* ------------------------------------------------------------------------ */
-static inline double ent64(const uint32_t *c, uint32_t K, uint64_t n, const double *L) {
+static inline double sum64(const uint32_t *c, uint32_t K, uint64_t n, const double *L) {
   double s = 0.0;
   for (uint32_t l = 0; l < K; l++) {
     uint64_t cl = c[l];
     if (cl != 0 && cl * 1000000ull > n) {
-      double pr = (double)cl / (double)n;
-      double lg = L[n] - L[cl];
-      s = s + pr * lg;
+      double d = L[n] - L[cl];
+      double t = (double)cl * d;
+      s = s + t;
     }
   }
   return s;
 }
-static inline double gain64(const uint32_t *tot, const uint32_t *cl, const uint32_t *cr, uint32_t K,
-                            uint64_t N, uint64_t nL, uint64_t nR, double hp, const double *L) {
-  double hl = ent64(cl, K, nL, L);
-  double hr = ent64(cr, K, nR, L);
-  double wl = (double)nL / (double)N;
-  double wr = (double)nR / (double)N;
-  double a = wl * hl;
-  double b = wr * hr;
-  double e = a + b;
-  (void)tot;
-  return hp - e;
+static inline double gain64(const uint32_t *cl, const uint32_t *cr, uint32_t K, uint64_t N, uint64_t nL,
+                            uint64_t nR, double hp, const double *L) {
+  double sl = sum64(cl, K, nL, L);
+  double sr = sum64(cr, K, nR, L);
+  double w = sl + sr;
+  double q = w / (double)N;
+  return hp - q;
 }
 /* The reference formula in FP32 (learn_best_feature.cl:75-93) with the integer
  * cutoff; used only to report the FP32/FP64 disagreement. */
@@ -441,7 +439,7 @@ int or_split(const or_params *p, const uint32_t *hist, const uint32_t *class_tot
     if (out_gain32_max) out_gain32_max[i] = 0.0f;
     if (N == 0) continue;
     if (N >= table_len) { rc = -1; continue; }
-    double hp = ent64(tot, K, N, L);
+    double hp = sum64(tot, K, N, L) / (double)N;
     float hp32 = ent32(tot, K, N);
     double best = 0.0;
     float best32 = 0.0f;
@@ -456,7 +454,7 @@ int or_split(const or_params *p, const uint32_t *hist, const uint32_t *class_tot
           cr[l] = tot[l] - cl[l];
           nL += cl[l]; nR += cr[l];
         }
-        double g = gain64(tot, cl, cr, K, N, nL, nR, hp, L);
+        double g = gain64(cl, cr, K, N, nL, nR, hp, L);
         float hl32 = ent32(cl, K, nL), hr32 = ent32(cr, K, nR);
         float g32 = hp32 - ((float)nL / (float)N * hl32 + (float)nR / (float)N * hr32);
         double err = fabs((double)g32 - g);

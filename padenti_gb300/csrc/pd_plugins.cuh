@@ -1,9 +1,13 @@
 // Built-in per-pixel feature plugins.  The reference compiles a user OpenCL C
 // computeFeature() into its kernels (kernels/hist_update.cl:33,
 // kernels/predict.cl:32; prototype in padenti.hpp.in:169-187).  Here a plugin is
-// a device functor in two steps: prepare() reads what depends only on the pixel
-// (done once per pixel), eval() computes the response for one candidate
-// feature vector (done once per candidate).
+// a device functor in steps:
+//   preload(im, x, y, pre)   loads what depends only on the pixel into kPreWords
+//                            words (a warp preloads 32 pixels at once, in parallel);
+//   prepare(im, x, y, pre)   builds the per-pixel state from those words;
+//   candidate(f)             per-candidate constants, computed once per tile;
+//   eval(prep, cand)         the response of one candidate at one pixel.
+// eval(prep, f) runs all of it for a single evaluation.
 #pragma once
 
 #include "pd_common.cuh"
@@ -106,16 +110,28 @@ struct DepthDiff2 {
   struct Cand {
     OffsetConst o[4];
   };
-  static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
+  static constexpr int kPreWords = 2;  // centre depth, its RoundDiv multiplier
+  static PD_D void preload(const ImageRef<uint16_t> &im, int32_t x, int32_t y, uint32_t *pre) {
+    const uint16_t c = ldg(im.data + (size_t)y * im.w + x);
+    pre[0] = c ? (uint32_t)c : (uint32_t)kBgDepth;
+    pre[1] = ldg(im.magic + pre[0]);
+  }
+  static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y, const uint32_t *pre) {
     Prep p;
     p.im = im.data;
     p.w = im.w;
     p.h = im.h;
     p.x = x;
     p.y = y;
-    const uint16_t c = ldg(im.data + (size_t)y * im.w + x);
-    p.div = RoundDiv::make(c ? (int32_t)c : kBgDepth, im.magic);
+    p.div.d = (int32_t)pre[0];
+    p.div.m = pre[1];
+    p.div.sh = 31u - (uint32_t)__clz((int)pre[0]);
     return p;
+  }
+  static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
+    uint32_t pre[kPreWords];
+    preload(im, x, y, pre);
+    return prepare(im, x, y, pre);
   }
   static PD_D Cand candidate(const int32_t *f) {
     Cand c;
@@ -159,16 +175,30 @@ struct DepthDiff1 {
     OffsetConst o[2];
     int16_t f[2];
   };
-  static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
+  static constexpr int kPreWords = 2;  // centre depth as short, multiplier of max(depth,1)
+  static PD_D void preload(const ImageRef<uint16_t> &im, int32_t x, int32_t y, uint32_t *pre) {
+    const int16_t depth = (int16_t)ldg(im.data + (size_t)y * im.w + x);
+    pre[0] = (uint32_t)(int32_t)depth;
+    pre[1] = ldg(im.magic + (depth > 0 ? depth : 1));
+  }
+  static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y, const uint32_t *pre) {
     Prep p;
     p.im = im.data;
     p.w = im.w;
     p.h = im.h;
     p.x = x;
     p.y = y;
-    p.depth = (int16_t)ldg(im.data + (size_t)y * im.w + x);
-    p.div = RoundDiv::make(p.depth > 0 ? (int32_t)p.depth : 1, im.magic);
+    p.depth = (int16_t)(int32_t)pre[0];
+    const int32_t d = p.depth > 0 ? (int32_t)p.depth : 1;
+    p.div.d = d;
+    p.div.m = pre[1];
+    p.div.sh = 31u - (uint32_t)__clz(d);
     return p;
+  }
+  static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
+    uint32_t pre[kPreWords];
+    preload(im, x, y, pre);
+    return prepare(im, x, y, pre);
   }
   static PD_D Cand candidate(const int16_t *f) {
     Cand c;
@@ -214,7 +244,9 @@ struct ChannelDiff {
   struct Cand {
     int32_t c1, c2, ux, uy, vx, vy;
   };
-  static PD_D Prep prepare(const ImageRef<uint8_t> &im, int32_t x, int32_t y) {
+  static constexpr int kPreWords = 1;
+  static PD_D void preload(const ImageRef<uint8_t> &, int32_t, int32_t, uint32_t *pre) { pre[0] = 0u; }
+  static PD_D Prep prepare(const ImageRef<uint8_t> &im, int32_t x, int32_t y, const uint32_t *) {
     Prep p;
     p.im = im.data;
     p.w = im.w;
@@ -223,6 +255,7 @@ struct ChannelDiff {
     p.y = y;
     return p;
   }
+  static PD_D Prep prepare(const ImageRef<uint8_t> &im, int32_t x, int32_t y) { return prepare(im, x, y, nullptr); }
   static PD_D Cand candidate(const int32_t *f) {
     Cand c;
     c.c1 = f[0] < 0 ? 0 : (f[0] > 2 ? 2 : f[0]);

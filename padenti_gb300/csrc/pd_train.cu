@@ -213,6 +213,17 @@ static uint64_t hist_algorithmic_bytes(const pd_ctx *ctx, const pd_train_params 
 template <bool CUM>
 static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const uint32_t *d_hist,
                         const uint8_t *d_perm, const uint32_t *d_class_tot) {
+  if (!n) return PD_OK;
+  const uint32_t F = p->n_features;
+  // Parts per node: enough CTAs to fill the GPU when the frontier is small.
+  const uint32_t max_parts = (F + kSplitCols - 1) / kSplitCols;
+  uint32_t parts = std::min<uint32_t>(max_parts, std::max<uint32_t>(1, (4 * 152 + n - 1) / n));
+  uint32_t cols = (F + parts - 1) / parts;
+  cols = (cols + 31) / 32 * 32;
+  parts = (F + cols - 1) / cols;
+  PD_TRY(ctx->split_scratch.ensure((size_t)n * 8 + (size_t)n * parts * sizeof(SplitPart) + 16));
+  unsigned *node_max = ctx->split_scratch.as<unsigned>();
+  PD_CUDA(cudaMemsetAsync(node_max, 0, (size_t)n * 8, ctx->stream));
   SplitArgs a;
   a.hist = d_hist;
   a.perm = d_perm;
@@ -220,23 +231,32 @@ static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const
   a.g32 = ctx->g32.as<float>();
   a.L = ctx->log2_tab.as<double>();
   a.L_len = ctx->log2_len;
-  a.F = p->n_features;
+  a.F = F;
   a.T = p->n_thresholds;
   a.K = ctx->cfg.n_classes;
   a.delta = kRecheckDelta;
+  a.cols = cols;
+  a.parts = parts;
+  a.node_max = node_max;
+  a.done = node_max + n;
+  a.part_best = reinterpret_cast<SplitPart *>(ctx->split_scratch.as<uint8_t>() + (size_t)n * 8);
   a.out = ctx->split_out.as<SplitOut>();
   a.out_cl = ctx->split_cl.as<uint32_t>();
   a.rechecked = ctx->recheck.as<unsigned long long>();
-  if (!n) return PD_OK;
+  const dim3 grid(parts, n);
+  auto run = [&]<int KM>() -> int {
+    k_split_g32<KM, CUM><<<grid, kSplitCols, 0, ctx->stream>>>(a);
+    k_split_pick<KM, CUM><<<grid, kSplitCols, 0, ctx->stream>>>(a);
+    PD_CUDA(cudaGetLastError());
+    ctx->launches += 2;
+    return PD_OK;
+  };
   const int K = ctx->cfg.n_classes;
-  if (K <= 4) k_split<4, CUM><<<n, kSplitThreads, 0, ctx->stream>>>(a);
-  else if (K <= 8) k_split<8, CUM><<<n, kSplitThreads, 0, ctx->stream>>>(a);
-  else if (K <= 16) k_split<16, CUM><<<n, kSplitThreads, 0, ctx->stream>>>(a);
-  else if (K <= 32) k_split<32, CUM><<<n, kSplitThreads, 0, ctx->stream>>>(a);
-  else k_split<64, CUM><<<n, kSplitThreads, 0, ctx->stream>>>(a);
-  PD_CUDA(cudaGetLastError());
-  ctx->launches++;
-  return PD_OK;
+  if (K <= 4) return run.template operator()<4>();
+  if (K <= 8) return run.template operator()<8>();
+  if (K <= 16) return run.template operator()<16>();
+  if (K <= 32) return run.template operator()<32>();
+  return run.template operator()<64>();
 }
 
 static float elapsed(cudaEvent_t a, cudaEvent_t b) {

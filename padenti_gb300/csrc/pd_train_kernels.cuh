@@ -12,7 +12,6 @@
 namespace pd {
 
 constexpr int kHistThreads = 256;  // 8 warps, each on its own samples
-constexpr int kSplitThreads = 256;
 constexpr int kScanItems = 4096;   // active samples per scan block (256 threads x 16)
 constexpr float kRecheckDelta = 5e-4f;  // FP32 gain window rechecked in FP64
 
@@ -144,44 +143,75 @@ __global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t
   __syncthreads();
 
   const FeatT *ta = sh_thr + lane, *tb = sh_thr + 32 + lane;
+  constexpr int PW = P::kPreWords;
   const unsigned full = 0xffffffffu;
+  // one evaluation pair (both candidates of the lane) on warp sample i
+  struct Eval {
+    FeatT ra, rb;
+    uint32_t lab;
+  };
   for (uint32_t base = w.begin + warp * 32; base < w.end; base += kHistThreads) {
     const uint32_t n_here = min(32u, w.end - base);
-    uint32_t my_xy = 0, my_wh = 0, my_lab = 0;
+    // lane-parallel preload of 32 samples: position, class, image, pixel words
+    uint32_t my_xy = 0, my_wh = 0, my_lab = 0, my_pre[PW];
     uint64_t my_off = 0;
+#pragma unroll
+    for (int k = 0; k < PW; k++) my_pre[k] = 0u;
     if ((uint32_t)lane < n_here) {
       const uint32_t s = act[base + lane];
       my_xy = ds.s_xy[s];
       my_lab = ds.s_label[s];
-      const uint32_t im = ds.s_img[s];
-      my_off = ds.img_off[im];
-      my_wh = ds.img_wh[im];
+      const uint32_t imi = ds.s_img[s];
+      my_off = ds.img_off[imi];
+      my_wh = ds.img_wh[imi];
+      ImageRef<ImgT> im;
+      im.data = reinterpret_cast<const ImgT *>(ds.pixels + my_off);
+      im.w = (int32_t)(my_wh & 0xffffu);
+      im.h = (int32_t)(my_wh >> 16);
+      im.magic = ds.magic;
+      P::preload(im, (int32_t)(my_xy & 0xffffu), (int32_t)(my_xy >> 16), my_pre);
     }
-    for (uint32_t i = 0; i < n_here; i++) {
+    auto eval_at = [&](uint32_t i) -> Eval {
       const uint32_t xy = __shfl_sync(full, my_xy, i);
       const uint32_t wh = __shfl_sync(full, my_wh, i);
-      const uint32_t lab = __shfl_sync(full, my_lab, i);
       const uint64_t off = __shfl_sync(full, my_off, i);
+      uint32_t pre[PW];
+#pragma unroll
+      for (int k = 0; k < PW; k++) pre[k] = __shfl_sync(full, my_pre[k], i);
       ImageRef<ImgT> im;
       im.data = reinterpret_cast<const ImgT *>(ds.pixels + off);
       im.w = (int32_t)(wh & 0xffffu);
       im.h = (int32_t)(wh >> 16);
       im.magic = ds.magic;
-      const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16));
-      const FeatT ra = P::eval(prep, ca);
-      const FeatT rb = P::eval(prep, cb);
-      // lower_bound over the padded sorted column: pa = #thresholds < ra
+      const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16), pre);
+      Eval e;
+      e.ra = P::eval(prep, ca);
+      e.rb = P::eval(prep, cb);
+      e.lab = __shfl_sync(full, my_lab, i);
+      return e;
+    };
+    auto accumulate = [&](const Eval &e) {
+      // lower_bound over the padded sorted column: k = #thresholds < r
       const FeatT *pa = ta, *pb = tb;
 #pragma unroll
       for (uint32_t step = TP >> 1; step > 0; step >>= 1) {
-        if (pa[(step - 1) * kTileF] < ra) pa += step * kTileF;
-        if (pb[(step - 1) * kTileF] < rb) pb += step * kTileF;
+        if (pa[(step - 1) * kTileF] < e.ra) pa += step * kTileF;
+        if (pb[(step - 1) * kTileF] < e.rb) pb += step * kTileF;
       }
       const uint32_t ka = (uint32_t)(pa - ta) / kTileF, kb = (uint32_t)(pb - tb) / kTileF;
-      uint32_t *row = sh_hist + (size_t)lab * T * 32 + lane;
+      uint32_t *row = sh_hist + (size_t)e.lab * T * 32 + lane;
       if (va && ka < T) atomicAdd(row + ka * 32, 1u);
       if (vb && kb < T) atomicAdd(row + kb * 32, 0x10000u);
+    };
+    // two samples per iteration: their probe loads are in flight together
+    uint32_t i = 0;
+    for (; i + 1 < n_here; i += 2) {
+      const Eval e0 = eval_at(i);
+      const Eval e1 = eval_at(i + 1);
+      accumulate(e0);
+      accumulate(e1);
     }
+    if (i < n_here) accumulate(eval_at(i));
   }
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) {
@@ -237,48 +267,39 @@ struct SplitOut {
   int32_t t, f, j, pad;
   double gain;
 };
+// Best candidate of one column range of one node.
+struct SplitPart {
+  double gain;
+  long long idx;  // t*F + f
+  int32_t j, pad;
+};
+
+constexpr int kSplitCols = 128;  // threads of a split CTA, one column each per pass
 
 // Reference-formula FP32 entropy (kernels/learn_best_feature.cl:75-93) with the
 // p <= 1e-6 cutoff as the integer test 1e6*c <= n; fast intrinsics, error well
 // inside kRecheckDelta/2.
-template <int KM>
-PD_D float ent32(const uint32_t *c, uint32_t K, uint32_t n) {
-  if (n == 0) return 0.0f;
-  const float inv = __frcp_rn((float)n);
-  float s = 0.0f;
-#pragma unroll
-  for (int l = 0; l < KM; l++) {
-    if ((uint32_t)l < K) {
-      const uint32_t cl = c[l];
-      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
-        const float p = (float)cl * inv;
-        s -= p * __log2f(p);
-      }
-    }
-  }
-  return s;
-}
-template <int KM>
-PD_D float ent32_right(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n) {
-  if (n == 0) return 0.0f;
-  const float inv = __frcp_rn((float)n);
-  float s = 0.0f;
-#pragma unroll
-  for (int l = 0; l < KM; l++) {
-    if ((uint32_t)l < K) {
-      const uint32_t cl = tot[l] - c[l];
-      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
-        const float p = (float)cl * inv;
-        s -= p * __log2f(p);
-      }
-    }
-  }
-  return s;
-}
-// Exact entropy: sum over classes of (c/n)(log2 n - log2 c), one IEEE double
-// operation at a time with the shared log2 table.
 template <int KM, bool RIGHT>
-PD_D double ent64(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n, const double *L) {
+PD_D float ent32(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n) {
+  if (n == 0) return 0.0f;
+  const float inv = __frcp_rn((float)n);
+  float s = 0.0f;
+#pragma unroll
+  for (int l = 0; l < KM; l++) {
+    if ((uint32_t)l < K) {
+      const uint32_t cl = RIGHT ? tot[l] - c[l] : c[l];
+      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
+        const float p = (float)cl * inv;
+        s -= p * __log2f(p);
+      }
+    }
+  }
+  return s;
+}
+// Exact n*entropy: sum over classes of c (log2 n - log2 c), one IEEE double
+// operation at a time with the shared log2 table (the oracle's sum64).
+template <int KM, bool RIGHT>
+PD_D double sum64(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n, const double *L) {
   double s = 0.0;
   if (n == 0) return s;
   const double ln = L[n];
@@ -286,11 +307,7 @@ PD_D double ent64(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n
   for (int l = 0; l < KM; l++) {
     if ((uint32_t)l < K) {
       const uint32_t cl = RIGHT ? tot[l] - c[l] : c[l];
-      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
-        const double p = ddiv((double)cl, (double)n);
-        const double lg = dsub(ln, L[cl]);
-        s = dadd(s, dmul(p, lg));
-      }
+      if (cl != 0u && (uint64_t)cl * 1000000ull > n) s = dadd(s, dmul((double)cl, dsub(ln, L[cl])));
     }
   }
   return s;
@@ -305,83 +322,137 @@ struct SplitArgs {
   uint64_t L_len;
   uint32_t F, T, K;
   float delta;
+  uint32_t cols;              // columns per part
+  uint32_t parts;             // parts per node
+  unsigned *node_max;         // [slots] order-preserving bits of the FP32 maximum
+  unsigned *done;             // [slots] finished parts
+  SplitPart *part_best;       // [slots][parts]
   SplitOut *out;
   uint32_t *out_cl;           // [slots][K] left class counts of the winner
   unsigned long long *rechecked;
 };
 
-// One CTA per node.  Pass 1: every (t,f) gain in FP32, kept in scratch, and the
-// node maximum.  Pass 2: candidates within delta of it are re-evaluated with
-// the exact FP64 gain; the largest exact gain wins, ties to the lowest t*F+f
-// (the first-max rule of learn_best_feature.cl:96-101 + std::max_element).
+PD_D unsigned f2ord(float f) {
+  const unsigned b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+PD_D float ord2f(unsigned u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
+
+// Loads the counts of sorted position j of column f into c (prefix-summed in
+// rank space, copied when cumulative); returns whether they changed.
 template <int KM, bool CUM>
-__global__ void __launch_bounds__(kSplitThreads) k_split(SplitArgs a) {
-  const uint32_t slot = blockIdx.x;
-  const uint32_t F = a.F, T = a.T, K = a.K;
-  __shared__ uint32_t tot[KM];
-  __shared__ float red_f[kSplitThreads / 32];
-  __shared__ double red_g[kSplitThreads / 32];
-  __shared__ long long red_i[kSplitThreads / 32];
-  __shared__ float s_gmax;
-  for (uint32_t l = threadIdx.x; l < KM; l += blockDim.x) tot[l] = l < K ? a.class_tot[(size_t)slot * K + l] : 0u;
+PD_D bool step_counts(const uint32_t *H, uint32_t K, uint32_t T, uint32_t F, uint32_t j, uint32_t f, uint32_t *c,
+                      uint32_t &nL) {
+  bool changed = false;
+  nL = 0;
+#pragma unroll
+  for (int l = 0; l < KM; l++) {
+    if ((uint32_t)l < K) {
+      const uint32_t h = H[((size_t)l * T + j) * F + f];
+      if (CUM) {
+        changed |= h != c[l];
+        c[l] = h;
+      } else {
+        changed |= h != 0u;
+        c[l] += h;
+      }
+      nL += c[l];
+    }
+  }
+  return changed;
+}
+
+template <int KM>
+PD_D void load_tot(const SplitArgs &a, uint32_t slot, uint32_t *tot, uint32_t &N) {
+  for (uint32_t l = threadIdx.x; l < KM; l += blockDim.x) tot[l] = l < a.K ? a.class_tot[(size_t)slot * a.K + l] : 0u;
   __syncthreads();
-  uint32_t N = 0;
+  N = 0;
 #pragma unroll
   for (int l = 0; l < KM; l++) N += tot[l];
-  if (N == 0 || (uint64_t)N >= a.L_len) {
-    if (threadIdx.x == 0) {
-      a.out[slot].t = -1;
-      a.out[slot].f = -1;
-      a.out[slot].j = -1;
-      a.out[slot].gain = 0.0;
-    }
-    return;
-  }
-  const float hp32 = ent32<KM>(tot, K, N);
+}
+
+// Pass 1: FP32 gain of every (t,f) of a column range, kept in scratch, and the
+// node maximum (atomic over the parts of the node).  A sorted position whose
+// rank bin is empty has the counts, hence the gain, of the previous one.
+template <int KM, bool CUM>
+__global__ void __launch_bounds__(kSplitCols) k_split_g32(SplitArgs a) {
+  const uint32_t slot = blockIdx.y, part = blockIdx.x;
+  const uint32_t F = a.F, T = a.T, K = a.K;
+  __shared__ uint32_t tot[KM];
+  __shared__ float red[kSplitCols / 32];
+  uint32_t N;
+  load_tot<KM>(a, slot, tot, N);
+  if (N == 0 || (uint64_t)N >= a.L_len) return;
+  const float hp32 = ent32<KM, false>(tot, tot, K, N);
+  const float invN = __frcp_rn((float)N);
   const uint32_t *H = a.hist + (size_t)slot * K * T * F;
   float *G = a.g32 + (size_t)slot * T * F;
-
+  const uint32_t fb = part * a.cols, fe = min(F, fb + a.cols);
   float lmax = -FLT_MAX;
-  for (uint32_t f = threadIdx.x; f < F; f += blockDim.x) {
+  for (uint32_t f = fb + threadIdx.x; f < fe; f += blockDim.x) {
     uint32_t c[KM];
 #pragma unroll
     for (int l = 0; l < KM; l++) c[l] = 0u;
+    float g = 0.0f;
     for (uint32_t j = 0; j < T; j++) {
-      uint32_t nL = 0;
-#pragma unroll
-      for (int l = 0; l < KM; l++) {
-        if ((uint32_t)l < K) {
-          const uint32_t h = H[((size_t)l * T + j) * F + f];
-          c[l] = CUM ? h : c[l] + h;
-          nL += c[l];
-        }
+      uint32_t nL;
+      const bool changed = step_counts<KM, CUM>(H, K, T, F, j, f, c, nL);
+      if (j == 0 || changed) {
+        const uint32_t nR = N - nL;
+        const float hl = ent32<KM, false>(tot, c, K, nL);
+        const float hr = ent32<KM, true>(tot, c, K, nR);
+        g = hp32 - ((float)nL * invN * hl + (float)nR * invN * hr);
       }
-      const uint32_t nR = N - nL;
-      const float hl = ent32<KM>(c, K, nL);
-      const float hr = ent32_right<KM>(tot, c, K, nR);
-      const float invN = __frcp_rn((float)N);
-      const float g = hp32 - ((float)nL * invN * hl + (float)nR * invN * hr);
       G[(size_t)j * F + f] = g;
       lmax = fmaxf(lmax, g);
     }
   }
   for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-  if ((threadIdx.x & 31) == 0) red_f[threadIdx.x >> 5] = lmax;
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lmax;
   __syncthreads();
   if (threadIdx.x == 0) {
-    float m = red_f[0];
-    for (int i = 1; i < kSplitThreads / 32; i++) m = fmaxf(m, red_f[i]);
-    s_gmax = m;
+    float m = red[0];
+    for (int i = 1; i < kSplitCols / 32; i++) m = fmaxf(m, red[i]);
+    atomicMax(a.node_max + slot, f2ord(m));
   }
-  __syncthreads();
-  const float cut = s_gmax - a.delta;
-  const double hp64 = ent64<KM, false>(tot, tot, K, N, a.L);
+}
 
+// Pass 2: candidates within delta of the node's FP32 maximum are re-evaluated
+// with the exact FP64 gain S(tot,N)/N - (S(L)+S(R))/N; the largest exact gain
+// wins, ties to the lowest t*F+f (the first-max rule of
+// learn_best_feature.cl:96-101 + std::max_element).  The last part of a node to
+// finish reduces the parts and writes the winner with its left class counts.
+template <int KM, bool CUM>
+__global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
+  const uint32_t slot = blockIdx.y, part = blockIdx.x;
+  const uint32_t F = a.F, T = a.T, K = a.K;
+  __shared__ uint32_t tot[KM];
+  __shared__ double red_g[kSplitCols / 32];
+  __shared__ long long red_i[kSplitCols / 32];
+  __shared__ int red_j[kSplitCols / 32];
+  __shared__ bool last;
+  uint32_t N;
+  load_tot<KM>(a, slot, tot, N);
+  if (N == 0 || (uint64_t)N >= a.L_len) {
+    if (part == 0 && threadIdx.x == 0) {
+      SplitOut o;
+      o.t = o.f = o.j = -1;
+      o.pad = 0;
+      o.gain = 0.0;
+      a.out[slot] = o;
+    }
+    return;
+  }
+  const float cut = ord2f(a.node_max[slot]) - a.delta;
+  const double hp64 = ddiv(sum64<KM, false>(tot, tot, K, N, a.L), (double)N);
+  const uint32_t *H = a.hist + (size_t)slot * K * T * F;
+  const float *G = a.g32 + (size_t)slot * T * F;
+  const uint32_t fb = part * a.cols, fe = min(F, fb + a.cols);
   double best = -DBL_MAX;
-  long long best_idx = LLONG_MAX;  // t*F + f
+  long long best_idx = LLONG_MAX;
   int best_j = -1;
   unsigned long long n_checked = 0;
-  for (uint32_t f = threadIdx.x; f < F; f += blockDim.x) {
+  for (uint32_t f = fb + threadIdx.x; f < fe; f += blockDim.x) {
     int jmax = -1;
     for (uint32_t j = 0; j < T; j++)
       if (G[(size_t)j * F + f] >= cut) jmax = (int)j;
@@ -389,24 +460,20 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(SplitArgs a) {
     uint32_t c[KM];
 #pragma unroll
     for (int l = 0; l < KM; l++) c[l] = 0u;
+    bool dirty = true;
+    double g = 0.0;
     for (int j = 0; j <= jmax; j++) {
-      uint32_t nL = 0;
-#pragma unroll
-      for (int l = 0; l < KM; l++) {
-        if ((uint32_t)l < K) {
-          const uint32_t h = H[((size_t)l * T + j) * F + f];
-          c[l] = CUM ? h : c[l] + h;
-          nL += c[l];
-        }
-      }
+      uint32_t nL;
+      dirty |= step_counts<KM, CUM>(H, K, T, F, (uint32_t)j, f, c, nL);
       if (!(G[(size_t)j * F + f] >= cut)) continue;
-      n_checked++;
-      const uint32_t nR = N - nL;
-      const double hl = ent64<KM, false>(tot, c, K, nL, a.L);
-      const double hr = ent64<KM, true>(tot, c, K, nR, a.L);
-      const double wl = ddiv((double)nL, (double)N);
-      const double wr = ddiv((double)nR, (double)N);
-      const double g = dsub(hp64, dadd(dmul(wl, hl), dmul(wr, hr)));
+      if (dirty) {
+        n_checked++;
+        const uint32_t nR = N - nL;
+        const double sl = sum64<KM, false>(tot, c, K, nL, a.L);
+        const double sr = sum64<KM, true>(tot, c, K, nR, a.L);
+        g = dsub(hp64, ddiv(dadd(sl, sr), (double)N));
+        dirty = false;
+      }
       const uint32_t t = a.perm ? a.perm[((size_t)slot * T + j) * F + f] : (uint32_t)j;
       const long long idx = (long long)t * F + f;
       if (g > best || (g == best && idx < best_idx)) {
@@ -417,7 +484,6 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(SplitArgs a) {
     }
   }
   if (n_checked) atomicAdd(a.rechecked, n_checked);
-  // block arg-max: larger gain, then smaller index
   for (int o = 16; o > 0; o >>= 1) {
     const double og = __shfl_xor_sync(0xffffffffu, best, o);
     const long long oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
@@ -428,7 +494,6 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(SplitArgs a) {
       best_j = oj;
     }
   }
-  __shared__ int red_j[kSplitThreads / 32];
   if ((threadIdx.x & 31) == 0) {
     red_g[threadIdx.x >> 5] = best;
     red_i[threadIdx.x >> 5] = best_idx;
@@ -436,37 +501,51 @@ __global__ void __launch_bounds__(kSplitThreads) k_split(SplitArgs a) {
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int i = 1; i < kSplitThreads / 32; i++) {
+    for (int i = 1; i < kSplitCols / 32; i++) {
       if (red_g[i] > red_g[0] || (red_g[i] == red_g[0] && red_i[i] < red_i[0])) {
         red_g[0] = red_g[i];
         red_i[0] = red_i[i];
         red_j[0] = red_j[i];
       }
     }
-    SplitOut o;
-    o.pad = 0;
-    if (red_i[0] == LLONG_MAX) {
-      o.t = -1;
-      o.f = -1;
-      o.j = -1;
-      o.gain = 0.0;
-    } else {
-      o.t = (int32_t)(red_i[0] / F);
-      o.f = (int32_t)(red_i[0] % F);
-      o.j = red_j[0];
-      o.gain = red_g[0];
-      for (uint32_t l = 0; l < K; l++) {
-        uint32_t c = 0;
-        if (CUM) {
-          c = H[((size_t)l * T + o.j) * F + o.f];
-        } else {
-          for (int j = 0; j <= o.j; j++) c += H[((size_t)l * T + j) * F + o.f];
-        }
-        a.out_cl[(size_t)slot * K + l] = c;
-      }
-    }
-    a.out[slot] = o;
+    SplitPart pb;
+    pb.gain = red_g[0];
+    pb.idx = red_i[0];
+    pb.j = red_j[0];
+    pb.pad = 0;
+    a.part_best[(size_t)slot * a.parts + part] = pb;
+    __threadfence();
+    last = atomicAdd(a.done + slot, 1u) == a.parts - 1;
   }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  SplitPart b = a.part_best[(size_t)slot * a.parts];
+  for (uint32_t i = 1; i < a.parts; i++) {
+    const SplitPart q = a.part_best[(size_t)slot * a.parts + i];
+    if (q.gain > b.gain || (q.gain == b.gain && q.idx < b.idx)) b = q;
+  }
+  SplitOut o;
+  o.pad = 0;
+  if (b.idx == LLONG_MAX) {
+    o.t = o.f = o.j = -1;
+    o.gain = 0.0;
+  } else {
+    o.t = (int32_t)(b.idx / F);
+    o.f = (int32_t)(b.idx % F);
+    o.j = b.j;
+    o.gain = b.gain;
+    for (uint32_t l = 0; l < K; l++) {
+      uint32_t c = 0;
+      if (CUM) {
+        c = H[((size_t)l * T + o.j) * F + o.f];
+      } else {
+        for (int j = 0; j <= o.j; j++) c += H[((size_t)l * T + j) * F + o.f];
+      }
+      a.out_cl[(size_t)slot * K + l] = c;
+    }
+  }
+  a.out[slot] = o;
 }
 
 // ------------------------------------------------------------ reassign ----
