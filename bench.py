@@ -56,6 +56,8 @@ def args_():
     a.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     a.add_argument("--no-cpu", action="store_true")
     a.add_argument("--seed", type=int, default=0)
+    a.add_argument("--chunk", type=int, default=None, help="histogram work-item size (samples)")
+    a.add_argument("--spi", type=int, default=None, help="samples per histogram-kernel iteration (2 or 4)")
     return a.parse_args()
 
 
@@ -240,6 +242,10 @@ def run_ours(a):
     from padenti_gb300 import _native as N
 
     tr = pg.TreeTrainer(cfg, device=local)
+    if a.chunk:
+        tr.set_tuning("chunk", a.chunk)
+    if a.spi:
+        tr.set_tuning("hist_spi", a.spi)
     tr.upload(ts)
     stream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(tr.h))
 
@@ -371,6 +377,7 @@ def run_ours(a):
                 config=dict(workload=WORKLOAD, images=a.images, width=a.width, height=a.height,
                             samples_per_image=a.samples, features=a.features, thresholds=a.thresholds,
                             depth=a.depth, min_leaf=a.min_leaf, trees_per_step=1,
+                            chunk=a.chunk or 4096, hist_spi=a.spi or 4,
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
                 roofline=roof, cpu_baseline=base, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),

@@ -130,6 +130,10 @@ int pd_ctx_destroy(pd_ctx *ctx);
  * frontiers whose histograms exceed it are processed in slices, as the
  * reference does with its 20 GiB host cap (cl_tree_trainer_impl.hpp:47-50). */
 int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
+/* Launch-shape knobs of the histogram kernel (results do not depend on them):
+ *   "chunk"     samples per histogram work item, [256, 65535] (default 4096);
+ *   "hist_spi"  samples evaluated together per warp iteration, 2 or 4 (default 4). */
+int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value);
 /* Synchronises the context's stream. */
 int pd_ctx_sync(pd_ctx *ctx);
 /* The CUDA stream (cudaStream_t) the context launches on. */

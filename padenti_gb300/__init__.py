@@ -275,6 +275,10 @@ class TreeTrainer(_Ctx):
         if hist_budget:
             check(lib().pd_ctx_set_hist_budget(self.h, hist_budget))
 
+    def set_tuning(self, name: str, value: int) -> None:
+        """Launch-shape knob of the histogram kernel ("chunk", "hist_spi"); results do not change."""
+        check(lib().pd_ctx_set_tuning(self.h, name.encode(), int(value)))
+
     def upload(self, ts: TrainingSet) -> None:
         key = (id(ts), ts._version, len(ts.images))
         if self._uploaded == key:

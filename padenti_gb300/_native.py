@@ -76,6 +76,7 @@ _SIGS = {
     "pd_ctx_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(_P)]),
     "pd_ctx_destroy": (C.c_int, [_P]),
     "pd_ctx_set_hist_budget": (C.c_int, [_P, C.c_uint64]),
+    "pd_ctx_set_tuning": (C.c_int, [_P, C.c_char_p, C.c_int64]),
     "pd_ctx_sync": (C.c_int, [_P]),
     "pd_ctx_stream": (_P, [_P]),
     "pd_ctx_transfer_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),

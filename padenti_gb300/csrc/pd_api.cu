@@ -98,6 +98,21 @@ extern "C" int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes) {
   return PD_OK;
 }
 
+extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
+  PD_CHECK(ctx && name, PD_ERR_INVALID, "null argument");
+  const std::string n(name);
+  if (n == "chunk") {
+    PD_CHECK(value >= 256 && value <= 65535, PD_ERR_INVALID, "chunk %lld outside [256,65535]", (long long)value);
+    ctx->chunk = (uint32_t)value;
+  } else if (n == "hist_spi") {
+    PD_CHECK(value == 2 || value == 4, PD_ERR_INVALID, "hist_spi must be 2 or 4");
+    ctx->hist_spi = (uint32_t)value;
+  } else {
+    return set_error(PD_ERR_INVALID, "unknown tuning knob '%s'", name);
+  }
+  return PD_OK;
+}
+
 extern "C" int pd_ctx_sync(pd_ctx *ctx) {
   PD_CHECK(ctx, PD_ERR_INVALID, "null context");
   PD_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -85,9 +85,12 @@ struct OffsetConst {
     }
     return o;
   }
-  // round_half_away(u / d), identical to (int)roundf((float)u / (float)d)
+  PD_D bool fast() const { return sg != 0; }
+  // round_half_away(u / d), identical to (int)roundf((float)u / (float)d);
+  // FAST assumes fast() (|u| <= 2^21).
+  template <bool FAST = false>
   PD_D int32_t apply(const RoundDiv &r) const {
-    if (sg == 0) return (int32_t)roundf(fdiv((float)(int32_t)n2, (float)r.d));
+    if (!FAST && sg == 0) return (int32_t)roundf(fdiv((float)(int32_t)n2, (float)r.d));
     return (int32_t)r.q(n2) * sg;
   }
 };
@@ -139,16 +142,22 @@ struct DepthDiff2 {
     for (int k = 0; k < 4; k++) c.o[k] = OffsetConst::make(f[k]);
     return c;
   }
-  static PD_D int32_t probe(const Prep &p, int32_t x, int32_t y) {
-    if ((uint32_t)x >= (uint32_t)p.w || (uint32_t)y >= (uint32_t)p.h) return kBgDepth;
-    const uint16_t v = ldg(p.im + (size_t)y * p.w + x);
-    return v ? (int32_t)v : kBgDepth;
+  static PD_D bool fast(const Cand &c) {
+    return c.o[0].fast() && c.o[1].fast() && c.o[2].fast() && c.o[3].fast();
   }
+  // Branch-free: an outside probe reads the (always valid) image origin and is
+  // then replaced by 10000.
+  static PD_D int32_t probe(const Prep &p, int32_t x, int32_t y) {
+    const bool in = (uint32_t)x < (uint32_t)p.w && (uint32_t)y < (uint32_t)p.h;
+    const uint32_t v = ldg(p.im + (in ? (size_t)y * p.w + x : 0));
+    return (in && v) ? (int32_t)v : kBgDepth;
+  }
+  template <bool FAST = false>
   static PD_D int32_t eval(const Prep &p, const Cand &c) {
-    const int32_t x1 = p.x + c.o[0].apply(p.div);
-    const int32_t y1 = p.y + c.o[1].apply(p.div);
-    const int32_t x2 = p.x + c.o[2].apply(p.div);
-    const int32_t y2 = p.y + c.o[3].apply(p.div);
+    const int32_t x1 = p.x + c.o[0].template apply<FAST>(p.div);
+    const int32_t y1 = p.y + c.o[1].template apply<FAST>(p.div);
+    const int32_t x2 = p.x + c.o[2].template apply<FAST>(p.div);
+    const int32_t y2 = p.y + c.o[3].template apply<FAST>(p.div);
     return probe(p, x1, y1) - probe(p, x2, y2);
   }
   static PD_D int32_t eval(const Prep &p, const int32_t *f) { return eval(p, candidate(f)); }
@@ -208,21 +217,23 @@ struct DepthDiff1 {
     c.f[1] = f[1];
     return c;
   }
+  static PD_D bool fast(const Cand &c) { return c.o[0].fast() && c.o[1].fast(); }
+  template <bool FAST = false>
   static PD_D int16_t eval(const Prep &p, const Cand &c) {
     int32_t probe = kBgDepth;
     if (p.depth != 0) {
       int32_t ox, oy;
       if (p.depth > 0) {
-        ox = p.x + c.o[0].apply(p.div);
-        oy = p.y + c.o[1].apply(p.div);
+        ox = p.x + c.o[0].template apply<FAST>(p.div);
+        oy = p.y + c.o[1].template apply<FAST>(p.div);
       } else {
         const float dd = (float)p.depth;
         ox = p.x + (int32_t)roundf(fdiv(fmul((float)c.f[0], 500.0f), dd));
         oy = p.y + (int32_t)roundf(fdiv(fmul((float)c.f[1], 500.0f), dd));
       }
-      const bool out = (uint32_t)ox >= (uint32_t)p.w || (uint32_t)oy >= (uint32_t)p.h;
-      const int16_t v = out ? (int16_t)kBgDepth : (int16_t)ldg(p.im + (size_t)oy * p.w + ox);
-      probe = v ? v : kBgDepth;
+      const bool in = (uint32_t)ox < (uint32_t)p.w && (uint32_t)oy < (uint32_t)p.h;
+      const int16_t v = (int16_t)ldg(p.im + (in ? (size_t)oy * p.w + ox : 0));
+      probe = !in ? kBgDepth : (v ? v : kBgDepth);
     }
     return (int16_t)((int32_t)p.depth - probe);
   }
@@ -266,10 +277,13 @@ struct ChannelDiff {
     c.vy = f[5];
     return c;
   }
+  static PD_D bool fast(const Cand &) { return true; }
   static PD_D int32_t read(const Prep &p, int32_t x, int32_t y, int32_t c) {
-    if ((uint32_t)x >= (uint32_t)p.w || (uint32_t)y >= (uint32_t)p.h) return 0;
-    return ldg(p.im + ((size_t)y * p.w + x) * 3 + c);
+    const bool in = (uint32_t)x < (uint32_t)p.w && (uint32_t)y < (uint32_t)p.h;
+    const int32_t v = ldg(p.im + (in ? ((size_t)y * p.w + x) * 3 + c : 0));
+    return in ? v : 0;
   }
+  template <bool FAST = false>
   static PD_D int32_t eval(const Prep &p, const Cand &c) {
     return read(p, p.x + c.ux, p.y + c.uy, c.c1) - read(p, p.x + c.vx, p.y + c.vy, c.c2);
   }

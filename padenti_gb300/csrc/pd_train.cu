@@ -170,12 +170,13 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   PD_CUDA(h2d(ctx, ctx->items.ptr, items.data(), items.size() * sizeof(WorkItem)));
   const size_t smem = hist_smem(ctx, T);
   auto run = [&]<uint32_t TP>() -> int {
-    PD_CUDA(cudaFuncSetAttribute(k_hist<P, TP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = ctx->hist_spi >= 4 ? k_hist<P, TP, 4> : k_hist<P, TP, 2>;
+    PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (ev_before) PD_CUDA(cudaEventRecord(ev_before, ctx->stream));
     // The grid is the work list; the hardware scheduler keeps every SM full.
     for (uint64_t b = 0; b < items.size(); b += 0x7fffffffull) {
       const uint64_t cnt = std::min<uint64_t>(items.size() - b, 0x7fffffffull);
-      k_hist<P, TP><<<(unsigned)cnt, kHistThreads, smem, ctx->stream>>>(
+      kern<<<(unsigned)cnt, kHistThreads, smem, ctx->stream>>>(
           devset(ctx), d_act, ctx->items.as<WorkItem>() + b, ctx->cand_feat.as<FeatT>(),
           ctx->cand_thr.as<FeatT>(), ctx->hist.as<uint32_t>(), F, T, K);
       PD_CUDA(cudaGetLastError());
@@ -251,10 +252,14 @@ static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const
     ctx->launches += 2;
     return PD_OK;
   };
+  // class loops are unrolled to KM >= K; the common class counts get exact KM
   const int K = ctx->cfg.n_classes;
+  if (K <= 3) return run.template operator()<3>();
   if (K <= 4) return run.template operator()<4>();
   if (K <= 8) return run.template operator()<8>();
+  if (K <= 9) return run.template operator()<9>();
   if (K <= 16) return run.template operator()<16>();
+  if (K <= 21) return run.template operator()<21>();
   if (K <= 32) return run.template operator()<32>();
   return run.template operator()<64>();
 }

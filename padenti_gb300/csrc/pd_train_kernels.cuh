@@ -104,44 +104,16 @@ constexpr int kCandPerLane = 2;
 constexpr int kTileF = 32 * kCandPerLane;
 constexpr uint32_t kMaxChunk = 65535;
 
-template <class P, uint32_t TP>
-__global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t *__restrict__ act,
-                                                       const WorkItem *__restrict__ items,
-                                                       const typename P::feat_t *__restrict__ cand_feat,
-                                                       const typename P::feat_t *__restrict__ cand_thr,
-                                                       uint32_t *__restrict__ hist, uint32_t F,
-                                                       uint32_t T, uint32_t K) {
+// The sample loop of k_hist: each warp walks its samples SPI at a time (their
+// probe loads in flight together) and adds both candidates of the lane into the
+// shared histogram.
+template <class P, uint32_t TP, bool FAST, int SPI>
+PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const WorkItem &w,
+                       const typename P::Cand &ca, const typename P::Cand &cb, uint32_t *sh_hist,
+                       const typename P::feat_t *sh_thr, uint32_t T, bool va, bool vb) {
   using FeatT = typename P::feat_t;
   using ImgT = typename P::img_t;
-  constexpr int D = P::kFeatDim;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);             // [K][T][32] packed
-  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32);  // [TP][64]
-
-  const WorkItem w = items[blockIdx.x];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t f0 = w.tile * kTileF;
-  const uint32_t fa = f0 + lane, fb = f0 + 32 + lane;
-  const bool va = fa < F, vb = fb < F;
-
-  for (uint32_t j = threadIdx.x; j < TP * kTileF; j += blockDim.x) {
-    const uint32_t t = j / kTileF, ff = f0 + (j % kTileF);
-    sh_thr[j] = (t < T && ff < F) ? cand_thr[((size_t)w.slot * T + t) * F + ff] : max_of<FeatT>();
-  }
-  for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) sh_hist[j] = 0u;
-  typename P::Cand ca, cb;
-  {
-    FeatT fva[D], fvb[D];
-#pragma unroll
-    for (int d = 0; d < D; d++) {
-      fva[d] = va ? cand_feat[((size_t)w.slot * D + d) * F + fa] : (FeatT)0;
-      fvb[d] = vb ? cand_feat[((size_t)w.slot * D + d) * F + fb] : (FeatT)0;
-    }
-    ca = P::candidate(fva);
-    cb = P::candidate(fvb);
-  }
-  __syncthreads();
-
   const FeatT *ta = sh_thr + lane, *tb = sh_thr + 32 + lane;
   constexpr int PW = P::kPreWords;
   const unsigned full = 0xffffffffu;
@@ -185,8 +157,8 @@ __global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t
       im.magic = ds.magic;
       const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16), pre);
       Eval e;
-      e.ra = P::eval(prep, ca);
-      e.rb = P::eval(prep, cb);
+      e.ra = P::template eval<FAST>(prep, ca);
+      e.rb = P::template eval<FAST>(prep, cb);
       e.lab = __shfl_sync(full, my_lab, i);
       return e;
     };
@@ -203,16 +175,60 @@ __global__ void __launch_bounds__(kHistThreads) k_hist(DevSet ds, const uint32_t
       if (va && ka < T) atomicAdd(row + ka * 32, 1u);
       if (vb && kb < T) atomicAdd(row + kb * 32, 0x10000u);
     };
-    // two samples per iteration: their probe loads are in flight together
+    // SPI samples per iteration: their probe loads are in flight together
     uint32_t i = 0;
-    for (; i + 1 < n_here; i += 2) {
-      const Eval e0 = eval_at(i);
-      const Eval e1 = eval_at(i + 1);
-      accumulate(e0);
-      accumulate(e1);
+    for (; i + SPI <= n_here; i += SPI) {
+      Eval e[SPI];
+#pragma unroll
+      for (int k = 0; k < SPI; k++) e[k] = eval_at(i + k);
+#pragma unroll
+      for (int k = 0; k < SPI; k++) accumulate(e[k]);
     }
-    if (i < n_here) accumulate(eval_at(i));
+    for (; i < n_here; i++) accumulate(eval_at(i));
   }
+}
+
+template <class P, uint32_t TP, int SPI>
+__global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet ds, const uint32_t *__restrict__ act,
+                                                       const WorkItem *__restrict__ items,
+                                                       const typename P::feat_t *__restrict__ cand_feat,
+                                                       const typename P::feat_t *__restrict__ cand_thr,
+                                                       uint32_t *__restrict__ hist, uint32_t F,
+                                                       uint32_t T, uint32_t K) {
+  using FeatT = typename P::feat_t;
+  using ImgT = typename P::img_t;
+  constexpr int D = P::kFeatDim;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);             // [K][T][32] packed
+  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32);  // [TP][64]
+
+  const WorkItem w = items[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t f0 = w.tile * kTileF;
+  const uint32_t fa = f0 + lane, fb = f0 + 32 + lane;
+  const bool va = fa < F, vb = fb < F;
+
+  for (uint32_t j = threadIdx.x; j < TP * kTileF; j += blockDim.x) {
+    const uint32_t t = j / kTileF, ff = f0 + (j % kTileF);
+    sh_thr[j] = (t < T && ff < F) ? cand_thr[((size_t)w.slot * T + t) * F + ff] : max_of<FeatT>();
+  }
+  for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) sh_hist[j] = 0u;
+  typename P::Cand ca, cb;
+  {
+    FeatT fva[D], fvb[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+      fva[d] = va ? cand_feat[((size_t)w.slot * D + d) * F + fa] : (FeatT)0;
+      fvb[d] = vb ? cand_feat[((size_t)w.slot * D + d) * F + fb] : (FeatT)0;
+    }
+    ca = P::candidate(fva);
+    cb = P::candidate(fvb);
+  }
+  // the exact-division fast path when every candidate of the tile allows it
+  const bool fast = __syncthreads_and(P::fast(ca) && P::fast(cb));
+  if (fast) hist_samples<P, TP, true, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, va, vb);
+  else hist_samples<P, TP, false, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, va, vb);
+
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) {
     const uint32_t v = sh_hist[j];

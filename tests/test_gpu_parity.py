@@ -145,6 +145,23 @@ def test_train_tree_sliced_histograms_identical():
     _assert_same_tree(a, _oracle_tree(cfg, ts, tp, 4, 7))
 
 
+def test_launch_shape_knobs_do_not_change_the_tree():
+    cfg, ts, tp, _ = depth_case(n_images=16, n_features=96, n_thresholds=20)
+    a = pg.Tree(cfg, 5, 7)
+    pg.TreeTrainer(cfg).train(a, ts, tp)
+    for chunk, spi in [(256, 4), (1000, 2), (65535, 4)]:
+        tr = pg.TreeTrainer(cfg)
+        tr.set_tuning("chunk", chunk)
+        tr.set_tuning("hist_spi", spi)
+        b = pg.Tree(cfg, 5, 7)
+        tr.train(b, ts, tp)
+        assert np.array_equal(a.left_child, b.left_child)
+        assert np.array_equal(a.features, b.features) and np.array_equal(a.thresholds, b.thresholds)
+        assert np.array_equal(a.posteriors, b.posteriors)
+    with pytest.raises(pg.PadentiError):
+        pg.TreeTrainer(cfg).set_tuning("hist_spi", 3)
+
+
 def test_train_tree_nine_classes_bit_exact():
     cfg, ts, tp, _ = depth_case(n_images=12, width=320, height=240, n_features=64, n_thresholds=50, parts=1,
                                 samples=1000)
