@@ -66,11 +66,13 @@ PD_HD void md5_block(const uint32_t in[4], uint32_t out[4]) {
 }
 
 // low + (feat_t)((float)r / (float)0xFFFFFFFF * (float)(up - low)), with the
-// narrowing of feat_t (kernels/hist_update.cl:94-111,150-151).
+// narrowing of feat_t (kernels/hist_update.cl:94-111,150-151).  (float)0xFFFFFFFF
+// is 2^32, and dividing a normal float by a power of two is exact, so the
+// quotient is computed as the (identical) product with 2^-32.
 template <typename FeatT>
 PD_HD FeatT draw(uint32_t r, int32_t lo, int32_t hi) {
   const float range = (float)(int32_t)((uint32_t)hi - (uint32_t)lo);
-  const float x = fmul(fdiv(u2f(r), 4294967296.0f), range);
+  const float x = fmul(fmul(u2f(r), 0x1p-32f), range);
   const FeatT delta = (FeatT)(int32_t)x;  // conversion toward zero
   return (FeatT)((int32_t)(FeatT)lo + (int32_t)delta);
 }

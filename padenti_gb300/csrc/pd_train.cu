@@ -107,7 +107,9 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
   using FeatT = typename P::feat_t;
   const uint64_t total = (uint64_t)n * p->n_features;
   if (!total) return PD_OK;
-  k_candidates<FeatT><<<(unsigned)((total + 127) / 128), 128, 0, ctx->stream>>>(
+  const size_t smem = (size_t)p->n_thresholds * kCandThreads * (sizeof(FeatT) + 1);
+  PD_CUDA(cudaFuncSetAttribute(k_candidates<FeatT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_candidates<FeatT><<<(unsigned)((total + kCandThreads - 1) / kCandThreads), kCandThreads, smem, ctx->stream>>>(
       d_nodes, n, tree, p->n_features, p->n_thresholds, P::kFeatDim, bounds(p, P::kFeatDim),
       ctx->cand_feat.as<FeatT>(), ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>());
   PD_CUDA(cudaGetLastError());

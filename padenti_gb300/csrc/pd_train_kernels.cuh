@@ -46,46 +46,56 @@ PD_D T max_of() {
 // ------------------------------------------------------ candidate table ----
 // Thread per (slot, candidate).  Thresholds are written sorted ascending with
 // their original index, so a response needs one binary search instead of T
-// comparisons and the split can prefix-sum the counts back.
-template <typename FeatT>
-__global__ void __launch_bounds__(128) k_candidates(const int32_t *__restrict__ nodes, uint32_t n_nodes,
-                                                    uint32_t tree, uint32_t F, uint32_t T, int D,
-                                                    CandBounds b, FeatT *__restrict__ feat,
-                                                    FeatT *__restrict__ thr_sorted,
-                                                    uint8_t *__restrict__ perm) {
-  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (uint64_t)n_nodes * F) return;
-  const uint32_t n = (uint32_t)(idx / F), f = (uint32_t)(idx % F);
-  const uint32_t node = (uint32_t)nodes[n];
-  FeatT fv[PD_MAX_FEAT_DIM];
-  candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
-  for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + f] = fv[d];
+// comparisons and the split can prefix-sum the counts back.  The insertion
+// sort runs in the thread's own shared-memory column (conflict-free), and the
+// sorted column is written out row by row, coalesced across candidates.
+constexpr int kCandThreads = 128;
 
-  FeatT v[PD_MAX_THRESHOLDS];
-  uint8_t id[PD_MAX_THRESHOLDS];
-  uint32_t seed[4] = {tree, node, f, 1u}, st[4] = {0u, 0u, 0u, 0u};
-  for (uint32_t t = 0; t < T; t++) {
-    if ((t & 3u) == 0) {
-      md5_block(seed, st);
-      seed[0] = st[0];
-      seed[1] = st[1];
-      seed[2] = st[2];
-      seed[3] = st[3];
+template <typename FeatT>
+__global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__restrict__ nodes, uint32_t n_nodes,
+                                                             uint32_t tree, uint32_t F, uint32_t T, int D,
+                                                             CandBounds b, FeatT *__restrict__ feat,
+                                                             FeatT *__restrict__ thr_sorted,
+                                                             uint8_t *__restrict__ perm) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FeatT *sv = reinterpret_cast<FeatT *>(smem_raw);                               // [T][128]
+  uint8_t *si = reinterpret_cast<uint8_t *>(sv + (size_t)T * kCandThreads);      // [T][128]
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = idx < (uint64_t)n_nodes * F;
+  const uint32_t n = active ? (uint32_t)(idx / F) : 0u, f = active ? (uint32_t)(idx % F) : 0u;
+  if (active) {
+    const uint32_t node = (uint32_t)nodes[n];
+    FeatT fv[PD_MAX_FEAT_DIM];
+    candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
+    for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + f] = fv[d];
+    FeatT *v = sv + threadIdx.x;
+    uint8_t *id = si + threadIdx.x;
+    uint32_t seed[4] = {tree, node, f, 1u}, st[4] = {0u, 0u, 0u, 0u};
+    for (uint32_t t = 0; t < T; t++) {
+      if ((t & 3u) == 0) {
+        md5_block(seed, st);
+        seed[0] = st[0];
+        seed[1] = st[1];
+        seed[2] = st[2];
+        seed[3] = st[3];
+      }
+      const FeatT x = draw<FeatT>(st[t & 3u], b.thr_lo, b.thr_hi);
+      // stable insertion
+      uint32_t j = t;
+      while (j > 0 && v[(j - 1) * kCandThreads] > x) {
+        v[j * kCandThreads] = v[(j - 1) * kCandThreads];
+        id[j * kCandThreads] = id[(j - 1) * kCandThreads];
+        j--;
+      }
+      v[j * kCandThreads] = x;
+      id[j * kCandThreads] = (uint8_t)t;
     }
-    const FeatT x = draw<FeatT>(st[t & 3u], b.thr_lo, b.thr_hi);
-    // stable insertion
-    uint32_t j = t;
-    while (j > 0 && v[j - 1] > x) {
-      v[j] = v[j - 1];
-      id[j] = id[j - 1];
-      j--;
-    }
-    v[j] = x;
-    id[j] = (uint8_t)t;
   }
+  __syncwarp();
+  if (!active) return;
   for (uint32_t j = 0; j < T; j++) {
-    thr_sorted[((size_t)n * T + j) * F + f] = v[j];
-    perm[((size_t)n * T + j) * F + f] = id[j];
+    thr_sorted[((size_t)n * T + j) * F + f] = sv[j * kCandThreads + threadIdx.x];
+    perm[((size_t)n * T + j) * F + f] = si[j * kCandThreads + threadIdx.x];
   }
 }
 
@@ -291,6 +301,7 @@ struct SplitPart {
 };
 
 constexpr int kSplitCols = 128;  // threads of a split CTA, one column each per pass
+constexpr int kSplitRows = 4;    // histogram rows loaded together in pass 1
 
 // Reference-formula FP32 entropy (kernels/learn_best_feature.cl:75-93) with the
 // p <= 1e-6 cutoff as the integer test 1e6*c <= n; fast intrinsics, error well
@@ -410,17 +421,42 @@ __global__ void __launch_bounds__(kSplitCols) k_split_g32(SplitArgs a) {
 #pragma unroll
     for (int l = 0; l < KM; l++) c[l] = 0u;
     float g = 0.0f;
-    for (uint32_t j = 0; j < T; j++) {
-      uint32_t nL;
-      const bool changed = step_counts<KM, CUM>(H, K, T, F, j, f, c, nL);
-      if (j == 0 || changed) {
-        const uint32_t nR = N - nL;
-        const float hl = ent32<KM, false>(tot, c, K, nL);
-        const float hr = ent32<KM, true>(tot, c, K, nR);
-        g = hp32 - ((float)nL * invN * hl + (float)nR * invN * hr);
+    // rows are loaded kSplitRows at a time so their loads are in flight together
+    for (uint32_t j0 = 0; j0 < T; j0 += kSplitRows) {
+      uint32_t h[kSplitRows][KM];
+#pragma unroll
+      for (int r = 0; r < kSplitRows; r++)
+#pragma unroll
+        for (int l = 0; l < KM; l++)
+          h[r][l] = ((uint32_t)l < K && j0 + r < T) ? H[((size_t)l * T + j0 + r) * F + f] : 0u;
+#pragma unroll
+      for (int r = 0; r < kSplitRows; r++) {
+        const uint32_t j = j0 + r;
+        if (j >= T) break;
+        bool changed = false;
+        uint32_t nL = 0;
+#pragma unroll
+        for (int l = 0; l < KM; l++) {
+          if ((uint32_t)l < K) {
+            if (CUM) {
+              changed |= h[r][l] != c[l];
+              c[l] = h[r][l];
+            } else {
+              changed |= h[r][l] != 0u;
+              c[l] += h[r][l];
+            }
+            nL += c[l];
+          }
+        }
+        if (j == 0 || changed) {
+          const uint32_t nR = N - nL;
+          const float hl = ent32<KM, false>(tot, c, K, nL);
+          const float hr = ent32<KM, true>(tot, c, K, nR);
+          g = hp32 - ((float)nL * invN * hl + (float)nR * invN * hr);
+        }
+        G[(size_t)j * F + f] = g;
+        lmax = fmaxf(lmax, g);
       }
-      G[(size_t)j * F + f] = g;
-      lmax = fmaxf(lmax, g);
     }
   }
   for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
