@@ -41,7 +41,7 @@ struct pd_ctx {
   pd::DevBuf cand_feat, cand_thr, cand_perm;
   pd::DevBuf hist, g32;
   pd::DevBuf items, zero_slots;
-  pd::DevBuf split_out, split_cl, recheck, split_scratch;
+  pd::DevBuf split_out, split_cl, recheck, split_scratch, fused_scratch;
   pd::DevBuf t_lc, t_feat, t_thr, t_post;  // device copy of the tree being trained
   pd_train_stats stats{};
 

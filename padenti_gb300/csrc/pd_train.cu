@@ -23,7 +23,8 @@ static uint32_t padded_rows(uint32_t T) {
 }
 
 static size_t hist_smem(const pd_ctx *ctx, uint32_t T) {
-  return (size_t)ctx->cfg.n_classes * T * 32 * 4 + (size_t)padded_rows(T) * kTileF * feat_size(ctx->cfg.feat_type);
+  return (size_t)ctx->cfg.n_classes * T * 32 * 4 + (size_t)padded_rows(T) * kTileF * feat_size(ctx->cfg.feat_type) +
+         (size_t)T * kTileF * 4;
 }
 
 static DevSet devset(const pd_ctx *ctx) {
@@ -120,9 +121,13 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
 // Builds the work list of slots [0, n) whose samples are act[off[i], off[i+1])
 // and launches the histogram kernel.
 template <class P>
+// With `split_slots` non-null, nodes whose samples fit one work item get their
+// split fused into the histogram kernel (multi = 2, rows never written) and the
+// other slots are returned for the split kernels.
 static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *off, uint32_t n,
                        const uint32_t *d_act, uint64_t *n_items_out, cudaEvent_t ev_before = nullptr,
-                       cudaEvent_t ev_after = nullptr) {
+                       cudaEvent_t ev_after = nullptr, std::vector<uint32_t> *split_slots = nullptr,
+                       const uint32_t *d_class_tot = nullptr) {
   using FeatT = typename P::feat_t;
   const uint32_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
   const uint32_t tiles = (F + kTileF - 1) / kTileF;
@@ -134,10 +139,13 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     const uint64_t cnt = e - b;
     if (!cnt) {
       zero.push_back(i);
+      if (split_slots) split_slots->push_back(i);
       continue;
     }
     const uint64_t chunks = (cnt + ctx->chunk - 1) / ctx->chunk;
     if (chunks > 1) zero.push_back(i);
+    const bool fused = split_slots && chunks == 1;
+    if (split_slots && !fused) split_slots->push_back(i);
     for (uint64_t c = 0; c < chunks; c++) {
       const uint32_t cb = (uint32_t)(b + c * ctx->chunk);
       const uint32_t ce = (uint32_t)std::min<uint64_t>(e, b + (c + 1) * ctx->chunk);
@@ -148,7 +156,7 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
         w.tile = t;
         w.begin = cb;
         w.end = ce;
-        w.multi = chunks > 1 ? 1u : 0u;
+        w.multi = chunks > 1 ? 1u : (fused ? 2u : 0u);
         items.push_back(w);
       }
     }
@@ -171,6 +179,24 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   }
   PD_CUDA(h2d(ctx, ctx->items.ptr, items.data(), items.size() * sizeof(WorkItem)));
   const size_t smem = hist_smem(ctx, T);
+  FusedSplit fs;
+  memset(&fs, 0, sizeof(fs));
+  if (split_slots) {
+    PD_TRY(ctx->fused_scratch.ensure((size_t)n * 4 + (size_t)n * tiles * (sizeof(SplitPart) + 4 * K) + 64));
+    fs.done = ctx->fused_scratch.as<unsigned>();
+    fs.part_best = reinterpret_cast<SplitPart *>(ctx->fused_scratch.as<uint8_t>() + ((size_t)n * 4 + 15) / 16 * 16);
+    fs.part_cl = reinterpret_cast<uint32_t *>(fs.part_best + (size_t)n * tiles);
+    PD_CUDA(cudaMemsetAsync(fs.done, 0, (size_t)n * 4, ctx->stream));
+    fs.class_tot = d_class_tot;
+    fs.perm = ctx->cand_perm.as<uint8_t>();
+    fs.L = ctx->log2_tab.as<double>();
+    fs.L_len = ctx->log2_len;
+    fs.delta = kRecheckDelta;
+    fs.tiles = tiles;
+    fs.out = ctx->split_out.as<SplitOut>();
+    fs.out_cl = ctx->split_cl.as<uint32_t>();
+    fs.rechecked = ctx->recheck.as<unsigned long long>();
+  }
   auto run = [&]<uint32_t TP>() -> int {
     auto kern = ctx->hist_spi >= 4 ? k_hist<P, TP, 4> : k_hist<P, TP, 2>;
     PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -180,7 +206,7 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
       const uint64_t cnt = std::min<uint64_t>(items.size() - b, 0x7fffffffull);
       kern<<<(unsigned)cnt, kHistThreads, smem, ctx->stream>>>(
           devset(ctx), d_act, ctx->items.as<WorkItem>() + b, ctx->cand_feat.as<FeatT>(),
-          ctx->cand_thr.as<FeatT>(), ctx->hist.as<uint32_t>(), F, T, K);
+          ctx->cand_thr.as<FeatT>(), ctx->hist.as<uint32_t>(), F, T, K, fs);
       PD_CUDA(cudaGetLastError());
       ctx->launches++;
     }
@@ -213,10 +239,14 @@ static uint64_t hist_algorithmic_bytes(const pd_ctx *ctx, const pd_train_params 
   return image_bytes + 9ull * n_samples + (uint64_t)n_slots * (K * T * F * 4 + T * F * fs + ctx->cfg.feat_dim * F * fs);
 }
 
+// Split kernels over n slots: slots[0..n) of the slice, or 0..n-1 when
+// d_slot_list is null.
 template <bool CUM>
 static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const uint32_t *d_hist,
-                        const uint8_t *d_perm, const uint32_t *d_class_tot) {
+                        const uint8_t *d_perm, const uint32_t *d_class_tot,
+                        const uint32_t *d_slot_list = nullptr, uint32_t slice_slots = 0) {
   if (!n) return PD_OK;
+  const uint32_t all = d_slot_list ? slice_slots : n;
   const uint32_t F = p->n_features;
   // Parts per node: enough CTAs to fill the GPU when the frontier is small.
   const uint32_t max_parts = (F + kSplitCols - 1) / kSplitCols;
@@ -224,9 +254,9 @@ static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const
   uint32_t cols = (F + parts - 1) / parts;
   cols = (cols + 31) / 32 * 32;
   parts = (F + cols - 1) / cols;
-  PD_TRY(ctx->split_scratch.ensure((size_t)n * 8 + (size_t)n * parts * sizeof(SplitPart) + 16));
+  PD_TRY(ctx->split_scratch.ensure((size_t)all * 8 + (size_t)all * parts * sizeof(SplitPart) + 16));
   unsigned *node_max = ctx->split_scratch.as<unsigned>();
-  PD_CUDA(cudaMemsetAsync(node_max, 0, (size_t)n * 8, ctx->stream));
+  PD_CUDA(cudaMemsetAsync(node_max, 0, (size_t)all * 8, ctx->stream));
   SplitArgs a;
   a.hist = d_hist;
   a.perm = d_perm;
@@ -241,8 +271,9 @@ static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const
   a.cols = cols;
   a.parts = parts;
   a.node_max = node_max;
-  a.done = node_max + n;
-  a.part_best = reinterpret_cast<SplitPart *>(ctx->split_scratch.as<uint8_t>() + (size_t)n * 8);
+  a.done = node_max + all;
+  a.part_best = reinterpret_cast<SplitPart *>(ctx->split_scratch.as<uint8_t>() + (size_t)all * 8);
+  a.slot_list = d_slot_list;
   a.out = ctx->split_out.as<SplitOut>();
   a.out_cl = ctx->split_cl.as<uint32_t>();
   a.rechecked = ctx->recheck.as<unsigned long long>();
@@ -324,7 +355,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   uint64_t n_act = S;
   const uint64_t per_slot = slot_bytes(ctx, p);
   const uint32_t max_slots = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ctx->hist_budget / per_slot, 1u << 30));
-  DevBuf d_nodes, d_ctot, d_next;
+  DevBuf d_nodes, d_ctot, d_next, d_split_list;
   std::vector<SplitOut> h_out;
   std::vector<uint32_t> h_cl;
   cudaEvent_t *ev = ctx->ev;
@@ -341,6 +372,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
     PD_TRY(ensure_slice(ctx, p, cap));
     PD_TRY(d_nodes.ensure((size_t)cap * 4));
     PD_TRY(d_ctot.ensure((size_t)cap * K * 4));
+    PD_TRY(d_split_list.ensure((size_t)cap * 4));
     std::vector<uint8_t> split_now(nf, 0);
 
     for (uint32_t s0 = 0; s0 < nf; s0 += cap) {
@@ -356,11 +388,16 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns));
       PD_CUDA(cudaEventRecord(ev[1], st));
       uint64_t n_items = 0;
-      PD_TRY(launch_hist<P>(ctx, p, off.data(), ns, ctx->act[cur].as<uint32_t>(), &n_items, ev[6], ev[2]));
+      std::vector<uint32_t> split_slots;
+      PD_TRY(launch_hist<P>(ctx, p, off.data(), ns, ctx->act[cur].as<uint32_t>(), &n_items, ev[6], ev[2],
+                            &split_slots, d_ctot.as<uint32_t>()));
       stats.hist_launches++;
       stats.hist_bytes += hist_algorithmic_bytes(ctx, p, off.back() - off.front(), ns, image_bytes);
-      PD_TRY(launch_split<false>(ctx, p, ns, ctx->hist.as<uint32_t>(), ctx->cand_perm.as<uint8_t>(),
-                                 d_ctot.as<uint32_t>()));
+      if (!split_slots.empty())
+        PD_CUDA(h2d(ctx, d_split_list.ptr, split_slots.data(), split_slots.size() * 4));
+      PD_TRY(launch_split<false>(ctx, p, (uint32_t)split_slots.size(), ctx->hist.as<uint32_t>(),
+                                 ctx->cand_perm.as<uint8_t>(), d_ctot.as<uint32_t>(), d_split_list.as<uint32_t>(),
+                                 ns));
       PD_CUDA(cudaEventRecord(ev[3], st));
       h_out.resize(ns);
       h_cl.resize((size_t)ns * K);

@@ -22,8 +22,10 @@ struct CandBounds {
 };
 
 // One histogram work item: candidates [tile*64, tile*64+64) of frontier slot
-// `slot` over the active samples act[begin, end) (end - begin <= 65535).  multi=1 when other work
-// items add into the same histogram rows.
+// `slot` over the active samples act[begin, end) (end - begin <= 65535).
+// multi = 0: the only work item of its rows, stores them; 1: other work items
+// add into the same rows (atomics); 2: the only work item of its rows, and the
+// node's split is fused into the kernel (no rows are written).
 struct WorkItem {
   uint32_t slot, tile, begin, end, multi, pad0, pad1, pad2;
 };
@@ -98,6 +100,84 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
     perm[((size_t)n * T + j) * F + f] = si[j * kCandThreads + threadIdx.x];
   }
 }
+
+// ---------------------------------------------------------------- split ----
+struct SplitOut {
+  int32_t t, f, j, pad;
+  double gain;
+};
+// Best candidate of one column range of one node.
+struct SplitPart {
+  double gain;
+  long long idx;  // t*F + f
+  int32_t j, pad;
+};
+
+constexpr int kSplitCols = 128;  // threads of a split CTA, one column each per pass
+constexpr int kSplitRows = 4;    // histogram rows loaded together in pass 1
+
+// Reference-formula FP32 entropy (kernels/learn_best_feature.cl:75-93) with the
+// p <= 1e-6 cutoff as the integer test 1e6*c <= n; fast intrinsics, error well
+// inside kRecheckDelta/2.
+template <int KM, bool RIGHT>
+PD_D float ent32(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n) {
+  if (n == 0) return 0.0f;
+  const float inv = __frcp_rn((float)n);
+  float s = 0.0f;
+#pragma unroll
+  for (int l = 0; l < KM; l++) {
+    if ((uint32_t)l < K) {
+      const uint32_t cl = RIGHT ? tot[l] - c[l] : c[l];
+      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
+        const float p = (float)cl * inv;
+        s -= p * __log2f(p);
+      }
+    }
+  }
+  return s;
+}
+// Exact n*entropy: sum over classes of c (log2 n - log2 c), one IEEE double
+// operation at a time with the shared log2 table (the oracle's sum64).
+template <int KM, bool RIGHT>
+PD_D double sum64(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n, const double *L) {
+  double s = 0.0;
+  if (n == 0) return s;
+  const double ln = L[n];
+#pragma unroll
+  for (int l = 0; l < KM; l++) {
+    if ((uint32_t)l < K) {
+      const uint32_t cl = RIGHT ? tot[l] - c[l] : c[l];
+      if (cl != 0u && (uint64_t)cl * 1000000ull > n) s = dadd(s, dmul((double)cl, dsub(ln, L[cl])));
+    }
+  }
+  return s;
+}
+
+struct SplitArgs {
+  const uint32_t *hist;       // [slots][K][T][F]: rank space, or cumulative when CUM
+  const uint8_t *perm;        // [slots][T][F] original threshold of sorted position (null: identity)
+  const uint32_t *class_tot;  // [slots][K]
+  float *g32;                 // scratch [slots][T][F]
+  const double *L;
+  uint64_t L_len;
+  uint32_t F, T, K;
+  float delta;
+  uint32_t cols;              // columns per part
+  uint32_t parts;             // parts per node
+  unsigned *node_max;         // [slots] order-preserving bits of the FP32 maximum
+  unsigned *done;             // [slots] finished parts
+  SplitPart *part_best;       // [slots][parts]
+  SplitOut *out;
+  uint32_t *out_cl;           // [slots][K] left class counts of the winner
+  unsigned long long *rechecked;
+  const uint32_t *slot_list;  // slots to process (null: blockIdx.y)
+};
+
+PD_D unsigned f2ord(float f) {
+  const unsigned b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+PD_D float ord2f(unsigned u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
 
 // ------------------------------------------------------------ histogram ----
 // Each CTA owns one (slot, 64-candidate tile, sample chunk).  Lane l evaluates
@@ -198,20 +278,222 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
   }
 }
 
+// Split of a node whose samples all went through one work item, fused into the
+// histogram CTA: the tile histogram (packed pairs of 16-bit counters) is
+// prefix-summed in place over the ranks, so word (l, j, lane) holds the left
+// counts of sorted position j; the FP32 gain of every (j, candidate) goes to
+// shared memory; every candidate within delta of the tile's own FP32 maximum is
+// re-evaluated with the exact FP64 gain.  The tile maximum is at most the node
+// maximum, so this set contains the node-wide recheck set and the node's
+// winner.  The last tile of the node to finish reduces the tiles.
+struct FusedSplit {
+  const uint32_t *class_tot;  // [slots][K]
+  const uint8_t *perm;        // [slots][T][F]
+  const double *L;
+  uint64_t L_len;
+  float delta;
+  uint32_t tiles;             // tiles per slot
+  SplitPart *part_best;       // [slots][tiles]
+  uint32_t *part_cl;          // [slots][tiles][K]
+  unsigned *done;             // [slots]
+  SplitOut *out;
+  uint32_t *out_cl;           // [slots][K]
+  unsigned long long *rechecked;
+};
+
+PD_D uint32_t half16(uint32_t word, uint32_t c) { return (word >> ((c >> 5) * 16)) & 0xffffu; }
+
+PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist, float *sh_g, uint32_t F,
+                      uint32_t T, uint32_t K) {
+  __shared__ uint32_t s_tot[PD_MAX_CLASSES];
+  __shared__ float s_red[kHistThreads / 32];
+  __shared__ double s_g[kHistThreads / 32];
+  __shared__ long long s_i[kHistThreads / 32];
+  __shared__ int s_j[kHistThreads / 32];
+  __shared__ bool s_last;
+  const uint32_t slot = w.slot, f0 = w.tile * kTileF;
+  for (uint32_t l = threadIdx.x; l < K; l += blockDim.x) s_tot[l] = fs.class_tot[(size_t)slot * K + l];
+  // in-place prefix over the ranks of each (class, packed column)
+  for (uint32_t q = threadIdx.x; q < K * 32; q += blockDim.x) {
+    const uint32_t l = q >> 5, col = q & 31;
+    uint32_t run = 0;
+    for (uint32_t j = 0; j < T; j++) {
+      run += sh_hist[(l * T + j) * 32 + col];
+      sh_hist[(l * T + j) * 32 + col] = run;
+    }
+  }
+  __syncthreads();
+  uint32_t N = 0;
+  for (uint32_t l = 0; l < K; l++) N += s_tot[l];
+  const bool ok = N != 0 && (uint64_t)N < fs.L_len;
+  const uint32_t pairs = T * kTileF;
+  // FP32 gains (reference formula, learn_best_feature.cl:75-93) and the tile maximum
+  float lmax = -FLT_MAX;
+  if (ok) {
+    float hp = 0.0f;
+    {
+      const float inv = __frcp_rn((float)N);
+      for (uint32_t l = 0; l < K; l++) {
+        const uint32_t cl = s_tot[l];
+        if (cl != 0u && (uint64_t)cl * 1000000ull > N) {
+          const float p = (float)cl * inv;
+          hp -= p * __log2f(p);
+        }
+      }
+    }
+    const float invN = __frcp_rn((float)N);
+    for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
+      const uint32_t j = q / kTileF, c = q % kTileF;
+      float g = -FLT_MAX;
+      if (f0 + c < F) {
+        uint32_t nL = 0;
+        for (uint32_t l = 0; l < K; l++) nL += half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
+        const uint32_t nR = N - nL;
+        const float iL = nL ? __frcp_rn((float)nL) : 0.0f, iR = nR ? __frcp_rn((float)nR) : 0.0f;
+        float hl = 0.0f, hr = 0.0f;
+        for (uint32_t l = 0; l < K; l++) {
+          const uint32_t cl = half16(sh_hist[(l * T + j) * 32 + (c & 31)], c), cr = s_tot[l] - cl;
+          if (cl != 0u && (uint64_t)cl * 1000000ull > nL) {
+            const float p = (float)cl * iL;
+            hl -= p * __log2f(p);
+          }
+          if (cr != 0u && (uint64_t)cr * 1000000ull > nR) {
+            const float p = (float)cr * iR;
+            hr -= p * __log2f(p);
+          }
+        }
+        g = hp - ((float)nL * invN * hl + (float)nR * invN * hr);
+      }
+      sh_g[q] = g;
+      lmax = fmaxf(lmax, g);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = lmax;
+  __syncthreads();
+  float tmax = s_red[0];
+  for (int i = 1; i < kHistThreads / 32; i++) tmax = fmaxf(tmax, s_red[i]);
+  const float cut = tmax - fs.delta;
+  // exact FP64 gains of the near-maximum candidates
+  double best = -DBL_MAX;
+  long long best_idx = LLONG_MAX;
+  int best_j = -1;
+  unsigned long long n_checked = 0;
+  if (ok) {
+    const double *L = fs.L;
+    double hp64 = 0.0;
+    for (uint32_t l = 0; l < K; l++) {
+      const uint32_t cl = s_tot[l];
+      if (cl != 0u && (uint64_t)cl * 1000000ull > N) hp64 = dadd(hp64, dmul((double)cl, dsub(L[N], L[cl])));
+    }
+    hp64 = ddiv(hp64, (double)N);
+    for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
+      if (!(sh_g[q] >= cut)) continue;
+      const uint32_t j = q / kTileF, c = q % kTileF;
+      n_checked++;
+      uint32_t nL = 0;
+      for (uint32_t l = 0; l < K; l++) nL += half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
+      const uint32_t nR = N - nL;
+      double sl = 0.0, sr = 0.0;
+      for (uint32_t l = 0; l < K; l++) {
+        const uint32_t cl = half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
+        if (cl != 0u && (uint64_t)cl * 1000000ull > nL) sl = dadd(sl, dmul((double)cl, dsub(L[nL], L[cl])));
+      }
+      for (uint32_t l = 0; l < K; l++) {
+        const uint32_t cr = s_tot[l] - half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
+        if (cr != 0u && (uint64_t)cr * 1000000ull > nR) sr = dadd(sr, dmul((double)cr, dsub(L[nR], L[cr])));
+      }
+      const double g = dsub(hp64, ddiv(dadd(sl, sr), (double)N));
+      const uint32_t f = f0 + c;
+      const uint32_t t = fs.perm[((size_t)slot * T + j) * F + f];
+      const long long idx = (long long)t * F + f;
+      if (g > best || (g == best && idx < best_idx)) {
+        best = g;
+        best_idx = idx;
+        best_j = (int)j;
+      }
+    }
+  }
+  if (n_checked) atomicAdd(fs.rechecked, n_checked);
+  for (int o = 16; o > 0; o >>= 1) {
+    const double og = __shfl_xor_sync(0xffffffffu, best, o);
+    const long long oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
+    const int oj = __shfl_xor_sync(0xffffffffu, best_j, o);
+    if (og > best || (og == best && oi < best_idx)) {
+      best = og;
+      best_idx = oi;
+      best_j = oj;
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_g[threadIdx.x >> 5] = best;
+    s_i[threadIdx.x >> 5] = best_idx;
+    s_j[threadIdx.x >> 5] = best_j;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < kHistThreads / 32; i++) {
+      if (s_g[i] > s_g[0] || (s_g[i] == s_g[0] && s_i[i] < s_i[0])) {
+        s_g[0] = s_g[i];
+        s_i[0] = s_i[i];
+        s_j[0] = s_j[i];
+      }
+    }
+    SplitPart pb;
+    pb.gain = s_g[0];
+    pb.idx = s_i[0];
+    pb.j = s_j[0];
+    pb.pad = 0;
+    const size_t pi = (size_t)slot * fs.tiles + w.tile;
+    fs.part_best[pi] = pb;
+    if (pb.idx != LLONG_MAX) {
+      const uint32_t c = (uint32_t)(pb.idx % F) - f0;
+      for (uint32_t l = 0; l < K; l++) fs.part_cl[pi * K + l] = half16(sh_hist[(l * T + pb.j) * 32 + (c & 31)], c);
+    }
+    __threadfence();
+    s_last = atomicAdd(fs.done + slot, 1u) == fs.tiles - 1;
+  }
+  __syncthreads();
+  if (!s_last || threadIdx.x != 0) return;
+  __threadfence();
+  size_t bi = (size_t)slot * fs.tiles;
+  SplitPart b = fs.part_best[bi];
+  for (uint32_t i = 1; i < fs.tiles; i++) {
+    const SplitPart q = fs.part_best[(size_t)slot * fs.tiles + i];
+    if (q.gain > b.gain || (q.gain == b.gain && q.idx < b.idx)) {
+      b = q;
+      bi = (size_t)slot * fs.tiles + i;
+    }
+  }
+  SplitOut o;
+  o.pad = 0;
+  if (b.idx == LLONG_MAX) {
+    o.t = o.f = o.j = -1;
+    o.gain = 0.0;
+  } else {
+    o.t = (int32_t)(b.idx / F);
+    o.f = (int32_t)(b.idx % F);
+    o.j = b.j;
+    o.gain = b.gain;
+    for (uint32_t l = 0; l < K; l++) fs.out_cl[(size_t)slot * K + l] = fs.part_cl[bi * K + l];
+  }
+  fs.out[slot] = o;
+}
+
 template <class P, uint32_t TP, int SPI>
 __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet ds, const uint32_t *__restrict__ act,
                                                        const WorkItem *__restrict__ items,
                                                        const typename P::feat_t *__restrict__ cand_feat,
                                                        const typename P::feat_t *__restrict__ cand_thr,
                                                        uint32_t *__restrict__ hist, uint32_t F,
-                                                       uint32_t T, uint32_t K) {
+                                                       uint32_t T, uint32_t K, FusedSplit fs) {
   using FeatT = typename P::feat_t;
   using ImgT = typename P::img_t;
   constexpr int D = P::kFeatDim;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);             // [K][T][32] packed
   FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32);  // [TP][64]
-
+  float *sh_g = reinterpret_cast<float *>(sh_thr + (size_t)TP * kTileF);   // [T][64] fused split
   const WorkItem w = items[blockIdx.x];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t f0 = w.tile * kTileF;
@@ -240,6 +522,10 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   else hist_samples<P, TP, false, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, va, vb);
 
   __syncthreads();
+  if (w.multi == 2) {
+    fused_split(fs, w, sh_hist, sh_g, F, T, K);
+    return;
+  }
   for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) {
     const uint32_t v = sh_hist[j];
     const uint32_t l = j & 31;
@@ -288,83 +574,6 @@ __global__ void k_hist_to_ref(const uint32_t *__restrict__ rank_hist, const uint
   }
 }
 
-// ---------------------------------------------------------------- split ----
-struct SplitOut {
-  int32_t t, f, j, pad;
-  double gain;
-};
-// Best candidate of one column range of one node.
-struct SplitPart {
-  double gain;
-  long long idx;  // t*F + f
-  int32_t j, pad;
-};
-
-constexpr int kSplitCols = 128;  // threads of a split CTA, one column each per pass
-constexpr int kSplitRows = 4;    // histogram rows loaded together in pass 1
-
-// Reference-formula FP32 entropy (kernels/learn_best_feature.cl:75-93) with the
-// p <= 1e-6 cutoff as the integer test 1e6*c <= n; fast intrinsics, error well
-// inside kRecheckDelta/2.
-template <int KM, bool RIGHT>
-PD_D float ent32(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n) {
-  if (n == 0) return 0.0f;
-  const float inv = __frcp_rn((float)n);
-  float s = 0.0f;
-#pragma unroll
-  for (int l = 0; l < KM; l++) {
-    if ((uint32_t)l < K) {
-      const uint32_t cl = RIGHT ? tot[l] - c[l] : c[l];
-      if (cl != 0u && (uint64_t)cl * 1000000ull > n) {
-        const float p = (float)cl * inv;
-        s -= p * __log2f(p);
-      }
-    }
-  }
-  return s;
-}
-// Exact n*entropy: sum over classes of c (log2 n - log2 c), one IEEE double
-// operation at a time with the shared log2 table (the oracle's sum64).
-template <int KM, bool RIGHT>
-PD_D double sum64(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n, const double *L) {
-  double s = 0.0;
-  if (n == 0) return s;
-  const double ln = L[n];
-#pragma unroll
-  for (int l = 0; l < KM; l++) {
-    if ((uint32_t)l < K) {
-      const uint32_t cl = RIGHT ? tot[l] - c[l] : c[l];
-      if (cl != 0u && (uint64_t)cl * 1000000ull > n) s = dadd(s, dmul((double)cl, dsub(ln, L[cl])));
-    }
-  }
-  return s;
-}
-
-struct SplitArgs {
-  const uint32_t *hist;       // [slots][K][T][F]: rank space, or cumulative when CUM
-  const uint8_t *perm;        // [slots][T][F] original threshold of sorted position (null: identity)
-  const uint32_t *class_tot;  // [slots][K]
-  float *g32;                 // scratch [slots][T][F]
-  const double *L;
-  uint64_t L_len;
-  uint32_t F, T, K;
-  float delta;
-  uint32_t cols;              // columns per part
-  uint32_t parts;             // parts per node
-  unsigned *node_max;         // [slots] order-preserving bits of the FP32 maximum
-  unsigned *done;             // [slots] finished parts
-  SplitPart *part_best;       // [slots][parts]
-  SplitOut *out;
-  uint32_t *out_cl;           // [slots][K] left class counts of the winner
-  unsigned long long *rechecked;
-};
-
-PD_D unsigned f2ord(float f) {
-  const unsigned b = __float_as_uint(f);
-  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
-PD_D float ord2f(unsigned u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
-
 // Loads the counts of sorted position j of column f into c (prefix-summed in
 // rank space, copied when cumulative); returns whether they changed.
 template <int KM, bool CUM>
@@ -403,7 +612,7 @@ PD_D void load_tot(const SplitArgs &a, uint32_t slot, uint32_t *tot, uint32_t &N
 // rank bin is empty has the counts, hence the gain, of the previous one.
 template <int KM, bool CUM>
 __global__ void __launch_bounds__(kSplitCols) k_split_g32(SplitArgs a) {
-  const uint32_t slot = blockIdx.y, part = blockIdx.x;
+  const uint32_t slot = a.slot_list ? a.slot_list[blockIdx.y] : blockIdx.y, part = blockIdx.x;
   const uint32_t F = a.F, T = a.T, K = a.K;
   __shared__ uint32_t tot[KM];
   __shared__ float red[kSplitCols / 32];
@@ -476,7 +685,7 @@ __global__ void __launch_bounds__(kSplitCols) k_split_g32(SplitArgs a) {
 // finish reduces the parts and writes the winner with its left class counts.
 template <int KM, bool CUM>
 __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
-  const uint32_t slot = blockIdx.y, part = blockIdx.x;
+  const uint32_t slot = a.slot_list ? a.slot_list[blockIdx.y] : blockIdx.y, part = blockIdx.x;
   const uint32_t F = a.F, T = a.T, K = a.K;
   __shared__ uint32_t tot[KM];
   __shared__ double red_g[kSplitCols / 32];
