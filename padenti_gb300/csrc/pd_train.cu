@@ -191,7 +191,7 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     fs.perm = ctx->cand_perm.as<uint8_t>();
     fs.L = ctx->log2_tab.as<double>();
     fs.L_len = ctx->log2_len;
-    fs.delta = kRecheckDelta;
+    fs.delta = recheck_delta(K);
     fs.tiles = tiles;
     fs.out = ctx->split_out.as<SplitOut>();
     fs.out_cl = ctx->split_cl.as<uint32_t>();
@@ -267,7 +267,7 @@ static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const
   a.F = F;
   a.T = p->n_thresholds;
   a.K = ctx->cfg.n_classes;
-  a.delta = kRecheckDelta;
+  a.delta = recheck_delta(ctx->cfg.n_classes);
   a.cols = cols;
   a.parts = parts;
   a.node_max = node_max;

@@ -13,7 +13,12 @@ namespace pd {
 
 constexpr int kHistThreads = 256;  // 8 warps, each on its own samples
 constexpr int kScanItems = 4096;   // active samples per scan block (256 threads x 16)
-constexpr float kRecheckDelta = 5e-4f;  // FP32 gain window rechecked in FP64
+// FP32 gain window rechecked in FP64.  Each FP32 entropy term -p log2 p (fast
+// reciprocal and log2) is within about 2e-7 of its exact value and each of the
+// ~K additions of an entropy adds at most 2.4e-7, so |gain32 - gain64| stays
+// below eps(K) = (3K + 3) * 4.4e-7; a candidate within 2*eps of the FP32 maximum
+// can be the exact winner.  The window is 4.5x that.
+PD_HD float recheck_delta(uint32_t K) { return (3.0f * (float)K + 3.0f) * 4.0e-6f; }
 
 struct CandBounds {
   int32_t low[PD_MAX_FEAT_DIM];
@@ -118,7 +123,7 @@ constexpr int kSplitRows = 4;    // histogram rows loaded together in pass 1
 
 // Reference-formula FP32 entropy (kernels/learn_best_feature.cl:75-93) with the
 // p <= 1e-6 cutoff as the integer test 1e6*c <= n; fast intrinsics, error well
-// inside kRecheckDelta/2.
+// inside recheck_delta(K)/2.
 template <int KM, bool RIGHT>
 PD_D float ent32(const uint32_t *tot, const uint32_t *c, uint32_t K, uint32_t n) {
   if (n == 0) return 0.0f;
@@ -303,6 +308,13 @@ struct FusedSplit {
 
 PD_D uint32_t half16(uint32_t word, uint32_t c) { return (word >> ((c >> 5) * 16)) & 0xffffu; }
 
+// Left total of candidate c at sorted position j from the prefixed tile.
+PD_D uint32_t left_total(const uint32_t *sh_hist, uint32_t K, uint32_t T, uint32_t j, uint32_t c) {
+  uint32_t n = 0;
+  for (uint32_t l = 0; l < K; l++) n += half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
+  return n;
+}
+
 PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist, float *sh_g, uint32_t F,
                       uint32_t T, uint32_t K) {
   __shared__ uint32_t s_tot[PD_MAX_CLASSES];
@@ -344,25 +356,27 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     const float invN = __frcp_rn((float)N);
     for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
       const uint32_t j = q / kTileF, c = q % kTileF;
-      float g = -FLT_MAX;
+      float g = -FLT_MAX;  // duplicates of the previous position stay -max
       if (f0 + c < F) {
-        uint32_t nL = 0;
-        for (uint32_t l = 0; l < K; l++) nL += half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
-        const uint32_t nR = N - nL;
-        const float iL = nL ? __frcp_rn((float)nL) : 0.0f, iR = nR ? __frcp_rn((float)nR) : 0.0f;
-        float hl = 0.0f, hr = 0.0f;
-        for (uint32_t l = 0; l < K; l++) {
-          const uint32_t cl = half16(sh_hist[(l * T + j) * 32 + (c & 31)], c), cr = s_tot[l] - cl;
-          if (cl != 0u && (uint64_t)cl * 1000000ull > nL) {
-            const float p = (float)cl * iL;
-            hl -= p * __log2f(p);
+        const uint32_t nL = left_total(sh_hist, K, T, j, c);
+        // counts are monotone in j: an equal total means equal counts
+        if (j == 0 || left_total(sh_hist, K, T, j - 1, c) != nL) {
+          const uint32_t nR = N - nL;
+          const float iL = nL ? __frcp_rn((float)nL) : 0.0f, iR = nR ? __frcp_rn((float)nR) : 0.0f;
+          float hl = 0.0f, hr = 0.0f;
+          for (uint32_t l = 0; l < K; l++) {
+            const uint32_t cl = half16(sh_hist[(l * T + j) * 32 + (c & 31)], c), cr = s_tot[l] - cl;
+            if (cl != 0u && (uint64_t)cl * 1000000ull > nL) {
+              const float p = (float)cl * iL;
+              hl -= p * __log2f(p);
+            }
+            if (cr != 0u && (uint64_t)cr * 1000000ull > nR) {
+              const float p = (float)cr * iR;
+              hr -= p * __log2f(p);
+            }
           }
-          if (cr != 0u && (uint64_t)cr * 1000000ull > nR) {
-            const float p = (float)cr * iR;
-            hr -= p * __log2f(p);
-          }
+          g = hp - ((float)nL * invN * hl + (float)nR * invN * hr);
         }
-        g = hp - ((float)nL * invN * hl + (float)nR * invN * hr);
       }
       sh_g[q] = g;
       lmax = fmaxf(lmax, g);
@@ -388,11 +402,10 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     }
     hp64 = ddiv(hp64, (double)N);
     for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
-      if (!(sh_g[q] >= cut)) continue;
+      if (!(sh_g[q] >= cut)) continue;  // below the window, or a duplicate position
       const uint32_t j = q / kTileF, c = q % kTileF;
       n_checked++;
-      uint32_t nL = 0;
-      for (uint32_t l = 0; l < K; l++) nL += half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
+      const uint32_t nL = left_total(sh_hist, K, T, j, c);
       const uint32_t nR = N - nL;
       double sl = 0.0, sr = 0.0;
       for (uint32_t l = 0; l < K; l++) {
@@ -405,7 +418,10 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
       }
       const double g = dsub(hp64, ddiv(dadd(sl, sr), (double)N));
       const uint32_t f = f0 + c;
-      const uint32_t t = fs.perm[((size_t)slot * T + j) * F + f];
+      // the positions j..je share these counts: the lowest original threshold wins
+      uint32_t t = fs.perm[((size_t)slot * T + j) * F + f];
+      for (uint32_t je = j + 1; je < T && left_total(sh_hist, K, T, je, c) == nL; je++)
+        t = min(t, (uint32_t)fs.perm[((size_t)slot * T + je) * F + f]);
       const long long idx = (long long)t * F + f;
       if (g > best || (g == best && idx < best_idx)) {
         best = g;

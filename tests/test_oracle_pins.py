@@ -119,7 +119,8 @@ def test_split_agrees_with_reference_kernel(K, T, F):
         agree += (rt, rf) == (int(t[i]), int(f[i]))
     # distinct random histograms: the FP32 and exact winners coincide except at FP32 near-ties
     assert agree >= n - 2
-    assert err < 5e-5
+    # the FP32 error bound the CUDA split sizes its FP64 recheck window from
+    assert err < (3 * K + 3) * 4.4e-7
 
 
 def test_split_ties_lowest_index_and_empty():
