@@ -58,6 +58,7 @@ def args_():
     a.add_argument("--seed", type=int, default=0)
     a.add_argument("--chunk", type=int, default=None, help="histogram work-item size (samples)")
     a.add_argument("--spi", type=int, default=None, help="samples per histogram-kernel iteration (2 or 4)")
+    a.add_argument("--fuse-max", type=int, default=None, help="largest node (samples) with the fused split")
     return a.parse_args()
 
 
@@ -246,6 +247,8 @@ def run_ours(a):
         tr.set_tuning("chunk", a.chunk)
     if a.spi:
         tr.set_tuning("hist_spi", a.spi)
+    if a.fuse_max is not None:
+        tr.set_tuning("fuse_max", a.fuse_max)
     tr.upload(ts)
     stream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(tr.h))
 

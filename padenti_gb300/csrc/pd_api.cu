@@ -107,6 +107,9 @@ extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
   } else if (n == "hist_spi") {
     PD_CHECK(value == 2 || value == 4, PD_ERR_INVALID, "hist_spi must be 2 or 4");
     ctx->hist_spi = (uint32_t)value;
+  } else if (n == "fuse_max") {
+    PD_CHECK(value >= 0 && value <= 65535, PD_ERR_INVALID, "fuse_max %lld outside [0,65535]", (long long)value);
+    ctx->fuse_max = (uint32_t)value;
   } else {
     return set_error(PD_ERR_INVALID, "unknown tuning knob '%s'", name);
   }

@@ -13,6 +13,7 @@ struct pd_ctx {
   uint64_t hist_budget = 8ull << 30;
   uint32_t chunk = 4096;  // samples per histogram work item (at most 65535)
   uint32_t hist_spi = 4;  // samples per iteration of the histogram kernel (2 or 4)
+  uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
 
   // ---- training set in HBM (cl_tree_trainer_impl_init.hpp:99-154 streams it
   // image by image; here it stays resident) ----

@@ -24,7 +24,7 @@ static uint32_t padded_rows(uint32_t T) {
 
 static size_t hist_smem(const pd_ctx *ctx, uint32_t T) {
   return (size_t)ctx->cfg.n_classes * T * 32 * 4 + (size_t)padded_rows(T) * kTileF * feat_size(ctx->cfg.feat_type) +
-         (size_t)T * kTileF * 4;
+         (size_t)T * kTileF * 4 + (size_t)T * 32 * 4;
 }
 
 static DevSet devset(const pd_ctx *ctx) {
@@ -144,7 +144,7 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     }
     const uint64_t chunks = (cnt + ctx->chunk - 1) / ctx->chunk;
     if (chunks > 1) zero.push_back(i);
-    const bool fused = split_slots && chunks == 1;
+    const bool fused = split_slots && chunks == 1 && cnt <= ctx->fuse_max;
     if (split_slots && !fused) split_slots->push_back(i);
     for (uint64_t c = 0; c < chunks; c++) {
       const uint32_t cb = (uint32_t)(b + c * ctx->chunk);

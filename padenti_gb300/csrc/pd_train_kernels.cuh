@@ -308,15 +308,9 @@ struct FusedSplit {
 
 PD_D uint32_t half16(uint32_t word, uint32_t c) { return (word >> ((c >> 5) * 16)) & 0xffffu; }
 
-// Left total of candidate c at sorted position j from the prefixed tile.
-PD_D uint32_t left_total(const uint32_t *sh_hist, uint32_t K, uint32_t T, uint32_t j, uint32_t c) {
-  uint32_t n = 0;
-  for (uint32_t l = 0; l < K; l++) n += half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
-  return n;
-}
 
-PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist, float *sh_g, uint32_t F,
-                      uint32_t T, uint32_t K) {
+PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist, float *sh_g, uint32_t *sh_nl,
+                      uint32_t F, uint32_t T, uint32_t K) {
   __shared__ uint32_t s_tot[PD_MAX_CLASSES];
   __shared__ float s_red[kHistThreads / 32];
   __shared__ double s_g[kHistThreads / 32];
@@ -333,6 +327,14 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
       run += sh_hist[(l * T + j) * 32 + col];
       sh_hist[(l * T + j) * 32 + col] = run;
     }
+  }
+  __syncthreads();
+  // packed left totals of every (position, column pair)
+  for (uint32_t q = threadIdx.x; q < T * 32; q += blockDim.x) {
+    const uint32_t j = q >> 5, col = q & 31;
+    uint32_t n = 0;
+    for (uint32_t l = 0; l < K; l++) n += sh_hist[(l * T + j) * 32 + col];
+    sh_nl[q] = n;
   }
   __syncthreads();
   uint32_t N = 0;
@@ -358,9 +360,9 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
       const uint32_t j = q / kTileF, c = q % kTileF;
       float g = -FLT_MAX;  // duplicates of the previous position stay -max
       if (f0 + c < F) {
-        const uint32_t nL = left_total(sh_hist, K, T, j, c);
+        const uint32_t nL = half16(sh_nl[j * 32 + (c & 31)], c);
         // counts are monotone in j: an equal total means equal counts
-        if (j == 0 || left_total(sh_hist, K, T, j - 1, c) != nL) {
+        if (j == 0 || half16(sh_nl[(j - 1) * 32 + (c & 31)], c) != nL) {
           const uint32_t nR = N - nL;
           const float iL = nL ? __frcp_rn((float)nL) : 0.0f, iR = nR ? __frcp_rn((float)nR) : 0.0f;
           float hl = 0.0f, hr = 0.0f;
@@ -405,7 +407,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
       if (!(sh_g[q] >= cut)) continue;  // below the window, or a duplicate position
       const uint32_t j = q / kTileF, c = q % kTileF;
       n_checked++;
-      const uint32_t nL = left_total(sh_hist, K, T, j, c);
+      const uint32_t nL = half16(sh_nl[j * 32 + (c & 31)], c);
       const uint32_t nR = N - nL;
       double sl = 0.0, sr = 0.0;
       for (uint32_t l = 0; l < K; l++) {
@@ -420,7 +422,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
       const uint32_t f = f0 + c;
       // the positions j..je share these counts: the lowest original threshold wins
       uint32_t t = fs.perm[((size_t)slot * T + j) * F + f];
-      for (uint32_t je = j + 1; je < T && left_total(sh_hist, K, T, je, c) == nL; je++)
+      for (uint32_t je = j + 1; je < T && half16(sh_nl[je * 32 + (c & 31)], c) == nL; je++)
         t = min(t, (uint32_t)fs.perm[((size_t)slot * T + je) * F + f]);
       const long long idx = (long long)t * F + f;
       if (g > best || (g == best && idx < best_idx)) {
@@ -510,6 +512,7 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);             // [K][T][32] packed
   FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32);  // [TP][64]
   float *sh_g = reinterpret_cast<float *>(sh_thr + (size_t)TP * kTileF);   // [T][64] fused split
+  uint32_t *sh_nl = reinterpret_cast<uint32_t *>(sh_g + (size_t)T * kTileF); // [T][32] fused split
   const WorkItem w = items[blockIdx.x];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t f0 = w.tile * kTileF;
@@ -539,7 +542,7 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
 
   __syncthreads();
   if (w.multi == 2) {
-    fused_split(fs, w, sh_hist, sh_g, F, T, K);
+    fused_split(fs, w, sh_hist, sh_g, sh_nl, F, T, K);
     return;
   }
   for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) {

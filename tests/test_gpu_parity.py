@@ -149,10 +149,11 @@ def test_launch_shape_knobs_do_not_change_the_tree():
     cfg, ts, tp, _ = depth_case(n_images=16, n_features=96, n_thresholds=20)
     a = pg.Tree(cfg, 5, 7)
     pg.TreeTrainer(cfg).train(a, ts, tp)
-    for chunk, spi in [(256, 4), (1000, 2), (65535, 4)]:
+    for chunk, spi, fuse in [(256, 4, 0), (1000, 2, 300), (65535, 4, 65535), (4096, 4, 0)]:
         tr = pg.TreeTrainer(cfg)
         tr.set_tuning("chunk", chunk)
         tr.set_tuning("hist_spi", spi)
+        tr.set_tuning("fuse_max", fuse)
         b = pg.Tree(cfg, 5, 7)
         tr.train(b, ts, tp)
         assert np.array_equal(a.left_child, b.left_child)
