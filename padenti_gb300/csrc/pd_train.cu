@@ -22,9 +22,14 @@ static uint32_t padded_rows(uint32_t T) {
   return p;
 }
 
-static size_t hist_smem(const pd_ctx *ctx, uint32_t T) {
-  return (size_t)ctx->cfg.n_classes * T * 32 * 4 + (size_t)padded_rows(T) * kTileF * feat_size(ctx->cfg.feat_type) +
-         (size_t)T * kTileF * 4 + (size_t)T * 32 * 4;
+// Shared memory of a histogram launch: packed tile histogram, threshold table
+// and, when the launch has fused-split items, the larger of the table and the
+// fused scratch (gains + packed left totals) that overlays it.
+static size_t hist_smem(const pd_ctx *ctx, uint32_t T, bool fused = true) {
+  const size_t hist = (size_t)ctx->cfg.n_classes * T * 32 * 4;
+  const size_t thr = (size_t)padded_rows(T) * kTileF * feat_size(ctx->cfg.feat_type);
+  const size_t scratch = (size_t)T * kTileF * 4 + (size_t)T * 32 * 4;
+  return hist + (fused ? std::max(thr, scratch) : thr);
 }
 
 static DevSet devset(const pd_ctx *ctx) {
@@ -178,7 +183,9 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     return PD_OK;
   }
   PD_CUDA(h2d(ctx, ctx->items.ptr, items.data(), items.size() * sizeof(WorkItem)));
-  const size_t smem = hist_smem(ctx, T);
+  bool any_fused = false;
+  for (const WorkItem &w : items) any_fused |= w.multi == 2;
+  const size_t smem = hist_smem(ctx, T, any_fused);
   FusedSplit fs;
   memset(&fs, 0, sizeof(fs));
   if (split_slots) {
@@ -200,6 +207,12 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   auto run = [&]<uint32_t TP>() -> int {
     auto kern = ctx->hist_spi >= 4 ? k_hist<P, TP, 4> : k_hist<P, TP, 2>;
     PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // carve out only the shared memory the resident CTAs need; the rest stays L1
+    // for the probe gathers (resident CTAs are register-limited: 2 at 4 samples
+    // per iteration, 3 at 2)
+    const int resident = ctx->hist_spi >= 4 ? 2 : 3;
+    const int pct = (int)std::min<size_t>(100, (resident * (smem + 1024) * 100 + 233471) / 233472);
+    PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
     if (ev_before) PD_CUDA(cudaEventRecord(ev_before, ctx->stream));
     // The grid is the work list; the hardware scheduler keeps every SM full.
     for (uint64_t b = 0; b < items.size(); b += 0x7fffffffull) {

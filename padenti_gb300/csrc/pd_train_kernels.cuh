@@ -511,8 +511,10 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);             // [K][T][32] packed
   FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32);  // [TP][64]
-  float *sh_g = reinterpret_cast<float *>(sh_thr + (size_t)TP * kTileF);   // [T][64] fused split
-  uint32_t *sh_nl = reinterpret_cast<uint32_t *>(sh_g + (size_t)T * kTileF); // [T][32] fused split
+  // fused split scratch, over the threshold table (dead after the sample loop):
+  // sh_g [T][64] gains, sh_nl [T][32] packed left totals
+  float *sh_g = reinterpret_cast<float *>(sh_thr);
+  uint32_t *sh_nl = reinterpret_cast<uint32_t *>(sh_g + (size_t)T * kTileF);
   const WorkItem w = items[blockIdx.x];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t f0 = w.tile * kTileF;
