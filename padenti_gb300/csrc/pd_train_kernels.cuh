@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   }
 }
 
-__global__ void k_zero_slots(uint32_t *__restrict__ hist, const uint32_t *__restrict__ slots, uint32_t n,
+static __global__ void k_zero_slots(uint32_t *__restrict__ hist, const uint32_t *__restrict__ slots, uint32_t n,
                              uint64_t per_slot) {
   const uint64_t total = (uint64_t)n * per_slot;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
@@ -580,7 +580,7 @@ __global__ void k_zero_slots(uint32_t *__restrict__ hist, const uint32_t *__rest
 
 // Rank-space counts -> the reference layout hist[n][l][t][f] (number of
 // samples with response <= threshold t).
-__global__ void k_hist_to_ref(const uint32_t *__restrict__ rank_hist, const uint8_t *__restrict__ perm,
+static __global__ void k_hist_to_ref(const uint32_t *__restrict__ rank_hist, const uint8_t *__restrict__ perm,
                               uint32_t *__restrict__ out, uint32_t n_nodes, uint32_t K, uint32_t T,
                               uint32_t F) {
   const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -878,7 +878,7 @@ __global__ void k_reassign(DevSet ds, const uint32_t *__restrict__ act, const ui
 }
 
 // Per scan block: number of flags equal to 1 (low 32 bits) and 2 (high 32).
-__global__ void __launch_bounds__(256) k_scan_reduce(const uint8_t *__restrict__ flags, uint32_t n,
+static __global__ void __launch_bounds__(256) k_scan_reduce(const uint8_t *__restrict__ flags, uint32_t n,
                                                      unsigned long long *__restrict__ bsum) {
   const uint32_t b0 = blockIdx.x * kScanItems;
   unsigned long long acc = 0;
@@ -898,7 +898,7 @@ __global__ void __launch_bounds__(256) k_scan_reduce(const uint8_t *__restrict__
 }
 
 // Exclusive scan of the block sums in one CTA (any count).
-__global__ void __launch_bounds__(1024) k_scan_blocks(unsigned long long *__restrict__ bsum, uint32_t nb,
+static __global__ void __launch_bounds__(1024) k_scan_blocks(unsigned long long *__restrict__ bsum, uint32_t nb,
                                                       unsigned long long *__restrict__ total) {
   const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
   const uint32_t b = threadIdx.x * per, e = min(nb, b + per);
@@ -926,7 +926,7 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(unsigned long long *__rest
 // adj[p] + (number of earlier samples with the same flag).  Because parents are
 // in slot order and their children in the same order, this keeps every child's
 // samples in their previous (image-major) order.
-__global__ void __launch_bounds__(256) k_scatter(const uint8_t *__restrict__ flags, uint32_t n,
+static __global__ void __launch_bounds__(256) k_scatter(const uint8_t *__restrict__ flags, uint32_t n,
                                                  const unsigned long long *__restrict__ bsum,
                                                  const uint32_t *__restrict__ act,
                                                  const uint32_t *__restrict__ act_slot,
@@ -980,7 +980,7 @@ __global__ void __launch_bounds__(256) k_scatter(const uint8_t *__restrict__ fla
   }
 }
 
-__global__ void k_iota(uint32_t *__restrict__ a, uint32_t *__restrict__ slot, uint32_t n) {
+static __global__ void k_iota(uint32_t *__restrict__ a, uint32_t *__restrict__ slot, uint32_t n) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     a[i] = i;
@@ -988,12 +988,12 @@ __global__ void k_iota(uint32_t *__restrict__ a, uint32_t *__restrict__ slot, ui
   }
 }
 
-__global__ void k_magic_table(uint32_t *__restrict__ out) {
+static __global__ void k_magic_table(uint32_t *__restrict__ out) {
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d < 65536u) out[d] = d ? RoundDiv::multiplier(d) : 0u;
 }
 
-__global__ void k_log2_table(double *__restrict__ out, uint64_t n, DD inv_ln2) {
+static __global__ void k_log2_table(double *__restrict__ out, uint64_t n, DD inv_ln2) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = dd_log2_u32((uint32_t)i, inv_ln2);
 }
