@@ -177,6 +177,24 @@ int pd_hist(pd_ctx *ctx, const pd_train_params *params, uint32_t tree_id,
 int pd_split(pd_ctx *ctx, const pd_train_params *params, const uint32_t *hist,
              const uint32_t *class_tot, uint32_t n_nodes, int32_t *out_t, int32_t *out_f,
              double *out_gain);
+/* pd_split for callers that cannot allocate device memory.  It has no
+ * counterpart in the reference.  Code running inside a CUDA graph capture, or a
+ * host that only hands out memory from its own pre-allocated pool, cannot call
+ * cudaMalloc; this entry point takes DEVICE pointers for its inputs
+ * (hist_device: [n_nodes][K][T][F] cumulative counts as pd_split takes them,
+ * class_tot_device: [n_nodes][K]) and outputs (out_t/out_f int32, out_gain
+ * double, n_nodes each), needs no context, and keeps every intermediate result
+ * in one fixed 32 MiB device array inside the library (held by every GPU that
+ * loads it until the process exits).  Limits: the working set must fit the
+ * array (PD_ERR_UNSUPPORTED otherwise: about n_nodes*T*F*4 bytes plus 8 MiB of
+ * log2 table), and every node must hold fewer than 2^20 - 1 samples.  The first
+ * call on a device sets the array up and synchronises `stream`: make it before
+ * any stream capture.  Calls share the array, so calls that overlap on the GPU
+ * race; serialise them.  Each call synchronises `stream` (a cudaStream_t, NULL
+ * for the default stream) before returning. */
+int pd_split_noalloc(const pd_train_params *params, uint32_t n_classes, const uint32_t *hist_device,
+                     const uint32_t *class_tot_device, uint32_t n_nodes, int32_t *out_t_device,
+                     int32_t *out_f_device, double *out_gain_device, void *stream);
 /* Exact per-integer log2 table used by the split: out[n] = log2(n), out[0]=0. */
 int pd_log2_table(pd_ctx *ctx, uint32_t n, double *out);
 

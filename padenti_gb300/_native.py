@@ -89,6 +89,7 @@ _SIGS = {
     "pd_hist": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, _P, _P, C.c_uint32, _P]),
     "pd_split": (C.c_int, [_P, C.POINTER(TrainParams), _P, _P, C.c_uint32, _P, _P, _P]),
     "pd_log2_table": (C.c_int, [_P, C.c_uint32, _P]),
+    "pd_split_noalloc": (C.c_int, [C.POINTER(TrainParams), C.c_uint32, _P, _P, C.c_uint32, _P, _P, _P, _P]),
     "pd_forest_clear": (C.c_int, [_P]),
     "pd_forest_add_tree": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P]),
     "pd_forest_size": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
