@@ -75,8 +75,9 @@ def measured_peaks():
 
 
 def profile_traffic():
-    """dram bytes per histogram launch from the committed ncu summary, or None."""
-    p = ROOT / "profiles" / "hist_traffic.json"
+    """DRAM bytes per histogram launch (mean over the launches of one tree of this
+    workload) from the committed ncu summary profiles/k_hist_dram_2000x640x480.json."""
+    p = ROOT / "profiles" / "k_hist_dram_2000x640x480.json"
     if p.exists():
         try:
             return json.loads(p.read_text())

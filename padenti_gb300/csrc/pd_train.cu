@@ -242,14 +242,15 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
 }
 
 // Algorithmic HBM bytes of one histogram launch: the training-set images read
-// once, 9 bytes per active sample (index 4, packed x|y 4,
-// class 1), the candidate table of the slots read once and the K*T*F uint32
-// histogram of each slot written once.
+// once, 9 bytes per active sample (index 4, packed x|y 4, class 1), the
+// candidate table of every slot read once, and the K*T*F uint32 histogram
+// written once for each slot whose split is not fused into the kernel.
 static uint64_t hist_algorithmic_bytes(const pd_ctx *ctx, const pd_train_params *p, uint64_t n_samples,
-                                       uint32_t n_slots, uint64_t image_bytes) {
+                                       uint32_t n_slots, uint32_t n_written, uint64_t image_bytes) {
   const uint64_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
   const uint64_t fs = feat_size(ctx->cfg.feat_type);
-  return image_bytes + 9ull * n_samples + (uint64_t)n_slots * (K * T * F * 4 + T * F * fs + ctx->cfg.feat_dim * F * fs);
+  return image_bytes + 9ull * n_samples + (uint64_t)n_slots * (T * F * fs + ctx->cfg.feat_dim * F * fs) +
+         (uint64_t)n_written * K * T * F * 4;
 }
 
 // Split kernels over n slots: slots[0..n) of the slice, or 0..n-1 when
@@ -405,7 +406,8 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       PD_TRY(launch_hist<P>(ctx, p, off.data(), ns, ctx->act[cur].as<uint32_t>(), &n_items, ev[6], ev[2],
                             &split_slots, d_ctot.as<uint32_t>()));
       stats.hist_launches++;
-      stats.hist_bytes += hist_algorithmic_bytes(ctx, p, off.back() - off.front(), ns, image_bytes);
+      stats.hist_bytes += hist_algorithmic_bytes(ctx, p, off.back() - off.front(), ns, (uint32_t)split_slots.size(),
+                                                 image_bytes);
       if (!split_slots.empty())
         PD_CUDA(h2d(ctx, d_split_list.ptr, split_slots.data(), split_slots.size() * 4));
       PD_TRY(launch_split<false>(ctx, p, (uint32_t)split_slots.size(), ctx->hist.as<uint32_t>(),
