@@ -205,10 +205,11 @@ constexpr uint32_t kMaxChunk = 65535;
 template <class P, uint32_t TP, bool FAST, int SPI>
 PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const WorkItem &w,
                        const typename P::Cand &ca, const typename P::Cand &cb, uint32_t *sh_hist,
-                       const typename P::feat_t *sh_thr, uint32_t T, bool va, bool vb) {
+                       const typename P::feat_t *sh_thr, uint32_t T, uint32_t K, bool va, bool vb) {
   using FeatT = typename P::feat_t;
   using ImgT = typename P::img_t;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *spare = sh_hist + (size_t)K * T * 32 + lane;
   const FeatT *ta = sh_thr + lane, *tb = sh_thr + 32 + lane;
   constexpr int PW = P::kPreWords;
   const unsigned full = 0xffffffffu;
@@ -266,9 +267,11 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
         if (pb[(step - 1) * kTileF] < e.rb) pb += step * kTileF;
       }
       const uint32_t ka = (uint32_t)(pa - ta) / kTileF, kb = (uint32_t)(pb - tb) / kTileF;
+      // unconditional atomics: a dropped count (rank T, or a candidate past F)
+      // goes to the lane's spare word after the histogram
       uint32_t *row = sh_hist + (size_t)e.lab * T * 32 + lane;
-      if (va && ka < T) atomicAdd(row + ka * 32, 1u);
-      if (vb && kb < T) atomicAdd(row + kb * 32, 0x10000u);
+      atomicAdd((va && ka < T) ? row + ka * 32 : spare, 1u);
+      atomicAdd((vb && kb < T) ? row + kb * 32 : spare, 0x10000u);
     };
     // SPI samples per iteration: their probe loads are in flight together
     uint32_t i = 0;
@@ -509,8 +512,8 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   using ImgT = typename P::img_t;
   constexpr int D = P::kFeatDim;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);             // [K][T][32] packed
-  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32);  // [TP][64]
+  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);                  // [K][T][32] packed + 32 spare
+  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32 + 32);  // [TP][64]
   // fused split scratch, over the threshold table (dead after the sample loop):
   // sh_g [T][64] gains, sh_nl [T][32] packed left totals
   float *sh_g = reinterpret_cast<float *>(sh_thr);
@@ -539,8 +542,8 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   }
   // the exact-division fast path when every candidate of the tile allows it
   const bool fast = __syncthreads_and(P::fast(ca) && P::fast(cb));
-  if (fast) hist_samples<P, TP, true, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, va, vb);
-  else hist_samples<P, TP, false, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, va, vb);
+  if (fast) hist_samples<P, TP, true, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, K, va, vb);
+  else hist_samples<P, TP, false, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, K, va, vb);
 
   __syncthreads();
   if (w.multi == 2) {
