@@ -50,6 +50,7 @@ PD_D T ldg(const T *p) {
 struct RoundDiv {
   uint32_t m, sh;  // multiplier and shift for M = 2d
   int32_t d;
+  uint64_t dm;     // d * m: (n2 + d) * m is then one wide multiply-add
   static PD_HD uint32_t multiplier(uint32_t d) {
     const uint32_t M = 2u * d;
     uint32_t s = 31;
@@ -62,10 +63,21 @@ struct RoundDiv {
     r.d = d;
     r.m = ldg(magic + d);
     r.sh = 31u - (uint32_t)__clz(d);  // floor(log2 2d) - 1 = floor(log2 d)
+    r.dm = (uint64_t)(uint32_t)d * r.m;
     return r;
   }
-  // n2 = 2|u| (|u| <= 2^21): floor((2|u| + d) / (2d))
-  PD_D uint32_t q(uint32_t n2) const { return __umulhi(n2 + (uint32_t)d, m) >> sh; }
+  // From the depth d and its multiplier m (magic[d]).
+  static PD_D RoundDiv of(uint32_t d, uint32_t m) {
+    RoundDiv r;
+    r.d = (int32_t)d;
+    r.m = m;
+    r.sh = 31u - (uint32_t)__clz((int)d);
+    r.dm = (uint64_t)d * m;
+    return r;
+  }
+  // n2 = 2|u| (|u| <= 2^21): floor((2|u| + d) / (2d)), the high word of
+  // (n2 + d) * m = n2 * m + dm (< 2^55) shifted right by sh
+  PD_D uint32_t q(uint32_t n2) const { return (uint32_t)(((uint64_t)n2 * m + dm) >> 32) >> sh; }
 };
 
 // Per-candidate constants of an offset: 2|u| and the sign, or the raw u when
@@ -107,7 +119,8 @@ struct DepthDiff2 {
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF2;
   struct Prep {
     const uint16_t *im;
-    int32_t w, h, x, y;
+    uint32_t w, h;
+    int32_t x, y;
     RoundDiv div;
   };
   struct Cand {
@@ -122,13 +135,11 @@ struct DepthDiff2 {
   static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y, const uint32_t *pre) {
     Prep p;
     p.im = im.data;
-    p.w = im.w;
-    p.h = im.h;
+    p.w = (uint32_t)im.w;
+    p.h = (uint32_t)im.h;
     p.x = x;
     p.y = y;
-    p.div.d = (int32_t)pre[0];
-    p.div.m = pre[1];
-    p.div.sh = 31u - (uint32_t)__clz((int)pre[0]);
+    p.div = RoundDiv::of(pre[0], pre[1]);
     return p;
   }
   static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
@@ -145,12 +156,12 @@ struct DepthDiff2 {
   static PD_D bool fast(const Cand &c) {
     return c.o[0].fast() && c.o[1].fast() && c.o[2].fast() && c.o[3].fast();
   }
-  // Branch-free: an outside probe reads the (always valid) image origin and is
-  // then replaced by 10000.
+  // A predicated load: an outside probe loads nothing and reads as 0, then
+  // 10000.  Sides are below 2^16, so an inside index y*w + x fits 32 bits.
   static PD_D int32_t probe(const Prep &p, int32_t x, int32_t y) {
-    const bool in = (uint32_t)x < (uint32_t)p.w && (uint32_t)y < (uint32_t)p.h;
-    const uint32_t v = ldg(p.im + (in ? (size_t)y * p.w + x : 0));
-    return (in && v) ? (int32_t)v : kBgDepth;
+    uint32_t v = 0u;
+    if ((uint32_t)x < p.w && (uint32_t)y < p.h) v = ldg(p.im + ((uint32_t)y * p.w + (uint32_t)x));
+    return v ? (int32_t)v : kBgDepth;
   }
   template <bool FAST = false>
   static PD_D int32_t eval(const Prep &p, const Cand &c) {
@@ -176,7 +187,8 @@ struct DepthDiff1 {
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF1;
   struct Prep {
     const uint16_t *im;
-    int32_t w, h, x, y;
+    uint32_t w, h;
+    int32_t x, y;
     int16_t depth;
     RoundDiv div;
   };
@@ -193,15 +205,12 @@ struct DepthDiff1 {
   static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y, const uint32_t *pre) {
     Prep p;
     p.im = im.data;
-    p.w = im.w;
-    p.h = im.h;
+    p.w = (uint32_t)im.w;
+    p.h = (uint32_t)im.h;
     p.x = x;
     p.y = y;
     p.depth = (int16_t)(int32_t)pre[0];
-    const int32_t d = p.depth > 0 ? (int32_t)p.depth : 1;
-    p.div.d = d;
-    p.div.m = pre[1];
-    p.div.sh = 31u - (uint32_t)__clz(d);
+    p.div = RoundDiv::of(p.depth > 0 ? (uint32_t)p.depth : 1u, pre[1]);
     return p;
   }
   static PD_D Prep prepare(const ImageRef<uint16_t> &im, int32_t x, int32_t y) {
@@ -231,9 +240,9 @@ struct DepthDiff1 {
         ox = p.x + (int32_t)roundf(fdiv(fmul((float)c.f[0], 500.0f), dd));
         oy = p.y + (int32_t)roundf(fdiv(fmul((float)c.f[1], 500.0f), dd));
       }
-      const bool in = (uint32_t)ox < (uint32_t)p.w && (uint32_t)oy < (uint32_t)p.h;
-      const int16_t v = (int16_t)ldg(p.im + (in ? (size_t)oy * p.w + ox : 0));
-      probe = !in ? kBgDepth : (v ? v : kBgDepth);
+      int16_t v = 0;
+      if ((uint32_t)ox < p.w && (uint32_t)oy < p.h) v = (int16_t)ldg(p.im + ((uint32_t)oy * p.w + (uint32_t)ox));
+      probe = v ? v : kBgDepth;
     }
     return (int16_t)((int32_t)p.depth - probe);
   }
@@ -250,7 +259,8 @@ struct ChannelDiff {
   static constexpr int kId = PD_PLUGIN_CHANNEL_DIFF;
   struct Prep {
     const uint8_t *im;
-    int32_t w, h, x, y;
+    uint32_t w, h;
+    int32_t x, y;
   };
   struct Cand {
     int32_t c1, c2, ux, uy, vx, vy;
@@ -260,8 +270,8 @@ struct ChannelDiff {
   static PD_D Prep prepare(const ImageRef<uint8_t> &im, int32_t x, int32_t y, const uint32_t *) {
     Prep p;
     p.im = im.data;
-    p.w = im.w;
-    p.h = im.h;
+    p.w = (uint32_t)im.w;
+    p.h = (uint32_t)im.h;
     p.x = x;
     p.y = y;
     return p;
@@ -279,9 +289,10 @@ struct ChannelDiff {
   }
   static PD_D bool fast(const Cand &) { return true; }
   static PD_D int32_t read(const Prep &p, int32_t x, int32_t y, int32_t c) {
-    const bool in = (uint32_t)x < (uint32_t)p.w && (uint32_t)y < (uint32_t)p.h;
-    const int32_t v = ldg(p.im + (in ? ((size_t)y * p.w + x) * 3 + c : 0));
-    return in ? v : 0;
+    int32_t v = 0;
+    if ((uint32_t)x < p.w && (uint32_t)y < p.h)
+      v = ldg(p.im + ((uint64_t)((uint32_t)y * p.w + (uint32_t)x) * 3u + (uint32_t)c));
+    return v;
   }
   template <bool FAST = false>
   static PD_D int32_t eval(const Prep &p, const Cand &c) {

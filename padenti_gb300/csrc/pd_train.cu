@@ -26,7 +26,7 @@ static uint32_t padded_rows(uint32_t T) {
 // and, when the launch has fused-split items, the larger of the table and the
 // fused scratch (gains + packed left totals) that overlays it.
 static size_t hist_smem(const pd_ctx *ctx, uint32_t T, bool fused = true) {
-  const size_t hist = (size_t)ctx->cfg.n_classes * T * 32 * 4 + 32 * 4;  // + one spare word per lane
+  const size_t hist = (size_t)ctx->cfg.n_classes * (T + 1) * 32 * 4;  // rank T rows are never read
   const size_t thr = (size_t)padded_rows(T) * kTileF * feat_size(ctx->cfg.feat_type);
   const size_t scratch = (size_t)T * kTileF * 4 + (size_t)T * 32 * 4;
   return hist + (fused ? std::max(thr, scratch) : thr);

@@ -205,30 +205,32 @@ constexpr uint32_t kMaxChunk = 65535;
 template <class P, uint32_t TP, bool FAST, int SPI>
 PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const WorkItem &w,
                        const typename P::Cand &ca, const typename P::Cand &cb, uint32_t *sh_hist,
-                       const typename P::feat_t *sh_thr, uint32_t T, uint32_t K, bool va, bool vb) {
+                       const typename P::feat_t *sh_thr, uint32_t T) {
   using FeatT = typename P::feat_t;
   using ImgT = typename P::img_t;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *spare = sh_hist + (size_t)K * T * 32 + lane;
-  const FeatT *ta = sh_thr + lane, *tb = sh_thr + 32 + lane;
+  // the lane's two threshold columns (rows of 32 entries, like the histogram)
+  const FeatT *ta = sh_thr + lane, *tb = sh_thr + TP * 32 + lane;
+  uint32_t *hl = sh_hist + lane;
+  const uint32_t class_words = (T + 1) * 32;
   constexpr int PW = P::kPreWords;
   const unsigned full = 0xffffffffu;
   // one evaluation pair (both candidates of the lane) on warp sample i
   struct Eval {
     FeatT ra, rb;
-    uint32_t lab;
+    uint32_t row;  // class * (T + 1) * 32: the class block of the histogram
   };
   for (uint32_t base = w.begin + warp * 32; base < w.end; base += kHistThreads) {
     const uint32_t n_here = min(32u, w.end - base);
     // lane-parallel preload of 32 samples: position, class, image, pixel words
-    uint32_t my_xy = 0, my_wh = 0, my_lab = 0, my_pre[PW];
+    uint32_t my_xy = 0, my_wh = 0, my_row = 0, my_pre[PW];
     uint64_t my_off = 0;
 #pragma unroll
     for (int k = 0; k < PW; k++) my_pre[k] = 0u;
     if ((uint32_t)lane < n_here) {
       const uint32_t s = act[base + lane];
       my_xy = ds.s_xy[s];
-      my_lab = ds.s_label[s];
+      my_row = (uint32_t)ds.s_label[s] * class_words;
       const uint32_t imi = ds.s_img[s];
       my_off = ds.img_off[imi];
       my_wh = ds.img_wh[imi];
@@ -255,7 +257,7 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
       Eval e;
       e.ra = P::template eval<FAST>(prep, ca);
       e.rb = P::template eval<FAST>(prep, cb);
-      e.lab = __shfl_sync(full, my_lab, i);
+      e.row = __shfl_sync(full, my_row, i);
       return e;
     };
     auto accumulate = [&](const Eval &e) {
@@ -263,15 +265,16 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
       const FeatT *pa = ta, *pb = tb;
 #pragma unroll
       for (uint32_t step = TP >> 1; step > 0; step >>= 1) {
-        if (pa[(step - 1) * kTileF] < e.ra) pa += step * kTileF;
-        if (pb[(step - 1) * kTileF] < e.rb) pb += step * kTileF;
+        if (pa[(step - 1) * 32] < e.ra) pa += step * 32;
+        if (pb[(step - 1) * 32] < e.rb) pb += step * 32;
       }
-      const uint32_t ka = (uint32_t)(pa - ta) / kTileF, kb = (uint32_t)(pb - tb) / kTileF;
-      // unconditional atomics: a dropped count (rank T, or a candidate past F)
-      // goes to the lane's spare word after the histogram
-      uint32_t *row = sh_hist + (size_t)e.lab * T * 32 + lane;
-      atomicAdd((va && ka < T) ? row + ka * 32 : spare, 1u);
-      atomicAdd((vb && kb < T) ? row + kb * 32 : spare, 0x10000u);
+      // rank k = (pa - ta) / 32 in [0, T]; histogram rows also hold 32 words,
+      // so the word of rank k is (pa - ta) words into the class block.  Rank T
+      // (no threshold >= r) and the columns past F (all-max thresholds, rank
+      // 0) land in words that are never read.
+      uint32_t *row = hl + e.row;
+      atomicAdd(row + (pa - ta), 1u);
+      atomicAdd(row + (pb - tb), 0x10000u);
     };
     // SPI samples per iteration: their probe loads are in flight together
     uint32_t i = 0;
@@ -321,14 +324,15 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   __shared__ int s_j[kHistThreads / 32];
   __shared__ bool s_last;
   const uint32_t slot = w.slot, f0 = w.tile * kTileF;
+  const uint32_t TS = T + 1;  // histogram rows per class
   for (uint32_t l = threadIdx.x; l < K; l += blockDim.x) s_tot[l] = fs.class_tot[(size_t)slot * K + l];
   // in-place prefix over the ranks of each (class, packed column)
   for (uint32_t q = threadIdx.x; q < K * 32; q += blockDim.x) {
     const uint32_t l = q >> 5, col = q & 31;
     uint32_t run = 0;
     for (uint32_t j = 0; j < T; j++) {
-      run += sh_hist[(l * T + j) * 32 + col];
-      sh_hist[(l * T + j) * 32 + col] = run;
+      run += sh_hist[(l * TS + j) * 32 + col];
+      sh_hist[(l * TS + j) * 32 + col] = run;
     }
   }
   __syncthreads();
@@ -336,7 +340,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   for (uint32_t q = threadIdx.x; q < T * 32; q += blockDim.x) {
     const uint32_t j = q >> 5, col = q & 31;
     uint32_t n = 0;
-    for (uint32_t l = 0; l < K; l++) n += sh_hist[(l * T + j) * 32 + col];
+    for (uint32_t l = 0; l < K; l++) n += sh_hist[(l * TS + j) * 32 + col];
     sh_nl[q] = n;
   }
   __syncthreads();
@@ -370,7 +374,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
           const float iL = nL ? __frcp_rn((float)nL) : 0.0f, iR = nR ? __frcp_rn((float)nR) : 0.0f;
           float hl = 0.0f, hr = 0.0f;
           for (uint32_t l = 0; l < K; l++) {
-            const uint32_t cl = half16(sh_hist[(l * T + j) * 32 + (c & 31)], c), cr = s_tot[l] - cl;
+            const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c), cr = s_tot[l] - cl;
             if (cl != 0u && (uint64_t)cl * 1000000ull > nL) {
               const float p = (float)cl * iL;
               hl -= p * __log2f(p);
@@ -414,11 +418,11 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
       const uint32_t nR = N - nL;
       double sl = 0.0, sr = 0.0;
       for (uint32_t l = 0; l < K; l++) {
-        const uint32_t cl = half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
+        const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
         if (cl != 0u && (uint64_t)cl * 1000000ull > nL) sl = dadd(sl, dmul((double)cl, dsub(L[nL], L[cl])));
       }
       for (uint32_t l = 0; l < K; l++) {
-        const uint32_t cr = s_tot[l] - half16(sh_hist[(l * T + j) * 32 + (c & 31)], c);
+        const uint32_t cr = s_tot[l] - half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
         if (cr != 0u && (uint64_t)cr * 1000000ull > nR) sr = dadd(sr, dmul((double)cr, dsub(L[nR], L[cr])));
       }
       const double g = dsub(hp64, ddiv(dadd(sl, sr), (double)N));
@@ -469,7 +473,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     fs.part_best[pi] = pb;
     if (pb.idx != LLONG_MAX) {
       const uint32_t c = (uint32_t)(pb.idx % F) - f0;
-      for (uint32_t l = 0; l < K; l++) fs.part_cl[pi * K + l] = half16(sh_hist[(l * T + pb.j) * 32 + (c & 31)], c);
+      for (uint32_t l = 0; l < K; l++) fs.part_cl[pi * K + l] = half16(sh_hist[(l * TS + pb.j) * 32 + (c & 31)], c);
     }
     __threadfence();
     s_last = atomicAdd(fs.done + slot, 1u) == fs.tiles - 1;
@@ -512,8 +516,8 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   using ImgT = typename P::img_t;
   constexpr int D = P::kFeatDim;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);                  // [K][T][32] packed + 32 spare
-  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * T * 32 + 32);  // [TP][64]
+  uint32_t *sh_hist = reinterpret_cast<uint32_t *>(smem_raw);                   // [K][T+1][32] packed
+  FeatT *sh_thr = reinterpret_cast<FeatT *>(sh_hist + (size_t)K * (T + 1) * 32);  // [2][TP][32]
   // fused split scratch, over the threshold table (dead after the sample loop):
   // sh_g [T][64] gains, sh_nl [T][32] packed left totals
   float *sh_g = reinterpret_cast<float *>(sh_thr);
@@ -524,11 +528,14 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   const uint32_t fa = f0 + lane, fb = f0 + 32 + lane;
   const bool va = fa < F, vb = fb < F;
 
+  // sorted thresholds: column c of the tile at [c / 32][t][c % 32]; padding rows
+  // and candidates past F hold the maximum, which no response exceeds
   for (uint32_t j = threadIdx.x; j < TP * kTileF; j += blockDim.x) {
-    const uint32_t t = j / kTileF, ff = f0 + (j % kTileF);
-    sh_thr[j] = (t < T && ff < F) ? cand_thr[((size_t)w.slot * T + t) * F + ff] : max_of<FeatT>();
+    const uint32_t t = j / kTileF, c = j % kTileF, ff = f0 + c;
+    sh_thr[(c >> 5) * (TP * 32) + t * 32 + (c & 31)] =
+        (t < T && ff < F) ? cand_thr[((size_t)w.slot * T + t) * F + ff] : max_of<FeatT>();
   }
-  for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) sh_hist[j] = 0u;
+  for (uint32_t j = threadIdx.x; j < K * (T + 1) * 32; j += blockDim.x) sh_hist[j] = 0u;
   typename P::Cand ca, cb;
   {
     FeatT fva[D], fvb[D];
@@ -542,30 +549,32 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   }
   // the exact-division fast path when every candidate of the tile allows it
   const bool fast = __syncthreads_and(P::fast(ca) && P::fast(cb));
-  if (fast) hist_samples<P, TP, true, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, K, va, vb);
-  else hist_samples<P, TP, false, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T, K, va, vb);
+  if (fast) hist_samples<P, TP, true, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T);
+  else hist_samples<P, TP, false, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T);
 
   __syncthreads();
   if (w.multi == 2) {
     fused_split(fs, w, sh_hist, sh_g, sh_nl, F, T, K);
     return;
   }
-  for (uint32_t j = threadIdx.x; j < K * T * 32; j += blockDim.x) {
-    const uint32_t v = sh_hist[j];
-    const uint32_t l = j & 31;
-    uint32_t *dst = hist + ((size_t)w.slot * K * T + (j >> 5)) * F + f0 + l;
-    if (f0 + l < F) {
-      if (w.multi) {
-        if (v & 0xffffu) atomicAdd(dst, v & 0xffffu);
-      } else {
-        *dst = v & 0xffffu;
+  for (uint32_t l = 0; l < K; l++) {
+    for (uint32_t q = threadIdx.x; q < T * 32; q += blockDim.x) {
+      const uint32_t v = sh_hist[l * (T + 1) * 32 + q];
+      const uint32_t c = q & 31;
+      uint32_t *dst = hist + ((size_t)w.slot * K * T + l * T + (q >> 5)) * F + f0 + c;
+      if (f0 + c < F) {
+        if (w.multi) {
+          if (v & 0xffffu) atomicAdd(dst, v & 0xffffu);
+        } else {
+          *dst = v & 0xffffu;
+        }
       }
-    }
-    if (f0 + 32 + l < F) {
-      if (w.multi) {
-        if (v >> 16) atomicAdd(dst + 32, v >> 16);
-      } else {
-        dst[32] = v >> 16;
+      if (f0 + 32 + c < F) {
+        if (w.multi) {
+          if (v >> 16) atomicAdd(dst + 32, v >> 16);
+        } else {
+          dst[32] = v >> 16;
+        }
       }
     }
   }
