@@ -6,9 +6,12 @@ another implementation: if the library is missing or fails to load, calls raise.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import pathlib
 
-LIB_PATH = pathlib.Path(__file__).resolve().parent / "_build" / "libpadenti_gb300.so"
+# PADENTI_GB300_LIB selects another build of the library (same C ABI).
+LIB_PATH = pathlib.Path(os.environ.get("PADENTI_GB300_LIB") or
+                        pathlib.Path(__file__).resolve().parent / "_build" / "libpadenti_gb300.so")
 
 PD_OK = 0
 PD_IMG_U8, PD_IMG_U16 = 1, 2
