@@ -57,8 +57,10 @@ def args_():
     a.add_argument("--no-cpu", action="store_true")
     a.add_argument("--seed", type=int, default=0)
     a.add_argument("--chunk", type=int, default=None, help="histogram work-item size (samples)")
-    a.add_argument("--spi", type=int, default=None, help="samples per histogram-kernel iteration (2 or 4)")
+    a.add_argument("--spi", type=int, default=None, help="samples per histogram-kernel iteration (2, 4 or 8)")
     a.add_argument("--fuse-max", type=int, default=None, help="largest node (samples) with the fused split")
+    a.add_argument("--cand-order", type=int, default=None, choices=(0, 1),
+                   help="1: candidate columns ordered by first-probe offset (default), 0: index order")
     return a.parse_args()
 
 
@@ -250,6 +252,8 @@ def run_ours(a):
         tr.set_tuning("hist_spi", a.spi)
     if a.fuse_max is not None:
         tr.set_tuning("fuse_max", a.fuse_max)
+    if a.cand_order is not None:
+        tr.set_tuning("cand_order", a.cand_order)
     tr.upload(ts)
     stream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(tr.h))
 
@@ -381,7 +385,8 @@ def run_ours(a):
                 config=dict(workload=WORKLOAD, images=a.images, width=a.width, height=a.height,
                             samples_per_image=a.samples, features=a.features, thresholds=a.thresholds,
                             depth=a.depth, min_leaf=a.min_leaf, trees_per_step=1,
-                            chunk=a.chunk or 4096, hist_spi=a.spi or 4,
+                            chunk=a.chunk or 4096, hist_spi=a.spi or 8,
+                            cand_order=1 if a.cand_order is None else a.cand_order,
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
                 roofline=roof, cpu_baseline=base, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),

@@ -132,9 +132,12 @@ int pd_ctx_destroy(pd_ctx *ctx);
 int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
 /* Launch-shape knobs of the histogram kernel (results do not depend on them):
  *   "chunk"     samples per histogram work item, [256, 65535] (default 4096);
- *   "hist_spi"  samples evaluated together per warp iteration, 2 or 4 (default 4);
+ *   "hist_spi"  samples evaluated together per warp iteration, 2, 4 or 8 (default 8);
  *   "fuse_max"  nodes with at most this many samples (and within one work item)
- *               get their split computed inside the histogram kernel, [0, 65535]. */
+ *               get their split computed inside the histogram kernel, [0, 65535];
+ *   "cand_order" 1 (default): each node's candidate table is laid out in the
+ *               order of the candidates' first probe offsets (n_features <= 8192),
+ *               so that neighbouring lanes probe neighbouring pixels; 0: index order. */
 int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value);
 /* Synchronises the context's stream. */
 int pd_ctx_sync(pd_ctx *ctx);

@@ -276,7 +276,7 @@ class TreeTrainer(_Ctx):
             check(lib().pd_ctx_set_hist_budget(self.h, hist_budget))
 
     def set_tuning(self, name: str, value: int) -> None:
-        """Launch-shape knob of the histogram kernel ("chunk", "hist_spi"); results do not change."""
+        """Launch-shape knob of the histogram kernel ("chunk", "hist_spi", "fuse_max", "cand_order"); results do not change."""
         check(lib().pd_ctx_set_tuning(self.h, name.encode(), int(value)))
 
     def upload(self, ts: TrainingSet) -> None:

@@ -79,7 +79,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
   DevBuf *bufs[] = {&ctx->pixels, &ctx->img_off, &ctx->img_wh, &ctx->s_xy, &ctx->s_img, &ctx->s_label,
                     &ctx->log2_tab, &ctx->magic_tab, &ctx->snode, &ctx->act[0], &ctx->act[1], &ctx->act_slot[0],
                     &ctx->act_slot[1], &ctx->flags, &ctx->scan_blocks, &ctx->slot_adj, &ctx->scatter_err,
-                    &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->hist, &ctx->g32, &ctx->items,
+                    &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->cand_ord, &ctx->hist, &ctx->g32, &ctx->items,
                     &ctx->zero_slots, &ctx->split_out, &ctx->split_cl, &ctx->recheck, &ctx->split_scratch, &ctx->fused_scratch, &ctx->t_lc,
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
                     &ctx->f_post, &ctx->f_meta, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
@@ -105,11 +105,14 @@ extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
     PD_CHECK(value >= 256 && value <= 65535, PD_ERR_INVALID, "chunk %lld outside [256,65535]", (long long)value);
     ctx->chunk = (uint32_t)value;
   } else if (n == "hist_spi") {
-    PD_CHECK(value == 2 || value == 4, PD_ERR_INVALID, "hist_spi must be 2 or 4");
+    PD_CHECK(valid_hist_spi((uint32_t)value), PD_ERR_INVALID, "hist_spi must be 2, 4 or 8");
     ctx->hist_spi = (uint32_t)value;
   } else if (n == "fuse_max") {
     PD_CHECK(value >= 0 && value <= 65535, PD_ERR_INVALID, "fuse_max %lld outside [0,65535]", (long long)value);
     ctx->fuse_max = (uint32_t)value;
+  } else if (n == "cand_order") {
+    PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "cand_order must be 0 or 1");
+    ctx->cand_order = value != 0;
   } else {
     return set_error(PD_ERR_INVALID, "unknown tuning knob '%s'", name);
   }

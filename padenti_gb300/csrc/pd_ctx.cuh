@@ -6,14 +6,18 @@
 
 #include "pd_common.cuh"
 
+// Samples per iteration of the histogram kernel the tuning accepts (2, 4 or 8).
+inline bool valid_hist_spi(uint32_t spi) { return spi == 2 || spi == 4 || spi == 8; }
+
 struct pd_ctx {
   pd_config cfg{};
   int device = 0;
   cudaStream_t stream = nullptr;
   uint64_t hist_budget = 8ull << 30;
   uint32_t chunk = 4096;  // samples per histogram work item (at most 65535)
-  uint32_t hist_spi = 4;  // samples per iteration of the histogram kernel (2 or 4)
+  uint32_t hist_spi = 8;  // samples per iteration of the histogram kernel (2, 4 or 8)
   uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
+  bool cand_order = true;    // order each node's candidate columns by first-probe offset
 
   // ---- training set in HBM (cl_tree_trainer_impl_init.hpp:99-154 streams it
   // image by image; here it stays resident) ----
@@ -40,6 +44,7 @@ struct pd_ctx {
   pd::DevBuf slot_adj;               // int64 [4] per slot: adjL, adjR, kL, kR
   pd::DevBuf scatter_err;            // uint32 error counter
   pd::DevBuf cand_feat, cand_thr, cand_perm;
+  pd::DevBuf cand_ord;       // [slots][F] original candidate index of each column
   pd::DevBuf hist, g32;
   pd::DevBuf items, zero_slots;
   pd::DevBuf split_out, split_cl, recheck, split_scratch, fused_scratch;

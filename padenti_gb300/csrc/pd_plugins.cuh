@@ -6,7 +6,9 @@
 //                            words (a warp preloads 32 pixels at once, in parallel);
 //   prepare(im, x, y, pre)   builds the per-pixel state from those words;
 //   candidate(f)             per-candidate constants, computed once per tile;
-//   eval(prep, cand)         the response of one candidate at one pixel.
+//   eval(prep, cand)         the response of one candidate at one pixel;
+// and kOrderDim, the feature dims (kOrderDim, kOrderDim + 1) of its first probe
+// offset, by which the trainer orders a node's candidates.
 // eval(prep, f) runs all of it for a single evaluation.
 #pragma once
 
@@ -117,6 +119,7 @@ struct DepthDiff2 {
   static constexpr int kFeatDim = 4;
   static constexpr int kChannels = 1;
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF2;
+  static constexpr int kOrderDim = 0;  // feature dims (0, 1): the first probe offset
   struct Prep {
     const uint16_t *im;
     uint32_t w, h;
@@ -185,6 +188,7 @@ struct DepthDiff1 {
   static constexpr int kFeatDim = 2;
   static constexpr int kChannels = 1;
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF1;
+  static constexpr int kOrderDim = 0;  // feature dims (0, 1): the probe offset
   struct Prep {
     const uint16_t *im;
     uint32_t w, h;
@@ -257,6 +261,7 @@ struct ChannelDiff {
   static constexpr int kFeatDim = 6;
   static constexpr int kChannels = 3;
   static constexpr int kId = PD_PLUGIN_CHANNEL_DIFF;
+  static constexpr int kOrderDim = 2;  // feature dims (2, 3): the first probe offset
   struct Prep {
     const uint8_t *im;
     uint32_t w, h;

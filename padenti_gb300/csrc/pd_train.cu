@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "pd_ctx.cuh"
+#include "pd_hist_grid.cuh"
 #include "pd_train_kernels.cuh"
 
 namespace pd {
@@ -92,6 +93,7 @@ static int ensure_slice(pd_ctx *ctx, const pd_train_params *p, uint32_t slots) {
   PD_TRY(ctx->cand_feat.ensure(slots * ctx->cfg.feat_dim * F * fs));
   PD_TRY(ctx->cand_thr.ensure(slots * T * F * fs));
   PD_TRY(ctx->cand_perm.ensure(slots * T * F));
+  PD_TRY(ctx->cand_ord.ensure(slots * F * 4));
   PD_TRY(ctx->hist.ensure(slots * K * T * F * 4));
   PD_TRY(ctx->g32.ensure(slots * T * F * 4));
   PD_TRY(ctx->split_out.ensure(slots * sizeof(SplitOut)));
@@ -103,23 +105,42 @@ static int ensure_slice(pd_ctx *ctx, const pd_train_params *p, uint32_t slots) {
 static uint64_t slot_bytes(const pd_ctx *ctx, const pd_train_params *p) {
   const uint64_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
   const uint64_t fs = feat_size(ctx->cfg.feat_type);
-  return K * T * F * 4 + T * F * 4 + T * F * (fs + 1) + ctx->cfg.feat_dim * F * fs;
+  return K * T * F * 4 + T * F * 4 + T * F * (fs + 1) + ctx->cfg.feat_dim * F * fs + F * 4;
 }
 
 // ----------------------------------------------------------- launches ----
+// Candidate tables of n slots.  With `ordered` (and F <= kOrderMaxF) the
+// columns of each slot are sorted by first-probe offset and *ord_out receives
+// the column -> original index map; otherwise column f is candidate f and
+// *ord_out is null.
 template <class P>
 static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tree, const int32_t *d_nodes,
-                             uint32_t n) {
+                             uint32_t n, bool ordered = false, const uint32_t **ord_out = nullptr) {
   using FeatT = typename P::feat_t;
-  const uint64_t total = (uint64_t)n * p->n_features;
+  const uint32_t F = p->n_features;
+  const uint64_t total = (uint64_t)n * F;
+  const uint32_t *ord = nullptr;
+  if (ord_out) *ord_out = nullptr;
   if (!total) return PD_OK;
+  const CandBounds b = bounds(p, P::kFeatDim);
+  if (ordered && F <= kOrderMaxF) {
+    uint32_t N = 1;
+    while (N < F) N <<= 1;
+    const size_t osmem = (size_t)N * 8;
+    PD_CUDA(cudaFuncSetAttribute(k_cand_order<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)osmem));
+    k_cand_order<P><<<n, kOrderThreads, osmem, ctx->stream>>>(d_nodes, tree, F, b, ctx->cand_ord.as<uint32_t>());
+    PD_CUDA(cudaGetLastError());
+    ctx->launches++;
+    ord = ctx->cand_ord.as<uint32_t>();
+  }
   const size_t smem = (size_t)p->n_thresholds * kCandThreads * (sizeof(FeatT) + 1);
   PD_CUDA(cudaFuncSetAttribute(k_candidates<FeatT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_candidates<FeatT><<<(unsigned)((total + kCandThreads - 1) / kCandThreads), kCandThreads, smem, ctx->stream>>>(
-      d_nodes, n, tree, p->n_features, p->n_thresholds, P::kFeatDim, bounds(p, P::kFeatDim),
-      ctx->cand_feat.as<FeatT>(), ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>());
+      d_nodes, n, tree, F, p->n_thresholds, P::kFeatDim, b, ord, ctx->cand_feat.as<FeatT>(),
+      ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>());
   PD_CUDA(cudaGetLastError());
   ctx->launches++;
+  if (ord_out) *ord_out = ord;
   return PD_OK;
 }
 
@@ -132,7 +153,7 @@ template <class P>
 static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *off, uint32_t n,
                        const uint32_t *d_act, uint64_t *n_items_out, cudaEvent_t ev_before = nullptr,
                        cudaEvent_t ev_after = nullptr, std::vector<uint32_t> *split_slots = nullptr,
-                       const uint32_t *d_class_tot = nullptr) {
+                       const uint32_t *d_class_tot = nullptr, const uint32_t *d_ord = nullptr) {
   using FeatT = typename P::feat_t;
   const uint32_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
   const uint32_t tiles = (F + kTileF - 1) / kTileF;
@@ -203,40 +224,24 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     fs.out = ctx->split_out.as<SplitOut>();
     fs.out_cl = ctx->split_cl.as<uint32_t>();
     fs.rechecked = ctx->recheck.as<unsigned long long>();
+    fs.ord = d_ord;
   }
-  auto run = [&]<uint32_t TP>() -> int {
-    auto kern = ctx->hist_spi >= 4 ? k_hist<P, TP, 4> : k_hist<P, TP, 2>;
-    PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    // carve out only the shared memory the resident CTAs need; the rest stays L1
-    // for the probe gathers (resident CTAs are register-limited: 2 at 4 samples
-    // per iteration, 3 at 2)
-    const int resident = ctx->hist_spi >= 4 ? 2 : 3;
-    const int pct = (int)std::min<size_t>(100, (resident * (smem + 1024) * 100 + 233471) / 233472);
-    PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
-    if (ev_before) PD_CUDA(cudaEventRecord(ev_before, ctx->stream));
-    // The grid is the work list; the hardware scheduler keeps every SM full.
-    for (uint64_t b = 0; b < items.size(); b += 0x7fffffffull) {
-      const uint64_t cnt = std::min<uint64_t>(items.size() - b, 0x7fffffffull);
-      kern<<<(unsigned)cnt, kHistThreads, smem, ctx->stream>>>(
-          devset(ctx), d_act, ctx->items.as<WorkItem>() + b, ctx->cand_feat.as<FeatT>(),
-          ctx->cand_thr.as<FeatT>(), ctx->hist.as<uint32_t>(), F, T, K, fs);
-      PD_CUDA(cudaGetLastError());
-      ctx->launches++;
-    }
-    return PD_OK;
-  };
-  switch (padded_rows(T)) {
-    case 2: PD_TRY(run.template operator()<2>()); break;
-    case 4: PD_TRY(run.template operator()<4>()); break;
-    case 8: PD_TRY(run.template operator()<8>()); break;
-    case 16: PD_TRY(run.template operator()<16>()); break;
-    case 32: PD_TRY(run.template operator()<32>()); break;
-    case 64: PD_TRY(run.template operator()<64>()); break;
-    case 128: PD_TRY(run.template operator()<128>()); break;
-    case 256: PD_TRY(run.template operator()<256>()); break;
-    case 512: PD_TRY(run.template operator()<512>()); break;
-    default: return set_error(PD_ERR_UNSUPPORTED, "n_thresholds %u", T);
-  }
+  HistGrid g;
+  g.ds = devset(ctx);
+  g.act = d_act;
+  g.items = ctx->items.as<WorkItem>();
+  g.n_items = items.size();
+  g.cand_feat = ctx->cand_feat.ptr;
+  g.cand_thr = ctx->cand_thr.ptr;
+  g.hist = ctx->hist.as<uint32_t>();
+  g.F = F;
+  g.T = T;
+  g.K = K;
+  g.TP = padded_rows(T);
+  g.smem = smem;
+  g.fs = fs;
+  g.ev_before = ev_before;
+  PD_TRY(launch_hist_grid<P>(ctx, g));
   if (ev_after) PD_CUDA(cudaEventRecord(ev_after, ctx->stream));
   return PD_OK;
 }
@@ -258,7 +263,8 @@ static uint64_t hist_algorithmic_bytes(const pd_ctx *ctx, const pd_train_params 
 template <bool CUM>
 static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const uint32_t *d_hist,
                         const uint8_t *d_perm, const uint32_t *d_class_tot,
-                        const uint32_t *d_slot_list = nullptr, uint32_t slice_slots = 0) {
+                        const uint32_t *d_slot_list = nullptr, uint32_t slice_slots = 0,
+                        const uint32_t *d_ord = nullptr) {
   if (!n) return PD_OK;
   const uint32_t all = d_slot_list ? slice_slots : n;
   const uint32_t F = p->n_features;
@@ -288,6 +294,7 @@ static int launch_split(pd_ctx *ctx, const pd_train_params *p, uint32_t n, const
   a.done = node_max + all;
   a.part_best = reinterpret_cast<SplitPart *>(ctx->split_scratch.as<uint8_t>() + (size_t)all * 8);
   a.slot_list = d_slot_list;
+  a.ord = d_ord;
   a.out = ctx->split_out.as<SplitOut>();
   a.out_cl = ctx->split_cl.as<uint32_t>();
   a.rechecked = ctx->recheck.as<unsigned long long>();
@@ -399,12 +406,13 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       PD_CUDA(cudaMemsetAsync(ctx->recheck.ptr, 0, sizeof(unsigned long long), st));
       std::vector<uint64_t> off(cur_off.begin() + s0, cur_off.begin() + s0 + ns + 1);
       PD_CUDA(cudaEventRecord(ev[0], st));
-      PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns));
+      const uint32_t *d_ord = nullptr;
+      PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, ctx->cand_order, &d_ord));
       PD_CUDA(cudaEventRecord(ev[1], st));
       uint64_t n_items = 0;
       std::vector<uint32_t> split_slots;
       PD_TRY(launch_hist<P>(ctx, p, off.data(), ns, ctx->act[cur].as<uint32_t>(), &n_items, ev[6], ev[2],
-                            &split_slots, d_ctot.as<uint32_t>()));
+                            &split_slots, d_ctot.as<uint32_t>(), d_ord));
       stats.hist_launches++;
       stats.hist_bytes += hist_algorithmic_bytes(ctx, p, off.back() - off.front(), ns, (uint32_t)split_slots.size(),
                                                  image_bytes);
@@ -412,7 +420,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
         PD_CUDA(h2d(ctx, d_split_list.ptr, split_slots.data(), split_slots.size() * 4));
       PD_TRY(launch_split<false>(ctx, p, (uint32_t)split_slots.size(), ctx->hist.as<uint32_t>(),
                                  ctx->cand_perm.as<uint8_t>(), d_ctot.as<uint32_t>(), d_split_list.as<uint32_t>(),
-                                 ns));
+                                 ns, d_ord));
       PD_CUDA(cudaEventRecord(ev[3], st));
       h_out.resize(ns);
       h_cl.resize((size_t)ns * K);

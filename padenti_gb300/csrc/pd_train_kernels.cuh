@@ -58,10 +58,12 @@ PD_D T max_of() {
 // sorted column is written out row by row, coalesced across candidates.
 constexpr int kCandThreads = 128;
 
+// Column c of slot n holds candidate ord[n][c] (c itself when ord is null).
 template <typename FeatT>
 __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__restrict__ nodes, uint32_t n_nodes,
                                                              uint32_t tree, uint32_t F, uint32_t T, int D,
-                                                             CandBounds b, FeatT *__restrict__ feat,
+                                                             CandBounds b, const uint32_t *__restrict__ ord,
+                                                             FeatT *__restrict__ feat,
                                                              FeatT *__restrict__ thr_sorted,
                                                              uint8_t *__restrict__ perm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -69,12 +71,13 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
   uint8_t *si = reinterpret_cast<uint8_t *>(sv + (size_t)T * kCandThreads);      // [T][128]
   const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = idx < (uint64_t)n_nodes * F;
-  const uint32_t n = active ? (uint32_t)(idx / F) : 0u, f = active ? (uint32_t)(idx % F) : 0u;
+  const uint32_t n = active ? (uint32_t)(idx / F) : 0u, c = active ? (uint32_t)(idx % F) : 0u;
   if (active) {
     const uint32_t node = (uint32_t)nodes[n];
+    const uint32_t f = ord ? ord[(size_t)n * F + c] : c;
     FeatT fv[PD_MAX_FEAT_DIM];
     candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
-    for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + f] = fv[d];
+    for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + c] = fv[d];
     FeatT *v = sv + threadIdx.x;
     uint8_t *id = si + threadIdx.x;
     uint32_t seed[4] = {tree, node, f, 1u}, st[4] = {0u, 0u, 0u, 0u};
@@ -101,9 +104,74 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
   __syncwarp();
   if (!active) return;
   for (uint32_t j = 0; j < T; j++) {
-    thr_sorted[((size_t)n * T + j) * F + f] = sv[j * kCandThreads + threadIdx.x];
-    perm[((size_t)n * T + j) * F + f] = si[j * kCandThreads + threadIdx.x];
+    thr_sorted[((size_t)n * T + j) * F + c] = sv[j * kCandThreads + threadIdx.x];
+    perm[((size_t)n * T + j) * F + c] = si[j * kCandThreads + threadIdx.x];
   }
+}
+
+// ------------------------------------------------------ candidate order ----
+// Column order of a node's candidate table: the candidates sorted by the Morton
+// code of their first probe offset (feature dims kOrderDim and kOrderDim + 1,
+// each scaled to 10 bits over its bounds).  The 32 lanes of a histogram warp
+// then probe nearby pixels and share cache sectors.  Only the placement
+// changes: split decisions use the original index f (ties to the lowest
+// t*F + f).  Block per slot; bitonic sort of (code << 32 | f) in shared memory
+// over the next power of two of F.
+constexpr uint32_t kOrderMaxF = 8192;
+constexpr int kOrderThreads = 512;
+
+PD_D uint32_t order_quant10(int32_t v, int32_t lo, int32_t up) {
+  const int64_t span = (int64_t)up - lo + 1, x = (int64_t)v - lo;
+  const int64_t q = span > 0 ? x * 1024 / span : 0;
+  return (uint32_t)(q < 0 ? 0 : (q > 1023 ? 1023 : q));
+}
+// bits 0..15 of v to the even bits of the result
+PD_D uint32_t order_spread(uint32_t v) {
+  v &= 0xffffu;
+  v = (v | (v << 8)) & 0x00ff00ffu;
+  v = (v | (v << 4)) & 0x0f0f0f0fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+
+template <class P>
+__global__ void __launch_bounds__(kOrderThreads) k_cand_order(const int32_t *__restrict__ nodes, uint32_t tree,
+                                                              uint32_t F, CandBounds b, uint32_t *__restrict__ ord) {
+  using FeatT = typename P::feat_t;
+  constexpr int D = P::kFeatDim, X = P::kOrderDim;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned long long *key = reinterpret_cast<unsigned long long *>(smem_raw);  // [N]
+  const uint32_t n = blockIdx.x, node = (uint32_t)nodes[n];
+  uint32_t N = 1;
+  while (N < F) N <<= 1;
+  for (uint32_t f = threadIdx.x; f < N; f += blockDim.x) {
+    unsigned long long k = ~0ull;  // padding sorts last
+    if (f < F) {
+      FeatT fv[D];
+      candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
+      const uint32_t qx = order_quant10((int32_t)fv[X], b.low[X], b.up[X]);
+      const uint32_t qy = order_quant10((int32_t)fv[X + 1], b.low[X + 1], b.up[X + 1]);
+      k = ((unsigned long long)(order_spread(qx) | (order_spread(qy) << 1)) << 32) | f;
+    }
+    key[f] = k;
+  }
+  __syncthreads();
+  for (uint32_t size = 2; size <= N; size <<= 1) {
+    for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+      for (uint32_t i = threadIdx.x; i < N / 2; i += blockDim.x) {
+        const uint32_t lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+        const bool ascending = (lo & size) == 0;
+        const unsigned long long a = key[lo], c = key[hi];
+        if ((a > c) == ascending) {
+          key[lo] = c;
+          key[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (uint32_t c = threadIdx.x; c < F; c += blockDim.x) ord[(size_t)n * F + c] = (uint32_t)key[c];
 }
 
 // ---------------------------------------------------------------- split ----
@@ -114,8 +182,9 @@ struct SplitOut {
 // Best candidate of one column range of one node.
 struct SplitPart {
   double gain;
-  long long idx;  // t*F + f
-  int32_t j, pad;
+  long long idx;  // t*F + f (f the original candidate index)
+  int32_t j;      // sorted threshold position
+  int32_t col;    // column of the candidate table
 };
 
 constexpr int kSplitCols = 128;  // threads of a split CTA, one column each per pass
@@ -176,6 +245,7 @@ struct SplitArgs {
   uint32_t *out_cl;           // [slots][K] left class counts of the winner
   unsigned long long *rechecked;
   const uint32_t *slot_list;  // slots to process (null: blockIdx.y)
+  const uint32_t *ord;        // [slots][F] original index of each column (null: identity)
 };
 
 PD_D unsigned f2ord(float f) {
@@ -310,6 +380,7 @@ struct FusedSplit {
   SplitOut *out;
   uint32_t *out_cl;           // [slots][K]
   unsigned long long *rechecked;
+  const uint32_t *ord;        // [slots][F] original index of each column (null: identity)
 };
 
 PD_D uint32_t half16(uint32_t word, uint32_t c) { return (word >> ((c >> 5) * 16)) & 0xffffu; }
@@ -322,6 +393,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   __shared__ double s_g[kHistThreads / 32];
   __shared__ long long s_i[kHistThreads / 32];
   __shared__ int s_j[kHistThreads / 32];
+  __shared__ int s_c[kHistThreads / 32];
   __shared__ bool s_last;
   const uint32_t slot = w.slot, f0 = w.tile * kTileF;
   const uint32_t TS = T + 1;  // histogram rows per class
@@ -400,7 +472,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   // exact FP64 gains of the near-maximum candidates
   double best = -DBL_MAX;
   long long best_idx = LLONG_MAX;
-  int best_j = -1;
+  int best_j = -1, best_c = -1;
   unsigned long long n_checked = 0;
   if (ok) {
     const double *L = fs.L;
@@ -431,11 +503,12 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
       uint32_t t = fs.perm[((size_t)slot * T + j) * F + f];
       for (uint32_t je = j + 1; je < T && half16(sh_nl[je * 32 + (c & 31)], c) == nL; je++)
         t = min(t, (uint32_t)fs.perm[((size_t)slot * T + je) * F + f]);
-      const long long idx = (long long)t * F + f;
+      const long long idx = (long long)t * F + (fs.ord ? fs.ord[(size_t)slot * F + f] : f);
       if (g > best || (g == best && idx < best_idx)) {
         best = g;
         best_idx = idx;
         best_j = (int)j;
+        best_c = (int)f;
       }
     }
   }
@@ -444,16 +517,19 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     const double og = __shfl_xor_sync(0xffffffffu, best, o);
     const long long oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
     const int oj = __shfl_xor_sync(0xffffffffu, best_j, o);
+    const int oc = __shfl_xor_sync(0xffffffffu, best_c, o);
     if (og > best || (og == best && oi < best_idx)) {
       best = og;
       best_idx = oi;
       best_j = oj;
+      best_c = oc;
     }
   }
   if ((threadIdx.x & 31) == 0) {
     s_g[threadIdx.x >> 5] = best;
     s_i[threadIdx.x >> 5] = best_idx;
     s_j[threadIdx.x >> 5] = best_j;
+    s_c[threadIdx.x >> 5] = best_c;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -462,17 +538,18 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
         s_g[0] = s_g[i];
         s_i[0] = s_i[i];
         s_j[0] = s_j[i];
+        s_c[0] = s_c[i];
       }
     }
     SplitPart pb;
     pb.gain = s_g[0];
     pb.idx = s_i[0];
     pb.j = s_j[0];
-    pb.pad = 0;
+    pb.col = s_c[0];
     const size_t pi = (size_t)slot * fs.tiles + w.tile;
     fs.part_best[pi] = pb;
     if (pb.idx != LLONG_MAX) {
-      const uint32_t c = (uint32_t)(pb.idx % F) - f0;
+      const uint32_t c = (uint32_t)pb.col - f0;
       for (uint32_t l = 0; l < K; l++) fs.part_cl[pi * K + l] = half16(sh_hist[(l * TS + pb.j) * 32 + (c & 31)], c);
     }
     __threadfence();
@@ -724,6 +801,7 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
   __shared__ double red_g[kSplitCols / 32];
   __shared__ long long red_i[kSplitCols / 32];
   __shared__ int red_j[kSplitCols / 32];
+  __shared__ int red_c[kSplitCols / 32];
   __shared__ bool last;
   uint32_t N;
   load_tot<KM>(a, slot, tot, N);
@@ -744,7 +822,7 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
   const uint32_t fb = part * a.cols, fe = min(F, fb + a.cols);
   double best = -DBL_MAX;
   long long best_idx = LLONG_MAX;
-  int best_j = -1;
+  int best_j = -1, best_c = -1;
   unsigned long long n_checked = 0;
   for (uint32_t f = fb + threadIdx.x; f < fe; f += blockDim.x) {
     int jmax = -1;
@@ -769,11 +847,12 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
         dirty = false;
       }
       const uint32_t t = a.perm ? a.perm[((size_t)slot * T + j) * F + f] : (uint32_t)j;
-      const long long idx = (long long)t * F + f;
+      const long long idx = (long long)t * F + (a.ord ? a.ord[(size_t)slot * F + f] : f);
       if (g > best || (g == best && idx < best_idx)) {
         best = g;
         best_idx = idx;
         best_j = j;
+        best_c = (int)f;
       }
     }
   }
@@ -782,16 +861,19 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
     const double og = __shfl_xor_sync(0xffffffffu, best, o);
     const long long oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
     const int oj = __shfl_xor_sync(0xffffffffu, best_j, o);
+    const int oc = __shfl_xor_sync(0xffffffffu, best_c, o);
     if (og > best || (og == best && oi < best_idx)) {
       best = og;
       best_idx = oi;
       best_j = oj;
+      best_c = oc;
     }
   }
   if ((threadIdx.x & 31) == 0) {
     red_g[threadIdx.x >> 5] = best;
     red_i[threadIdx.x >> 5] = best_idx;
     red_j[threadIdx.x >> 5] = best_j;
+    red_c[threadIdx.x >> 5] = best_c;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -800,13 +882,14 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
         red_g[0] = red_g[i];
         red_i[0] = red_i[i];
         red_j[0] = red_j[i];
+        red_c[0] = red_c[i];
       }
     }
     SplitPart pb;
     pb.gain = red_g[0];
     pb.idx = red_i[0];
     pb.j = red_j[0];
-    pb.pad = 0;
+    pb.col = red_c[0];
     a.part_best[(size_t)slot * a.parts + part] = pb;
     __threadfence();
     last = atomicAdd(a.done + slot, 1u) == a.parts - 1;
@@ -829,12 +912,13 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
     o.f = (int32_t)(b.idx % F);
     o.j = b.j;
     o.gain = b.gain;
+    const uint32_t col = (uint32_t)b.col;
     for (uint32_t l = 0; l < K; l++) {
       uint32_t c = 0;
       if (CUM) {
-        c = H[((size_t)l * T + o.j) * F + o.f];
+        c = H[((size_t)l * T + o.j) * F + col];
       } else {
-        for (int j = 0; j <= o.j; j++) c += H[((size_t)l * T + j) * F + o.f];
+        for (int j = 0; j <= o.j; j++) c += H[((size_t)l * T + j) * F + col];
       }
       a.out_cl[(size_t)slot * K + l] = c;
     }

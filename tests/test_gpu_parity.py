@@ -149,11 +149,12 @@ def test_launch_shape_knobs_do_not_change_the_tree():
     cfg, ts, tp, _ = depth_case(n_images=16, n_features=96, n_thresholds=20)
     a = pg.Tree(cfg, 5, 7)
     pg.TreeTrainer(cfg).train(a, ts, tp)
-    for chunk, spi, fuse in [(256, 4, 0), (1000, 2, 300), (65535, 4, 65535), (4096, 4, 0)]:
+    for chunk, spi, fuse, order in [(256, 4, 0, 1), (1000, 2, 300, 0), (65535, 8, 65535, 1), (4096, 8, 0, 0)]:
         tr = pg.TreeTrainer(cfg)
         tr.set_tuning("chunk", chunk)
         tr.set_tuning("hist_spi", spi)
         tr.set_tuning("fuse_max", fuse)
+        tr.set_tuning("cand_order", order)
         b = pg.Tree(cfg, 5, 7)
         tr.train(b, ts, tp)
         assert np.array_equal(a.left_child, b.left_child)
@@ -161,6 +162,8 @@ def test_launch_shape_knobs_do_not_change_the_tree():
         assert np.array_equal(a.posteriors, b.posteriors)
     with pytest.raises(pg.PadentiError):
         pg.TreeTrainer(cfg).set_tuning("hist_spi", 3)
+    with pytest.raises(pg.PadentiError):
+        pg.TreeTrainer(cfg).set_tuning("cand_order", 2)
 
 
 def test_train_tree_nine_classes_bit_exact():
