@@ -385,7 +385,7 @@ def run_ours(a):
                 config=dict(workload=WORKLOAD, images=a.images, width=a.width, height=a.height,
                             samples_per_image=a.samples, features=a.features, thresholds=a.thresholds,
                             depth=a.depth, min_leaf=a.min_leaf, trees_per_step=1,
-                            chunk=a.chunk or 4096, hist_spi=a.spi or 8,
+                            chunk=a.chunk or 16384, fuse_max=4096 if a.fuse_max is None else a.fuse_max, hist_spi=a.spi or 8,
                             cand_order=1 if a.cand_order is None else a.cand_order,
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),

@@ -131,7 +131,7 @@ int pd_ctx_destroy(pd_ctx *ctx);
  * reference does with its 20 GiB host cap (cl_tree_trainer_impl.hpp:47-50). */
 int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
 /* Launch-shape knobs of the histogram kernel (results do not depend on them):
- *   "chunk"     samples per histogram work item, [256, 65535] (default 4096);
+ *   "chunk"     samples per histogram work item, [256, 65535] (default 16384);
  *   "hist_spi"  samples evaluated together per warp iteration, 2, 4 or 8 (default 8);
  *   "fuse_max"  nodes with at most this many samples (and within one work item)
  *               get their split computed inside the histogram kernel, [0, 65535];

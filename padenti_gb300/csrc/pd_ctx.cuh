@@ -14,7 +14,7 @@ struct pd_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   uint64_t hist_budget = 8ull << 30;
-  uint32_t chunk = 4096;  // samples per histogram work item (at most 65535)
+  uint32_t chunk = 16384;  // samples per histogram work item (at most 65535)
   uint32_t hist_spi = 8;  // samples per iteration of the histogram kernel (2, 4 or 8)
   uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
   bool cand_order = true;    // order each node's candidate columns by first-probe offset
