@@ -33,6 +33,7 @@ struct pd_ctx {
   pd::DevBuf s_label;   // uint8 class (0..K-1) per sample
   std::vector<uint8_t> h_label;  // host copy of the sample classes
   pd::DevBuf log2_tab;  // double log2(n), n < log2_len
+  pd::DevBuf xlog2_tab; // float c*log2(c), c < min(log2_len, 65536): the fused split's filter
   pd::DevBuf magic_tab; // uint32 RoundDiv multiplier by depth value (65536)
   uint64_t log2_len = 0;
 

@@ -52,6 +52,10 @@ int ensure_log2_table(pd_ctx *ctx, uint64_t n) {
   const DD inv = dd_inv_ln2();
   k_log2_table<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(ctx->log2_tab.as<double>(), n, inv);
   PD_CUDA(cudaGetLastError());
+  const uint32_t m = (uint32_t)std::min<uint64_t>(n, kXlog2Len);
+  PD_TRY(ctx->xlog2_tab.ensure((size_t)kXlog2Len * sizeof(float)));
+  k_xlog2_table<<<(m + 255) / 256, 256, 0, ctx->stream>>>(ctx->xlog2_tab.as<float>(), ctx->log2_tab.as<double>(), m);
+  PD_CUDA(cudaGetLastError());
   ctx->log2_len = n;
   return PD_OK;
 }
@@ -219,7 +223,7 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     fs.perm = ctx->cand_perm.as<uint8_t>();
     fs.L = ctx->log2_tab.as<double>();
     fs.L_len = ctx->log2_len;
-    fs.delta = recheck_delta(K);
+    fs.xlog2 = ctx->xlog2_tab.as<float>();
     fs.tiles = tiles;
     fs.out = ctx->split_out.as<SplitOut>();
     fs.out_cl = ctx->split_cl.as<uint32_t>();

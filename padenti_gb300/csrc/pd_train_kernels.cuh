@@ -20,6 +20,20 @@ constexpr int kScanItems = 4096;   // active samples per scan block (256 threads
 // can be the exact winner.  The window is 4.5x that.
 PD_HD float recheck_delta(uint32_t K) { return (3.0f * (float)K + 3.0f) * 4.0e-6f; }
 
+// Filter of the fused split (nodes of N <= 65535 samples, so 1e6*c > N for every
+// c >= 1 and the cutoff never applies).  The exact split maximises -(S_L + S_R),
+// S(c, n) = n log2 n - sum_l c_l log2 c_l, the canonical gain times N minus a
+// per-node constant.  In FP32 with the table X[c] = fl(c log2 c) and sequential
+// sums the error is at most (K + 3) u N log2 N (u = 2^-24): per side K + 1
+// table roundings of terms whose magnitudes add up to at most 2 n log2 n, K
+// additions of partial sums bounded by n log2 n, and one final addition, with
+// nL log2 nL + nR log2 nR <= N log2 N.  The exact winner is therefore within
+// 2 (K + 3) u N log2 N of the FP32 maximum; the window is 2 (2K + 5) u N log2 N.
+constexpr uint32_t kXlog2Len = 65536;
+PD_D float fused_window(uint32_t K, uint32_t N) {
+  return 2.0f * (2.0f * (float)K + 5.0f) * 5.9604645e-8f * (float)N * log2f((float)N);
+}
+
 struct CandBounds {
   int32_t low[PD_MAX_FEAT_DIM];
   int32_t up[PD_MAX_FEAT_DIM];
@@ -362,17 +376,18 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
 // Split of a node whose samples all went through one work item, fused into the
 // histogram CTA: the tile histogram (packed pairs of 16-bit counters) is
 // prefix-summed in place over the ranks, so word (l, j, lane) holds the left
-// counts of sorted position j; the FP32 gain of every (j, candidate) goes to
-// shared memory; every candidate within delta of the tile's own FP32 maximum is
-// re-evaluated with the exact FP64 gain.  The tile maximum is at most the node
-// maximum, so this set contains the node-wide recheck set and the node's
-// winner.  The last tile of the node to finish reduces the tiles.
+// counts of sorted position j; the FP32 filter -(S_L + S_R) of every
+// (j, candidate) goes to shared memory; every candidate within fused_window of
+// the tile's own FP32 maximum is re-evaluated with the exact FP64 gain.  The
+// window holds the tile's exact best (and its ties), so the best of the tiles'
+// rechecked candidates is the node's winner.  The last tile of the node to
+// finish reduces the tiles.
 struct FusedSplit {
   const uint32_t *class_tot;  // [slots][K]
   const uint8_t *perm;        // [slots][T][F]
   const double *L;
   uint64_t L_len;
-  float delta;
+  const float *xlog2;         // c log2 c for c < kXlog2Len (fused nodes have N <= 65535)
   uint32_t tiles;             // tiles per slot
   SplitPart *part_best;       // [slots][tiles]
   uint32_t *part_cl;          // [slots][tiles][K]
@@ -420,21 +435,10 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   for (uint32_t l = 0; l < K; l++) N += s_tot[l];
   const bool ok = N != 0 && (uint64_t)N < fs.L_len;
   const uint32_t pairs = T * kTileF;
-  // FP32 gains (reference formula, learn_best_feature.cl:75-93) and the tile maximum
+  // FP32 filter -(S_L + S_R) from the c log2 c table (fused_window) and the tile maximum
   float lmax = -FLT_MAX;
   if (ok) {
-    float hp = 0.0f;
-    {
-      const float inv = __frcp_rn((float)N);
-      for (uint32_t l = 0; l < K; l++) {
-        const uint32_t cl = s_tot[l];
-        if (cl != 0u && (uint64_t)cl * 1000000ull > N) {
-          const float p = (float)cl * inv;
-          hp -= p * __log2f(p);
-        }
-      }
-    }
-    const float invN = __frcp_rn((float)N);
+    const float *X = fs.xlog2;
     for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
       const uint32_t j = q / kTileF, c = q % kTileF;
       float g = -FLT_MAX;  // duplicates of the previous position stay -max
@@ -442,21 +446,13 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
         const uint32_t nL = half16(sh_nl[j * 32 + (c & 31)], c);
         // counts are monotone in j: an equal total means equal counts
         if (j == 0 || half16(sh_nl[(j - 1) * 32 + (c & 31)], c) != nL) {
-          const uint32_t nR = N - nL;
-          const float iL = nL ? __frcp_rn((float)nL) : 0.0f, iR = nR ? __frcp_rn((float)nR) : 0.0f;
-          float hl = 0.0f, hr = 0.0f;
+          float sl = __ldg(X + nL), sr = __ldg(X + (N - nL));
           for (uint32_t l = 0; l < K; l++) {
-            const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c), cr = s_tot[l] - cl;
-            if (cl != 0u && (uint64_t)cl * 1000000ull > nL) {
-              const float p = (float)cl * iL;
-              hl -= p * __log2f(p);
-            }
-            if (cr != 0u && (uint64_t)cr * 1000000ull > nR) {
-              const float p = (float)cr * iR;
-              hr -= p * __log2f(p);
-            }
+            const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
+            sl -= __ldg(X + cl);
+            sr -= __ldg(X + (s_tot[l] - cl));
           }
-          g = hp - ((float)nL * invN * hl + (float)nR * invN * hr);
+          g = -(sl + sr);
         }
       }
       sh_g[q] = g;
@@ -468,7 +464,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   __syncthreads();
   float tmax = s_red[0];
   for (int i = 1; i < kHistThreads / 32; i++) tmax = fmaxf(tmax, s_red[i]);
-  const float cut = tmax - fs.delta;
+  const float cut = tmax - fused_window(K, N);
   // exact FP64 gains of the near-maximum candidates
   double best = -DBL_MAX;
   long long best_idx = LLONG_MAX;
@@ -1092,6 +1088,12 @@ static __global__ void k_magic_table(uint32_t *__restrict__ out) {
 static __global__ void k_log2_table(double *__restrict__ out, uint64_t n, DD inv_ln2) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = dd_log2_u32((uint32_t)i, inv_ln2);
+}
+
+// c*log2(c) rounded to float (0 for c = 0), from the exact log2 table.
+static __global__ void k_xlog2_table(float *__restrict__ out, const double *__restrict__ L, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i ? __double2float_rn(dmul((double)i, L[i])) : 0.0f;
 }
 
 }  // namespace pd
