@@ -15,7 +15,10 @@ static int launch_hist_grid_as(pd_ctx *ctx, const HistGrid &g) {
   // for the probe gathers (resident CTAs are register-limited: 3 at 2 samples
   // per iteration, 2 at 4 or 8)
   const int resident = SPI <= 2 ? 3 : 2;
-  const int pct = (int)std::min<size_t>(100, (resident * (g.smem + 1024) * 100 + 233471) / 233472);
+  cudaFuncAttributes fa;
+  PD_CUDA(cudaFuncGetAttributes(&fa, kern));
+  const size_t per_cta = g.smem + fa.sharedSizeBytes + 1024;  // dynamic + static + reserved
+  const int pct = (int)std::min<size_t>(100, (resident * per_cta * 100 + 233471) / 233472);
   PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
   if (g.ev_before) PD_CUDA(cudaEventRecord(g.ev_before, ctx->stream));
   // The grid is the work list; the hardware scheduler keeps every SM full.

@@ -224,6 +224,12 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     fs.L = ctx->log2_tab.as<double>();
     fs.L_len = ctx->log2_len;
     fs.xlog2 = ctx->xlog2_tab.as<float>();
+    PD_TRY(ctx->parent.ensure((size_t)n * sizeof(double)));
+    k_parent_term<<<(n + 127) / 128, 128, 0, ctx->stream>>>(d_class_tot, n, K, fs.L, fs.L_len,
+                                                            ctx->parent.as<double>());
+    PD_CUDA(cudaGetLastError());
+    ctx->launches++;
+    fs.parent = ctx->parent.as<double>();
     fs.tiles = tiles;
     fs.out = ctx->split_out.as<SplitOut>();
     fs.out_cl = ctx->split_cl.as<uint32_t>();

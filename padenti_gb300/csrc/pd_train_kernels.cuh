@@ -30,6 +30,7 @@ PD_HD float recheck_delta(uint32_t K) { return (3.0f * (float)K + 3.0f) * 4.0e-6
 // nL log2 nL + nR log2 nR <= N log2 N.  The exact winner is therefore within
 // 2 (K + 3) u N log2 N of the FP32 maximum; the window is 2 (2K + 5) u N log2 N.
 constexpr uint32_t kXlog2Len = 65536;
+constexpr uint32_t kRecheckList = 512;  // recheck list of a fused split (pairs, u16)
 PD_D float fused_window(uint32_t K, uint32_t N) {
   return 2.0f * (2.0f * (float)K + 5.0f) * 5.9604645e-8f * (float)N * log2f((float)N);
 }
@@ -267,6 +268,11 @@ PD_D unsigned f2ord(float f) {
   return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 PD_D float ord2f(unsigned u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
+// int64 key whose order is the order of the (non-NaN) doubles
+PD_D long long gain_order_key(double g) {
+  const long long b = __double_as_longlong(g);
+  return b < 0 ? (LLONG_MIN - b - 1) : b;
+}
 
 // ------------------------------------------------------------ histogram ----
 // Each CTA owns one (slot, 64-candidate tile, sample chunk).  Lane l evaluates
@@ -388,6 +394,7 @@ struct FusedSplit {
   const double *L;
   uint64_t L_len;
   const float *xlog2;         // c log2 c for c < kXlog2Len (fused nodes have N <= 65535)
+  const double *parent;       // [slots] parent term of the exact gain (k_parent_term)
   uint32_t tiles;             // tiles per slot
   SplitPart *part_best;       // [slots][tiles]
   uint32_t *part_cl;          // [slots][tiles][K]
@@ -410,9 +417,18 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   __shared__ int s_j[kHistThreads / 32];
   __shared__ int s_c[kHistThreads / 32];
   __shared__ bool s_last;
+  __shared__ uint32_t s_nlist;
+  __shared__ uint16_t s_list[kRecheckList];
+  __shared__ unsigned long long s_pmin;
+  __shared__ int s_j0;
   const uint32_t slot = w.slot, f0 = w.tile * kTileF;
   const uint32_t TS = T + 1;  // histogram rows per class
   for (uint32_t l = threadIdx.x; l < K; l += blockDim.x) s_tot[l] = fs.class_tot[(size_t)slot * K + l];
+  if (threadIdx.x == 0) {
+    s_nlist = 0u;
+    s_pmin = ~0ull;
+    s_j0 = 0;
+  }
   // in-place prefix over the ranks of each (class, packed column)
   for (uint32_t q = threadIdx.x; q < K * 32; q += blockDim.x) {
     const uint32_t l = q >> 5, col = q & 31;
@@ -423,98 +439,138 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     }
   }
   __syncthreads();
-  // packed left totals of every (position, column pair)
-  for (uint32_t q = threadIdx.x; q < T * 32; q += blockDim.x) {
-    const uint32_t j = q >> 5, col = q & 31;
-    uint32_t n = 0;
-    for (uint32_t l = 0; l < K; l++) n += sh_hist[(l * TS + j) * 32 + col];
-    sh_nl[q] = n;
+  uint32_t N = 0, classes = 0;
+  for (uint32_t l = 0; l < K; l++) {
+    N += s_tot[l];
+    classes += s_tot[l] != 0u;
   }
-  __syncthreads();
-  uint32_t N = 0;
-  for (uint32_t l = 0; l < K; l++) N += s_tot[l];
   const bool ok = N != 0 && (uint64_t)N < fs.L_len;
-  const uint32_t pairs = T * kTileF;
-  // FP32 filter -(S_L + S_R) from the c log2 c table (fused_window) and the tile maximum
-  float lmax = -FLT_MAX;
-  if (ok) {
-    const float *X = fs.xlog2;
-    for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
-      const uint32_t j = q / kTileF, c = q % kTileF;
-      float g = -FLT_MAX;  // duplicates of the previous position stay -max
-      if (f0 + c < F) {
-        const uint32_t nL = half16(sh_nl[j * 32 + (c & 31)], c);
-        // counts are monotone in j: an equal total means equal counts
-        if (j == 0 || half16(sh_nl[(j - 1) * 32 + (c & 31)], c) != nL) {
-          float sl = __ldg(X + nL), sr = __ldg(X + (N - nL));
-          for (uint32_t l = 0; l < K; l++) {
-            const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
-            sl -= __ldg(X + cl);
-            sr -= __ldg(X + (s_tot[l] - cl));
-          }
-          g = -(sl + sr);
-        }
-      }
-      sh_g[q] = g;
-      lmax = fmaxf(lmax, g);
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = lmax;
-  __syncthreads();
-  float tmax = s_red[0];
-  for (int i = 1; i < kHistThreads / 32; i++) tmax = fmaxf(tmax, s_red[i]);
-  const float cut = tmax - fused_window(K, N);
-  // exact FP64 gains of the near-maximum candidates
   double best = -DBL_MAX;
   long long best_idx = LLONG_MAX;
   int best_j = -1, best_c = -1;
   unsigned long long n_checked = 0;
-  if (ok) {
-    const double *L = fs.L;
-    double hp64 = 0.0;
-    for (uint32_t l = 0; l < K; l++) {
-      const uint32_t cl = s_tot[l];
-      if (cl != 0u && (uint64_t)cl * 1000000ull > N) hp64 = dadd(hp64, dmul((double)cl, dsub(L[N], L[cl])));
-    }
-    hp64 = ddiv(hp64, (double)N);
-    for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
-      if (!(sh_g[q] >= cut)) continue;  // below the window, or a duplicate position
-      const uint32_t j = q / kTileF, c = q % kTileF;
-      n_checked++;
-      const uint32_t nL = half16(sh_nl[j * 32 + (c & 31)], c);
-      const uint32_t nR = N - nL;
-      double sl = 0.0, sr = 0.0;
-      for (uint32_t l = 0; l < K; l++) {
-        const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
-        if (cl != 0u && (uint64_t)cl * 1000000ull > nL) sl = dadd(sl, dmul((double)cl, dsub(L[nL], L[cl])));
-      }
-      for (uint32_t l = 0; l < K; l++) {
-        const uint32_t cr = s_tot[l] - half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
-        if (cr != 0u && (uint64_t)cr * 1000000ull > nR) sr = dadd(sr, dmul((double)cr, dsub(L[nR], L[cr])));
-      }
-      const double g = dsub(hp64, ddiv(dadd(sl, sr), (double)N));
+  if (ok && classes == 1) {
+    // A pure node: every exact gain is 0 (each term is c (log2 n - log2 c) with
+    // c = n), so the winner is the lowest index t*F + f, the original threshold
+    // 0 of the tile's lowest original candidate; its counts are those of the
+    // sorted position of that threshold.
+    for (uint32_t c = threadIdx.x; c < kTileF; c += blockDim.x) {
       const uint32_t f = f0 + c;
-      // the positions j..je share these counts: the lowest original threshold wins
-      uint32_t t = fs.perm[((size_t)slot * T + j) * F + f];
-      for (uint32_t je = j + 1; je < T && half16(sh_nl[je * 32 + (c & 31)], c) == nL; je++)
-        t = min(t, (uint32_t)fs.perm[((size_t)slot * T + je) * F + f]);
-      const long long idx = (long long)t * F + (fs.ord ? fs.ord[(size_t)slot * F + f] : f);
-      if (g > best || (g == best && idx < best_idx)) {
-        best = g;
-        best_idx = idx;
-        best_j = (int)j;
-        best_c = (int)f;
+      if (f < F) atomicMin(&s_pmin, ((unsigned long long)(fs.ord ? fs.ord[(size_t)slot * F + f] : f) << 8) | c);
+    }
+    __syncthreads();
+    const uint32_t c = (uint32_t)(s_pmin & 0xffu), f = f0 + c;
+    for (uint32_t t = threadIdx.x; t < T; t += blockDim.x)
+      if (fs.perm[((size_t)slot * T + t) * F + f] == 0) s_j0 = (int)t;
+    __syncthreads();
+    best = 0.0;
+    best_idx = (long long)(s_pmin >> 8);
+    best_j = s_j0;
+    best_c = (int)f;
+  } else {
+    // packed left totals of every (position, column pair)
+    for (uint32_t q = threadIdx.x; q < T * 32; q += blockDim.x) {
+      const uint32_t j = q >> 5, col = q & 31;
+      uint32_t n = 0;
+      for (uint32_t l = 0; l < K; l++) n += sh_hist[(l * TS + j) * 32 + col];
+      sh_nl[q] = n;
+    }
+    __syncthreads();
+    const uint32_t pairs = T * kTileF;
+    // FP32 filter -(S_L + S_R) from the c log2 c table (fused_window) and the tile maximum
+    float lmax = -FLT_MAX;
+    if (ok) {
+      const float *X = fs.xlog2;
+      for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
+        const uint32_t j = q / kTileF, c = q % kTileF;
+        float g = -FLT_MAX;  // duplicates of the previous position stay -max
+        if (f0 + c < F) {
+          const uint32_t nL = half16(sh_nl[j * 32 + (c & 31)], c);
+          // counts are monotone in j: an equal total means equal counts
+          if (j == 0 || half16(sh_nl[(j - 1) * 32 + (c & 31)], c) != nL) {
+            float sl = __ldg(X + nL), sr = __ldg(X + (N - nL));
+            for (uint32_t l = 0; l < K; l++) {
+              const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
+              sl -= __ldg(X + cl);
+              sr -= __ldg(X + (s_tot[l] - cl));
+            }
+            g = -(sl + sr);
+          }
+        }
+        sh_g[q] = g;
+        lmax = fmaxf(lmax, g);
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = lmax;
+    __syncthreads();
+    float tmax = s_red[0];
+    for (int i = 1; i < kHistThreads / 32; i++) tmax = fmaxf(tmax, s_red[i]);
+    const float cut = tmax - fused_window(K, N);
+    // exact FP64 gains of the near-maximum candidates
+    if (ok) {
+      const double *L = fs.L;
+      const double hp64 = fs.parent[slot];
+      auto recheck = [&](uint32_t q) {
+        const uint32_t j = q / kTileF, c = q % kTileF;
+        n_checked++;
+        const uint32_t nL = half16(sh_nl[j * 32 + (c & 31)], c);
+        const uint32_t nR = N - nL;
+        // both sides in one loop (two independent chains; each sums in class order)
+        const double Ll = L[nL], Lr = L[nR];
+        double sl = 0.0, sr = 0.0;
+#pragma unroll 3
+        for (uint32_t l = 0; l < K; l++) {
+          const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c), cr = s_tot[l] - cl;
+          if (cl != 0u && (uint64_t)cl * 1000000ull > nL) sl = dadd(sl, dmul((double)cl, dsub(Ll, L[cl])));
+          if (cr != 0u && (uint64_t)cr * 1000000ull > nR) sr = dadd(sr, dmul((double)cr, dsub(Lr, L[cr])));
+        }
+        const double g = dsub(hp64, ddiv(dadd(sl, sr), (double)N));
+        const uint32_t f = f0 + c;
+        // the positions j..je share these counts: the lowest original threshold wins
+        uint32_t t = fs.perm[((size_t)slot * T + j) * F + f];
+        for (uint32_t je = j + 1; je < T && half16(sh_nl[je * 32 + (c & 31)], c) == nL; je++)
+          t = min(t, (uint32_t)fs.perm[((size_t)slot * T + je) * F + f]);
+        const long long idx = (long long)t * F + (fs.ord ? fs.ord[(size_t)slot * F + f] : f);
+        if (g > best || (g == best && idx < best_idx)) {
+          best = g;
+          best_idx = idx;
+          best_j = (int)j;
+          best_c = (int)f;
+        }
+      };
+      // The pairs within the window cluster in few columns, i.e. in few threads of
+      // the pair loop: list them first, then deal the list out over all threads
+      // (the winner does not depend on the order).  A list that overflows falls
+      // back to the pair loop.
+      for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
+        if (sh_g[q] >= cut) {  // within the window (duplicate positions hold -max)
+          const uint32_t i = atomicAdd(&s_nlist, 1u);
+          if (i < kRecheckList) s_list[i] = (uint16_t)q;
+        }
+      }
+      __syncthreads();
+      const uint32_t n_list = s_nlist;
+      if (n_list <= kRecheckList) {
+        for (uint32_t i = threadIdx.x; i < n_list; i += blockDim.x) recheck(s_list[i]);
+      } else {
+        for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x)
+          if (sh_g[q] >= cut) recheck(q);
       }
     }
   }
   if (n_checked) atomicAdd(fs.rechecked, n_checked);
+  // warp reduction on integer keys of the gains (no FP64 compares: the FP64
+  // pipe is narrow); gains are never -0 (hp >= 0), so the keys order as the doubles
+  long long best_key = gain_order_key(best);
   for (int o = 16; o > 0; o >>= 1) {
+    const long long okey = __shfl_xor_sync(0xffffffffu, best_key, o);
     const double og = __shfl_xor_sync(0xffffffffu, best, o);
     const long long oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
     const int oj = __shfl_xor_sync(0xffffffffu, best_j, o);
     const int oc = __shfl_xor_sync(0xffffffffu, best_c, o);
-    if (og > best || (og == best && oi < best_idx)) {
+    if (okey > best_key || (okey == best_key && oi < best_idx)) {
+      best_key = okey;
       best = og;
       best_idx = oi;
       best_j = oj;
@@ -661,6 +717,26 @@ static __global__ void k_zero_slots(uint32_t *__restrict__ hist, const uint32_t 
     const uint64_t s = i / per_slot;
     hist[(uint64_t)slots[s] * per_slot + (i - s * per_slot)] = 0u;
   }
+}
+
+// The parent term S(tot, N) / N of the exact FP64 gain of every slot, the same
+// IEEE operation sequence as sum64 (0 for an empty slot or one beyond the table).
+static __global__ void k_parent_term(const uint32_t *__restrict__ class_tot, uint32_t n, uint32_t K,
+                                     const double *__restrict__ L, uint64_t L_len, double *__restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t *tot = class_tot + (size_t)i * K;
+  uint32_t N = 0;
+  for (uint32_t l = 0; l < K; l++) N += tot[l];
+  double h = 0.0;
+  if (N != 0 && (uint64_t)N < L_len) {
+    for (uint32_t l = 0; l < K; l++) {
+      const uint32_t cl = tot[l];
+      if (cl != 0u && (uint64_t)cl * 1000000ull > N) h = dadd(h, dmul((double)cl, dsub(L[N], L[cl])));
+    }
+    h = ddiv(h, (double)N);
+  }
+  out[i] = h;
 }
 
 // Rank-space counts -> the reference layout hist[n][l][t][f] (number of
@@ -853,12 +929,17 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
     }
   }
   if (n_checked) atomicAdd(a.rechecked, n_checked);
+  // warp reduction on integer keys of the gains (no FP64 compares: the FP64
+  // pipe is narrow); gains are never -0 (hp >= 0), so the keys order as the doubles
+  long long best_key = gain_order_key(best);
   for (int o = 16; o > 0; o >>= 1) {
+    const long long okey = __shfl_xor_sync(0xffffffffu, best_key, o);
     const double og = __shfl_xor_sync(0xffffffffu, best, o);
     const long long oi = __shfl_xor_sync(0xffffffffu, best_idx, o);
     const int oj = __shfl_xor_sync(0xffffffffu, best_j, o);
     const int oc = __shfl_xor_sync(0xffffffffu, best_c, o);
-    if (og > best || (og == best && oi < best_idx)) {
+    if (okey > best_key || (okey == best_key && oi < best_idx)) {
+      best_key = okey;
       best = og;
       best_idx = oi;
       best_j = oj;

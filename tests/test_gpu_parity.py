@@ -119,6 +119,25 @@ def _assert_same_tree(g: pg.Tree, o: dict):
     assert np.array_equal(g.posteriors.view(np.uint32), o["posteriors"].view(np.uint32))
 
 
+def test_pure_nodes_bit_exact():
+    """Single-class and half-single-class training sets: every node (or every node of the
+    right-half subtrees) is pure, every exact gain there is 0 and the split is the lowest
+    index t*F + f -- the closed form of the fused split; also through the unfused split."""
+    cfg, ts, tp, (px, lb, sm) = depth_case(n_images=12, n_features=96, n_thresholds=20, min_leaf=5)
+    one = np.where(lb > 0, 1, 0).astype(lb.dtype)
+    x = np.arange(lb.shape[-1])
+    half = np.where((lb > 0) & (x >= lb.shape[-1] // 2), 1, lb).astype(lb.dtype)
+    for labels in (one, half):
+        ts1 = pg.training_set(3, px, labels, sm)
+        o = _oracle_tree(cfg, ts1, tp, 2, 7)
+        for fuse in (4096, 0):
+            tr = pg.TreeTrainer(cfg)
+            tr.set_tuning("fuse_max", fuse)
+            t = pg.Tree(cfg, 2, 7)
+            tr.train(t, ts1, tp)
+            _assert_same_tree(t, o)
+
+
 def test_train_tree_config0_bit_exact():
     """The full 64-image 160x120 configuration: F=200, T=20, depth 8, min 20 pixels per leaf."""
     cfg, ts, tp, _ = depth_case(n_images=64, n_features=200, n_thresholds=20)
