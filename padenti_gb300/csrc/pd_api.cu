@@ -79,7 +79,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
   DevBuf *bufs[] = {&ctx->pixels, &ctx->img_off, &ctx->img_wh, &ctx->s_xy, &ctx->s_img, &ctx->s_label,
                     &ctx->log2_tab, &ctx->magic_tab, &ctx->snode, &ctx->act[0], &ctx->act[1], &ctx->act_slot[0],
                     &ctx->act_slot[1], &ctx->flags, &ctx->scan_blocks, &ctx->slot_adj, &ctx->scatter_err,
-                    &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->cand_ord, &ctx->parent, &ctx->xlog2_tab, &ctx->hist, &ctx->g32, &ctx->items,
+                    &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->cand_ord, &ctx->parent, &ctx->xlog2_tab, &ctx->split_par, &ctx->hist, &ctx->g32, &ctx->items,
                     &ctx->zero_slots, &ctx->split_out, &ctx->split_cl, &ctx->recheck, &ctx->split_scratch, &ctx->fused_scratch, &ctx->t_lc,
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
                     &ctx->f_post, &ctx->f_meta, &ctx->p_img, &ctx->p_mask, &ctx->p_out};

@@ -35,6 +35,7 @@ struct pd_ctx {
   pd::DevBuf log2_tab;  // double log2(n), n < log2_len
   pd::DevBuf xlog2_tab; // float c*log2(c), c < min(log2_len, 65536): the fused split's filter
   pd::DevBuf parent;    // [slots] parent term of the exact gain, for the fused split
+  pd::DevBuf split_par; // [slots][D + 1] feature values and threshold of each winner
   pd::DevBuf magic_tab; // uint32 RoundDiv multiplier by depth value (65536)
   uint64_t log2_len = 0;
 

@@ -101,6 +101,7 @@ static int ensure_slice(pd_ctx *ctx, const pd_train_params *p, uint32_t slots) {
   PD_TRY(ctx->hist.ensure(slots * K * T * F * 4));
   PD_TRY(ctx->g32.ensure(slots * T * F * 4));
   PD_TRY(ctx->split_out.ensure(slots * sizeof(SplitOut)));
+  PD_TRY(ctx->split_par.ensure(slots * (ctx->cfg.feat_dim + 1) * fs));
   PD_TRY(ctx->split_cl.ensure(slots * K * 4));
   PD_TRY(ctx->recheck.ensure(sizeof(unsigned long long) + slots * K * 4 + slots * 4));
   return PD_OK;
@@ -389,6 +390,8 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   DevBuf d_nodes, d_ctot, d_next, d_split_list;
   std::vector<SplitOut> h_out;
   std::vector<uint32_t> h_cl;
+  std::vector<FeatT> h_par;
+  std::vector<uint32_t> cl(K), cr(K);
   cudaEvent_t *ev = ctx->ev;
 
   for (uint32_t depth = 1; depth < end_depth; depth++) {
@@ -431,12 +434,20 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       PD_TRY(launch_split<false>(ctx, p, (uint32_t)split_slots.size(), ctx->hist.as<uint32_t>(),
                                  ctx->cand_perm.as<uint8_t>(), d_ctot.as<uint32_t>(), d_split_list.as<uint32_t>(),
                                  ns, d_ord));
+      // the winners' feature values and thresholds, from the candidate tables
+      k_split_params<FeatT><<<(ns + 127) / 128, 128, 0, st>>>(
+          ctx->split_out.as<SplitOut>(), ns, ctx->cand_feat.as<FeatT>(), ctx->cand_thr.as<FeatT>(),
+          ctx->cand_perm.as<uint8_t>(), p->n_features, p->n_thresholds, D, ctx->split_par.as<FeatT>());
+      PD_CUDA(cudaGetLastError());
+      ctx->launches++;
       PD_CUDA(cudaEventRecord(ev[3], st));
       h_out.resize(ns);
       h_cl.resize((size_t)ns * K);
+      h_par.resize((size_t)ns * (D + 1));
       unsigned long long rechecked = 0;
       PD_CUDA(d2h(ctx, h_out.data(), ctx->split_out.ptr, ns * sizeof(SplitOut)));
       PD_CUDA(d2h(ctx, h_cl.data(), ctx->split_cl.ptr, (size_t)ns * K * 4));
+      PD_CUDA(d2h(ctx, h_par.data(), ctx->split_par.ptr, (size_t)ns * (D + 1) * sizeof(FeatT)));
       PD_CUDA(d2h(ctx, &rechecked, ctx->recheck.ptr, 8));
       PD_CUDA(cudaStreamSynchronize(st));
       stats.ms_candidates += elapsed(ev[0], ev[1]);
@@ -450,7 +461,6 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
         if (o.t < 0) continue;
         const uint32_t n = (uint32_t)frontier[s0 + i];
         uint32_t lsum = 0, rsum = 0;
-        std::vector<uint32_t> cl(K), cr(K);
         for (uint32_t l = 0; l < K; l++) {
           cl[l] = h_cl[(size_t)i * K + l];
           cr[l] = class_tot[(size_t)n * K + l] - cl[l];
@@ -469,8 +479,9 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
         }
         lc[L] = -1;
         lc[R] = -1;
-        candidate_feature<FeatT>(tree_id, n, (uint32_t)o.f, D, p->feat_low, p->feat_up, feats + (size_t)n * D);
-        thrs[n] = candidate_threshold<FeatT>(tree_id, n, (uint32_t)o.f, (uint32_t)o.t, p->thr_low, p->thr_up);
+        // = candidate_feature / candidate_threshold of (o.f, o.t), read from the tables
+        for (int d = 0; d < D; d++) feats[(size_t)n * D + d] = h_par[(size_t)i * (D + 1) + d];
+        thrs[n] = h_par[(size_t)i * (D + 1) + D];
         lc[n] = (int32_t)L;
         split_now[s0 + i] = 1;
         stats.nodes_split++;

@@ -191,7 +191,8 @@ __global__ void __launch_bounds__(kOrderThreads) k_cand_order(const int32_t *__r
 
 // ---------------------------------------------------------------- split ----
 struct SplitOut {
-  int32_t t, f, j, pad;
+  int32_t t, f, j;  // original threshold and candidate of the winner, its sorted position
+  int32_t col;      // its column in the candidate table (-1: no split)
   double gain;
 };
 // Best candidate of one column range of one node.
@@ -620,14 +621,14 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     }
   }
   SplitOut o;
-  o.pad = 0;
   if (b.idx == LLONG_MAX) {
-    o.t = o.f = o.j = -1;
+    o.t = o.f = o.j = o.col = -1;
     o.gain = 0.0;
   } else {
     o.t = (int32_t)(b.idx / F);
     o.f = (int32_t)(b.idx % F);
     o.j = b.j;
+    o.col = b.col;
     o.gain = b.gain;
     for (uint32_t l = 0; l < K; l++) fs.out_cl[(size_t)slot * K + l] = fs.part_cl[bi * K + l];
   }
@@ -717,6 +718,25 @@ static __global__ void k_zero_slots(uint32_t *__restrict__ hist, const uint32_t 
     const uint64_t s = i / per_slot;
     hist[(uint64_t)slots[s] * per_slot + (i - s * per_slot)] = 0u;
   }
+}
+
+// Split parameters of the winners read from the candidate tables: the D
+// feature values of column `col` and the threshold of original index t (the
+// sorted entry whose permutation is t) -- the values candidate_feature and
+// candidate_threshold regenerate from MD5.  params [n][D + 1]; slots without a
+// split are left as they are.
+template <typename FeatT>
+__global__ void k_split_params(const SplitOut *__restrict__ out, uint32_t n, const FeatT *__restrict__ cand_feat,
+                               const FeatT *__restrict__ cand_thr, const uint8_t *__restrict__ perm, uint32_t F,
+                               uint32_t T, int D, FeatT *__restrict__ params) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const SplitOut o = out[i];
+  if (o.t < 0 || o.col < 0) return;
+  const uint32_t col = (uint32_t)o.col;
+  for (int d = 0; d < D; d++) params[(size_t)i * (D + 1) + d] = cand_feat[((size_t)i * D + d) * F + col];
+  for (uint32_t j = 0; j < T; j++)
+    if (perm[((size_t)i * T + j) * F + col] == (uint8_t)o.t) params[(size_t)i * (D + 1) + D] = cand_thr[((size_t)i * T + j) * F + col];
 }
 
 // The parent term S(tot, N) / N of the exact FP64 gain of every slot, the same
@@ -880,8 +900,7 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
   if (N == 0 || (uint64_t)N >= a.L_len) {
     if (part == 0 && threadIdx.x == 0) {
       SplitOut o;
-      o.t = o.f = o.j = -1;
-      o.pad = 0;
+      o.t = o.f = o.j = o.col = -1;
       o.gain = 0.0;
       a.out[slot] = o;
     }
@@ -980,14 +999,14 @@ __global__ void __launch_bounds__(kSplitCols) k_split_pick(SplitArgs a) {
     if (q.gain > b.gain || (q.gain == b.gain && q.idx < b.idx)) b = q;
   }
   SplitOut o;
-  o.pad = 0;
   if (b.idx == LLONG_MAX) {
-    o.t = o.f = o.j = -1;
+    o.t = o.f = o.j = o.col = -1;
     o.gain = 0.0;
   } else {
     o.t = (int32_t)(b.idx / F);
     o.f = (int32_t)(b.idx % F);
     o.j = b.j;
+    o.col = b.col;
     o.gain = b.gain;
     const uint32_t col = (uint32_t)b.col;
     for (uint32_t l = 0; l < K; l++) {
