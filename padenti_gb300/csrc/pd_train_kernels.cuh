@@ -303,6 +303,19 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
   // the lane's two threshold columns (rows of 32 entries, like the histogram)
   const FeatT *ta = sh_thr + lane, *tb = sh_thr + TP * 32 + lane;
   uint32_t *hl = sh_hist + lane;
+  // the first two levels of each column's search, in registers (two shared
+  // loads fewer per evaluation); not at 2 samples per iteration, whose register
+  // budget (3 CTAs per SM) has no room for them
+  constexpr bool kPivots = TP >= 8 && SPI >= 4;
+  FeatT a_p1 = 0, a_p2 = 0, a_p3 = 0, b_p1 = 0, b_p2 = 0, b_p3 = 0;
+  if constexpr (kPivots) {
+    a_p1 = ta[(TP / 2 - 1) * 32];
+    a_p2 = ta[(TP / 4 - 1) * 32];
+    a_p3 = ta[(3 * TP / 4 - 1) * 32];
+    b_p1 = tb[(TP / 2 - 1) * 32];
+    b_p2 = tb[(TP / 4 - 1) * 32];
+    b_p3 = tb[(3 * TP / 4 - 1) * 32];
+  }
   const uint32_t class_words = (T + 1) * 32;
   constexpr int PW = P::kPreWords;
   const unsigned full = 0xffffffffu;
@@ -354,10 +367,24 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
     auto accumulate = [&](const Eval &e) {
       // lower_bound over the padded sorted column: k = #thresholds < r
       const FeatT *pa = ta, *pb = tb;
+      if constexpr (kPivots) {
+        uint32_t ka = a_p1 < e.ra ? TP / 2 : 0u, kb = b_p1 < e.rb ? TP / 2 : 0u;
+        const FeatT qa = ka ? a_p3 : a_p2, qb = kb ? b_p3 : b_p2;
+        ka += qa < e.ra ? TP / 4 : 0u;
+        kb += qb < e.rb ? TP / 4 : 0u;
+        pa += ka * 32;
+        pb += kb * 32;
 #pragma unroll
-      for (uint32_t step = TP >> 1; step > 0; step >>= 1) {
-        if (pa[(step - 1) * 32] < e.ra) pa += step * 32;
-        if (pb[(step - 1) * 32] < e.rb) pb += step * 32;
+        for (uint32_t step = TP >> 3; step > 0; step >>= 1) {
+          if (pa[(step - 1) * 32] < e.ra) pa += step * 32;
+          if (pb[(step - 1) * 32] < e.rb) pb += step * 32;
+        }
+      } else {
+#pragma unroll
+        for (uint32_t step = TP >> 1; step > 0; step >>= 1) {
+          if (pa[(step - 1) * 32] < e.ra) pa += step * 32;
+          if (pb[(step - 1) * 32] < e.rb) pb += step * 32;
+        }
       }
       // rank k = (pa - ta) / 32 in [0, T]; histogram rows also hold 32 words,
       // so the word of rank k is (pa - ta) words into the class block.  Rank T
