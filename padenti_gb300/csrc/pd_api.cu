@@ -152,6 +152,9 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
     PD_CHECK(ds->width[i] >= 1 && ds->height[i] >= 1 && ds->width[i] < 65536 && ds->height[i] < 65536,
              PD_ERR_UNSUPPORTED, "image %u is %ux%u (sides must be in [1,65535])", i, ds->width[i], ds->height[i]);
     PD_CHECK(ds->samp_off[i + 1] >= ds->samp_off[i], PD_ERR_INVALID, "sample offsets not monotone at image %u", i);
+    PD_CHECK(ds->pix_off[i] % img_size(ctx->cfg.img_type) == 0, PD_ERR_INVALID,
+             "image %u starts at byte %llu, not a multiple of the pixel type size", i,
+             (unsigned long long)ds->pix_off[i]);
     off[i] = ds->pix_off[i];
     wh[i] = ds->width[i] | (ds->height[i] << 16);
     bytes = std::max<uint64_t>(bytes, ds->pix_off[i] + (uint64_t)ds->width[i] * ds->height[i] * px);
@@ -180,6 +183,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   PD_TRY(ctx->s_img.ensure(S * 4 + 4));
   PD_TRY(ctx->s_label.ensure(S + 4));
   PD_CUDA(h2d(ctx, ctx->pixels.ptr, ds->pixels, bytes));
+  PD_TRY(map_training_pixels(ctx, bytes));
   PD_CUDA(h2d(ctx, ctx->img_off.ptr, off.data(), n * 8));
   PD_CUDA(h2d(ctx, ctx->img_wh.ptr, wh.data(), n * 4));
   if (S) {

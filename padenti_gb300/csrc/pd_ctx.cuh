@@ -83,4 +83,6 @@ inline cudaError_t d2h(pd_ctx *c, void *dst, const void *src, size_t n) {
 namespace pd {
 int ensure_log2_table(pd_ctx *ctx, uint64_t n);
 int init_tables(pd_ctx *ctx);
+// Prepares the uploaded images for the plugin's eval_train (zero depths).
+int map_training_pixels(pd_ctx *ctx, uint64_t bytes);
 }

@@ -7,6 +7,9 @@
 //   prepare(im, x, y, pre)   builds the per-pixel state from those words;
 //   candidate(f)             per-candidate constants, computed once per tile;
 //   eval(prep, cand)         the response of one candidate at one pixel;
+//   eval_train(prep, cand)   the same on the trainer's copy of the images, which
+//                            kTrainMapsZero plugins store with 0 replaced by the
+//                            background depth (equal responses, one test fewer);
 // and kOrderDim, the feature dims (kOrderDim, kOrderDim + 1) of its first probe
 // offset, by which the trainer orders a node's candidates.
 // eval(prep, f) runs all of it for a single evaluation.
@@ -120,6 +123,7 @@ struct DepthDiff2 {
   static constexpr int kChannels = 1;
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF2;
   static constexpr int kOrderDim = 0;  // feature dims (0, 1): the first probe offset
+  static constexpr bool kTrainMapsZero = true;  // 0 and 10000 read alike everywhere
   struct Prep {
     const uint16_t *im;
     uint32_t w, h;
@@ -166,14 +170,24 @@ struct DepthDiff2 {
     if ((uint32_t)x < p.w && (uint32_t)y < p.h) v = ldg(p.im + ((uint32_t)y * p.w + (uint32_t)x));
     return v ? (int32_t)v : kBgDepth;
   }
-  template <bool FAST = false>
+  // On the trainer's copy (zeros stored as 10000): one predicated load, 10000
+  // outside the image.
+  static PD_D int32_t probe_train(const Prep &p, int32_t x, int32_t y) {
+    uint32_t v = (uint32_t)kBgDepth;
+    if ((uint32_t)x < p.w && (uint32_t)y < p.h) v = ldg(p.im + ((uint32_t)y * p.w + (uint32_t)x));
+    return (int32_t)v;
+  }
+  template <bool FAST = false, bool TRAIN = false>
   static PD_D int32_t eval(const Prep &p, const Cand &c) {
     const int32_t x1 = p.x + c.o[0].template apply<FAST>(p.div);
     const int32_t y1 = p.y + c.o[1].template apply<FAST>(p.div);
     const int32_t x2 = p.x + c.o[2].template apply<FAST>(p.div);
     const int32_t y2 = p.y + c.o[3].template apply<FAST>(p.div);
+    if (TRAIN) return probe_train(p, x1, y1) - probe_train(p, x2, y2);
     return probe(p, x1, y1) - probe(p, x2, y2);
   }
+  template <bool FAST = false>
+  static PD_D int32_t eval_train(const Prep &p, const Cand &c) { return eval<FAST, true>(p, c); }
   static PD_D int32_t eval(const Prep &p, const int32_t *f) { return eval(p, candidate(f)); }
 };
 
@@ -189,6 +203,7 @@ struct DepthDiff1 {
   static constexpr int kChannels = 1;
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF1;
   static constexpr int kOrderDim = 0;  // feature dims (0, 1): the probe offset
+  static constexpr bool kTrainMapsZero = false;  // the centre depth is used as read
   struct Prep {
     const uint16_t *im;
     uint32_t w, h;
@@ -250,6 +265,8 @@ struct DepthDiff1 {
     }
     return (int16_t)((int32_t)p.depth - probe);
   }
+  template <bool FAST = false>
+  static PD_D int16_t eval_train(const Prep &p, const Cand &c) { return eval<FAST>(p, c); }
   static PD_D int16_t eval(const Prep &p, const int16_t *f) { return eval(p, candidate(f)); }
 };
 
@@ -262,6 +279,7 @@ struct ChannelDiff {
   static constexpr int kChannels = 3;
   static constexpr int kId = PD_PLUGIN_CHANNEL_DIFF;
   static constexpr int kOrderDim = 2;  // feature dims (2, 3): the first probe offset
+  static constexpr bool kTrainMapsZero = false;
   struct Prep {
     const uint8_t *im;
     uint32_t w, h;
@@ -303,6 +321,8 @@ struct ChannelDiff {
   static PD_D int32_t eval(const Prep &p, const Cand &c) {
     return read(p, p.x + c.ux, p.y + c.uy, c.c1) - read(p, p.x + c.vx, p.y + c.vy, c.c2);
   }
+  template <bool FAST = false>
+  static PD_D int32_t eval_train(const Prep &p, const Cand &c) { return eval<FAST>(p, c); }
   static PD_D int32_t eval(const Prep &p, const int32_t *f) { return eval(p, candidate(f)); }
 };
 

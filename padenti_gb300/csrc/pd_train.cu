@@ -60,6 +60,20 @@ int ensure_log2_table(pd_ctx *ctx, uint64_t n) {
   return PD_OK;
 }
 
+int map_training_pixels(pd_ctx *ctx, uint64_t bytes) {
+  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() -> int {
+    if constexpr (P::kTrainMapsZero) {
+      static_assert(sizeof(typename P::img_t) == 2, "zero mapping of 16-bit images");
+      const uint64_t n = bytes / 2;
+      if (n) {
+        k_zero_to_background<<<4 * 152, 256, 0, ctx->stream>>>(ctx->pixels.as<uint16_t>(), n);
+        PD_CUDA(cudaGetLastError());
+      }
+    }
+    return PD_OK;
+  });
+}
+
 int init_tables(pd_ctx *ctx) {
   PD_TRY(ctx->magic_tab.ensure(65536 * 4));
   k_magic_table<<<256, 256, 0, ctx->stream>>>(ctx->magic_tab.as<uint32_t>());

@@ -359,8 +359,8 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
       im.magic = ds.magic;
       const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16), pre);
       Eval e;
-      e.ra = P::template eval<FAST>(prep, ca);
-      e.rb = P::template eval<FAST>(prep, cb);
+      e.ra = P::template eval_train<FAST>(prep, ca);
+      e.rb = P::template eval_train<FAST>(prep, cb);
       e.row = __shfl_sync(full, my_row, i);
       return e;
     };
@@ -1205,6 +1205,13 @@ static __global__ void k_iota(uint32_t *__restrict__ a, uint32_t *__restrict__ s
     a[i] = i;
     slot[i] = 0u;
   }
+}
+
+// The trainer's copy of uint16 depth images with 0 stored as the background
+// depth (plugins with kTrainMapsZero read both alike).
+static __global__ void k_zero_to_background(uint16_t *__restrict__ px, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    if (px[i] == 0) px[i] = (uint16_t)kBgDepth;
 }
 
 static __global__ void k_magic_table(uint32_t *__restrict__ out) {
