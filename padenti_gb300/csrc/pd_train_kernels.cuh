@@ -60,6 +60,13 @@ struct DevSet {
   const uint8_t *s_label;
 };
 
+// Brings the line holding p to L2 (no register result, no wait).
+PD_D void prefetch_l2(const void *p) {
+#if defined(__CUDA_ARCH__)
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+#endif
+}
+
 template <typename T>
 PD_D T max_of() {
   return (T)(sizeof(T) == 2 ? 32767 : 2147483647);
@@ -555,11 +562,15 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
         }
         const double g = dsub(hp64, ddiv(dadd(sl, sr), (double)N));
         const uint32_t f = f0 + c;
-        // the positions j..je share these counts: the lowest original threshold wins
-        uint32_t t = fs.perm[((size_t)slot * T + j) * F + f];
-        for (uint32_t je = j + 1; je < T && half16(sh_nl[je * 32 + (c & 31)], c) == nL; je++)
-          t = min(t, (uint32_t)fs.perm[((size_t)slot * T + je) * F + f]);
-        const long long idx = (long long)t * F + (fs.ord ? fs.ord[(size_t)slot * F + f] : f);
+        // the positions j..je share these counts: the lowest original threshold
+        // wins (the run's end first, then its loads all in flight together)
+        const uint32_t orig = fs.ord ? fs.ord[(size_t)slot * F + f] : f;
+        uint32_t je = j + 1;
+        while (je < T && half16(sh_nl[je * 32 + (c & 31)], c) == nL) je++;
+        uint32_t t = 0xffu;
+#pragma unroll 4
+        for (uint32_t jj = j; jj < je; jj++) t = min(t, (uint32_t)fs.perm[((size_t)slot * T + jj) * F + f]);
+        const long long idx = (long long)t * F + orig;
         if (g > best || (g == best && idx < best_idx)) {
           best = g;
           best_idx = idx;
@@ -693,6 +704,18 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
         (t < T && ff < F) ? cand_thr[((size_t)w.slot * T + t) * F + ff] : max_of<FeatT>();
   }
   for (uint32_t j = threadIdx.x; j < K * (T + 1) * 32; j += blockDim.x) sh_hist[j] = 0u;
+  if (w.multi == 2) {
+    // the fused split reads the tile's threshold permutation and column order
+    // at the end; bring them to L2 now
+    const uint32_t last = min(F - 1, f0 + kTileF - 1);  // the tile's last column
+    if (threadIdx.x < T) {
+      const uint8_t *r = fs.perm + ((size_t)w.slot * T + threadIdx.x) * F;
+      prefetch_l2(r + f0);
+      prefetch_l2(r + last);
+    } else if (fs.ord && threadIdx.x < T + 2) {
+      prefetch_l2(fs.ord + (size_t)w.slot * F + (threadIdx.x == T ? f0 : last));
+    }
+  }
   typename P::Cand ca, cb;
   {
     FeatT fva[D], fvb[D];
