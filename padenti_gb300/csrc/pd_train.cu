@@ -152,9 +152,14 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
     ctx->launches++;
     ord = ctx->cand_ord.as<uint32_t>();
   }
-  const size_t smem = (size_t)p->n_thresholds * kCandThreads * (sizeof(FeatT) + 1);
-  PD_CUDA(cudaFuncSetAttribute(k_candidates<FeatT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_candidates<FeatT><<<(unsigned)((total + kCandThreads - 1) / kCandThreads), kCandThreads, smem, ctx->stream>>>(
+  // draws lie in [lo, hi] (no narrowing wrap) and their offsets fit 24 bits:
+  // value and index sort as one word
+  const int64_t span = (int64_t)p->thr_up - p->thr_low;
+  const bool packed = span >= 0 && span < (1 << 24) && (sizeof(FeatT) == 4 || span <= 32767);
+  const size_t smem = (size_t)p->n_thresholds * kCandThreads * (packed ? 4 : sizeof(FeatT) + 1);
+  auto kern = packed ? k_candidates<FeatT, true> : k_candidates<FeatT, false>;
+  PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)((total + kCandThreads - 1) / kCandThreads), kCandThreads, smem, ctx->stream>>>(
       d_nodes, n, tree, F, p->n_thresholds, P::kFeatDim, b, ord, ctx->cand_feat.as<FeatT>(),
       ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>());
   PD_CUDA(cudaGetLastError());

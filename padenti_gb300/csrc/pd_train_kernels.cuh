@@ -81,7 +81,10 @@ PD_D T max_of() {
 constexpr int kCandThreads = 128;
 
 // Column c of slot n holds candidate ord[n][c] (c itself when ord is null).
-template <typename FeatT>
+// PACKED (threshold range below 2^24): value and original index sort as one
+// word (v - lo) << 8 | t, whose order is the stable order of the values; else
+// two shared-memory columns.
+template <typename FeatT, bool PACKED>
 __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__restrict__ nodes, uint32_t n_nodes,
                                                              uint32_t tree, uint32_t F, uint32_t T, int D,
                                                              CandBounds b, const uint32_t *__restrict__ ord,
@@ -89,6 +92,7 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
                                                              FeatT *__restrict__ thr_sorted,
                                                              uint8_t *__restrict__ perm) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint32_t *sk = reinterpret_cast<uint32_t *>(smem_raw);                         // PACKED: [T][128]
   FeatT *sv = reinterpret_cast<FeatT *>(smem_raw);                               // [T][128]
   uint8_t *si = reinterpret_cast<uint8_t *>(sv + (size_t)T * kCandThreads);      // [T][128]
   const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -100,6 +104,7 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
     FeatT fv[PD_MAX_FEAT_DIM];
     candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
     for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + c] = fv[d];
+    uint32_t *k = sk + threadIdx.x;
     FeatT *v = sv + threadIdx.x;
     uint8_t *id = si + threadIdx.x;
     uint32_t seed[4] = {tree, node, f, 1u}, st[4] = {0u, 0u, 0u, 0u};
@@ -114,20 +119,35 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
       const FeatT x = draw<FeatT>(st[t & 3u], b.thr_lo, b.thr_hi);
       // stable insertion
       uint32_t j = t;
-      while (j > 0 && v[(j - 1) * kCandThreads] > x) {
-        v[j * kCandThreads] = v[(j - 1) * kCandThreads];
-        id[j * kCandThreads] = id[(j - 1) * kCandThreads];
-        j--;
+      if (PACKED) {
+        const uint32_t key = ((uint32_t)((int32_t)x - b.thr_lo) << 8) | t;
+        while (j > 0 && k[(j - 1) * kCandThreads] > key) {
+          k[j * kCandThreads] = k[(j - 1) * kCandThreads];
+          j--;
+        }
+        k[j * kCandThreads] = key;
+      } else {
+        while (j > 0 && v[(j - 1) * kCandThreads] > x) {
+          v[j * kCandThreads] = v[(j - 1) * kCandThreads];
+          id[j * kCandThreads] = id[(j - 1) * kCandThreads];
+          j--;
+        }
+        v[j * kCandThreads] = x;
+        id[j * kCandThreads] = (uint8_t)t;
       }
-      v[j * kCandThreads] = x;
-      id[j * kCandThreads] = (uint8_t)t;
     }
   }
   __syncwarp();
   if (!active) return;
   for (uint32_t j = 0; j < T; j++) {
-    thr_sorted[((size_t)n * T + j) * F + c] = sv[j * kCandThreads + threadIdx.x];
-    perm[((size_t)n * T + j) * F + c] = si[j * kCandThreads + threadIdx.x];
+    if (PACKED) {
+      const uint32_t key = sk[j * kCandThreads + threadIdx.x];
+      thr_sorted[((size_t)n * T + j) * F + c] = (FeatT)((int32_t)(key >> 8) + b.thr_lo);
+      perm[((size_t)n * T + j) * F + c] = (uint8_t)(key & 0xffu);
+    } else {
+      thr_sorted[((size_t)n * T + j) * F + c] = sv[j * kCandThreads + threadIdx.x];
+      perm[((size_t)n * T + j) * F + c] = si[j * kCandThreads + threadIdx.x];
+    }
   }
 }
 

@@ -30,8 +30,12 @@ def test_log2_table_bit_identical():
     assert np.array_equal(g.view(np.uint64), o.view(np.uint64))
 
 
-def test_candidates_match_oracle():
+@pytest.mark.parametrize("thr_bounds", [(-500, 500), (-(1 << 30), 1 << 30)])
+def test_candidates_match_oracle(thr_bounds):
+    """Narrow threshold bounds sort (value, index) packed in one word; wide bounds
+    (a range of 2^24 or more) sort them as two columns."""
     cfg, ts, tp, _ = depth_case(n_images=2, n_features=100, n_thresholds=50)
+    tp = pg.TreeTrainerParameters(100, 50, [-60000] * 4, [60000] * 4, thr_bounds[0], thr_bounds[1], 20)
     tr = pg.TreeTrainer(cfg)
     nodes = np.array([0, 1, 2, 77, 4095, 123456], np.int32)
     feat, thr = tr.candidates(tp, 7, nodes)
