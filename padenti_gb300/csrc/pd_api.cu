@@ -77,7 +77,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   DevBuf *bufs[] = {&ctx->pixels, &ctx->img_off, &ctx->img_wh, &ctx->s_xy, &ctx->s_img, &ctx->s_label,
-                    &ctx->log2_tab, &ctx->magic_tab, &ctx->snode, &ctx->act[0], &ctx->act[1], &ctx->act_slot[0],
+                    &ctx->log2_tab, &ctx->magic_tab, &ctx->snode, &ctx->act[0], &ctx->act[1], &ctx->act_rec[0], &ctx->act_rec[1], &ctx->s_rec, &ctx->act_slot[0],
                     &ctx->act_slot[1], &ctx->flags, &ctx->scan_blocks, &ctx->slot_adj, &ctx->scatter_err,
                     &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->cand_ord, &ctx->parent, &ctx->xlog2_tab, &ctx->split_par, &ctx->hist, &ctx->g32, &ctx->items,
                     &ctx->zero_slots, &ctx->split_out, &ctx->split_cl, &ctx->recheck, &ctx->split_scratch, &ctx->fused_scratch, &ctx->t_lc,
@@ -144,6 +144,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   const uint32_t n = ds->n_images;
   const size_t px = img_size(ctx->cfg.img_type) * ctx->cfg.n_channels;
   const uint64_t S = ds->samp_off[n];
+  PD_CHECK(n < (1u << 24), PD_ERR_UNSUPPORTED, "%u images (max 2^24-1)", n);
   PD_CHECK(S < (1ull << 31), PD_ERR_UNSUPPORTED, "%llu samples (max 2^31-1)", (unsigned long long)S);
   uint64_t bytes = 0;
   std::vector<uint64_t> off(n);
@@ -191,6 +192,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
     PD_CUDA(h2d(ctx, ctx->s_img.ptr, im.data(), S * 4));
     PD_CUDA(h2d(ctx, ctx->s_label.ptr, lab.data(), S));
   }
+  PD_TRY(build_sample_records(ctx, S));
   PD_CUDA(cudaStreamSynchronize(st));
   ctx->h_label.swap(lab);
   ctx->pixels_bytes = bytes;

@@ -42,6 +42,8 @@ struct pd_ctx {
   // ---- training scratch ----
   pd::DevBuf snode;                  // int32 node per sample
   pd::DevBuf act[2], act_slot[2];    // active samples sorted by frontier slot
+  pd::DevBuf act_rec[2];             // their SampleRec, in the same order
+  pd::DevBuf s_rec;                  // SampleRec of every uploaded sample
   pd::DevBuf flags;                  // uint8 per active sample
   pd::DevBuf scan_blocks;            // uint64 per scan block
   pd::DevBuf slot_adj;               // int64 [4] per slot: adjL, adjR, kL, kR
@@ -85,4 +87,6 @@ int ensure_log2_table(pd_ctx *ctx, uint64_t n);
 int init_tables(pd_ctx *ctx);
 // Prepares the uploaded images for the plugin's eval_train (zero depths).
 int map_training_pixels(pd_ctx *ctx, uint64_t bytes);
+// The SampleRec of every uploaded sample (after map_training_pixels).
+int build_sample_records(pd_ctx *ctx, uint64_t n_samples);
 }

@@ -11,7 +11,7 @@ namespace pd {
 
 struct HistGrid {
   DevSet ds;
-  const uint32_t *act;
+  const SampleRec *rec;   // active samples of the work list's ranges
   const WorkItem *items;  // device work list
   uint64_t n_items;
   const void *cand_feat, *cand_thr;

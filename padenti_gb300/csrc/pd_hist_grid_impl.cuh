@@ -25,7 +25,7 @@ static int launch_hist_grid_as(pd_ctx *ctx, const HistGrid &g) {
   for (uint64_t b = 0; b < g.n_items; b += 0x7fffffffull) {
     const uint64_t cnt = std::min<uint64_t>(g.n_items - b, 0x7fffffffull);
     kern<<<(unsigned)cnt, kHistThreads, g.smem, ctx->stream>>>(
-        g.ds, g.act, g.items + b, static_cast<const FeatT *>(g.cand_feat), static_cast<const FeatT *>(g.cand_thr),
+        g.ds, g.rec, g.items + b, static_cast<const FeatT *>(g.cand_feat), static_cast<const FeatT *>(g.cand_thr),
         g.hist, g.F, g.T, g.K, g.fs);
     PD_CUDA(cudaGetLastError());
     ctx->launches++;

@@ -74,6 +74,17 @@ int map_training_pixels(pd_ctx *ctx, uint64_t bytes) {
   });
 }
 
+int build_sample_records(pd_ctx *ctx, uint64_t S) {
+  PD_TRY(ctx->s_rec.ensure(S * sizeof(SampleRec) + sizeof(SampleRec)));
+  if (!S) return PD_OK;
+  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() -> int {
+    k_build_rec<P><<<(unsigned)((S + 255) / 256), 256, 0, ctx->stream>>>(devset(ctx), (uint32_t)S,
+                                                                         ctx->s_rec.as<SampleRec>());
+    PD_CUDA(cudaGetLastError());
+    return PD_OK;
+  });
+}
+
 int init_tables(pd_ctx *ctx) {
   PD_TRY(ctx->magic_tab.ensure(65536 * 4));
   k_magic_table<<<256, 256, 0, ctx->stream>>>(ctx->magic_tab.as<uint32_t>());
@@ -175,7 +186,7 @@ template <class P>
 // split fused into the histogram kernel (multi = 2, rows never written) and the
 // other slots are returned for the split kernels.
 static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *off, uint32_t n,
-                       const uint32_t *d_act, uint64_t *n_items_out, cudaEvent_t ev_before = nullptr,
+                       const SampleRec *d_rec, uint64_t *n_items_out, cudaEvent_t ev_before = nullptr,
                        cudaEvent_t ev_after = nullptr, std::vector<uint32_t> *split_slots = nullptr,
                        const uint32_t *d_class_tot = nullptr, const uint32_t *d_ord = nullptr) {
   using FeatT = typename P::feat_t;
@@ -258,7 +269,7 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   }
   HistGrid g;
   g.ds = devset(ctx);
-  g.act = d_act;
+  g.rec = d_rec;
   g.items = ctx->items.as<WorkItem>();
   g.n_items = items.size();
   g.cand_feat = ctx->cand_feat.ptr;
@@ -277,14 +288,14 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
 }
 
 // Algorithmic HBM bytes of one histogram launch: the training-set images read
-// once, 9 bytes per active sample (index 4, packed x|y 4, class 1), the
+// once, 16 bytes per active sample (its SampleRec), the
 // candidate table of every slot read once, and the K*T*F uint32 histogram
 // written once for each slot whose split is not fused into the kernel.
 static uint64_t hist_algorithmic_bytes(const pd_ctx *ctx, const pd_train_params *p, uint64_t n_samples,
                                        uint32_t n_slots, uint32_t n_written, uint64_t image_bytes) {
   const uint64_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
   const uint64_t fs = feat_size(ctx->cfg.feat_type);
-  return image_bytes + 9ull * n_samples + (uint64_t)n_slots * (T * F * fs + ctx->cfg.feat_dim * F * fs) +
+  return image_bytes + (uint64_t)sizeof(SampleRec) * n_samples + (uint64_t)n_slots * (T * F * fs + ctx->cfg.feat_dim * F * fs) +
          (uint64_t)n_written * K * T * F * 4;
 }
 
@@ -387,6 +398,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   for (int b = 0; b < 2; b++) {
     PD_TRY(ctx->act[b].ensure(S * 4 + 4));
     PD_TRY(ctx->act_slot[b].ensure(S * 4 + 4));
+    PD_TRY(ctx->act_rec[b].ensure(S * sizeof(SampleRec) + sizeof(SampleRec)));
   }
   PD_TRY(ctx->flags.ensure(S + 16));
   PD_TRY(ctx->scan_blocks.ensure((S / kScanItems + 2) * 8 + 16));
@@ -394,7 +406,9 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   PD_CUDA(cudaMemsetAsync(ctx->snode.ptr, 0, S * 4, st));
   if (S) {
     k_iota<<<(unsigned)((S + 255) / 256), 256, 0, st>>>(ctx->act[0].as<uint32_t>(), ctx->act_slot[0].as<uint32_t>(), (uint32_t)S);
-    ctx->launches++;
+    k_gather_rec<<<(unsigned)((S + 255) / 256), 256, 0, st>>>(ctx->act[0].as<uint32_t>(), (uint32_t)S,
+                                                               ctx->s_rec.as<SampleRec>(), ctx->act_rec[0].as<SampleRec>());
+    ctx->launches += 2;
   }
   PD_CUDA(cudaGetLastError());
 
@@ -443,7 +457,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       PD_CUDA(cudaEventRecord(ev[1], st));
       uint64_t n_items = 0;
       std::vector<uint32_t> split_slots;
-      PD_TRY(launch_hist<P>(ctx, p, off.data(), ns, ctx->act[cur].as<uint32_t>(), &n_items, ev[6], ev[2],
+      PD_TRY(launch_hist<P>(ctx, p, off.data(), ns, ctx->act_rec[cur].as<SampleRec>(), &n_items, ev[6], ev[2],
                             &split_slots, d_ctot.as<uint32_t>(), d_ord));
       stats.hist_launches++;
       stats.hist_bytes += hist_algorithmic_bytes(ctx, p, off.back() - off.front(), ns, (uint32_t)split_slots.size(),
@@ -549,7 +563,8 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
     PD_CUDA(cudaEventRecord(ev[4], st));
     if (n_act) {
       k_reassign<P><<<(unsigned)((n_act + 255) / 256), 256, 0, st>>>(
-          devset(ctx), ctx->act[cur].as<uint32_t>(), ctx->act_slot[cur].as<uint32_t>(), (uint32_t)n_act,
+          devset(ctx), ctx->act[cur].as<uint32_t>(), ctx->act_rec[cur].as<SampleRec>(),
+          ctx->act_slot[cur].as<uint32_t>(), (uint32_t)n_act,
           ctx->snode.as<int32_t>(), ctx->t_lc.as<int32_t>(), ctx->t_feat.as<FeatT>(), ctx->t_thr.as<FeatT>(),
           d_next.as<SlotNext>(), ctx->flags.as<uint8_t>());
       PD_CUDA(cudaGetLastError());
@@ -565,6 +580,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       k_scatter<<<nb, 256, 0, st>>>(ctx->flags.as<uint8_t>(), (uint32_t)n_act, bs, ctx->act[cur].as<uint32_t>(),
                                     ctx->act_slot[cur].as<uint32_t>(), d_next.as<SlotNext>(), (uint32_t)n_next,
                                     ctx->act[1 - cur].as<uint32_t>(), ctx->act_slot[1 - cur].as<uint32_t>(),
+                                    ctx->act_rec[cur].as<SampleRec>(), ctx->act_rec[1 - cur].as<SampleRec>(),
                                     ctx->scatter_err.as<uint32_t>());
       PD_CUDA(cudaGetLastError());
       ctx->launches += 3;
@@ -696,16 +712,22 @@ extern "C" int pd_hist(pd_ctx *ctx, const pd_train_params *params, uint32_t tree
     if (slot_of[s] >= 0) act[pos[slot_of[s]]++] = (uint32_t)s;
   return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
     PD_TRY(ensure_slice(ctx, params, n_nodes));
-    DevBuf dn, da, dref;
+    DevBuf dn, da, drec, dref;
     PD_TRY(dn.ensure((size_t)n_nodes * 4));
     PD_TRY(da.ensure(act.size() * 4 + 4));
+    PD_TRY(drec.ensure(act.size() * sizeof(SampleRec) + sizeof(SampleRec)));
     PD_TRY(dref.ensure((size_t)n_nodes * K * T * F * 4 + 4));
     PD_CUDA(h2d(ctx, dn.ptr, nodes, (size_t)n_nodes * 4));
-    if (!act.empty())
+    if (!act.empty()) {
       PD_CUDA(h2d(ctx, da.ptr, act.data(), act.size() * 4));
+      k_gather_rec<<<(unsigned)((act.size() + 255) / 256), 256, 0, ctx->stream>>>(
+          da.as<uint32_t>(), (uint32_t)act.size(), ctx->s_rec.as<SampleRec>(), drec.as<SampleRec>());
+      PD_CUDA(cudaGetLastError());
+      ctx->launches++;
+    }
     PD_TRY(launch_candidates<P>(ctx, params, tree_id, dn.as<int32_t>(), n_nodes));
     uint64_t n_items = 0;
-    PD_TRY(launch_hist<P>(ctx, params, cnt.data(), n_nodes, da.as<uint32_t>(), &n_items));
+    PD_TRY(launch_hist<P>(ctx, params, cnt.data(), n_nodes, drec.as<SampleRec>(), &n_items));
     const uint64_t total = (uint64_t)n_nodes * K * F;
     if (total) {
       k_hist_to_ref<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(

@@ -60,6 +60,16 @@ struct DevSet {
   const uint8_t *s_label;
 };
 
+// What the kernels need of a sample, in one 16-byte word: its position, image
+// and class, and the plugin's preload words of its pixel (static per sample).
+// The active samples of a depth are kept as these records, in slot order, so a
+// warp reads 32 samples with one coalesced load.
+struct __align__(16) SampleRec {
+  uint32_t xy;       // x | y << 16
+  uint32_t img_lab;  // image | class << 24
+  uint32_t pre[2];   // P::preload words (kPreWords <= 2)
+};
+
 // Brings the line holding p to L2 (no register result, no wait).
 PD_D void prefetch_l2(const void *p) {
 #if defined(__CUDA_ARCH__)
@@ -321,7 +331,7 @@ constexpr uint32_t kMaxChunk = 65535;
 // probe loads in flight together) and adds both candidates of the lane into the
 // shared histogram.
 template <class P, uint32_t TP, bool FAST, int SPI>
-PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const WorkItem &w,
+PD_D void hist_samples(const DevSet &ds, const SampleRec *__restrict__ rec, const WorkItem &w,
                        const typename P::Cand &ca, const typename P::Cand &cb, uint32_t *sh_hist,
                        const typename P::feat_t *sh_thr, uint32_t T) {
   using FeatT = typename P::feat_t;
@@ -359,18 +369,14 @@ PD_D void hist_samples(const DevSet &ds, const uint32_t *__restrict__ act, const
 #pragma unroll
     for (int k = 0; k < PW; k++) my_pre[k] = 0u;
     if ((uint32_t)lane < n_here) {
-      const uint32_t s = act[base + lane];
-      my_xy = ds.s_xy[s];
-      my_row = (uint32_t)ds.s_label[s] * class_words;
-      const uint32_t imi = ds.s_img[s];
+      const uint4 r = ldg(reinterpret_cast<const uint4 *>(rec + base + lane));
+      my_xy = r.x;
+      my_row = (r.y >> 24) * class_words;
+      const uint32_t imi = r.y & 0xffffffu;
+      my_pre[0] = r.z;
+      if (PW > 1) my_pre[PW - 1] = r.w;
       my_off = ds.img_off[imi];
       my_wh = ds.img_wh[imi];
-      ImageRef<ImgT> im;
-      im.data = reinterpret_cast<const ImgT *>(ds.pixels + my_off);
-      im.w = (int32_t)(my_wh & 0xffffu);
-      im.h = (int32_t)(my_wh >> 16);
-      im.magic = ds.magic;
-      P::preload(im, (int32_t)(my_xy & 0xffffu), (int32_t)(my_xy >> 16), my_pre);
     }
     auto eval_at = [&](uint32_t i) -> Eval {
       const uint32_t xy = __shfl_sync(full, my_xy, i);
@@ -694,7 +700,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
 }
 
 template <class P, uint32_t TP, int SPI>
-__global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet ds, const uint32_t *__restrict__ act,
+__global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet ds, const SampleRec *__restrict__ rec,
                                                        const WorkItem *__restrict__ items,
                                                        const typename P::feat_t *__restrict__ cand_feat,
                                                        const typename P::feat_t *__restrict__ cand_thr,
@@ -749,8 +755,8 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   }
   // the exact-division fast path when every candidate of the tile allows it
   const bool fast = __syncthreads_and(P::fast(ca) && P::fast(cb));
-  if (fast) hist_samples<P, TP, true, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T);
-  else hist_samples<P, TP, false, SPI>(ds, act, w, ca, cb, sh_hist, sh_thr, T);
+  if (fast) hist_samples<P, TP, true, SPI>(ds, rec, w, ca, cb, sh_hist, sh_thr, T);
+  else hist_samples<P, TP, false, SPI>(ds, rec, w, ca, cb, sh_hist, sh_thr, T);
 
   __syncthreads();
   if (w.multi == 2) {
@@ -1103,7 +1109,8 @@ struct SlotNext {
 };
 
 template <class P>
-__global__ void k_reassign(DevSet ds, const uint32_t *__restrict__ act, const uint32_t *__restrict__ act_slot,
+__global__ void k_reassign(DevSet ds, const uint32_t *__restrict__ act, const SampleRec *__restrict__ rec,
+                           const uint32_t *__restrict__ act_slot,
                            uint32_t n_act, int32_t *__restrict__ snode, const int32_t *__restrict__ lc,
                            const typename P::feat_t *__restrict__ feat,
                            const typename P::feat_t *__restrict__ thr, const SlotNext *__restrict__ nxt,
@@ -1118,7 +1125,8 @@ __global__ void k_reassign(DevSet ds, const uint32_t *__restrict__ act, const ui
   const int32_t c = lc[n];
   uint8_t flag = 0;
   if (c >= 0) {
-    const uint32_t xy = ds.s_xy[s], im_i = ds.s_img[s];
+    const SampleRec r = rec[i];
+    const uint32_t xy = r.xy, im_i = r.img_lab & 0xffffffu;
     const uint32_t wh = ds.img_wh[im_i];
     ImageRef<ImgT> im;
     im.data = reinterpret_cast<const ImgT *>(ds.pixels + ds.img_off[im_i]);
@@ -1128,9 +1136,9 @@ __global__ void k_reassign(DevSet ds, const uint32_t *__restrict__ act, const ui
     FeatT fv[D];
 #pragma unroll
     for (int d = 0; d < D; d++) fv[d] = feat[(size_t)n * D + d];
-    const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16));
-    const FeatT r = P::eval(prep, fv);
-    const bool right = r > thr[n];
+    const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16), r.pre);
+    const FeatT resp = P::eval(prep, fv);
+    const bool right = resp > thr[n];
     snode[s] = c + (right ? 1 : 0);
     const SlotNext sn = nxt[act_slot[i]];
     if (right) flag = sn.k_r >= 0 ? 2 : 0;
@@ -1195,6 +1203,8 @@ static __global__ void __launch_bounds__(256) k_scatter(const uint8_t *__restric
                                                  const SlotNext *__restrict__ nxt, uint32_t n_next,
                                                  uint32_t *__restrict__ act_out,
                                                  uint32_t *__restrict__ slot_out,
+                                                 const SampleRec *__restrict__ rec,
+                                                 SampleRec *__restrict__ rec_out,
                                                  uint32_t *__restrict__ err) {
   constexpr int PER = kScanItems / 256;
   const uint32_t b0 = blockIdx.x * kScanItems + threadIdx.x * PER;
@@ -1239,7 +1249,39 @@ static __global__ void __launch_bounds__(256) k_scatter(const uint8_t *__restric
     }
     act_out[pos] = act[i];
     slot_out[pos] = kslot;
+    rec_out[pos] = rec[i];
   }
+}
+
+// rec[i] = the static record of sample act[i].
+static __global__ void k_gather_rec(const uint32_t *__restrict__ act, uint32_t n, const SampleRec *__restrict__ all,
+                                    SampleRec *__restrict__ rec) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) rec[i] = all[act[i]];
+}
+
+// The static record of every uploaded sample (after the plugin's image mapping).
+template <class P>
+__global__ void k_build_rec(DevSet ds, uint32_t n, SampleRec *__restrict__ rec) {
+  using ImgT = typename P::img_t;
+  static_assert(P::kPreWords <= 2, "a sample record holds two preload words");
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  SampleRec r;
+  r.xy = ds.s_xy[s];
+  const uint32_t imi = ds.s_img[s];
+  r.img_lab = imi | ((uint32_t)ds.s_label[s] << 24);
+  const uint32_t wh = ds.img_wh[imi];
+  ImageRef<ImgT> im;
+  im.data = reinterpret_cast<const ImgT *>(ds.pixels + ds.img_off[imi]);
+  im.w = (int32_t)(wh & 0xffffu);
+  im.h = (int32_t)(wh >> 16);
+  im.magic = ds.magic;
+  uint32_t pre[2] = {0u, 0u};
+  P::preload(im, (int32_t)(r.xy & 0xffffu), (int32_t)(r.xy >> 16), pre);
+  r.pre[0] = pre[0];
+  r.pre[1] = pre[1];
+  rec[s] = r;
 }
 
 static __global__ void k_iota(uint32_t *__restrict__ a, uint32_t *__restrict__ slot, uint32_t n) {
