@@ -162,10 +162,11 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
 }
 
 // ------------------------------------------------------ candidate order ----
-// Column order of a node's candidate table: the candidates sorted by the Morton
-// code of their first probe offset (feature dims kOrderDim and kOrderDim + 1,
+// Column order of a node's candidate table: the candidates sorted row-major by
+// their first probe offset (feature dims kOrderDim + 1 = y, then kOrderDim = x,
 // each scaled to 10 bits over its bounds).  The 32 lanes of a histogram warp
-// then probe nearby pixels and share cache sectors.  Only the placement
+// then probe pixels of few image rows and share cache sectors (a sector is 16
+// pixels of one row: row-major groups beat square ones).  Only the placement
 // changes: split decisions use the original index f (ties to the lowest
 // t*F + f).  Block per slot; bitonic sort of (code << 32 | f) in shared memory
 // over the next power of two of F.
@@ -177,16 +178,6 @@ PD_D uint32_t order_quant10(int32_t v, int32_t lo, int32_t up) {
   const int64_t q = span > 0 ? x * 1024 / span : 0;
   return (uint32_t)(q < 0 ? 0 : (q > 1023 ? 1023 : q));
 }
-// bits 0..15 of v to the even bits of the result
-PD_D uint32_t order_spread(uint32_t v) {
-  v &= 0xffffu;
-  v = (v | (v << 8)) & 0x00ff00ffu;
-  v = (v | (v << 4)) & 0x0f0f0f0fu;
-  v = (v | (v << 2)) & 0x33333333u;
-  v = (v | (v << 1)) & 0x55555555u;
-  return v;
-}
-
 template <class P>
 __global__ void __launch_bounds__(kOrderThreads) k_cand_order(const int32_t *__restrict__ nodes, uint32_t tree,
                                                               uint32_t F, CandBounds b, uint32_t *__restrict__ ord) {
@@ -204,7 +195,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_cand_order(const int32_t *__r
       candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
       const uint32_t qx = order_quant10((int32_t)fv[X], b.low[X], b.up[X]);
       const uint32_t qy = order_quant10((int32_t)fv[X + 1], b.low[X + 1], b.up[X + 1]);
-      k = ((unsigned long long)(order_spread(qx) | (order_spread(qy) << 1)) << 32) | f;
+      k = ((unsigned long long)((qy << 10) | qx) << 32) | f;
     }
     key[f] = k;
   }
@@ -340,11 +331,20 @@ PD_D void hist_samples(const DevSet &ds, const SampleRec *__restrict__ rec, cons
   // the lane's two threshold columns (rows of 32 entries, like the histogram)
   const FeatT *ta = sh_thr + lane, *tb = sh_thr + TP * 32 + lane;
   uint32_t *hl = sh_hist + lane;
-  // the first two levels of each column's search, in registers (two shared
-  // loads fewer per evaluation); not at 2 samples per iteration, whose register
-  // budget (3 CTAs per SM) has no room for them
+  // the first levels of each column's search in registers -- two at 8 rows,
+  // three from 16 rows up (3 pivots, then 4 more per column): that many shared
+  // loads fewer per evaluation.  Not at 2 samples per iteration, whose register
+  // budget (3 CTAs per SM) has no room for them.
   constexpr bool kPivots = TP >= 8 && SPI >= 4;
   FeatT a_p1 = 0, a_p2 = 0, a_p3 = 0, b_p1 = 0, b_p2 = 0, b_p3 = 0;
+  FeatT a_q[4] = {0, 0, 0, 0}, b_q[4] = {0, 0, 0, 0};
+  if constexpr (kPivots && TP >= 16) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      a_q[k] = ta[((2 * k + 1) * TP / 8 - 1) * 32];
+      b_q[k] = tb[((2 * k + 1) * TP / 8 - 1) * 32];
+    }
+  }
   if constexpr (kPivots) {
     a_p1 = ta[(TP / 2 - 1) * 32];
     a_p2 = ta[(TP / 4 - 1) * 32];
@@ -405,10 +405,19 @@ PD_D void hist_samples(const DevSet &ds, const SampleRec *__restrict__ rec, cons
         const FeatT qa = ka ? a_p3 : a_p2, qb = kb ? b_p3 : b_p2;
         ka += qa < e.ra ? TP / 4 : 0u;
         kb += qb < e.rb ? TP / 4 : 0u;
+        constexpr uint32_t first = TP >= 16 ? (TP >> 4) : (TP >> 3);
+        if constexpr (TP >= 16) {
+          // third level: the pivot of the quarter reached so far
+          const uint32_t ia = ka / (TP / 4), ib = kb / (TP / 4);
+          const FeatT ra = ia & 2 ? (ia & 1 ? a_q[3] : a_q[2]) : (ia & 1 ? a_q[1] : a_q[0]);
+          const FeatT rb = ib & 2 ? (ib & 1 ? b_q[3] : b_q[2]) : (ib & 1 ? b_q[1] : b_q[0]);
+          ka += ra < e.ra ? TP / 8 : 0u;
+          kb += rb < e.rb ? TP / 8 : 0u;
+        }
         pa += ka * 32;
         pb += kb * 32;
 #pragma unroll
-        for (uint32_t step = TP >> 3; step > 0; step >>= 1) {
+        for (uint32_t step = first; step > 0; step >>= 1) {
           if (pa[(step - 1) * 32] < e.ra) pa += step * 32;
           if (pb[(step - 1) * 32] < e.rb) pb += step * 32;
         }
