@@ -375,7 +375,8 @@ def run_ours(a):
                 algorithmic_bytes_per_launch=hist_bytes / max(1, hist_launches),
                 launch_ms=hist_ms / max(1, hist_launches),
                 evals_per_s_in_kernel=evals / hist_s if hist_s > 0 else None,
-                note="the histogram kernel is issue-bound (integer ALU + shared atomics), not HBM-bound")
+                note="the histogram kernel is bound by instruction issue and the L1 data pipe (probe gathers, "
+                     "threshold search), not by HBM")
     base = None
     if not a.no_cpu:
         base, _ = cpu_sample(a, cfg, ts, tp, a.cpu_seconds)
