@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "pd_ctx.cuh"
@@ -84,6 +85,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
                     &ctx->f_post, &ctx->f_meta, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
   for (DevBuf *b : bufs) b->release();
+  ctx->h_stage.release();
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);
@@ -160,21 +162,54 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
     wh[i] = ds->width[i] | (ds->height[i] << 16);
     bytes = std::max<uint64_t>(bytes, ds->pix_off[i] + (uint64_t)ds->width[i] * ds->height[i] * px);
   }
-  std::vector<uint32_t> xy(S), im(S);
-  std::vector<uint8_t> lab(S);
-  for (uint32_t i = 0; i < n; i++) {
-    const uint32_t w = ds->width[i], h = ds->height[i];
-    for (uint64_t k = ds->samp_off[i]; k < ds->samp_off[i + 1]; k++) {
-      const uint32_t p = ds->samples[k];
-      PD_CHECK((uint64_t)p < (uint64_t)w * h, PD_ERR_INVALID, "sample %llu of image %u outside the image", (unsigned long long)k, i);
-      const uint8_t l = ds->labels[ds->lab_off[i] + p];
-      PD_CHECK(l >= 1 && l <= ctx->cfg.n_classes, PD_ERR_INVALID,
-               "sample %llu of image %u has label %u (sampled pixels need a label in [1,%d])",
-               (unsigned long long)k, i, l, ctx->cfg.n_classes);
-      xy[k] = (p % w) | ((p / w) << 16);
-      im[k] = i;
-      lab[k] = (uint8_t)(l - 1);
+  // per-sample position, image and class: host threads over interleaved images,
+  // into pinned staging; each thread keeps its first bad sample and the lowest
+  // one is reported (the one a sequential pass meets first)
+  PD_TRY(ctx->h_stage.ensure(S * 9 + 16));
+  uint32_t *xy = ctx->h_stage.as<uint32_t>(), *im = xy + S;
+  uint8_t *lab = reinterpret_cast<uint8_t *>(im + S);
+  const unsigned nt = std::max(1u, std::min({16u, std::thread::hardware_concurrency(), n}));
+  struct Bad {
+    uint64_t k = UINT64_MAX;
+    uint32_t image = 0;
+    int label = -1;  // -1: the sample lies outside the image
+  };
+  std::vector<Bad> bad(nt);
+  auto work = [&](unsigned t) {
+    for (uint32_t i = t; i < n; i += nt) {
+      const uint32_t w = ds->width[i], h = ds->height[i];
+      for (uint64_t k = ds->samp_off[i]; k < ds->samp_off[i + 1]; k++) {
+        const uint32_t p = ds->samples[k];
+        if ((uint64_t)p >= (uint64_t)w * h) {
+          if (k < bad[t].k) bad[t] = {k, i, -1};
+          continue;
+        }
+        const uint8_t l = ds->labels[ds->lab_off[i] + p];
+        if (l < 1 || l > ctx->cfg.n_classes) {
+          if (k < bad[t].k) bad[t] = {k, i, (int)l};
+          continue;
+        }
+        xy[k] = (p % w) | ((p / w) << 16);
+        im[k] = i;
+        lab[k] = (uint8_t)(l - 1);
+      }
     }
+  };
+  {
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nt; t++) th.emplace_back(work, t);
+    work(0);
+    for (auto &x : th) x.join();
+  }
+  Bad first;
+  for (const Bad &b : bad)
+    if (b.k < first.k) first = b;
+  if (first.k != UINT64_MAX) {
+    if (first.label < 0)
+      return set_error(PD_ERR_INVALID, "sample %llu of image %u outside the image", (unsigned long long)first.k,
+                       first.image);
+    return set_error(PD_ERR_INVALID, "sample %llu of image %u has label %d (sampled pixels need a label in [1,%d])",
+                     (unsigned long long)first.k, first.image, first.label, ctx->cfg.n_classes);
   }
   cudaStream_t st = ctx->stream;
   PD_TRY(ctx->pixels.ensure(bytes));
@@ -188,13 +223,13 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   PD_CUDA(h2d(ctx, ctx->img_off.ptr, off.data(), n * 8));
   PD_CUDA(h2d(ctx, ctx->img_wh.ptr, wh.data(), n * 4));
   if (S) {
-    PD_CUDA(h2d(ctx, ctx->s_xy.ptr, xy.data(), S * 4));
-    PD_CUDA(h2d(ctx, ctx->s_img.ptr, im.data(), S * 4));
-    PD_CUDA(h2d(ctx, ctx->s_label.ptr, lab.data(), S));
+    PD_CUDA(h2d(ctx, ctx->s_xy.ptr, xy, S * 4));
+    PD_CUDA(h2d(ctx, ctx->s_img.ptr, im, S * 4));
+    PD_CUDA(h2d(ctx, ctx->s_label.ptr, lab, S));
   }
   PD_TRY(build_sample_records(ctx, S));
+  ctx->h_label.assign(lab, lab + S);
   PD_CUDA(cudaStreamSynchronize(st));
-  ctx->h_label.swap(lab);
   ctx->pixels_bytes = bytes;
   ctx->n_images = n;
   ctx->n_samples = S;

@@ -128,6 +128,32 @@ struct DevBuf {
   template <typename T> T *as() const { return static_cast<T *>(ptr); }
 };
 
+// Grow-only page-locked host buffer (staging for host -> device copies).
+struct HostBuf {
+  void *ptr = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return PD_OK;
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMallocHost(&ptr, bytes);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      cudaGetLastError();
+      return set_error(PD_ERR_NOMEM, "cudaMallocHost(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    cap = bytes;
+    return PD_OK;
+  }
+  void release() {
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
 inline size_t feat_size(int feat_type) { return feat_type == PD_FEAT_I16 ? 2 : 4; }
 inline size_t img_size(int img_type) { return img_type == PD_IMG_U8 ? 1 : 2; }
 

@@ -142,6 +142,38 @@ def test_pure_nodes_bit_exact():
             _assert_same_tree(t, o)
 
 
+def test_upload_rejects_bad_samples_and_keeps_the_previous_set():
+    """A sample outside its image or on an unlabelled pixel fails the upload with the first
+    bad sample in sample order (the check runs on several host threads); the training set
+    uploaded before stays in place."""
+    import ctypes as C
+    from padenti_gb300 import _native as N
+
+    cfg, ts, tp, _ = depth_case(n_images=10, n_features=32, n_thresholds=10)
+    tr = pg.TreeTrainer(cfg)
+    tr.upload(ts)
+    a = pg.Tree(cfg, 0, 5)
+    tr.train(a, ts, tp)
+    flat = ts.flat()
+    w, h = int(flat["width"][0]), int(flat["height"][0])
+    first7, first3 = int(flat["samp_off"][7]) + 5, int(flat["samp_off"][3]) + 2
+    bad = {k: v.copy() for k, v in flat.items()}
+    bad["samples"][first7] = w * h          # outside image 7
+    bad["samples"][first3] = w * h + 10     # outside image 3: the first in sample order
+    with pytest.raises(pg.PadentiError, match=f"sample {first3} of image 3 outside the image"):
+        N.check(N.lib().pd_dataset_upload(tr.h, C.byref(pg.TrainingSet.desc(bad))))
+    unl = {k: v.copy() for k, v in flat.items()}
+    lab_off = int(flat["lab_off"][4])
+    k4 = int(flat["samp_off"][4])
+    unl["labels"][lab_off + int(unl["samples"][k4])] = 0
+    with pytest.raises(pg.PadentiError, match=f"sample {k4} of image 4 has label 0"):
+        N.check(N.lib().pd_dataset_upload(tr.h, C.byref(pg.TrainingSet.desc(unl))))
+    b = pg.Tree(cfg, 0, 5)
+    tr.train(b, ts, tp)  # the set uploaded first is still there
+    assert np.array_equal(a.left_child, b.left_child)
+    assert np.array_equal(a.features, b.features) and np.array_equal(a.thresholds, b.thresholds)
+
+
 def test_train_tree_config0_bit_exact():
     """The full 64-image 160x120 configuration: F=200, T=20, depth 8, min 20 pixels per leaf."""
     cfg, ts, tp, _ = depth_case(n_images=64, n_features=200, n_thresholds=20)
