@@ -86,6 +86,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
                     &ctx->f_post, &ctx->f_meta, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
   for (DevBuf *b : bufs) b->release();
   ctx->h_stage.release();
+  ctx->h_items.release();
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   cudaStreamDestroy(ctx->stream);

@@ -33,6 +33,7 @@ struct pd_ctx {
   pd::DevBuf s_label;   // uint8 class (0..K-1) per sample
   std::vector<uint8_t> h_label;  // host copy of the sample classes
   pd::HostBuf h_stage;           // pinned staging of the per-sample upload arrays
+  pd::HostBuf h_items;           // pinned staging of a histogram launch's work list
   pd::DevBuf log2_tab;  // double log2(n), n < log2_len
   pd::DevBuf xlog2_tab; // float c*log2(c), c < min(log2_len, 65536): the fused split's filter
   pd::DevBuf parent;    // [slots] parent term of the exact gain, for the fused split

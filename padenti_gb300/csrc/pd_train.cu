@@ -193,7 +193,12 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   const uint32_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
   const uint32_t tiles = (F + kTileF - 1) / kTileF;
   PD_CHECK(ctx->chunk >= 1 && ctx->chunk <= kMaxChunk, PD_ERR_INVALID, "chunk %u outside [1,%u]", ctx->chunk, kMaxChunk);
-  std::vector<WorkItem> items;
+  // the work list is written straight into pinned staging (sized by a first pass)
+  uint64_t n_items = 0;
+  for (uint32_t i = 0; i < n; i++) n_items += (off[i + 1] - off[i] + ctx->chunk - 1) / ctx->chunk * tiles;
+  PD_TRY(ctx->h_items.ensure(std::max<uint64_t>(1, n_items) * sizeof(WorkItem)));
+  WorkItem *items = ctx->h_items.as<WorkItem>();
+  uint64_t ni = 0;
   std::vector<uint32_t> zero;
   for (uint32_t i = 0; i < n; i++) {
     const uint64_t b = off[i], e = off[i + 1];
@@ -218,12 +223,12 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
         w.begin = cb;
         w.end = ce;
         w.multi = chunks > 1 ? 1u : (fused ? 2u : 0u);
-        items.push_back(w);
+        items[ni++] = w;
       }
     }
   }
-  *n_items_out = items.size();
-  PD_TRY(ctx->items.ensure(std::max<size_t>(1, items.size()) * sizeof(WorkItem)));
+  *n_items_out = ni;
+  PD_TRY(ctx->items.ensure(std::max<size_t>(1, ni) * sizeof(WorkItem)));
   PD_TRY(ctx->zero_slots.ensure(std::max<size_t>(1, zero.size()) * 4));
   const uint64_t per_slot = (uint64_t)K * T * F;
   if (!zero.empty()) {
@@ -233,14 +238,14 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     PD_CUDA(cudaGetLastError());
   }
   if (!zero.empty()) ctx->launches++;
-  if (items.empty()) {
+  if (!ni) {
     if (ev_before) PD_CUDA(cudaEventRecord(ev_before, ctx->stream));
     if (ev_after) PD_CUDA(cudaEventRecord(ev_after, ctx->stream));
     return PD_OK;
   }
-  PD_CUDA(h2d(ctx, ctx->items.ptr, items.data(), items.size() * sizeof(WorkItem)));
+  PD_CUDA(h2d(ctx, ctx->items.ptr, items, ni * sizeof(WorkItem)));
   bool any_fused = false;
-  for (const WorkItem &w : items) any_fused |= w.multi == 2;
+  for (uint64_t k = 0; k < ni; k++) any_fused |= items[k].multi == 2;
   const size_t smem = hist_smem(ctx, T, any_fused);
   FusedSplit fs;
   memset(&fs, 0, sizeof(fs));
@@ -271,7 +276,7 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   g.ds = devset(ctx);
   g.rec = d_rec;
   g.items = ctx->items.as<WorkItem>();
-  g.n_items = items.size();
+  g.n_items = ni;
   g.cand_feat = ctx->cand_feat.ptr;
   g.cand_thr = ctx->cand_thr.ptr;
   g.hist = ctx->hist.as<uint32_t>();
