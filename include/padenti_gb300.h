@@ -23,8 +23,10 @@
 #ifndef PADENTI_GB300_H
 #define PADENTI_GB300_H
 
+#if !defined(__CUDACC_RTC__)
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -56,6 +58,9 @@ extern "C" {
 #define PD_PLUGIN_DEPTH_DIFF2 1
 #define PD_PLUGIN_DEPTH_DIFF1 2
 #define PD_PLUGIN_CHANNEL_DIFF 3
+/* A feature compiled at run time from CUDA source (pd_plugin_compile), the
+ * counterpart of the reference's user feature.cl. */
+#define PD_PLUGIN_USER 100
 
 #define PD_MAX_FEAT_DIM 8
 #define PD_MAX_CLASSES 64
@@ -126,6 +131,27 @@ int pd_version(void);
 /* Context ------------------------------------------------------------------ */
 int pd_ctx_create(const pd_config *cfg, int device, pd_ctx **out);
 int pd_ctx_destroy(pd_ctx *ctx);
+
+/* User feature plugins -------------------------------------------------------
+ * Replaces the reference's run-time compiled feature.cl (CLTreeTrainer and
+ * CLClassifier build it into their OpenCL program: cl_tree_trainer_impl.hpp:73-198,
+ * cl_classifier_impl.hpp:72-140; prototype padenti.hpp.in:169-187).  A context
+ * created with plugin = PD_PLUGIN_USER compiles CUDA source that defines
+ *
+ *   __device__ feat_t computeFeature(const pd::ImageView &img, int2 coords,
+ *                                    const feat_t *features, unsigned featDim);
+ *
+ * with NVRTC for the context's GPU.  img_t, feat_t, PD_FEAT_DIM and PD_CHANNELS
+ * are defined before the source from the configuration (the reference generates
+ * feat_type.cl the same way); img.read(x, y, c) returns 0 outside the image.
+ * The configuration must have the types and dimensions of a built-in plugin:
+ * (uint16, 1 channel, int32, 4), (uint16, 1, int16, 2) or (uint8, 3, int32, 6).
+ * Compile before uploading a training set or adding trees; compiling again
+ * replaces the plugin (the training set must then be uploaded again). */
+int pd_plugin_compile(pd_ctx *ctx, const char *source);
+/* Compiles only (no GPU needed): PD_OK, or PD_ERR_INVALID with the compiler's
+ * log in log[0..log_size) (NUL-terminated; may be NULL). */
+int pd_plugin_check(const pd_config *cfg, const char *source, char *log, size_t log_size);
 /* Device memory the training pass may use for histograms (default 8 GiB);
  * frontiers whose histograms exceed it are processed in slices, as the
  * reference does with its 20 GiB host cap (cl_tree_trainer_impl.hpp:47-50). */

@@ -22,7 +22,7 @@ from ._native import PadentiError, check, lib
 
 __all__ = [
     "ForestConfig", "TreeTrainerParameters", "TrainingSetImage", "TrainingSet", "Tree", "TreeTrainer",
-    "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS",
+    "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS", "USER_SHAPES", "check_plugin",
 ]
 
 FEAT_DTYPE = {N.PD_FEAT_I16: np.int16, N.PD_FEAT_I32: np.int32}
@@ -38,6 +38,14 @@ PLUGINS = {
                          feat_type=N.PD_FEAT_I32, feat_dim=6),
 }
 
+# Types and dimensions a user feature (plugin "user", compiled at run time from
+# CUDA source defining computeFeature) may have: those of the built-in plugins.
+USER_SHAPES = {
+    "u16x1_i32x4": dict(img_type=N.PD_IMG_U16, n_channels=1, feat_type=N.PD_FEAT_I32, feat_dim=4),
+    "u16x1_i16x2": dict(img_type=N.PD_IMG_U16, n_channels=1, feat_type=N.PD_FEAT_I16, feat_dim=2),
+    "u8x3_i32x6": dict(img_type=N.PD_IMG_U8, n_channels=3, feat_type=N.PD_FEAT_I32, feat_dim=6),
+}
+
 
 def _ptr(a: np.ndarray | None) -> int | None:
     return None if a is None else a.ctypes.data
@@ -45,17 +53,26 @@ def _ptr(a: np.ndarray | None) -> int | None:
 
 @dataclass(frozen=True)
 class ForestConfig:
-    """<ImgType, nChannels, FeatType, FeatDim, nClasses> for one plugin."""
+    """<ImgType, nChannels, FeatType, FeatDim, nClasses> for one plugin: a built-in one, or
+    plugin="user" with the CUDA `source` of computeFeature (the reference's feature.cl) and one
+    of the USER_SHAPES."""
 
     plugin: str
     n_classes: int
+    source: str | None = None
+    shape: str | None = None
 
     def __post_init__(self):
-        if self.plugin not in PLUGINS:
-            raise ValueError(f"unknown plugin {self.plugin!r}; built-in: {sorted(PLUGINS)}")
+        if self.plugin == "user":
+            if self.shape not in USER_SHAPES or not self.source:
+                raise ValueError(f"a user plugin needs source and a shape in {sorted(USER_SHAPES)}")
+        elif self.plugin not in PLUGINS:
+            raise ValueError(f"unknown plugin {self.plugin!r}; built-in: {sorted(PLUGINS)} or 'user'")
 
     @property
     def spec(self) -> dict:
+        if self.plugin == "user":
+            return dict(plugin=N.PD_PLUGIN_USER, **USER_SHAPES[self.shape])
         return PLUGINS[self.plugin]
 
     @property
@@ -252,12 +269,23 @@ class Tree:
                 self.thresholds[i] = int(v[D])
 
 
+def check_plugin(config: ForestConfig) -> str:
+    """Compiles a user plugin's source without a GPU; returns the compiler log, raises
+    PadentiError (with the log) when it does not compile."""
+    buf = C.create_string_buffer(1 << 16)
+    rc = lib().pd_plugin_check(C.byref(config.c()), config.source.encode(), buf, len(buf))
+    check(rc)
+    return buf.value.decode()
+
+
 class _Ctx:
     def __init__(self, config: ForestConfig, device: int = 0):
         self.config = config
         h = C.c_void_p()
         check(lib().pd_ctx_create(C.byref(config.c()), device, C.byref(h)))
         self.h = h
+        if config.plugin == "user":
+            check(lib().pd_plugin_compile(h, config.source.encode()))
 
     def __del__(self):
         h = getattr(self, "h", None)

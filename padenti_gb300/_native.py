@@ -17,6 +17,7 @@ PD_OK = 0
 PD_IMG_U8, PD_IMG_U16 = 1, 2
 PD_FEAT_I16, PD_FEAT_I32 = 1, 2
 PD_PLUGIN_DEPTH_DIFF2, PD_PLUGIN_DEPTH_DIFF1, PD_PLUGIN_CHANNEL_DIFF = 1, 2, 3
+PD_PLUGIN_USER = 100
 PD_MAX_FEAT_DIM = 8
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "unsupported", -5: "bad state"}
@@ -78,6 +79,8 @@ _SIGS = {
     "pd_version": (C.c_int, []),
     "pd_ctx_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(_P)]),
     "pd_ctx_destroy": (C.c_int, [_P]),
+    "pd_plugin_compile": (C.c_int, [_P, C.c_char_p]),
+    "pd_plugin_check": (C.c_int, [C.POINTER(Config), C.c_char_p, C.c_char_p, C.c_size_t]),
     "pd_ctx_set_hist_budget": (C.c_int, [_P, C.c_uint64]),
     "pd_ctx_set_tuning": (C.c_int, [_P, C.c_char_p, C.c_int64]),
     "pd_ctx_sync": (C.c_int, [_P]),

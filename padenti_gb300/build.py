@@ -41,9 +41,29 @@ def _stale(obj: pathlib.Path, src: pathlib.Path, deps: list[pathlib.Path]) -> bo
     return any(d.stat().st_mtime > t for d in [src, *deps])
 
 
+# Headers compiled again at run time by NVRTC for user feature plugins; they are
+# embedded into the library as raw string literals (_build/pd_rtc_sources.inc).
+RTC_HEADERS = ["padenti_gb300.h", "pd_common.cuh", "pd_log2.cuh", "pd_rng.cuh", "pd_plugins.cuh",
+               "pd_train_kernels.cuh", "pd_predict_kernels.cuh", "pd_user_plugin.cuh", "pd_user_plugin_impl.cuh"]
+
+
+def _embed_rtc_sources() -> None:
+    out = OUT / "pd_rtc_sources.inc"
+    parts = []
+    for name in RTC_HEADERS:
+        path = (REPO / "include" / name) if name.endswith(".h") else (CSRC / name)
+        text = path.read_text()
+        if ")pdrtc\"" in text:
+            raise RuntimeError(f"{path} contains the raw-string delimiter")
+        parts.append(f'{{"{name}", R"pdrtc({text})pdrtc"}},\n')
+    data = "".join(parts)
+    if not out.exists() or out.read_text() != data:
+        out.write_text(data)
+
+
 def _compile(src: pathlib.Path, extra: list[str]) -> pathlib.Path:
     obj = OUT / (src.name + ".o")
-    inc = [f"-I{REPO / 'include'}", f"-I{CSRC}"]
+    inc = [f"-I{REPO / 'include'}", f"-I{CSRC}", f"-I{OUT}"]
     if src.suffix == ".cu":
         cmd = [_nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++20", "--expt-relaxed-constexpr",
                "-Xcompiler", "-fPIC,-ffp-contract=off", *inc, *extra, "-c", str(src), "-o", str(obj)]
@@ -61,6 +81,7 @@ def _compile(src: pathlib.Path, extra: list[str]) -> pathlib.Path:
 def build(force: bool = False, extra_nvcc: list[str] | None = None) -> pathlib.Path:
     """Builds (if needed) and returns the path of libpadenti_gb300.so."""
     OUT.mkdir(parents=True, exist_ok=True)
+    _embed_rtc_sources()
     srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     deps = _headers()
     todo = [s for s in srcs if force or _stale(OUT / (s.name + ".o"), s, deps)]
@@ -68,7 +89,7 @@ def build(force: bool = False, extra_nvcc: list[str] | None = None) -> pathlib.P
         list(ex.map(lambda s: _compile(s, extra_nvcc or []), todo))
     objs = [OUT / (s.name + ".o") for s in srcs]
     if force or todo or not LIB.exists():
-        cmd = [_nvcc(), ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart",
+        cmd = [_nvcc(), ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lnvrtc",
                "-Xlinker", f"-rpath,{CUDA_HOME}/lib64"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -7,6 +7,7 @@
 
 #include "pd_ctx.cuh"
 #include "pd_plugins.cuh"
+#include "pd_rtc.cuh"
 
 namespace pd {
 
@@ -28,7 +29,7 @@ static int check_config(const pd_config *c) {
   PD_CHECK(c, PD_ERR_INVALID, "null config");
   PD_CHECK(c->n_classes >= 1 && c->n_classes <= PD_MAX_CLASSES, PD_ERR_UNSUPPORTED, "nClasses %d outside [1,%d]",
            c->n_classes, PD_MAX_CLASSES);
-  return dispatch_plugin(c->plugin, [&]<class P>() {
+  return dispatch_config(*c, [&]<class P>() {
     const int img = sizeof(typename P::img_t) == 1 ? PD_IMG_U8 : PD_IMG_U16;
     const int ft = sizeof(typename P::feat_t) == 2 ? PD_FEAT_I16 : PD_FEAT_I32;
     PD_CHECK(c->img_type == img && c->n_channels == P::kChannels && c->feat_type == ft &&
@@ -85,6 +86,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
                     &ctx->f_post, &ctx->f_meta, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
   for (DevBuf *b : bufs) b->release();
+  rtc_release(ctx);
   ctx->h_stage.release();
   ctx->h_items.release();
   for (auto &ev : ctx->ev)
@@ -144,6 +146,10 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
                ds->samp_off,
            PD_ERR_INVALID, "null dataset array");
   PD_CUDA(cudaSetDevice(ctx->device));
+  if (is_user_plugin(ctx)) {
+    const RtcKernels *rk = nullptr;
+    PD_TRY(rtc_kernels(ctx, &rk));  // the sample records need the plugin
+  }
   const uint32_t n = ds->n_images;
   const size_t px = img_size(ctx->cfg.img_type) * ctx->cfg.n_channels;
   const uint64_t S = ds->samp_off[n];

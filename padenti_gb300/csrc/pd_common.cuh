@@ -3,12 +3,24 @@
 // grow-only device buffer.
 #pragma once
 
+#if defined(__CUDACC_RTC__)
+// compiled at run time by NVRTC (user feature plugins): device code only
+typedef signed char int8_t;
+typedef unsigned char uint8_t;
+typedef short int16_t;
+typedef unsigned short uint16_t;
+typedef int int32_t;
+typedef unsigned int uint32_t;
+typedef long long int64_t;
+typedef unsigned long long uint64_t;
+#else
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <cstdarg>
 #include <cstdio>
 #include <string>
+#endif
 
 #include "padenti_gb300.h"
 
@@ -22,6 +34,7 @@
 
 namespace pd {
 
+#if !defined(__CUDACC_RTC__)
 // ---------------------------------------------------------------- errors ----
 int set_error(int code, const char *fmt, ...);
 const char *last_error();
@@ -44,6 +57,7 @@ const char *last_error();
     int pd_rc_ = (expr);                                                           \
     if (pd_rc_ != PD_OK) return pd_rc_;                                            \
   } while (0)
+#endif
 
 // ---------------------------------------------- exact scalar arithmetic ----
 // Host code is compiled with -ffp-contract=off; device code uses the _rn
@@ -99,6 +113,7 @@ PD_HD float u2f(uint32_t v) {
 #endif
 }
 
+#if !defined(__CUDACC_RTC__)
 // ------------------------------------------------------- device buffers ----
 // Grow-only device allocation owned by a context.  Contents are not preserved
 // across growth.
@@ -156,5 +171,7 @@ struct HostBuf {
 
 inline size_t feat_size(int feat_type) { return feat_type == PD_FEAT_I16 ? 2 : 4; }
 inline size_t img_size(int img_type) { return img_type == PD_IMG_U8 ? 1 : 2; }
+
+#endif
 
 }  // namespace pd

@@ -9,9 +9,14 @@
 // Samples per iteration of the histogram kernel the tuning accepts (2, 4 or 8).
 inline bool valid_hist_spi(uint32_t spi) { return spi == 2 || spi == 4 || spi == 8; }
 
+namespace pd {
+struct RtcPlugin;  // pd_rtc.cu
+}
+
 struct pd_ctx {
   pd_config cfg{};
   int device = 0;
+  pd::RtcPlugin *rtc = nullptr;  // the compiled user feature plugin (PD_PLUGIN_USER)
   cudaStream_t stream = nullptr;
   uint64_t hist_budget = 8ull << 30;
   uint32_t chunk = 16384;  // samples per histogram work item (at most 65535)

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "pd_hist_grid.cuh"
+#include "pd_rtc.cuh"
 
 namespace pd {
 
@@ -19,6 +20,26 @@ static int launch_hist_grid_as(pd_ctx *ctx, const HistGrid &g) {
   PD_CUDA(cudaFuncGetAttributes(&fa, kern));
   const size_t per_cta = g.smem + fa.sharedSizeBytes + 1024;  // dynamic + static + reserved
   const int pct = (int)std::min<size_t>(100, (resident * per_cta * 100 + 233471) / 233472);
+  if (is_user_plugin(ctx)) {
+    // the same kernel compiled with the user's feature (same shared memory)
+    cudaKernel_t uk = nullptr;
+    PD_TRY(rtc_hist_kernel(ctx, TP, SPI, &uk));
+    PD_TRY(rtc_set_smem(ctx, uk, g.smem, pct));
+    if (g.ev_before) PD_CUDA(cudaEventRecord(g.ev_before, ctx->stream));
+    for (uint64_t b = 0; b < g.n_items; b += 0x7fffffffull) {
+      const uint64_t cnt = std::min<uint64_t>(g.n_items - b, 0x7fffffffull);
+      DevSet ds = g.ds;
+      const SampleRec *rec = g.rec;
+      const WorkItem *items = g.items + b;
+      const FeatT *cf = static_cast<const FeatT *>(g.cand_feat), *ct = static_cast<const FeatT *>(g.cand_thr);
+      uint32_t *hist = g.hist;
+      uint32_t F = g.F, T = g.T, K = g.K;
+      FusedSplit fs = g.fs;
+      void *args[] = {&ds, &rec, &items, &cf, &ct, &hist, &F, &T, &K, &fs};
+      PD_TRY(rtc_launch(ctx, uk, dim3((unsigned)cnt), dim3(kHistThreads), g.smem, args));
+    }
+    return PD_OK;
+  }
   PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
   if (g.ev_before) PD_CUDA(cudaEventRecord(g.ev_before, ctx->stream));
   // The grid is the work list; the hardware scheduler keeps every SM full.

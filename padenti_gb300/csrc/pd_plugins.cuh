@@ -338,4 +338,22 @@ int dispatch_plugin(int plugin, Fn &&fn) {
   }
 }
 
+// The plugin whose host paths serve a configuration: the built-in plugin, or
+// for PD_PLUGIN_USER the built-in plugin with the same types and dimensions
+// (its kernels are then the run-time compiled ones).
+template <typename Fn>
+int dispatch_config(const pd_config &c, Fn &&fn) {
+  if (c.plugin != PD_PLUGIN_USER) return dispatch_plugin(c.plugin, fn);
+  if (c.img_type == PD_IMG_U16 && c.n_channels == 1 && c.feat_type == PD_FEAT_I32 && c.feat_dim == 4)
+    return fn.template operator()<DepthDiff2>();
+  if (c.img_type == PD_IMG_U16 && c.n_channels == 1 && c.feat_type == PD_FEAT_I16 && c.feat_dim == 2)
+    return fn.template operator()<DepthDiff1>();
+  if (c.img_type == PD_IMG_U8 && c.n_channels == 3 && c.feat_type == PD_FEAT_I32 && c.feat_dim == 6)
+    return fn.template operator()<ChannelDiff>();
+  return set_error(PD_ERR_UNSUPPORTED,
+                   "user plugin with img_type %d, %d channel(s), feat_type %d, FeatDim %d: supported are "
+                   "(uint16, 1, int32, 4), (uint16, 1, int16, 2) and (uint8, 3, int32, 6)",
+                   c.img_type, c.n_channels, c.feat_type, c.feat_dim);
+}
+
 }  // namespace pd

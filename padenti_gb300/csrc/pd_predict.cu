@@ -11,97 +11,10 @@
 
 #include "pd_ctx.cuh"
 #include "pd_plugins.cuh"
+#include "pd_predict_kernels.cuh"
+#include "pd_rtc.cuh"
 
 namespace pd {
-
-struct TreeMeta {
-  unsigned long long off;  // first node of the tree in the forest arrays
-  uint32_t depth, pad;
-};
-
-constexpr int kPredX = 32, kPredY = 8, kPredThreads = kPredX * kPredY;
-
-template <class P>
-PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
-                  const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
-                  uint32_t depth) {
-  using FeatT = typename P::feat_t;
-  constexpr int D = P::kFeatDim;
-  int32_t node = 0;
-  for (uint32_t d = 1; d < depth; d++) {
-    const int32_t c = ldg(lc + node);
-    if (c < 0) break;  // leaf (-1); an untrained root (-2) also stops
-    FeatT fv[D];
-#pragma unroll
-    for (int k = 0; k < D; k++) fv[k] = ldg(feat + (size_t)node * D + k);
-    const FeatT r = P::eval(prep, fv);
-    node = c + (r <= ldg(thr + node) ? 0 : 1);
-  }
-  return node;
-}
-
-// grid (ceil(W/32), ceil(H/8), n_images); dynamic smem n_trees*256 int32.
-template <class P>
-__global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
-    const uint8_t *__restrict__ images, uint64_t img_bytes, uint32_t W, uint32_t H,
-    const uint8_t *__restrict__ masks, float *__restrict__ out, const int32_t *__restrict__ lc,
-    const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
-    const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
-    const uint32_t *__restrict__ magic) {
-  using ImgT = typename P::img_t;
-  constexpr int D = P::kFeatDim;
-  extern __shared__ int32_t leaf_s[];
-  const uint32_t tid = threadIdx.y * kPredX + threadIdx.x;
-  const uint32_t x = blockIdx.x * kPredX + threadIdx.x, y = blockIdx.y * kPredY + threadIdx.y, z = blockIdx.z;
-  if (x >= W || y >= H) return;
-  const size_t P_ = (size_t)W * H, pix = (size_t)y * W + x;
-  float *o = out + (size_t)z * K * P_ + pix;
-  if (masks && !masks[(size_t)z * P_ + pix]) {
-    for (uint32_t l = 0; l < K; l++) o[l * P_] = 0.0f;
-    return;
-  }
-  ImageRef<ImgT> im;
-  im.data = reinterpret_cast<const ImgT *>(images + (size_t)z * img_bytes);
-  im.w = (int32_t)W;
-  im.h = (int32_t)H;
-  im.magic = magic;
-  const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
-  for (uint32_t t = 0; t < n_trees; t++) {
-    const size_t off = meta[t].off;
-    leaf_s[t * kPredThreads + tid] = walk<P>(prep, lc + off, feat + off * D, thr + off, meta[t].depth);
-  }
-  const float nt = (float)n_trees;
-  for (uint32_t l = 0; l < K; l++) {
-    float acc = 0.0f;
-    for (uint32_t t = 0; t < n_trees; t++)
-      acc = acc + ldg(post + (meta[t].off + (size_t)leaf_s[t * kPredThreads + tid]) * K + l);
-    o[l * P_] = fdiv(acc, nt);
-  }
-}
-
-template <class P>
-__global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__restrict__ image, uint32_t W,
-                                                               uint32_t H, const uint8_t *__restrict__ mask,
-                                                               int32_t *__restrict__ out,
-                                                               const int32_t *__restrict__ lc,
-                                                               const typename P::feat_t *__restrict__ feat,
-                                                               const typename P::feat_t *__restrict__ thr,
-                                                               uint32_t depth, const uint32_t *__restrict__ magic) {
-  using ImgT = typename P::img_t;
-  const uint32_t x = blockIdx.x * kPredX + threadIdx.x, y = blockIdx.y * kPredY + threadIdx.y;
-  if (x >= W || y >= H) return;
-  const size_t pix = (size_t)y * W + x;
-  if (mask && !mask[pix]) {
-    out[pix] = 0;
-    return;
-  }
-  ImageRef<ImgT> im;
-  im.data = reinterpret_cast<const ImgT *>(image);
-  im.w = (int32_t)W;
-  im.h = (int32_t)H;
-  im.magic = magic;
-  out[pix] = walk<P>(P::prepare(im, (int32_t)x, (int32_t)y), lc, feat, thr, depth);
-}
 
 static int upload_forest(pd_ctx *ctx) {
   if (!ctx->forest_dirty) return PD_OK;
@@ -138,9 +51,24 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
   using FeatT = typename P::feat_t;
   const uint32_t nt = (uint32_t)ctx->tree_depth.size();
   const size_t smem = (size_t)nt * kPredThreads * 4;
-  PD_CUDA(cudaFuncSetAttribute(k_predict_posterior<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((W + kPredX - 1) / kPredX, (H + kPredY - 1) / kPredY, n);
   const uint64_t img_bytes = (uint64_t)W * H * P::kChannels * sizeof(typename P::img_t);
+  if (is_user_plugin(ctx)) {
+    const RtcKernels *rk = nullptr;
+    PD_TRY(rtc_kernels(ctx, &rk));
+    PD_TRY(rtc_set_smem(ctx, rk->predict_posterior, smem));
+    const uint8_t *im = static_cast<const uint8_t *>(images);
+    uint64_t ib = img_bytes;
+    uint32_t w_ = W, h_ = H, nt_ = nt, k_ = (uint32_t)ctx->cfg.n_classes;
+    const int32_t *lc = ctx->f_lc.as<int32_t>();
+    const FeatT *ft = ctx->f_feat.as<FeatT>(), *th = ctx->f_thr.as<FeatT>();
+    const float *po = ctx->f_post.as<float>();
+    const TreeMeta *me = ctx->f_meta.as<TreeMeta>();
+    const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
+    void *args[] = {&im, &ib, &w_, &h_, &masks, &out, &lc, &ft, &th, &po, &me, &nt_, &k_, &mg};
+    return rtc_launch(ctx, rk->predict_posterior, grid, dim3(kPredX, kPredY), smem, args);
+  }
+  PD_CUDA(cudaFuncSetAttribute(k_predict_posterior<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_predict_posterior<P><<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
       static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_lc.as<int32_t>(),
       ctx->f_feat.as<FeatT>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(), ctx->f_meta.as<TreeMeta>(), nt,
@@ -203,7 +131,7 @@ extern "C" int pd_predict_posterior_device(pd_ctx *ctx, uint32_t n_images, const
   PD_CHECK(width >= 1 && height >= 1 && n_images >= 1 && n_images <= 65535, PD_ERR_INVALID, "bad image batch");
   PD_CUDA(cudaSetDevice(ctx->device));
   PD_TRY(upload_forest(ctx));
-  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
+  return dispatch_config(ctx->cfg, [&]<class P>() {
     return launch_posterior<P>(ctx, n_images, images_device, width, height, masks_device, out_device);
   });
 }
@@ -247,9 +175,21 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
   if (mask) PD_CUDA(h2d(ctx, ctx->p_mask.ptr, mask, P_));
   const size_t off = ctx->tree_off[tree];
   const uint32_t depth = ctx->tree_depth[tree];
-  PD_TRY(dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
+  PD_TRY(dispatch_config(ctx->cfg, [&]<class P>() {
     using FeatT = typename P::feat_t;
     dim3 grid((width + kPredX - 1) / kPredX, (height + kPredY - 1) / kPredY, 1);
+    if (is_user_plugin(ctx)) {
+      const RtcKernels *rk = nullptr;
+      PD_TRY(rtc_kernels(ctx, &rk));
+      const uint8_t *im = ctx->p_img.as<uint8_t>(), *mk = mask ? ctx->p_mask.as<uint8_t>() : nullptr;
+      uint32_t w_ = width, h_ = height, dp = depth;
+      int32_t *o = ctx->p_out.as<int32_t>();
+      const int32_t *lc = ctx->f_lc.as<int32_t>() + off;
+      const FeatT *ft = ctx->f_feat.as<FeatT>() + off * P::kFeatDim, *th = ctx->f_thr.as<FeatT>() + off;
+      const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
+      void *args[] = {&im, &w_, &h_, &mk, &o, &lc, &ft, &th, &dp, &mg};
+      return rtc_launch(ctx, rk->predict_leaf, grid, dim3(kPredX, kPredY), 0, args);
+    }
     k_predict_leaf<P><<<grid, dim3(kPredX, kPredY), 0, st>>>(
         ctx->p_img.as<uint8_t>(), width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
         ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_feat.as<FeatT>() + off * P::kFeatDim,

@@ -11,6 +11,7 @@
 
 #include "pd_ctx.cuh"
 #include "pd_hist_grid.cuh"
+#include "pd_rtc.cuh"
 #include "pd_train_kernels.cuh"
 
 namespace pd {
@@ -61,10 +62,10 @@ int ensure_log2_table(pd_ctx *ctx, uint64_t n) {
 }
 
 int map_training_pixels(pd_ctx *ctx, uint64_t bytes) {
-  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() -> int {
+  return dispatch_config(ctx->cfg, [&]<class P>() -> int {
     if constexpr (P::kTrainMapsZero) {
       static_assert(sizeof(typename P::img_t) == 2, "zero mapping of 16-bit images");
-      const uint64_t n = bytes / 2;
+      const uint64_t n = is_user_plugin(ctx) ? 0 : bytes / 2;  // a user feature reads the images as given
       if (n) {
         k_zero_to_background<<<4 * 152, 256, 0, ctx->stream>>>(ctx->pixels.as<uint16_t>(), n);
         PD_CUDA(cudaGetLastError());
@@ -77,9 +78,18 @@ int map_training_pixels(pd_ctx *ctx, uint64_t bytes) {
 int build_sample_records(pd_ctx *ctx, uint64_t S) {
   PD_TRY(ctx->s_rec.ensure(S * sizeof(SampleRec) + sizeof(SampleRec)));
   if (!S) return PD_OK;
-  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() -> int {
-    k_build_rec<P><<<(unsigned)((S + 255) / 256), 256, 0, ctx->stream>>>(devset(ctx), (uint32_t)S,
-                                                                         ctx->s_rec.as<SampleRec>());
+  return dispatch_config(ctx->cfg, [&]<class P>() -> int {
+    const dim3 grid((unsigned)((S + 255) / 256));
+    if (is_user_plugin(ctx)) {
+      const RtcKernels *rk = nullptr;
+      PD_TRY(rtc_kernels(ctx, &rk));
+      DevSet ds = devset(ctx);
+      uint32_t n = (uint32_t)S;
+      SampleRec *rec = ctx->s_rec.as<SampleRec>();
+      void *args[] = {&ds, &n, &rec};
+      return rtc_launch(ctx, rk->build_rec, grid, dim3(256), 0, args);
+    }
+    k_build_rec<P><<<grid, 256, 0, ctx->stream>>>(devset(ctx), (uint32_t)S, ctx->s_rec.as<SampleRec>());
     PD_CUDA(cudaGetLastError());
     return PD_OK;
   });
@@ -157,10 +167,21 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
     uint32_t N = 1;
     while (N < F) N <<= 1;
     const size_t osmem = (size_t)N * 8;
-    PD_CUDA(cudaFuncSetAttribute(k_cand_order<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)osmem));
-    k_cand_order<P><<<n, kOrderThreads, osmem, ctx->stream>>>(d_nodes, tree, F, b, ctx->cand_ord.as<uint32_t>());
-    PD_CUDA(cudaGetLastError());
-    ctx->launches++;
+    if (is_user_plugin(ctx)) {
+      const RtcKernels *rk = nullptr;
+      PD_TRY(rtc_kernels(ctx, &rk));
+      PD_TRY(rtc_set_smem(ctx, rk->cand_order, osmem));
+      uint32_t tr = tree, f_ = F;
+      CandBounds bb = b;
+      uint32_t *o = ctx->cand_ord.as<uint32_t>();
+      void *args[] = {&d_nodes, &tr, &f_, &bb, &o};
+      PD_TRY(rtc_launch(ctx, rk->cand_order, dim3(n), dim3(kOrderThreads), osmem, args));
+    } else {
+      PD_CUDA(cudaFuncSetAttribute(k_cand_order<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)osmem));
+      k_cand_order<P><<<n, kOrderThreads, osmem, ctx->stream>>>(d_nodes, tree, F, b, ctx->cand_ord.as<uint32_t>());
+      PD_CUDA(cudaGetLastError());
+      ctx->launches++;
+    }
     ord = ctx->cand_ord.as<uint32_t>();
   }
   // draws lie in [lo, hi] (no narrowing wrap) and their offsets fit 24 bits:
@@ -566,7 +587,21 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
     PD_TRY(d_next.ensure((size_t)nf * sizeof(SlotNext)));
     PD_CUDA(h2d(ctx, d_next.ptr, sn.data(), (size_t)nf * sizeof(SlotNext)));
     PD_CUDA(cudaEventRecord(ev[4], st));
-    if (n_act) {
+    if (n_act && is_user_plugin(ctx)) {
+      const RtcKernels *rk = nullptr;
+      PD_TRY(rtc_kernels(ctx, &rk));
+      DevSet ds = devset(ctx);
+      const uint32_t *a_ = ctx->act[cur].as<uint32_t>(), *as_ = ctx->act_slot[cur].as<uint32_t>();
+      const SampleRec *r_ = ctx->act_rec[cur].as<SampleRec>();
+      uint32_t na = (uint32_t)n_act;
+      int32_t *sn_ = ctx->snode.as<int32_t>();
+      const int32_t *lc_ = ctx->t_lc.as<int32_t>();
+      const FeatT *tf = ctx->t_feat.as<FeatT>(), *tt = ctx->t_thr.as<FeatT>();
+      const SlotNext *nx = d_next.as<SlotNext>();
+      uint8_t *fl = ctx->flags.as<uint8_t>();
+      void *args[] = {&ds, &a_, &r_, &as_, &na, &sn_, &lc_, &tf, &tt, &nx, &fl};
+      PD_TRY(rtc_launch(ctx, rk->reassign, dim3((unsigned)((n_act + 255) / 256)), dim3(256), 0, args));
+    } else if (n_act) {
       k_reassign<P><<<(unsigned)((n_act + 255) / 256), 256, 0, st>>>(
           devset(ctx), ctx->act[cur].as<uint32_t>(), ctx->act_rec[cur].as<SampleRec>(),
           ctx->act_slot[cur].as<uint32_t>(), (uint32_t)n_act,
@@ -632,7 +667,7 @@ extern "C" int pd_train_tree(pd_ctx *ctx, const pd_train_params *params, uint32_
   PD_CHECK(root_prior && left_child && features && thresholds && posteriors, PD_ERR_INVALID, "null tree array");
   PD_TRY(check_params(ctx, params));
   PD_CUDA(cudaSetDevice(ctx->device));
-  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
+  return dispatch_config(ctx->cfg, [&]<class P>() {
     using FeatT = typename P::feat_t;
     return train_tree_impl<P>(ctx, params, tree_id, end_depth, root_prior, left_child,
                               static_cast<FeatT *>(features), static_cast<FeatT *>(thresholds), posteriors);
@@ -660,7 +695,7 @@ extern "C" int pd_candidates(pd_ctx *ctx, const pd_train_params *params, uint32_
   PD_CHECK(ctx && nodes && features_out && thresholds_out, PD_ERR_INVALID, "null argument");
   PD_TRY(check_params(ctx, params));
   PD_CUDA(cudaSetDevice(ctx->device));
-  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
+  return dispatch_config(ctx->cfg, [&]<class P>() {
     using FeatT = typename P::feat_t;
     constexpr int D = P::kFeatDim;
     const uint32_t F = params->n_features, T = params->n_thresholds;
@@ -715,7 +750,7 @@ extern "C" int pd_hist(pd_ctx *ctx, const pd_train_params *params, uint32_t tree
   std::vector<uint64_t> pos(cnt.begin(), cnt.end() - 1);
   for (uint64_t s = 0; s < S; s++)
     if (slot_of[s] >= 0) act[pos[slot_of[s]]++] = (uint32_t)s;
-  return dispatch_plugin(ctx->cfg.plugin, [&]<class P>() {
+  return dispatch_config(ctx->cfg, [&]<class P>() {
     PD_TRY(ensure_slice(ctx, params, n_nodes));
     DevBuf dn, da, drec, dref;
     PD_TRY(dn.ensure((size_t)n_nodes * 4));

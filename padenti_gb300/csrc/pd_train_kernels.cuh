@@ -3,7 +3,15 @@
 // active samples by frontier slot.
 #pragma once
 
+#if defined(__CUDACC_RTC__)
+#define FLT_MAX 3.402823466e+38F
+#define DBL_MAX 1.7976931348623158e+308
+#define LLONG_MAX 9223372036854775807LL
+#define LLONG_MIN (-LLONG_MAX - 1LL)
+#else
 #include <cfloat>
+#include <climits>
+#endif
 
 #include "pd_log2.cuh"
 #include "pd_plugins.cuh"

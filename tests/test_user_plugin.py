@@ -1,0 +1,116 @@
+"""User feature plugins compiled at run time (the reference's feature.cl, here CUDA
+source with computeFeature compiled by NVRTC).
+
+Each built-in feature is written again as user source; a tree trained with it and its
+forest prediction must be bit-identical to the built-in plugin's (which the parity tests
+pin to the oracle).  Compilation itself needs no GPU.
+"""
+import numpy as np
+import pytest
+
+import padenti_gb300 as pg
+from cases import depth1_case, depth_case, rgb_case
+
+# kernels/feature.cl-style features written against pd::ImageView (read() is 0 outside)
+SOURCES = {
+    # the depth-difference feature of the benchmark configurations
+    "depth_diff2": ("u16x1_i32x4", r"""
+__device__ feat_t computeFeature(const pd::ImageView &img, int2 c, const feat_t *f, unsigned featDim) {
+  int d = img.read(c.x, c.y, 0);
+  if (d == 0) d = 10000;
+  const float fd = (float)d;
+  const int x1 = c.x + (int)roundf(__fdiv_rn((float)f[0], fd)), y1 = c.y + (int)roundf(__fdiv_rn((float)f[1], fd));
+  const int x2 = c.x + (int)roundf(__fdiv_rn((float)f[2], fd)), y2 = c.y + (int)roundf(__fdiv_rn((float)f[3], fd));
+  int a = img.read(x1, y1, 0), b = img.read(x2, y2, 0);
+  if (a == 0) a = 10000;
+  if (b == 0) b = 10000;
+  return a - b;
+}
+"""),
+    # the reference's own test/feature.cl: D(x) - D(x + round(u*500/D(x)))
+    "depth_diff1": ("u16x1_i16x2", r"""
+__device__ feat_t computeFeature(const pd::ImageView &img, int2 c, const feat_t *f, unsigned featDim) {
+  const short depth = (short)img.read(c.x, c.y, 0);
+  int probe = 10000;
+  if (depth != 0) {
+    const int ox = c.x + (int)roundf(__fdiv_rn(__fmul_rn((float)f[0], 500.0f), (float)depth));
+    const int oy = c.y + (int)roundf(__fdiv_rn(__fmul_rn((float)f[1], 500.0f), (float)depth));
+    const short v = (short)img.read(ox, oy, 0);
+    probe = v ? v : 10000;
+  }
+  return (feat_t)(depth - probe);
+}
+"""),
+    # RGB channel difference; channel indices clamped to [0, 2]
+    "channel_diff": ("u8x3_i32x6", r"""
+__device__ feat_t computeFeature(const pd::ImageView &img, int2 c, const feat_t *f, unsigned featDim) {
+  const int c1 = min(max((int)f[0], 0), 2), c2 = min(max((int)f[1], 0), 2);
+  return (int)img.read(c.x + f[2], c.y + f[3], c1) - (int)img.read(c.x + f[4], c.y + f[5], c2);
+}
+"""),
+}
+CASES = {"depth_diff2": lambda: depth_case(n_images=12, n_features=64, n_thresholds=20),
+         "depth_diff1": lambda: depth1_case(),
+         "channel_diff": lambda: rgb_case()}
+
+
+def _user_config(name, n_classes):
+    shape, src = SOURCES[name]
+    return pg.ForestConfig("user", n_classes, source=src, shape=shape)
+
+
+@pytest.mark.parametrize("name", sorted(SOURCES))
+def test_user_plugin_compiles_without_a_gpu(name):
+    cfg, *_ = CASES[name]()
+    assert isinstance(pg.check_plugin(_user_config(name, cfg.n_classes)), str)
+
+
+def test_user_plugin_compile_errors_carry_the_log():
+    shape, src = SOURCES["depth_diff1"]
+    bad = pg.ForestConfig("user", 3, source=src.replace("roundf", "no_such_function"), shape=shape)
+    with pytest.raises(pg.PadentiError, match=r"feature\.cu\(\d+\): error: identifier \"no_such_function\""):
+        pg.check_plugin(bad)
+
+
+def test_user_plugin_config_needs_a_supported_shape():
+    with pytest.raises(ValueError):
+        pg.ForestConfig("user", 3, source="", shape="u16x1_i32x4")
+    with pytest.raises(ValueError):
+        pg.ForestConfig("user", 3, source="x", shape="u16x2_i32x4")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(SOURCES))
+def test_user_plugin_trains_and_predicts_like_the_builtin(name):
+    cfg, ts, tp, data = CASES[name]()
+    ucfg = _user_config(name, cfg.n_classes)
+    a = pg.Tree(cfg, 3, 7)
+    pg.TreeTrainer(cfg).train(a, ts, tp)
+    b = pg.Tree(ucfg, 3, 7)
+    pg.TreeTrainer(ucfg).train(b, ts, tp)
+    assert np.array_equal(a.left_child, b.left_child)
+    assert np.array_equal(a.features, b.features) and np.array_equal(a.thresholds, b.thresholds)
+    assert np.array_equal(a.posteriors.view(np.uint32), b.posteriors.view(np.uint32))
+    assert (a.left_child >= 0).sum() > 3
+    image = data[0][0]
+    ca, cb = pg.Classifier(cfg), pg.Classifier(ucfg)
+    ca << a
+    cb << b
+    assert np.array_equal(ca.predict(image).view(np.uint32), cb.predict(image).view(np.uint32))
+    assert np.array_equal(ca.predict_leaf(0, image), cb.predict_leaf(0, image))
+
+
+@pytest.mark.gpu
+def test_user_plugin_must_compile_before_use():
+    from padenti_gb300 import _native as N
+    import ctypes as C
+
+    cfg, ts, tp, _ = depth1_case()
+    ucfg = _user_config("depth_diff1", cfg.n_classes)
+    h = C.c_void_p()
+    N.check(N.lib().pd_ctx_create(C.byref(ucfg.c()), 0, C.byref(h)))
+    try:
+        rc = N.lib().pd_dataset_upload(h, C.byref(pg.TrainingSet.desc(ts.flat())))
+        assert rc != 0 and b"pd_plugin_compile" in N.lib().pd_last_error()
+    finally:
+        N.lib().pd_ctx_destroy(h)
