@@ -1,9 +1,11 @@
 // CUDATreeTrainer and CUDAClassifier: the GB300 counterparts of CLTreeTrainer
 // (cl_tree_trainer.hpp:115-120) and CLClassifier (cl_classifier.hpp:81-94),
-// forwarding to the C ABI of libpadenti_gb300 (padenti_gb300.h).  The OpenCL
-// classes take the directory of the user's feature.cl; here the feature plugin
-// is one of the plugins compiled into the library (PD_PLUGIN_*), and the
-// template parameters must match it (pd_ctx_create checks them).  Errors throw
+// forwarding to the C ABI of libpadenti_gb300 (padenti_gb300.h).  Like the
+// OpenCL classes, they take the user's feature: the path of a feature.cu (or of
+// the directory holding it) whose computeFeature is compiled at run time for
+// the template parameters' types (pd_plugin_compile).  They also take one of the
+// plugins compiled into the library (PD_PLUGIN_*), whose types the template
+// parameters must match (pd_ctx_create checks them).  Errors throw
 // std::runtime_error with the library's message (the reference throws
 // cl::Error / std::string).
 #ifndef PADENTI_GB300_CUDA_TREE_TRAINER_HPP
@@ -13,6 +15,8 @@
 #include <padenti/tree_trainer.hpp>
 #include <padenti_gb300.h>
 
+#include <fstream>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -37,6 +41,29 @@ pd_ctx *make_context(int plugin, int device) {
   return ctx;
 }
 
+// The source of a user feature: the file itself, or feature.cu in a directory
+// (the reference takes the directory of feature.cl).
+inline std::string read_feature_source(const std::string &path) {
+  std::ifstream f(path + "/feature.cu");
+  if (!f) f.open(path);
+  if (!f) throw std::runtime_error("padenti_gb300: cannot read the feature source " + path);
+  std::stringstream s;
+  s << f.rdbuf();
+  return s.str();
+}
+
+template <typename ImgType, unsigned int nChannels, typename FeatType, unsigned int FeatDim, unsigned int nClasses>
+pd_ctx *make_user_context(const std::string &feature_path, int device) {
+  pd_ctx *ctx = make_context<ImgType, nChannels, FeatType, FeatDim, nClasses>(PD_PLUGIN_USER, device);
+  const int rc = pd_plugin_compile(ctx, read_feature_source(feature_path).c_str());
+  if (rc != PD_OK) {
+    const std::string msg = pd_last_error();
+    pd_ctx_destroy(ctx);
+    throw std::runtime_error("padenti_gb300: " + msg);
+  }
+  return ctx;
+}
+
 }  // namespace padenti_gb300
 
 template <typename ImgType, unsigned int nChannels, typename FeatType, unsigned int FeatDim, unsigned int nClasses>
@@ -48,6 +75,9 @@ class CUDATreeTrainer : public TreeTrainer<ImgType, nChannels, FeatType, FeatDim
  public:
   explicit CUDATreeTrainer(int plugin, int device = 0)
       : m_ctx(padenti_gb300::make_context<ImgType, nChannels, FeatType, FeatDim, nClasses>(plugin, device)) {}
+  // CLTreeTrainer(featureKernelPath): a user feature compiled at run time.
+  explicit CUDATreeTrainer(const std::string &featurePath, int device = 0)
+      : m_ctx(padenti_gb300::make_user_context<ImgType, nChannels, FeatType, FeatDim, nClasses>(featurePath, device)) {}
   CUDATreeTrainer(const CUDATreeTrainer &) = delete;
   CUDATreeTrainer &operator=(const CUDATreeTrainer &) = delete;
   ~CUDATreeTrainer() { pd_ctx_destroy(m_ctx); }
@@ -119,6 +149,9 @@ class CUDAClassifier : public Classifier<ImgType, nChannels, FeatType, FeatDim, 
  public:
   explicit CUDAClassifier(int plugin, int device = 0)
       : m_ctx(padenti_gb300::make_context<ImgType, nChannels, FeatType, FeatDim, nClasses>(plugin, device)) {}
+  // CLClassifier(featureKernelPath): a user feature compiled at run time.
+  explicit CUDAClassifier(const std::string &featurePath, int device = 0)
+      : m_ctx(padenti_gb300::make_user_context<ImgType, nChannels, FeatType, FeatDim, nClasses>(featurePath, device)) {}
   CUDAClassifier(const CUDAClassifier &) = delete;
   CUDAClassifier &operator=(const CUDAClassifier &) = delete;
   ~CUDAClassifier() { pd_ctx_destroy(m_ctx); }

@@ -1,14 +1,15 @@
 // Trains one tree and predicts one image through the C++ facade
 // (CUDATreeTrainer / CUDAClassifier over libpadenti_gb300) on the seeded
 // synthetic depth set; writes the tree XML to argv[1] and the posterior of
-// image 0 (planar float32) to argv[2].
+// image 0 (planar float32) to argv[2].  With argv[3], the feature is the user
+// source at that path (compiled at run time) instead of the built-in plugin.
 #include <padenti/cuda_tree_trainer.hpp>
 
 #include <cstdio>
 #include <vector>
 
 int main(int argc, char **argv) {
-  if (argc != 3) return 2;
+  if (argc != 3 && argc != 4) return 2;
   const unsigned int n = 8, W = 160, H = 120, S = 500;
   std::vector<uint16_t> px((size_t)n * W * H);
   std::vector<uint8_t> lb((size_t)n * W * H);
@@ -30,10 +31,12 @@ int main(int argc, char **argv) {
   p.thrUpBound = 500;
   p.perLeafSamplesThr = 20;
   Tree<int, 4, 3> tree(3, 7);
-  CUDATreeTrainer<unsigned short, 1, int, 4, 3> trainer(PD_PLUGIN_DEPTH_DIFF2);
+  using Trainer = CUDATreeTrainer<unsigned short, 1, int, 4, 3>;
+  using Clf = CUDAClassifier<unsigned short, 1, int, 4, 3>;
+  Trainer trainer = argc == 4 ? Trainer(std::string(argv[3])) : Trainer(PD_PLUGIN_DEPTH_DIFF2);
   trainer.train(tree, ts, p, 1, 7);
   tree.save(argv[1]);
-  CUDAClassifier<unsigned short, 1, int, 4, 3> clf(PD_PLUGIN_DEPTH_DIFF2);
+  Clf clf = argc == 4 ? Clf(std::string(argv[3])) : Clf(PD_PLUGIN_DEPTH_DIFF2);
   clf << tree;
   Image<unsigned short, 1> image(px.data(), W, H);
   Image<float, 3> post(W, H);

@@ -75,3 +75,23 @@ def test_cpp_facade_trains_and_predicts_like_the_python_api(tmp_path):
     ref = clf.predict(px[0])
     got = np.fromfile(post, np.float32).reshape(ref.shape)
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_cpp_facade_with_a_user_feature_matches_the_builtin(tmp_path):
+    """CUDATreeTrainer / CUDAClassifier built from a feature.cu directory (the reference's
+    CLTreeTrainer(featureKernelPath)) train and predict exactly as with the built-in plugin."""
+    from test_user_plugin import SOURCES
+
+    exe = tmp_path / "facade_train"
+    _compile(CPP / "facade_train.cpp", exe, link=True)
+    fdir = tmp_path / "feature"
+    fdir.mkdir()
+    (fdir / "feature.cu").write_text(SOURCES["depth_diff2"][1])
+    out = {}
+    for tag, extra in (("builtin", []), ("user", [str(fdir)])):
+        xml, post = tmp_path / f"{tag}.xml", tmp_path / f"{tag}.bin"
+        r = subprocess.run([str(exe), str(xml), str(post), *extra], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr + r.stdout
+        out[tag] = (xml.read_text(), post.read_bytes())
+    assert out["user"] == out["builtin"]
