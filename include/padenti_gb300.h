@@ -242,6 +242,14 @@ int pd_predict_posterior(pd_ctx *ctx, const void *image, uint32_t width, uint32_
  * id per pixel; masked-out pixels are 0. */
 int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, uint32_t width,
                     uint32_t height, const uint8_t *mask, int32_t *out);
+/* A batch of n images of mixed sizes (host buffers: images[i] of widths[i] x
+ * heights[i], optional masks[i] (masks or an entry may be NULL), outs[i] planar
+ * [K][H][W] float) in one kernel launch, captured in a CUDA graph and replayed
+ * while the sizes, the masks' presence and the forest stay the same.  The
+ * reference predicts image by image (cl_classifier_impl.hpp:356-557); the
+ * results are those of pd_predict_posterior per image. */
+int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *const *images, const uint32_t *widths,
+                               const uint32_t *heights, const uint8_t *const *masks, float *const *outs);
 /* Batched posterior prediction of n same-size images already in device
  * memory: images n*H*W*C, masks n*H*W (or NULL), out n*K*H*W. */
 int pd_predict_posterior_device(pd_ctx *ctx, uint32_t n_images, const void *images_device,

@@ -404,6 +404,21 @@ class Classifier(_Ctx):
         check(lib().pd_predict_posterior(self.h, _ptr(image), W, H, _ptr(m), _ptr(out)))
         return out
 
+    def predict_batch(self, images: list, masks: list | None = None) -> list:
+        """Posteriors of images of mixed sizes in one launch (pd_predict_posterior_batch)."""
+        n = len(images)
+        ims = [np.ascontiguousarray(im, self.config.img_dtype) for im in images]
+        mks = [None if masks is None or masks[i] is None else np.ascontiguousarray(masks[i], np.uint8)
+               for i in range(n)]
+        outs = [np.empty((self.config.n_classes, im.shape[0], im.shape[1]), np.float32) for im in ims]
+        P = C.c_void_p * n
+        w = (C.c_uint32 * n)(*[im.shape[1] for im in ims])
+        h = (C.c_uint32 * n)(*[im.shape[0] for im in ims])
+        mp = P(*[None if m is None else m.ctypes.data for m in mks]) if masks is not None else None
+        check(lib().pd_predict_posterior_batch(self.h, n, P(*[im.ctypes.data for im in ims]), w, h, mp,
+                                               P(*[o.ctypes.data for o in outs])))
+        return outs
+
     def predict_leaf(self, tree: int, image: np.ndarray, mask: np.ndarray | None = None) -> np.ndarray:
         """Leaf node id per pixel (cl_classifier_impl.hpp:200-341); masked-out pixels are 0."""
         image = np.ascontiguousarray(image, self.config.img_dtype)

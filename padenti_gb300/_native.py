@@ -101,6 +101,7 @@ _SIGS = {
     "pd_forest_size": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
     "pd_predict_posterior": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, _P, _P]),
     "pd_predict_leaf": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
+    "pd_predict_posterior_batch": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P]),
     "pd_predict_posterior_device": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
     "pd_synth_depth": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]),

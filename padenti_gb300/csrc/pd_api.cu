@@ -86,6 +86,11 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
                     &ctx->f_post, &ctx->f_meta, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
   for (DevBuf *b : bufs) b->release();
+  if (ctx->batch_graph) cudaGraphExecDestroy(ctx->batch_graph);
+  ctx->b_img.release();
+  ctx->b_mask.release();
+  ctx->b_out.release();
+  ctx->b_desc.release();
   rtc_release(ctx);
   ctx->h_stage.release();
   ctx->h_items.release();

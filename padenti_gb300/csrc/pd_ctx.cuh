@@ -72,6 +72,12 @@ struct pd_ctx {
   bool forest_dirty = true;
   pd::DevBuf f_lc, f_feat, f_thr, f_post, f_meta;
   pd::DevBuf p_img, p_mask, p_out;     // staging for host-buffer prediction
+  uint64_t forest_version = 0;         // bumped when the forest arrays are uploaded again
+  // mixed-size prediction batches: buffers, the layout they were built for and
+  // the graph of the batch kernel (pd_predict_posterior_batch)
+  pd::DevBuf b_img, b_mask, b_out, b_desc;
+  std::vector<uint64_t> batch_key;
+  cudaGraphExec_t batch_graph = nullptr;
 
   cudaEvent_t ev[8] = {};
   uint64_t bytes_h2d = 0, bytes_d2h = 0, launches = 0;

@@ -42,6 +42,7 @@ static int upload_forest(pd_ctx *ctx) {
   }
   (void)fs;
   ctx->forest_dirty = false;
+  ctx->forest_version++;
   return PD_OK;
 }
 
@@ -154,6 +155,108 @@ extern "C" int pd_predict_posterior(pd_ctx *ctx, const void *image, uint32_t wid
   PD_TRY(pd_predict_posterior_device(ctx, 1, ctx->p_img.ptr, width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
                                      ctx->p_out.as<float>()));
   PD_CUDA(d2h(ctx, out, ctx->p_out.ptr, ob));
+  PD_CUDA(cudaStreamSynchronize(st));
+  return PD_OK;
+}
+
+// Config 3's serving form: a batch of images of mixed sizes in one launch of
+// k_predict_batch (one CTA per 32x8 tile of any image), captured in a CUDA graph
+// that is replayed while the batch layout (sizes, masks) and the forest stay the
+// same.  Inputs and outputs are the caller's host buffers, copied per image.
+extern "C" int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *const *images,
+                                          const uint32_t *widths, const uint32_t *heights,
+                                          const uint8_t *const *masks, float *const *outs) {
+  PD_CHECK(ctx && images && widths && heights && outs, PD_ERR_INVALID, "null argument");
+  PD_CHECK(n >= 1, PD_ERR_INVALID, "empty batch");
+  PD_CHECK(!ctx->tree_depth.empty(), PD_ERR_STATE, "empty forest");
+  PD_CUDA(cudaSetDevice(ctx->device));
+  PD_TRY(upload_forest(ctx));
+  const uint32_t K = (uint32_t)ctx->cfg.n_classes, nt = (uint32_t)ctx->tree_depth.size();
+  const size_t px = (size_t)ctx->cfg.n_channels * img_size(ctx->cfg.img_type);
+  auto up16 = [](uint64_t v) { return (v + 15) / 16 * 16; };
+  std::vector<BatchImage> desc(n);
+  std::vector<uint64_t> key{(uint64_t)n, ctx->forest_version};
+  uint64_t ib = 0, mb = 0, ob = 0, tiles = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    PD_CHECK(images[i] && outs[i] && widths[i] >= 1 && heights[i] >= 1 && widths[i] < 65536 && heights[i] < 65536,
+             PD_ERR_INVALID, "batch image %u: null buffer or size %ux%u", i, widths[i], heights[i]);
+    const uint64_t P_ = (uint64_t)widths[i] * heights[i];
+    BatchImage &d = desc[i];
+    d.w = widths[i];
+    d.h = heights[i];
+    d.tiles_x = (d.w + kPredX - 1) / kPredX;
+    d.tile0 = (uint32_t)tiles;
+    d.has_mask = masks && masks[i] ? 1u : 0u;
+    d.pad = 0;
+    d.img_off = ib;
+    d.mask_off = mb;
+    d.out_off = ob;
+    ib += up16(P_ * px);
+    if (d.has_mask) mb += up16(P_);
+    ob += up16(P_ * K * 4);
+    tiles += (uint64_t)d.tiles_x * ((d.h + kPredY - 1) / kPredY);
+    key.push_back(d.w | ((uint64_t)d.h << 16) | ((uint64_t)d.has_mask << 32));
+  }
+  PD_CHECK(tiles < (1ull << 31), PD_ERR_UNSUPPORTED, "batch of %llu tiles", (unsigned long long)tiles);
+  cudaStream_t st = ctx->stream;
+  if (key != ctx->batch_key || !ctx->batch_graph) {
+    // a new layout: buffers, descriptor table and the graph of the kernel
+    if (ctx->batch_graph) cudaGraphExecDestroy(ctx->batch_graph);
+    ctx->batch_graph = nullptr;
+    ctx->batch_key.clear();
+    PD_TRY(ctx->b_img.ensure(ib));
+    PD_TRY(ctx->b_mask.ensure(std::max<uint64_t>(16, mb)));
+    PD_TRY(ctx->b_out.ensure(ob));
+    PD_TRY(ctx->b_desc.ensure(n * sizeof(BatchImage)));
+    PD_CUDA(h2d(ctx, ctx->b_desc.ptr, desc.data(), n * sizeof(BatchImage)));
+    PD_CUDA(cudaStreamSynchronize(st));
+    const size_t smem = (size_t)nt * kPredThreads * 4;
+    const int rc = dispatch_config(ctx->cfg, [&]<class P>() -> int {
+      using FeatT = typename P::feat_t;
+      const uint8_t *im = ctx->b_img.as<uint8_t>(), *mk = ctx->b_mask.as<uint8_t>();
+      uint8_t *o = ctx->b_out.as<uint8_t>();
+      const BatchImage *bd = ctx->b_desc.as<BatchImage>();
+      uint32_t n_ = n, nt_ = nt, k_ = K;
+      const int32_t *lc = ctx->f_lc.as<int32_t>();
+      const FeatT *ft = ctx->f_feat.as<FeatT>(), *th = ctx->f_thr.as<FeatT>();
+      const float *po = ctx->f_post.as<float>();
+      const TreeMeta *me = ctx->f_meta.as<TreeMeta>();
+      const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
+      void *args[] = {&im, &mk, &o, &bd, &n_, &lc, &ft, &th, &po, &me, &nt_, &k_, &mg};
+      const void *fn = (const void *)k_predict_batch<P>;
+      if (is_user_plugin(ctx)) {
+        const RtcKernels *rk = nullptr;
+        PD_TRY(rtc_kernels(ctx, &rk));
+        PD_TRY(rtc_set_smem(ctx, rk->predict_batch, smem));
+        fn = (const void *)rk->predict_batch;
+      } else {
+        PD_CUDA(cudaFuncSetAttribute(k_predict_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      }
+      cudaGraph_t g = nullptr;
+      PD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      const cudaError_t le = cudaLaunchKernel(fn, dim3((unsigned)tiles), dim3(kPredX, kPredY), args, smem, st);
+      const cudaError_t ce = cudaStreamEndCapture(st, &g);
+      PD_CUDA(le);
+      PD_CUDA(ce);
+      const cudaError_t ie = cudaGraphInstantiate(&ctx->batch_graph, g, 0);
+      cudaGraphDestroy(g);
+      PD_CUDA(ie);
+      return PD_OK;
+    });
+    PD_TRY(rc);
+    ctx->batch_key = key;
+  }
+  for (uint32_t i = 0; i < n; i++) {
+    const uint64_t P_ = (uint64_t)desc[i].w * desc[i].h;
+    PD_CUDA(h2d(ctx, ctx->b_img.as<uint8_t>() + desc[i].img_off, images[i], P_ * px));
+    if (desc[i].has_mask) PD_CUDA(h2d(ctx, ctx->b_mask.as<uint8_t>() + desc[i].mask_off, masks[i], P_));
+  }
+  PD_CUDA(cudaGraphLaunch(ctx->batch_graph, st));
+  ctx->launches++;
+  for (uint32_t i = 0; i < n; i++) {
+    const uint64_t P_ = (uint64_t)desc[i].w * desc[i].h;
+    PD_CUDA(d2h(ctx, outs[i], ctx->b_out.as<uint8_t>() + desc[i].out_off, P_ * K * 4));
+  }
   PD_CUDA(cudaStreamSynchronize(st));
   return PD_OK;
 }

@@ -33,31 +33,20 @@ PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
   return node;
 }
 
-// grid (ceil(W/32), ceil(H/8), n_images); dynamic smem n_trees*256 int32.
+// The forest posterior of pixel (x, y): the leaf of every tree (kept in the
+// CTA's leaf_s, [tree][thread]), then the leaf posteriors summed in tree order
+// and divided by the tree count, written planar with stride plane.
 template <class P>
-__global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
-    const uint8_t *__restrict__ images, uint64_t img_bytes, uint32_t W, uint32_t H,
-    const uint8_t *__restrict__ masks, float *__restrict__ out, const int32_t *__restrict__ lc,
-    const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
-    const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
-    const uint32_t *__restrict__ magic) {
-  using ImgT = typename P::img_t;
+PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint32_t y, bool masked_out, float *o,
+                        size_t plane, const int32_t *__restrict__ lc, const typename P::feat_t *__restrict__ feat,
+                        const typename P::feat_t *__restrict__ thr, const float *__restrict__ post,
+                        const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K, int32_t *leaf_s,
+                        uint32_t tid) {
   constexpr int D = P::kFeatDim;
-  extern __shared__ int32_t leaf_s[];
-  const uint32_t tid = threadIdx.y * kPredX + threadIdx.x;
-  const uint32_t x = blockIdx.x * kPredX + threadIdx.x, y = blockIdx.y * kPredY + threadIdx.y, z = blockIdx.z;
-  if (x >= W || y >= H) return;
-  const size_t P_ = (size_t)W * H, pix = (size_t)y * W + x;
-  float *o = out + (size_t)z * K * P_ + pix;
-  if (masks && !masks[(size_t)z * P_ + pix]) {
-    for (uint32_t l = 0; l < K; l++) o[l * P_] = 0.0f;
+  if (masked_out) {
+    for (uint32_t l = 0; l < K; l++) o[l * plane] = 0.0f;
     return;
   }
-  ImageRef<ImgT> im;
-  im.data = reinterpret_cast<const ImgT *>(images + (size_t)z * img_bytes);
-  im.w = (int32_t)W;
-  im.h = (int32_t)H;
-  im.magic = magic;
   const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
   for (uint32_t t = 0; t < n_trees; t++) {
     const size_t off = meta[t].off;
@@ -68,8 +57,72 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
     float acc = 0.0f;
     for (uint32_t t = 0; t < n_trees; t++)
       acc = acc + ldg(post + (meta[t].off + (size_t)leaf_s[t * kPredThreads + tid]) * K + l);
-    o[l * P_] = fdiv(acc, nt);
+    o[l * plane] = fdiv(acc, nt);
   }
+}
+
+// grid (ceil(W/32), ceil(H/8), n_images); dynamic smem n_trees*256 int32.
+template <class P>
+__global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
+    const uint8_t *__restrict__ images, uint64_t img_bytes, uint32_t W, uint32_t H,
+    const uint8_t *__restrict__ masks, float *__restrict__ out, const int32_t *__restrict__ lc,
+    const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+    const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
+    const uint32_t *__restrict__ magic) {
+  using ImgT = typename P::img_t;
+  extern __shared__ int32_t leaf_s[];
+  const uint32_t tid = threadIdx.y * kPredX + threadIdx.x;
+  const uint32_t x = blockIdx.x * kPredX + threadIdx.x, y = blockIdx.y * kPredY + threadIdx.y, z = blockIdx.z;
+  if (x >= W || y >= H) return;
+  const size_t P_ = (size_t)W * H, pix = (size_t)y * W + x;
+  ImageRef<ImgT> im;
+  im.data = reinterpret_cast<const ImgT *>(images + (size_t)z * img_bytes);
+  im.w = (int32_t)W;
+  im.h = (int32_t)H;
+  im.magic = magic;
+  predict_pixel<P>(im, x, y, masks && !masks[(size_t)z * P_ + pix], out + (size_t)z * K * P_ + pix, P_, lc, feat,
+                   thr, post, meta, n_trees, K, leaf_s, tid);
+}
+
+// One image of a mixed-size batch: byte offsets of its pixels, mask and
+// posterior planes in the batch buffers, its size and its first tile.
+struct BatchImage {
+  unsigned long long img_off, mask_off, out_off;
+  uint32_t w, h, tiles_x, tile0;
+  uint32_t has_mask, pad;
+};
+
+// A mixed-size batch in one launch: CTA b serves tile b of the concatenated
+// tile lists (32x8 pixels; its image found by binary search over tile0).
+template <class P>
+__global__ void __launch_bounds__(kPredThreads) k_predict_batch(
+    const uint8_t *__restrict__ images, const uint8_t *__restrict__ masks, uint8_t *__restrict__ out,
+    const BatchImage *__restrict__ batch, uint32_t n, const int32_t *__restrict__ lc,
+    const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+    const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
+    const uint32_t *__restrict__ magic) {
+  using ImgT = typename P::img_t;
+  extern __shared__ int32_t leaf_s[];
+  uint32_t lo = 0, hi = n;  // the last image whose first tile is <= blockIdx.x
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (batch[mid].tile0 <= blockIdx.x) lo = mid;
+    else hi = mid;
+  }
+  const BatchImage b = batch[lo];
+  const uint32_t t = blockIdx.x - b.tile0;
+  const uint32_t x = (t % b.tiles_x) * kPredX + threadIdx.x, y = (t / b.tiles_x) * kPredY + threadIdx.y;
+  if (x >= b.w || y >= b.h) return;
+  const uint32_t tid = threadIdx.y * kPredX + threadIdx.x;
+  const size_t P_ = (size_t)b.w * b.h, pix = (size_t)y * b.w + x;
+  ImageRef<ImgT> im;
+  im.data = reinterpret_cast<const ImgT *>(images + b.img_off);
+  im.w = (int32_t)b.w;
+  im.h = (int32_t)b.h;
+  im.magic = magic;
+  const bool masked_out = b.has_mask && !masks[b.mask_off + pix];
+  predict_pixel<P>(im, x, y, masked_out, reinterpret_cast<float *>(out + b.out_off) + pix, P_, lc, feat, thr, post,
+                   meta, n_trees, K, leaf_s, tid);
 }
 
 template <class P>

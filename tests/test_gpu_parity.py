@@ -174,6 +174,60 @@ def test_upload_rejects_bad_samples_and_keeps_the_previous_set():
     assert np.array_equal(a.features, b.features) and np.array_equal(a.thresholds, b.thresholds)
 
 
+def _mixed_size_set(n_per_size=4, samples=600):
+    """Depth maps of the three sizes of the mixed-size configuration (160x120, 320x240,
+    640x480), 9 classes, in one training set."""
+    imgs, raw = [], []
+    for k, (w, h) in enumerate([(160, 120), (320, 240), (640, 480)]):
+        px, lb, sm = pg.synth_depth(7, n_per_size, w, h, first_image=n_per_size * k, parts=1, min_ellipses=2,
+                                    max_ellipses=5, samples_per_image=samples)
+        imgs += [pg.TrainingSetImage(px[i], lb[i], 9, sm[i]) for i in range(n_per_size)]
+        raw += [px[i] for i in range(n_per_size)]
+    return pg.TrainingSet(9, imgs), raw
+
+
+def test_mixed_image_sizes_bit_exact():
+    """One training set of mixed image sizes: the tree is the oracle's."""
+    ts, _ = _mixed_size_set()
+    cfg = pg.ForestConfig("depth_diff2", 9)
+    tp = pg.TreeTrainerParameters(96, 24, [-60000] * 4, [60000] * 4, -500, 500, 10)
+    tree = pg.Tree(cfg, 4, 10)
+    pg.TreeTrainer(cfg).train(tree, ts, tp)
+    _assert_same_tree(tree, _oracle_tree(cfg, ts, tp, 4, 10))
+    assert (tree.left_child >= 0).sum() > 20
+
+
+def test_mixed_size_batch_prediction_matches_per_image():
+    """A mixed-size batch (one launch replayed from a CUDA graph) gives the per-image
+    posteriors bit for bit: twice with the same layout, with another layout, and after the
+    forest grows (the cached graph must not be reused then)."""
+    ts, raw = _mixed_size_set(n_per_size=2, samples=400)
+    cfg = pg.ForestConfig("depth_diff2", 9)
+    tp = pg.TreeTrainerParameters(64, 16, [-60000] * 4, [60000] * 4, -500, 500, 10)
+    trees = []
+    for tid in range(2):
+        t = pg.Tree(cfg, tid, 8)
+        pg.TreeTrainer(cfg).train(t, ts, tp)
+        trees.append(t)
+    clf = pg.Classifier(cfg)
+    clf << trees[0]
+    rng = np.random.default_rng(1)
+    masks = [None, (rng.random(raw[1].shape) < 0.7).astype(np.uint8), None, None,
+             (rng.random(raw[4].shape) < 0.5).astype(np.uint8), None]
+
+    def check_batch(images, mks):
+        got = clf.predict_batch(images, mks)
+        for im, m, g in zip(images, mks, got):
+            ref = clf.predict(im, m)
+            assert np.array_equal(g.view(np.uint32), ref.view(np.uint32))
+
+    check_batch(raw, masks)
+    check_batch(raw, masks)                       # replayed graph
+    check_batch(raw[::-1], masks[::-1])           # another layout
+    clf << trees[1]                               # a grown forest
+    check_batch(raw, masks)
+
+
 def test_train_tree_config0_bit_exact():
     """The full 64-image 160x120 configuration: F=200, T=20, depth 8, min 20 pixels per leaf."""
     cfg, ts, tp, _ = depth_case(n_images=64, n_features=200, n_thresholds=20)

@@ -98,6 +98,8 @@ def test_user_plugin_trains_and_predicts_like_the_builtin(name):
     cb << b
     assert np.array_equal(ca.predict(image).view(np.uint32), cb.predict(image).view(np.uint32))
     assert np.array_equal(ca.predict_leaf(0, image), cb.predict_leaf(0, image))
+    (batch,) = cb.predict_batch([image])
+    assert np.array_equal(batch.view(np.uint32), cb.predict(image).view(np.uint32))
 
 
 @pytest.mark.gpu
