@@ -362,7 +362,7 @@ def run_ours(a):
                     hbm_gbs=bytes_alg / (pms / 1000) / 1e9,
                     note="500 held-out 640x480 images in one launch, forest of the timed trees, 38 algorithmic B/px")
         del dimg, dout
-        # mixed-size serving batch (config 3's form): 256 images, a third each of 160x120,
+        # mixed-size serving batch: 256 images, a third each of 160x120,
         # 320x240 and 640x480, host buffers in and out, one graph-replayed launch per batch
         sizes = [(160, 120), (320, 240), (640, 480)]
         mims = []
