@@ -163,7 +163,9 @@ int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
  *               get their split computed inside the histogram kernel, [0, 65535];
  *   "cand_order" 1 (default): each node's candidate table is laid out in the
  *               order of the candidates' first probe offsets (n_features <= 8192),
- *               so that neighbouring lanes probe neighbouring pixels; 0: index order. */
+ *               so that neighbouring lanes probe neighbouring pixels; 0: index order;
+ *   "sample_group" bytes of images and labels pd_sample stages per round trip,
+ *               >= 4096 (default 512 MiB). */
 int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value);
 /* Synchronises the context's stream. */
 int pd_ctx_sync(pd_ctx *ctx);
@@ -255,6 +257,58 @@ int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *const *image
 int pd_predict_posterior_device(pd_ctx *ctx, uint32_t n_images, const void *images_device,
                                 uint32_t width, uint32_t height, const uint8_t *masks_device,
                                 float *out_device);
+
+/* Pixel samplers (ImageSampler, image_sampler.hpp:31-73) ---------------------- */
+#define PD_SAMPLER_UNIFORM 1         /* UniformImageSampler (uniform_image_sampler_impl.hpp:34-63) */
+#define PD_SAMPLER_CLASS_WEIGHTED 2  /* ClassWeightedImageSampler (classweighted_image_sampler_impl.hpp:25-120) */
+/* Largest number of samples per image a sampler may produce (its stride). */
+#define PD_SAMPLER_MAX_STRIDE 16384
+
+/* The sampler's constructor arguments and template parameters. */
+typedef struct {
+  int32_t kind;            /* PD_SAMPLER_* */
+  uint32_t n_samples;      /* nSamples */
+  uint32_t seed;           /* seed (XORed into the CRC-32 of the image data) */
+  uint32_t n_classes;      /* nClasses (class-weighted; labels 1..nClasses) */
+  const float *weights;    /* per-class weights, NULL = 1/nClasses each (class-weighted) */
+  uint32_t pixel_bytes;    /* sizeof(type) * nChannels of the sampled images */
+} pd_sampler;
+
+/* Counters and CUDA-event times of the last pd_sample / pd_sample_device call. */
+typedef struct {
+  uint64_t images;
+  uint64_t data_bytes;       /* image bytes checksummed */
+  uint64_t label_bytes;      /* label bytes read */
+  uint64_t kernel_launches;
+  uint64_t h2d_bytes;
+  uint64_t d2h_bytes;
+  double ms_scan;            /* checksum + labelled-pixel count kernel */
+  double ms_draw;            /* per-image drawing / reservoir kernel */
+  double ms_total;           /* wall time of the call */
+} pd_sample_stats;
+
+/* Samples per image the output of pd_sample must hold: nSamples for the
+ * uniform sampler, the sum of the class buckets ceil(weight_k * nSamples) for
+ * the class-weighted one. */
+int pd_sampler_stride(const pd_sampler *s, uint32_t *stride);
+/* ImageSampler::sample over a batch of host images (mixed sizes): images[i]
+ * of widths[i] x heights[i] pixels of s->pixel_bytes bytes, labels[i] one byte
+ * per pixel (0 = unlabelled, class k stored as k+1).  The sorted pixel indices
+ * of image i go to samples + i*stride, their number to counts[i] (the value
+ * sample() returns; 0 for a uniform sampler on an image without labelled
+ * pixels, where the reference draws from an empty buffer).  A label above
+ * nClasses is an error for the class-weighted sampler (the reference indexes
+ * past its buckets). */
+int pd_sample(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, const void *const *images,
+              const uint8_t *const *labels, const uint32_t *widths, const uint32_t *heights,
+              uint32_t stride, uint32_t *samples, uint32_t *counts);
+/* The same over n same-size images already in device memory (images
+ * n*W*H*pixel_bytes, labels n*W*H, samples n*stride, counts n; all device
+ * pointers, 16-byte aligned, with W*H*pixel_bytes and W*H multiples of 16). */
+int pd_sample_device(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, const void *images_device,
+                     const uint8_t *labels_device, uint32_t width, uint32_t height, uint32_t stride,
+                     uint32_t *samples_device, uint32_t *counts_device);
+int pd_sample_get_stats(pd_ctx *ctx, pd_sample_stats *out);
 
 /* Synthetic data (seeded, bit-identical on every host) ------------------------ */
 /* Depth maps: background plane U(3000,4000) mm + N(0,5^2) noise, ellipses at

@@ -135,6 +135,26 @@ int or_predict_leaf(const or_params *p, const void *img, uint32_t w, uint32_t h,
                     const int32_t *left_child, const int32_t *features,
                     const int32_t *thresholds, int32_t *out, int n_threads);
 
+/* Pixel samplers (image_sampler.c): UniformImageSampler and
+ * ClassWeightedImageSampler with their Boost randomness restated. */
+typedef struct {
+  uint32_t x[624];
+  int i;
+} or_mt;
+uint32_t or_crc32(const uint8_t *p, uint64_t n);
+void or_mt_seed(or_mt *m, uint32_t s);
+uint32_t or_mt_next(or_mt *m);
+uint32_t or_uniform_int(or_mt *m, uint32_t range);
+double or_uniform01(or_mt *m);
+uint32_t or_bucket_sizes(uint32_t n_samples, uint32_t n_classes, const float *weights, uint32_t *sizes);
+uint32_t or_sample_uniform(const void *data, uint64_t data_bytes, const uint8_t *labels, uint32_t n_pix,
+                           uint32_t n_samples, uint32_t seed, uint32_t *out);
+int64_t or_sample_class_weighted(const void *data, uint64_t data_bytes, const uint8_t *labels, uint32_t n_pix,
+                                 uint32_t n_classes, const uint32_t *sizes, uint32_t seed, uint32_t *out);
+void or_sample_batch(int kind, const void *images, uint64_t data_bytes, const uint8_t *labels, uint32_t n_pix,
+                     uint32_t n_images, uint32_t n_samples, uint32_t n_classes, const uint32_t *sizes,
+                     uint32_t seed, uint32_t stride, uint32_t *out, int64_t *counts);
+
 #ifdef __cplusplus
 }
 #endif

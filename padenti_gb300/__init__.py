@@ -23,6 +23,7 @@ from ._native import PadentiError, check, lib
 __all__ = [
     "ForestConfig", "TreeTrainerParameters", "TrainingSetImage", "TrainingSet", "Tree", "TreeTrainer",
     "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS", "USER_SHAPES", "check_plugin",
+    "ImageSampler", "UniformImageSampler", "ClassWeightedImageSampler", "sampled_training_set",
 ]
 
 FEAT_DTYPE = {N.PD_FEAT_I16: np.int16, N.PD_FEAT_I32: np.int32}
@@ -427,6 +428,114 @@ class Classifier(_Ctx):
         m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
         check(lib().pd_predict_leaf(self.h, tree, _ptr(image), W, H, _ptr(m), _ptr(out)))
         return out
+
+
+_SAMPLER_CTX: dict = {}
+
+
+def _sampler_ctx(device: int):
+    """A context per device for the samplers (their own arguments fix the image type)."""
+    h = _SAMPLER_CTX.get(device)
+    if h is None:
+        h = C.c_void_p()
+        check(lib().pd_ctx_create(C.byref(ForestConfig("depth_diff2", 2).c()), device, C.byref(h)))
+        _SAMPLER_CTX[device] = h
+    return h
+
+
+class ImageSampler:
+    """ImageSampler (image_sampler.hpp:31-73) on the GPU: ``sample(data, labels)`` returns the
+    sorted sampled pixel indices of one image, ``sample_batch`` those of many images (of any
+    sizes) in one call.  The image's bytes (any dtype and channel count) seed the draws, as in
+    the reference."""
+
+    kind = 0
+
+    def __init__(self, n_samples: int, seed: int = 0, device: int = 0):
+        self.n_samples = int(n_samples)
+        self.seed = int(seed) & 0xFFFFFFFF
+        self.device = device
+        self.n_classes = 0
+        self._weights = None
+
+    def _c(self, pixel_bytes: int = 1) -> N.Sampler:
+        s = N.Sampler()
+        s.kind, s.n_samples, s.seed, s.n_classes = self.kind, self.n_samples, self.seed, self.n_classes
+        s.weights = None if self._weights is None else self._weights.ctypes.data
+        s.pixel_bytes = pixel_bytes
+        return s
+
+    @property
+    def stride(self) -> int:
+        """Most samples one image can get (nSamples, or the sum of the class buckets)."""
+        out = C.c_uint32()
+        check(lib().pd_sampler_stride(C.byref(self._c()), C.byref(out)))
+        return out.value
+
+    def sample(self, data: np.ndarray, labels: np.ndarray) -> np.ndarray:
+        return self.sample_batch([data], [labels])[0]
+
+    def sample_batch(self, images: list, labels: list) -> list:
+        n = len(images)
+        if n != len(labels):
+            raise ValueError("one label image per image")
+        imgs = [np.ascontiguousarray(a) for a in images]
+        lbs = [np.ascontiguousarray(a, np.uint8) for a in labels]
+        if n == 0:
+            return []
+        pb = {a.nbytes // max(a.shape[0] * a.shape[1], 1) for a in imgs}
+        if len(pb) != 1:
+            raise ValueError("all images of a batch need the same pixel type and channel count")
+        for a, lb in zip(imgs, lbs):
+            if a.shape[:2] != lb.shape:
+                raise ValueError(f"image {a.shape[:2]} and labels {lb.shape} differ in size")
+        stride = self.stride
+        out = np.zeros((n, max(stride, 1)), np.uint32)
+        counts = np.zeros(n, np.uint32)
+        iptr = (C.c_void_p * n)(*[a.ctypes.data for a in imgs])
+        lptr = (C.c_void_p * n)(*[a.ctypes.data for a in lbs])
+        w = np.array([a.shape[1] for a in lbs], np.uint32)
+        h = np.array([a.shape[0] for a in lbs], np.uint32)
+        check(lib().pd_sample(_sampler_ctx(self.device), C.byref(self._c(pb.pop())), n, iptr, lptr, _ptr(w), _ptr(h),
+                              max(stride, 1), _ptr(out), _ptr(counts)))
+        return [out[i, :counts[i]].copy() for i in range(n)]
+
+    def stats(self) -> dict:
+        st = N.SampleStats()
+        check(lib().pd_sample_get_stats(_sampler_ctx(self.device), C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+
+class UniformImageSampler(ImageSampler):
+    """UniformImageSampler (uniform_image_sampler_impl.hpp:34-63): n_samples labelled pixels,
+    uniformly with replacement."""
+
+    kind = N.PD_SAMPLER_UNIFORM
+
+
+class ClassWeightedImageSampler(ImageSampler):
+    """ClassWeightedImageSampler (classweighted_image_sampler_impl.hpp:25-120): a reservoir of
+    ceil(weight_k * n_samples) pixels per class (weights None: 1/n_classes each)."""
+
+    kind = N.PD_SAMPLER_CLASS_WEIGHTED
+
+    def __init__(self, n_samples: int, n_classes: int, weights=None, seed: int = 0, device: int = 0):
+        super().__init__(n_samples, seed, device)
+        self.n_classes = int(n_classes)
+        if weights is not None:
+            self._weights = np.ascontiguousarray(weights, np.float32)
+            if self._weights.shape != (self.n_classes,):
+                raise ValueError("one weight per class")
+
+
+def sampled_training_set(n_classes: int, images: list, labels: list, sampler: ImageSampler) -> TrainingSet:
+    """TrainingSet(tsPath, …, sampler) (training_set_impl.hpp:40-112) without the image loaders:
+    every image sampled by `sampler` (in one batch on the GPU), images and labels of different
+    sizes skipped as the reference skips them."""
+    keep = [i for i in range(len(images)) if np.shape(images[i])[:2] == np.shape(labels[i])]
+    samples = sampler.sample_batch([images[i] for i in keep], [labels[i] for i in keep])
+    return TrainingSet(n_classes, [TrainingSetImage(images[i], labels[i], n_classes, sm)
+                                   for i, sm in zip(keep, samples)])
 
 
 def synth_depth(seed: int, n_images: int, width: int, height: int, *, first_image: int = 0, min_ellipses: int = 1,

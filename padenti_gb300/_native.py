@@ -72,6 +72,34 @@ class TrainStats(C.Structure):
     ]
 
 
+class Sampler(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("n_samples", C.c_uint32),
+        ("seed", C.c_uint32),
+        ("n_classes", C.c_uint32),
+        ("weights", C.c_void_p),
+        ("pixel_bytes", C.c_uint32),
+    ]
+
+
+class SampleStats(C.Structure):
+    _fields_ = [
+        ("images", C.c_uint64),
+        ("data_bytes", C.c_uint64),
+        ("label_bytes", C.c_uint64),
+        ("kernel_launches", C.c_uint64),
+        ("h2d_bytes", C.c_uint64),
+        ("d2h_bytes", C.c_uint64),
+        ("ms_scan", C.c_double),
+        ("ms_draw", C.c_double),
+        ("ms_total", C.c_double),
+    ]
+
+
+PD_SAMPLER_UNIFORM = 1
+PD_SAMPLER_CLASS_WEIGHTED = 2
+
 # name -> (restype, argtypes)
 _P = C.c_void_p
 _SIGS = {
@@ -103,6 +131,11 @@ _SIGS = {
     "pd_predict_leaf": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
     "pd_predict_posterior_batch": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P]),
     "pd_predict_posterior_device": (C.c_int, [_P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, _P]),
+    "pd_sampler_stride": (C.c_int, [C.POINTER(Sampler), C.POINTER(C.c_uint32)]),
+    "pd_sample": (C.c_int, [_P, C.POINTER(Sampler), C.c_uint32, _P, _P, _P, _P, C.c_uint32, _P, _P]),
+    "pd_sample_device": (C.c_int, [_P, C.POINTER(Sampler), C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32,
+                                   _P, _P]),
+    "pd_sample_get_stats": (C.c_int, [_P, C.POINTER(SampleStats)]),
     "pd_synth_depth": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "pd_synth_rgb": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,

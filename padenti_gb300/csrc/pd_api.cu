@@ -92,6 +92,12 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
   ctx->b_out.release();
   ctx->b_desc.release();
   rtc_release(ctx);
+  ctx->sm_data.release();
+  ctx->sm_lab.release();
+  ctx->sm_desc.release();
+  ctx->sm_out.release();
+  ctx->h_sm.release();
+  ctx->h_sm_desc.release();
   ctx->h_stage.release();
   ctx->h_items.release();
   for (auto &ev : ctx->ev)
@@ -123,6 +129,9 @@ extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
   } else if (n == "cand_order") {
     PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "cand_order must be 0 or 1");
     ctx->cand_order = value != 0;
+  } else if (n == "sample_group") {
+    PD_CHECK(value >= 4096, PD_ERR_INVALID, "sample_group %lld below 4096 bytes", (long long)value);
+    ctx->sample_group = (uint64_t)value;
   } else {
     return set_error(PD_ERR_INVALID, "unknown tuning knob '%s'", name);
   }

@@ -23,6 +23,7 @@ struct pd_ctx {
   uint32_t hist_spi = 8;  // samples per iteration of the histogram kernel (2, 4 or 8)
   uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
   bool cand_order = true;    // order each node's candidate columns by first-probe offset
+  uint64_t sample_group = 512ull << 20;  // bytes of images + labels pd_sample stages per round trip
 
   // ---- training set in HBM (cl_tree_trainer_impl_init.hpp:99-154 streams it
   // image by image; here it stays resident) ----
@@ -78,6 +79,13 @@ struct pd_ctx {
   pd::DevBuf b_img, b_mask, b_out, b_desc;
   std::vector<uint64_t> batch_key;
   cudaGraphExec_t batch_graph = nullptr;
+
+  // ---- pixel samplers (pd_sample*) ----
+  pd::DevBuf sm_data, sm_lab;    // staged image data and labels of a host batch
+  pd::DevBuf sm_desc;            // SampImage per image, item -> image map, checksums, counts, error
+  pd::DevBuf sm_out;             // samples and counts of a host batch
+  pd::HostBuf h_sm, h_sm_desc;   // pinned staging of a host batch and of its descriptors
+  pd_sample_stats sample_stats{};
 
   cudaEvent_t ev[8] = {};
   uint64_t bytes_h2d = 0, bytes_d2h = 0, launches = 0;

@@ -48,3 +48,43 @@ def tree_tuple(tree):
 def sample_labels(ts) -> np.ndarray:
     """Class (0-based) of every sample of a TrainingSet, in upload order."""
     return np.concatenate([im.labels.reshape(-1)[im.samples] for im in ts.images]).astype(np.int64) - 1
+
+
+def sampler_images():
+    """Images for the pixel-sampler tests: (name, img_type, data, labels, n_classes).  Depth maps
+    of several sizes (an odd one among them), RGB images, and label images with one, two or no
+    labelled pixels."""
+    out = []
+    px, lb, _ = pg.synth_depth(5, 3, 80, 60, parts=1, min_ellipses=2, max_ellipses=4, samples_per_image=4)
+    out += [(f"depth80x60_{i}", 2, px[i], lb[i], 9) for i in range(3)]
+    px, lb, _ = pg.synth_depth(8, 2, 161, 121, parts=1, min_ellipses=2, max_ellipses=4, samples_per_image=4)
+    out += [(f"depth161x121_{i}", 2, px[i], lb[i], 9) for i in range(2)]
+    rgb, rlb, _ = pg.synth_rgb(5, 2, 47, 39, n_classes=6, samples_per_image=4)
+    out += [(f"rgb47x39_{i}", 1, rgb[i], rlb[i], 6) for i in range(2)]
+    sparse = np.zeros((60, 80), np.uint8)
+    sparse[10, 7], sparse[30, 50] = 2, 5
+    single = np.zeros((60, 80), np.uint8)
+    single[20, 20] = 1
+    out += [("sparse", 2, px[0][:60, :80].copy(), sparse, 9), ("single", 2, px[1][:60, :80].copy(), single, 9)]
+    return out
+
+
+# (name, kind, n_samples, seed, weights) of the sampler fixtures; weights name a rule
+SAMPLER_CONFIGS = [
+    ("uniform_500", 1, 500, 0, None),
+    ("uniform_37", 1, 37, 123456, None),
+    ("uniform_3000", 1, 3000, 7, None),
+    ("cw_300", 2, 300, 0, None),
+    ("cw_2000_skewed", 2, 2000, 99, "skewed"),
+    ("cw_250_zero", 2, 250, 5, "zero"),
+]
+
+
+def sampler_weights(rule, k):
+    if rule is None:
+        return None
+    if rule == "skewed":
+        return np.linspace(0.02, 0.3, k).astype(np.float32)
+    w = np.full(k, 1.0 / (k - 1), np.float32)
+    w[1] = 0
+    return w

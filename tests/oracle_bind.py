@@ -201,3 +201,101 @@ def predict_leaf(p: Params, image, mask, depth, lc, feats, thrs, n_channels=1, t
                                P(np.ascontiguousarray(np.asarray(thrs, np.int32))), P(out), threads)
     assert rc == 0
     return out
+
+
+# ---------------------------------------------------------------- samplers ----
+class MT(C.Structure):
+    _fields_ = [("x", C.c_uint32 * 624), ("i", C.c_int)]
+
+
+def crc32(data) -> int:
+    b = np.ascontiguousarray(data).view(np.uint8).reshape(-1)
+    lib().or_crc32.restype = C.c_uint32
+    return int(lib().or_crc32(P(b), C.c_uint64(b.size)))
+
+
+def mt_outputs(seed: int, n: int) -> np.ndarray:
+    m = MT()
+    lib().or_mt_seed(C.byref(m), C.c_uint32(seed))
+    lib().or_mt_next.restype = C.c_uint32
+    return np.array([lib().or_mt_next(C.byref(m)) for _ in range(n)], np.uint64).astype(np.uint32)
+
+
+def uniform_ints(seed: int, range_: int, n: int) -> np.ndarray:
+    m = MT()
+    lib().or_mt_seed(C.byref(m), C.c_uint32(seed))
+    lib().or_uniform_int.restype = C.c_uint32
+    return np.array([lib().or_uniform_int(C.byref(m), C.c_uint32(range_)) for _ in range(n)], np.uint32)
+
+
+def bucket_sizes(n_samples: int, n_classes: int, weights=None) -> np.ndarray:
+    out = np.zeros(n_classes, np.uint32)
+    w = None if weights is None else np.ascontiguousarray(weights, np.float32)
+    lib().or_bucket_sizes(C.c_uint32(n_samples), C.c_uint32(n_classes), P(w), P(out))
+    return out
+
+
+def sample_uniform(data, labels, n_samples: int, seed: int) -> np.ndarray:
+    d = np.ascontiguousarray(data)
+    lb = np.ascontiguousarray(labels, np.uint8).reshape(-1)
+    out = np.zeros(max(n_samples, 1), np.uint32)
+    lib().or_sample_uniform.restype = C.c_uint32
+    n = lib().or_sample_uniform(P(d), C.c_uint64(d.nbytes), P(lb), C.c_uint32(lb.size), C.c_uint32(n_samples),
+                                C.c_uint32(seed), P(out))
+    return out[:n]
+
+
+def sample_class_weighted(data, labels, n_samples: int, n_classes: int, weights, seed: int) -> np.ndarray:
+    d = np.ascontiguousarray(data)
+    lb = np.ascontiguousarray(labels, np.uint8).reshape(-1)
+    sizes = bucket_sizes(n_samples, n_classes, weights)
+    out = np.zeros(max(int(sizes.sum()), 1), np.uint32)
+    lib().or_sample_class_weighted.restype = C.c_int64
+    n = lib().or_sample_class_weighted(P(d), C.c_uint64(d.nbytes), P(lb), C.c_uint32(lb.size),
+                                       C.c_uint32(n_classes), P(sizes), C.c_uint32(seed), P(out))
+    assert n >= 0, "label above n_classes"
+    return out[:n]
+
+
+def sample_batch(kind: int, images, labels, n_samples: int, seed: int, n_classes=0, weights=None):
+    """Samples of a batch of same-size images on all host threads: (samples [n][stride], counts)."""
+    imgs = np.ascontiguousarray(images)
+    lbs = np.ascontiguousarray(labels, np.uint8)
+    n = imgs.shape[0]
+    sizes = bucket_sizes(n_samples, n_classes, weights) if kind == 2 else np.zeros(1, np.uint32)
+    stride = n_samples if kind == 1 else int(sizes.sum())
+    out = np.zeros((n, max(stride, 1)), np.uint32)
+    counts = np.zeros(n, np.int64)
+    lib().or_sample_batch(kind, P(imgs), C.c_uint64(imgs[0].nbytes), P(lbs), C.c_uint32(lbs[0].size),
+                          C.c_uint32(n), C.c_uint32(n_samples), C.c_uint32(n_classes), P(sizes), C.c_uint32(seed),
+                          C.c_uint32(max(stride, 1)), P(out), P(counts))
+    return out, counts
+
+
+def ref_sample_uniform(img_type: int, data, labels, n_samples: int, seed: int):
+    """The reference's UniformImageSampler compiled from its sources (None when absent)."""
+    r = ref("sampler")
+    if r is None:
+        return None
+    d = np.ascontiguousarray(data)
+    lb = np.ascontiguousarray(labels, np.uint8)
+    h, w = lb.shape
+    out = np.zeros(max(n_samples, 1), np.uint32)
+    r.ref_sample_uniform.restype = C.c_uint
+    n = r.ref_sample_uniform(img_type, P(d), P(lb), w, h, n_samples, C.c_uint(seed), P(out))
+    return out[:n]
+
+
+def ref_sample_class_weighted(img_type: int, data, labels, n_samples: int, n_classes: int, weights, seed: int):
+    r = ref("sampler")
+    if r is None:
+        return None
+    d = np.ascontiguousarray(data)
+    lb = np.ascontiguousarray(labels, np.uint8)
+    h, w = lb.shape
+    sizes = bucket_sizes(n_samples, n_classes, weights)
+    out = np.zeros(max(int(sizes.sum()), 1), np.uint32)
+    wt = None if weights is None else np.ascontiguousarray(weights, np.float32)
+    r.ref_sample_class_weighted.restype = C.c_uint
+    n = r.ref_sample_class_weighted(img_type, P(d), P(lb), w, h, n_samples, n_classes, P(wt), C.c_uint(seed), P(out))
+    return out[:n]
