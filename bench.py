@@ -53,6 +53,7 @@ def args_():
     a.add_argument("--min-leaf", type=int, default=20)
     a.add_argument("--predict-images", type=int, default=500)
     a.add_argument("--e2e-steps", type=int, default=None)
+    a.add_argument("--sampler-images", type=int, default=2000, help="images sampled by the pixel samplers (0: skip)")
     a.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     a.add_argument("--no-cpu", action="store_true")
     a.add_argument("--seed", type=int, default=0)
@@ -173,6 +174,76 @@ def cpu_sample(a, cfg, ts, tp, seconds: float):
                 sample=f"root depth (histogram + split) of the first {m} images ({n} samples x {tp.n_features} "
                        f"candidates x {tp.n_thresholds} thresholds), MD5 candidates regenerated per "
                        f"(sample, candidate) as the reference kernel does; {dt:.1f} s"), m
+
+
+def sampler_bench(a, pg, N, px, lb):
+    """UniformImageSampler / ClassWeightedImageSampler over the training images (2000 samples per
+    image, 9 classes): device-resident (pd_sample_device, CUDA-event kernel times) and from host
+    buffers (pd_sample, wall clock), with the oracle on the host cores beside them."""
+    import torch
+
+    n = min(a.sampler_images, len(px))
+    h = pg._sampler_ctx(torch.cuda.current_device())
+    dpx = torch.from_numpy(px[:n].view(np.int16)).cuda()
+    dlb = torch.from_numpy(lb[:n]).cuda()
+    peak, _ = measured_peaks()
+    out = {}
+    for name, sm in [("uniform", pg.UniformImageSampler(a.samples, 0)),
+                     ("class_weighted", pg.ClassWeightedImageSampler(a.samples, 9, seed=0))]:
+        stride = sm.stride
+        dout = torch.zeros((n, stride), dtype=torch.int32, device="cuda")
+        dcnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+        sc = sm._c(2)
+
+        def dstep():
+            N.check(N.lib().pd_sample_device(h, C.byref(sc), n, dpx.data_ptr(), dlb.data_ptr(), a.width, a.height,
+                                             stride, dout.data_ptr(), dcnt.data_ptr()))
+
+        torch.cuda.synchronize()
+        for _ in range(3):
+            dstep()
+        reps, scan, draw = 5, [], []
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            dstep()
+            st = sm.stats()
+            scan.append(st["ms_scan"])
+            draw.append(st["ms_draw"])
+        wall = (time.perf_counter() - t0) * 1000 / reps
+        ms_scan, ms_draw = float(np.median(scan)), float(np.median(draw))
+        scan_bytes = n * a.width * a.height * 3  # image bytes (2 per pixel) + label bytes (1 per pixel)
+        # host buffers in, samples out
+        imgs, lbs = [px[i] for i in range(n)], [lb[i] for i in range(n)]
+        sm.sample_batch(imgs, lbs)
+        t0 = time.perf_counter()
+        e_reps = 2
+        for _ in range(e_reps):
+            sm.sample_batch(imgs, lbs)
+        e2e_ms = (time.perf_counter() - t0) * 1000 / e_reps
+        est = sm.stats()
+        out[name] = dict(
+            metric="sampled images/s", value=n / ((ms_scan + ms_draw) / 1000), unit="images/s", images=n,
+            ms_kernels=ms_scan + ms_draw, ms_scan=ms_scan, ms_draw=ms_draw, ms_call=wall,
+            roofline=dict(kernel="k_sample_scan", bound="hbm", achieved=scan_bytes / (ms_scan / 1000) / 1e9,
+                          peak=peak, unit="GB/s", frac=scan_bytes / (ms_scan / 1000) / 1e9 / peak,
+                          algorithmic_bytes=scan_bytes),
+            e2e=dict(value=n / (e2e_ms / 1000), unit="images/s", ms=e2e_ms, h2d_bytes=est["h2d_bytes"],
+                     d2h_bytes=est["d2h_bytes"]))
+        del dout, dcnt
+    del dpx, dlb
+    if not a.no_cpu:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_bind as ob
+
+        m = n
+        for name, kind in [("uniform", 1), ("class_weighted", 2)]:
+            t0 = time.perf_counter()
+            ob.sample_batch(kind, px[:m], lb[:m], a.samples, 0, n_classes=9)
+            dt = time.perf_counter() - t0
+            out[name]["cpu_baseline"] = dict(value=m / dt, unit="images/s", cores=os.cpu_count() or 1, kind="port",
+                                             sample=f"the first {m} images, oracle restatement of the reference "
+                                                    f"sampler (table CRC-32, MT19937) on all host cores; {dt:.1f} s")
+    return out
 
 
 def run_reference(a):
@@ -395,6 +466,8 @@ def run_ours(a):
                                         "pd_predict_posterior_batch from host buffers: per-image copies in, one "
                                         "CUDA-graph replay of the batch kernel, posteriors out; wall clock")
 
+    samp = sampler_bench(a, pg, N, px, lb) if a.sampler_images > 0 else None
+
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -423,7 +496,7 @@ def run_ours(a):
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
                 roofline=roof, cpu_baseline=base, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
-                predict=pred, phases_per_step={k: v / a.steps for k, v in phases.items()}, impl="ours")
+                predict=pred, sampler=samp, phases_per_step={k: v / a.steps for k, v in phases.items()}, impl="ours")
     print(json.dumps(line), flush=True)
 
 

@@ -36,10 +36,16 @@ constexpr uint32_t kSmWarps = kSmThreads / 32;
 constexpr uint32_t kCrcPoly = 0xEDB88320u;  // CRC-32, reflected
 constexpr uint32_t kGfOne = 0x80000000u;    // x^0 in the reflected representation
 constexpr uint32_t kGfX8 = 0x00800000u;     // x^8
-constexpr uint32_t kChains = 4;             // independent CRC chains per thread
-constexpr uint32_t kChainBytes = 256;
-constexpr uint32_t kThreadBytes = kChains * kChainBytes;     // 1 KiB per thread
-constexpr uint32_t kSliceBytes = kThreadBytes * kSmThreads;  // 256 KiB per checksum work item
+// Checksum layout: a work item is a 256 KiB slice of an image's bytes, counted
+// from the image's end; warp w streams the slice's 32 KiB region w as 16
+// blocks of 2 KiB; lane l takes the 64 bytes at 64 l of every block, in two
+// chains (even and odd blocks) for instruction-level parallelism.
+constexpr uint32_t kPiece = 64;                              // bytes per lane per block
+constexpr uint32_t kBlock = 32 * kPiece;                     // 2 KiB
+constexpr uint32_t kRegionBlocks = 16;
+constexpr uint32_t kRegion = kBlock * kRegionBlocks;         // 32 KiB per warp
+constexpr uint32_t kSliceBytes = kRegion * kSmWarps;         // 256 KiB per checksum work item
+constexpr uint32_t kGap = 2 * kBlock - kPiece;               // from one piece of a chain to its next
 constexpr uint32_t kLabVecsPerItem = 16 * kSmThreads;        // 64 KiB of labels per count work item
 constexpr uint32_t kMtN = 624;
 constexpr uint32_t kWindow = 4 * kSmThreads;                  // pixels per reservoir step
@@ -55,7 +61,9 @@ struct SampImage {
   uint32_t n_pix;
   uint32_t lab_vecs;
   uint32_t n_slices;  // checksum work items (kSliceBytes each, counted from data_end)
-  uint32_t item0;     // first work item of the image
+  uint32_t crc0;      // its first checksum work item (checksum items come first)
+  uint32_t lab0;      // its first label work item
+  uint32_t pad;
 };
 
 // ---- arithmetic modulo the CRC-32 polynomial (reflected: bit 31 is x^0) ----
@@ -188,70 +196,106 @@ PD_D uint32_t reservoir_slot(uint32_t v, uint32_t c) {
 }
 
 // ------------------------------------------------------------------ kernels --
-// Work items: the checksum slices of each image (counted from its end), then
-// its label chunks.  crc[] starts at each image's initial-value term, count[]
-// at zero.
-__global__ void __launch_bounds__(kSmThreads) k_sample_scan(const uint8_t *__restrict__ data,
+// Shift constants of the checksum, computed once on the host (x^(8n) is the
+// effect of n zero bytes): multiplication tables [4][256] for x^(8 kGap) and
+// x^(8 kBlock) (a*X is the XOR of the entries of a's four bytes), x^(8 * bytes
+// after lane l's piece in its region) for l < 32, x^(8 * bytes after region
+// w in its slice) for w < 8, x^(8 kSliceBytes 2^k) for k < 32.
+constexpr uint32_t kShiftGap = 0, kShiftBlock = 1024, kShiftLane = 2048, kShiftWarp = 2080, kShiftSlice = 2088,
+                   kShiftWords = 2120;
+
+PD_D uint32_t mul_tab(uint32_t a, const uint32_t *M) {
+  return M[a & 0xFFu] ^ M[256 + ((a >> 8) & 0xFFu)] ^ M[512 + ((a >> 16) & 0xFFu)] ^ M[768 + (a >> 24)];
+}
+
+PD_D void prefetch_l2(const uint8_t *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// 64 bytes into the CRC register r, one table step per byte.
+PD_D uint32_t crc_piece(uint32_t r, const uint4 (&q)[4], const uint32_t *T) {
+#pragma unroll
+  for (uint32_t i = 0; i < 16; i++) {
+    const uint4 &x = q[i >> 2];
+    r ^= (i & 3) == 0 ? x.x : (i & 3) == 1 ? x.y : (i & 3) == 2 ? x.z : x.w;
+#pragma unroll
+    for (uint32_t s = 0; s < 4; s++) r = T[(r & 0xFFu) << 5] ^ (r >> 8);
+  }
+  return r;
+}
+
+// Work items: the checksum slices of all images (counted from each image's
+// end), then the label chunks of all images; CTAs take the next item from a
+// counter.  crc[] starts at each image's initial-value term, count[] and
+// *next at zero.
+__global__ void __launch_bounds__(kSmThreads, 4) k_sample_scan(const uint8_t *__restrict__ data,
                                                             const uint8_t *__restrict__ labels,
                                                             const SampImage *__restrict__ imgs,
                                                             const uint32_t *__restrict__ item_img, uint32_t n_items,
-                                                            uint32_t *__restrict__ crc, uint32_t *__restrict__ count) {
+                                                            uint32_t n_crc_items, const uint32_t *__restrict__ shifts,
+                                                            uint32_t *__restrict__ crc, uint32_t *__restrict__ count,
+                                                            uint32_t *__restrict__ next) {
   // byte table, one copy per bank: entry e of lane l at [e * 32 + l]
   __shared__ uint32_t tab[256 * 32];
-  __shared__ uint32_t xs[32];  // x^(8 * kSliceBytes * 2^k)
+  __shared__ uint32_t mgap[1024], mblock[1024];
+  __shared__ uint32_t xs[32];
   __shared__ uint32_t red[kSmWarps];
+  __shared__ uint32_t s_item;
   const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
   {
     uint32_t r = t;
     for (int k = 0; k < 8; k++) r = (r >> 1) ^ (kCrcPoly & (0u - (r & 1u)));
     for (uint32_t i = 0; i < 32; i++) tab[t * 32 + ((i + lane) & 31)] = r;
   }
-  if (warp == 0) {
-    uint32_t p = gf_x8n(kSliceBytes);
-    for (uint32_t k = 0; k < lane; k++) p = gf_mul(p, p);
-    xs[lane] = p;
+  if (t == 0) s_item = atomicAdd(next, 1u);
+  for (uint32_t i = t; i < 1024; i += kSmThreads) {
+    mgap[i] = shifts[kShiftGap + i];
+    mblock[i] = shifts[kShiftBlock + i];
   }
-  const uint32_t x_thread = gf_x8n((uint64_t)kThreadBytes * (kSmThreads - 1 - t));  // bytes after this thread's range
-  const uint32_t x_chain = gf_x8n(kChainBytes);
+  if (t < 32) xs[t] = shifts[kShiftSlice + t];
+  const uint32_t x_lane = shifts[kShiftLane + lane], x_warp = shifts[kShiftWarp + warp];
   __syncthreads();
   const uint32_t *T = tab + lane;
-  for (uint32_t item = blockIdx.x; item < n_items; item += gridDim.x) {
+  for (;;) {
+    const uint32_t item = s_item;
+    if (item >= n_items) break;
     const uint32_t im = item_img[item];
     const SampImage g = imgs[im];
-    const uint32_t local = item - g.item0;
-    if (local < g.n_slices) {
-      const int64_t t_end =
-          (int64_t)g.data_end - (int64_t)local * kSliceBytes - (int64_t)(kSmThreads - 1 - t) * kThreadBytes;
-      const int64_t t_beg = t_end - kThreadBytes, lo = (int64_t)g.data_lo;
-      uint32_t r[kChains] = {0, 0, 0, 0};
-      if (t_end > lo) {
-#pragma unroll 2
-        for (uint32_t v = 0; v < kChainBytes / 16; v++) {
-          uint4 q[kChains];
+    if (item < n_crc_items) {
+      const uint32_t local = item - g.crc0;
+      const int64_t r_end = (int64_t)g.data_end - (int64_t)local * kSliceBytes - (int64_t)(kSmWarps - 1 - warp) * kRegion;
+      const int64_t r_beg = r_end - kRegion, lo = (int64_t)g.data_lo;
+      uint32_t acc = 0;
+      if (r_end > lo) {  // warp-uniform: this warp's region holds image bytes
+        const uint8_t *rb = data + r_beg;  // only dereferenced at or after data + lo
+        // the first blocks into L2 (lanes 0-15: the 16 lines of one block)
+        if (lane < 16)
 #pragma unroll
-          for (uint32_t k = 0; k < kChains; k++) {
-            const int64_t a = t_beg + (int64_t)(k * kChainBytes + v * 16);
-            q[k] = a >= lo ? __ldg(reinterpret_cast<const uint4 *>(data + a)) : make_uint4(0, 0, 0, 0);
+          for (uint32_t j = 0; j < 4; j++)
+            if (r_beg + (int64_t)(j * kBlock) >= lo) prefetch_l2(rb + j * kBlock + lane * 128);
+        uint32_t s0 = 0, s1 = 0;
+#pragma unroll 1
+        for (uint32_t j = 0; j < kRegionBlocks; j += 2) {
+          if (j + 4 < kRegionBlocks) {
+            const uint32_t pj = j + 4 + (lane >> 4);
+            if (r_beg + (int64_t)(pj * kBlock) >= lo) prefetch_l2(rb + pj * kBlock + (lane & 15) * 128);
           }
+          uint4 q0[4], q1[4];
 #pragma unroll
-          for (uint32_t w = 0; w < 4; w++) {
-#pragma unroll
-            for (uint32_t k = 0; k < kChains; k++)
-              r[k] ^= w == 0 ? q[k].x : w == 1 ? q[k].y : w == 2 ? q[k].z : q[k].w;
-#pragma unroll
-            for (uint32_t s = 0; s < 4; s++)
-#pragma unroll
-              for (uint32_t k = 0; k < kChains; k++) r[k] = T[(r[k] & 0xFFu) << 5] ^ (r[k] >> 8);
+          for (uint32_t i = 0; i < 4; i++) {
+            const int64_t a0 = r_beg + (int64_t)(j * kBlock + lane * kPiece + i * 16);
+            const int64_t a1 = a0 + kBlock;
+            q0[i] = a0 >= lo ? __ldg(reinterpret_cast<const uint4 *>(data + a0)) : make_uint4(0, 0, 0, 0);
+            q1[i] = a1 >= lo ? __ldg(reinterpret_cast<const uint4 *>(data + a1)) : make_uint4(0, 0, 0, 0);
           }
+          s0 = crc_piece(mul_tab(s0, mgap), q0, T);
+          s1 = crc_piece(mul_tab(s1, mgap), q1, T);
         }
+        // chain 0 ends one block before chain 1; then to the end of the region
+        acc = mul_tab(s0, mblock) ^ s1;
+        if (acc) acc = gf_mul(acc, x_lane);
       }
-      uint32_t acc = r[0];
-#pragma unroll
-      for (uint32_t k = 1; k < kChains; k++) acc = gf_mul(acc, x_chain) ^ r[k];
-      if (acc) acc = gf_mul(acc, x_thread);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) acc ^= __shfl_xor_sync(0xFFFFFFFFu, acc, o);
-      if (lane == 0) red[warp] = acc;
+      if (lane == 0) red[warp] = acc ? gf_mul(acc, x_warp) : 0u;
       __syncthreads();
       if (t == 0) {
         uint32_t tot = 0;
@@ -263,7 +307,7 @@ __global__ void __launch_bounds__(kSmThreads) k_sample_scan(const uint8_t *__res
         }
       }
     } else {
-      const uint32_t v0 = (local - g.n_slices) * kLabVecsPerItem;
+      const uint32_t v0 = (item - g.lab0) * kLabVecsPerItem;
       const uint4 *L = reinterpret_cast<const uint4 *>(labels + g.lab_off);
       uint32_t n = 0;
 #pragma unroll 4
@@ -281,6 +325,8 @@ __global__ void __launch_bounds__(kSmThreads) k_sample_scan(const uint8_t *__res
         if (tot) atomicAdd(&count[im], tot);
       }
     }
+    __syncthreads();  // everyone has read s_item and red[]
+    if (t == 0) s_item = atomicAdd(next, 1u);
     __syncthreads();
   }
 }
@@ -537,31 +583,51 @@ int plan_sampler(const pd_sampler *s, SamplerPlan *pl) {
   return PD_OK;
 }
 
-uint32_t scan_items(uint64_t data_span, uint32_t lab_vecs, uint32_t *n_slices) {
-  *n_slices = (uint32_t)((data_span + kSliceBytes - 1) / kSliceBytes);
-  return *n_slices + (lab_vecs + kLabVecsPerItem - 1) / kLabVecsPerItem;
-}
 
 // Descriptors, item map, initial checksum terms, zero counts, the error word
 // and the class-weighted bucket sizes, in one pinned block uploaded with one
 // copy.
 struct DescLayout {
-  size_t imgs = 0, items = 0, crc = 0, count = 0, err = 0, bucket = 0, bytes = 0;
+  size_t shifts = 0, imgs = 0, items = 0, crc = 0, count = 0, err = 0, bucket = 0, bytes = 0;
+  uint32_t n_items = 0, n_crc_items = 0;
   DescLayout() = default;
   DescLayout(uint32_t n, uint32_t n_items, uint32_t n_classes) {
+    imgs = shifts + ((4ull * kShiftWords + 15) / 16 * 16);
     items = imgs + sizeof(SampImage) * n;
     crc = items + 4ull * n_items;
     count = crc + 4ull * n;
     err = count + 4ull * n;
-    bucket = err + 16;
+    bucket = err + 16;  // err[0], err[1]: errors; err[2]: the scan's work counter
     bytes = bucket + 4ull * n_classes;
+    this->n_items = n_items;
   }
 };
 
+// The checksum's shift constants (kShift*), computed once.
+const uint32_t *shift_constants() {
+  static const std::vector<uint32_t> tab = [] {
+    std::vector<uint32_t> v(kShiftWords);
+    const uint32_t xg = gf_x8n(kGap), xb = gf_x8n(kBlock);
+    for (uint32_t i = 0; i < 4; i++)
+      for (uint32_t e = 0; e < 256; e++) {
+        v[kShiftGap + i * 256 + e] = gf_mul(e << (8 * i), xg);
+        v[kShiftBlock + i * 256 + e] = gf_mul(e << (8 * i), xb);
+      }
+    for (uint32_t l = 0; l < 32; l++) v[kShiftLane + l] = gf_x8n((uint64_t)kPiece * (31 - l));
+    for (uint32_t w = 0; w < kSmWarps; w++) v[kShiftWarp + w] = gf_x8n((uint64_t)kRegion * (kSmWarps - 1 - w));
+    uint32_t p = gf_x8n(kSliceBytes);
+    for (uint32_t k = 0; k < 32; k++) {
+      v[kShiftSlice + k] = p;
+      p = gf_mul(p, p);
+    }
+    return v;
+  }();
+  return tab.data();
+}
+
 // Uploads the descriptor block and launches the two kernels on a batch that is
 // in device memory.  counts/err stay on the device.
-int launch_batch(pd_ctx *ctx, const pd_sampler *s, const SamplerPlan &pl, uint32_t n, uint32_t n_items,
-                 const uint8_t *data, const uint8_t *labels, uint32_t *out, uint32_t *counts, const DescLayout &lay,
+int launch_batch(pd_ctx *ctx, const pd_sampler *s, const SamplerPlan &pl, uint32_t n, const uint8_t *data, const uint8_t *labels, uint32_t *out, uint32_t *counts, const DescLayout &lay,
                  uint8_t *dev_desc) {
   cudaStream_t st = ctx->stream;
   PD_CUDA(h2d(ctx, dev_desc, ctx->h_sm_desc.ptr, lay.bytes));
@@ -573,9 +639,11 @@ int launch_batch(pd_ctx *ctx, const pd_sampler *s, const SamplerPlan &pl, uint32
   int sms = 0, per_sm = 0;
   PD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   PD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sample_scan, kSmThreads, 0));
-  const uint32_t grid = std::max(1u, std::min<uint32_t>(n_items, (uint32_t)(sms * std::max(per_sm, 1))));
+  const uint32_t grid = std::max(1u, std::min<uint32_t>(lay.n_items, (uint32_t)(sms * std::max(per_sm, 1))));
   PD_CUDA(cudaEventRecord(ctx->ev[0], st));
-  k_sample_scan<<<grid, kSmThreads, 0, st>>>(data, labels, imgs, item_img, n_items, crc, cnt);
+  k_sample_scan<<<grid, kSmThreads, 0, st>>>(data, labels, imgs, item_img, lay.n_items, lay.n_crc_items,
+                                             reinterpret_cast<const uint32_t *>(dev_desc + lay.shifts), crc, cnt,
+                                             err + 2);
   PD_CUDA(cudaGetLastError());
   PD_CUDA(cudaEventRecord(ctx->ev[1], st));
   if (s->kind == PD_SAMPLER_UNIFORM) {
@@ -605,36 +673,44 @@ struct ImagePlace {
   uint32_t n_pix;
 };
 
-int fill_desc(pd_ctx *ctx, const SamplerPlan &pl, const std::vector<ImagePlace> &place, uint32_t *n_items_out,
-              DescLayout *lay_out) {
+int fill_desc(pd_ctx *ctx, const SamplerPlan &pl, const std::vector<ImagePlace> &place, DescLayout *lay_out) {
   const uint32_t n = (uint32_t)place.size();
-  uint64_t items = 0;
-  std::vector<uint32_t> slices(n), per(n);
+  uint64_t n_crc = 0, n_lab = 0;
+  std::vector<uint32_t> slices(n), chunks(n);
   for (uint32_t i = 0; i < n; i++) {
-    per[i] = scan_items(place[i].data_end - place[i].data_lo, (place[i].n_pix + 15) / 16, &slices[i]);
-    items += per[i];
+    slices[i] = (uint32_t)((place[i].data_end - place[i].data_lo + kSliceBytes - 1) / kSliceBytes);
+    chunks[i] = ((place[i].n_pix + 15) / 16 + kLabVecsPerItem - 1) / kLabVecsPerItem;
+    n_crc += slices[i];
+    n_lab += chunks[i];
   }
-  PD_CHECK(items < (1ull << 32), PD_ERR_UNSUPPORTED, "batch too large");
-  const DescLayout lay(n, (uint32_t)items, (uint32_t)pl.bucket.size());
+  PD_CHECK(n_crc + n_lab < (1ull << 31), PD_ERR_UNSUPPORTED, "batch too large");
+  DescLayout lay(n, (uint32_t)(n_crc + n_lab), (uint32_t)pl.bucket.size());
+  lay.n_crc_items = (uint32_t)n_crc;
   PD_TRY(ctx->h_sm_desc.ensure(lay.bytes));
   uint8_t *h = ctx->h_sm_desc.as<uint8_t>();
   SampImage *im = reinterpret_cast<SampImage *>(h + lay.imgs);
   uint32_t *item_img = reinterpret_cast<uint32_t *>(h + lay.items);
   uint32_t *crc = reinterpret_cast<uint32_t *>(h + lay.crc);
   uint32_t *cnt = reinterpret_cast<uint32_t *>(h + lay.count);
-  uint32_t it = 0;
+  uint32_t ic = 0, il = (uint32_t)n_crc;
   for (uint32_t i = 0; i < n; i++) {
     const ImagePlace &p = place[i];
-    im[i] = SampImage{p.data_lo, p.data_end, p.lab_off, p.out_off, p.n_pix, (p.n_pix + 15) / 16, slices[i], it};
-    for (uint32_t k = 0; k < per[i]; k++) item_img[it++] = i;
+    im[i] = SampImage{p.data_lo, p.data_end, p.lab_off, p.out_off, p.n_pix, (p.n_pix + 15) / 16, slices[i], ic, il, 0};
+    for (uint32_t k = 0; k < slices[i]; k++) item_img[ic++] = i;
+    for (uint32_t k = 0; k < chunks[i]; k++) item_img[il++] = i;
     // the initial value 0xFFFFFFFF carried past the image bytes, and the final XOR
-    crc[i] = gf_mul(0xFFFFFFFFu, gf_x8n(p.data_bytes)) ^ 0xFFFFFFFFu;
+    // (images of a batch mostly share their size)
+    if (i == 0 || p.data_bytes != place[i - 1].data_bytes)
+      crc[i] = gf_mul(0xFFFFFFFFu, gf_x8n(p.data_bytes)) ^ 0xFFFFFFFFu;
+    else
+      crc[i] = crc[i - 1];
     cnt[i] = 0;
   }
+  std::memcpy(h + lay.shifts, shift_constants(), 4ull * kShiftWords);
   reinterpret_cast<uint32_t *>(h + lay.err)[0] = kNoError;  // first image with a label above nClasses
   reinterpret_cast<uint32_t *>(h + lay.err)[1] = kNoError;  // first image whose draws hit the block limit
+  reinterpret_cast<uint32_t *>(h + lay.err)[2] = 0;         // next work item of the scan
   if (!pl.bucket.empty()) std::memcpy(h + lay.bucket, pl.bucket.data(), pl.bucket.size() * 4);
-  *n_items_out = (uint32_t)items;
   *lay_out = lay;
   return PD_OK;
 }
@@ -699,7 +775,9 @@ extern "C" int pd_sample(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, co
                "image %u is %ux%u (1 to 2^31-1 pixels)", last, widths[last], heights[last]);
       const uint64_t db = np * s->pixel_bytes;
       PD_CHECK(db < (1ull << 40), PD_ERR_UNSUPPORTED, "image %u too large", last);
-      const uint64_t pad = (16 - db % 16) % 16;
+      // zeros before the bytes so that the image ends on a 256-byte block (the
+      // checksum reads 256-byte blocks counted from the end)
+      const uint64_t pad = (256 - db % 256) % 256;
       const uint64_t dsz = pad + db, lsz = (np + 15) / 16 * 16;
       if (last > first && data_cur + dsz + lab_cur + lsz > kGroupBytes) break;
       place.push_back(ImagePlace{data_cur, data_cur + dsz, lab_cur, (uint64_t)(last - first) * stride, db, (uint32_t)np});
@@ -727,16 +805,15 @@ extern "C" int pd_sample(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, co
       work(0);
       for (auto &x : th) x.join();
     }
-    uint32_t n_items = 0;
     DescLayout lay;
-    PD_TRY(fill_desc(ctx, pl, place, &n_items, &lay));
+    PD_TRY(fill_desc(ctx, pl, place, &lay));
     PD_TRY(ctx->sm_data.ensure(data_cur + lab_cur + 16));
     PD_TRY(ctx->sm_desc.ensure(lay.bytes));
     PD_TRY(ctx->sm_out.ensure(((uint64_t)n * stride + n) * 4 + 16));
     uint8_t *dd = ctx->sm_data.as<uint8_t>(), *dl = dd + data_cur;
     PD_CUDA(h2d(ctx, dd, hd, data_cur + lab_cur));
     uint32_t *dout = ctx->sm_out.as<uint32_t>(), *dcnt = dout + (uint64_t)n * stride;
-    PD_TRY(launch_batch(ctx, s, pl, n, n_items, dd, dl, dout, dcnt, lay, ctx->sm_desc.as<uint8_t>()));
+    PD_TRY(launch_batch(ctx, s, pl, n, dd, dl, dout, dcnt, lay, ctx->sm_desc.as<uint8_t>()));
     uint32_t err[2];
     PD_CUDA(d2h(ctx, samples + (uint64_t)first * stride, dout, (uint64_t)n * stride * 4));
     PD_CUDA(d2h(ctx, counts + first, dcnt, (uint64_t)n * 4));
@@ -782,11 +859,10 @@ extern "C" int pd_sample_device(pd_ctx *ctx, const pd_sampler *s, uint32_t n_ima
   std::vector<ImagePlace> place(n_images);
   for (uint32_t i = 0; i < n_images; i++)
     place[i] = ImagePlace{i * db, (i + 1) * db, i * np, (uint64_t)i * stride, db, (uint32_t)np};
-  uint32_t n_items = 0;
   DescLayout lay;
-  PD_TRY(fill_desc(ctx, pl, place, &n_items, &lay));
+  PD_TRY(fill_desc(ctx, pl, place, &lay));
   PD_TRY(ctx->sm_desc.ensure(lay.bytes));
-  PD_TRY(launch_batch(ctx, s, pl, n_images, n_items, static_cast<const uint8_t *>(images_device), labels_device,
+  PD_TRY(launch_batch(ctx, s, pl, n_images, static_cast<const uint8_t *>(images_device), labels_device,
                       samples_device, counts_device, lay, ctx->sm_desc.as<uint8_t>()));
   uint32_t err[2];
   PD_CUDA(d2h(ctx, err, ctx->sm_desc.as<uint8_t>() + lay.err, 8));
