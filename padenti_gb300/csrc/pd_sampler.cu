@@ -191,7 +191,12 @@ PD_D uint64_t round_sig(uint64_t x, int bits) {
 // in integers: the exact product v*c rounded to double's 53 bits, then to
 // float's 24, then halves away from zero (classweighted_image_sampler_impl.hpp:91).
 PD_D uint32_t reservoir_slot(uint32_t v, uint32_t c) {
-  const uint64_t r = round_sig(round_sig((uint64_t)v * c, 53), 24);
+  const uint64_t p = (uint64_t)v * c;
+  if (p < (1ull << 53)) {
+    // the double product is exact: one rounding to float, then an exact scaling
+    return (uint32_t)roundf(__fmul_rn(__ull2float_rn(p), 0x1p-32f));
+  }
+  const uint64_t r = round_sig(round_sig(p, 53), 24);
   return (uint32_t)((r + 0x80000000ull) >> 32);
 }
 
@@ -331,6 +336,13 @@ __global__ void __launch_bounds__(kSmThreads, 4) k_sample_scan(const uint8_t *__
   }
 }
 
+constexpr uint32_t kWalkVecs = 4;  // label vectors (64 pixels) per thread per step of the rank walk
+
+PD_D void walk_load(uint4 (&x)[kWalkVecs], const uint4 *L, uint32_t v, uint32_t n_vecs) {
+#pragma unroll
+  for (uint32_t i = 0; i < kWalkVecs; i++) x[i] = v + i < n_vecs ? __ldg(L + v + i) : make_uint4(0, 0, 0, 0);
+}
+
 // UniformImageSampler::sample, one CTA per image.  Dynamic shared memory:
 // sort_n words (a power of two >= n_samples).
 __global__ void __launch_bounds__(kSmThreads) k_sample_uniform(const uint8_t *__restrict__ labels,
@@ -390,27 +402,50 @@ __global__ void __launch_bounds__(kSmThreads) k_sample_uniform(const uint8_t *__
   for (uint32_t i = n_samples + t; i < sort_n; i += kSmThreads) keys[i] = 0xFFFFFFFFu;
   __syncthreads();
   bitonic_sort(keys, sort_n);
-  // ranks among the labelled pixels -> pixel indices, in one pass over the labels
+  // ranks among the labelled pixels -> pixel indices, in one pass over the
+  // labels: kWalkVecs label vectors per thread per step, the next step's loaded
+  // ahead
   const uint4 *L = reinterpret_cast<const uint4 *>(labels + g.lab_off);
   const uint32_t last = keys[n_samples - 1];
   uint32_t *o = out + g.out_off;
   uint32_t run = 0;
-  for (uint32_t v0 = 0; v0 < g.lab_vecs && run <= last; v0 += kSmThreads) {
-    const uint32_t vi = v0 + t;
-    const uint4 x = vi < g.lab_vecs ? __ldg(L + vi) : make_uint4(0, 0, 0, 0);
-    const uint32_t c = nonzero_bytes(x);
+  uint4 xa[kWalkVecs], xb[kWalkVecs];
+  walk_load(xa, L, t * kWalkVecs, g.lab_vecs);
+  for (uint32_t v0 = 0; v0 < g.lab_vecs && run <= last; v0 += kSmThreads * kWalkVecs) {
+    walk_load(xb, L, v0 + kSmThreads * kWalkVecs + t * kWalkVecs, g.lab_vecs);
+    uint32_t c[kWalkVecs], ct = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < kWalkVecs; i++) {
+      c[i] = nonzero_bytes(xa[i]);
+      ct += c[i];
+    }
     uint32_t total;
-    const uint32_t base = run + block_scan(c, wtot, &total);
-    if (c) {
+    const uint32_t base = run + block_scan(ct, wtot, &total);
+    if (ct) {
       uint32_t lo = 0, hi = n_samples;
       while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
         if (keys[mid] < base) lo = mid + 1;
         else hi = mid;
       }
-      for (uint32_t i = lo; i < n_samples && keys[i] < base + c; i++) o[i] = vi * 16 + nth_nonzero(x, keys[i] - base);
+      for (uint32_t i = lo; i < n_samples && keys[i] < base + ct; i++) {
+        uint32_t r = keys[i] - base, k = 0;
+#pragma unroll
+        for (uint32_t j = 0; j + 1 < kWalkVecs; j++)
+          if (k == j && r >= c[j]) {
+            r -= c[j];
+            k = j + 1;
+          }
+        uint4 x = xa[0];
+#pragma unroll
+        for (uint32_t j = 1; j < kWalkVecs; j++)
+          if (k == j) x = xa[j];
+        o[i] = (v0 + t * kWalkVecs + k) * 16 + nth_nonzero(x, r);
+      }
     }
     run += total;
+#pragma unroll
+    for (uint32_t i = 0; i < kWalkVecs; i++) xa[i] = xb[i];
   }
   if (t == 0) out_count[im] = n_samples;
 }
@@ -451,13 +486,20 @@ __global__ void __launch_bounds__(kSmThreads) k_sample_class_weighted(
   __syncthreads();
   const uint8_t *lab = labels + g.lab_off;
   uint32_t gen = 0, d_base = 0;
+  uint32_t nxt[4];  // the labels of the next step, loaded ahead
+#pragma unroll
+  for (uint32_t j = 0; j < 4; j++) {
+    const uint32_t p = warp * 128 + j * 32 + lane;
+    nxt[j] = p < g.n_pix ? lab[p] : 0u;
+  }
   for (uint32_t win = 0; win < g.n_pix; win += kWindow) {
     uint32_t cls[4], rank[4];
     bool valid[4];
 #pragma unroll
     for (uint32_t j = 0; j < 4; j++) {
-      const uint32_t p = win + warp * 128 + j * 32 + lane;
-      cls[j] = p < g.n_pix ? lab[p] : 0u;
+      cls[j] = nxt[j];
+      const uint32_t p = win + kWindow + warp * 128 + j * 32 + lane;
+      nxt[j] = p < g.n_pix ? lab[p] : 0u;
     }
 #pragma unroll
     for (uint32_t j = 0; j < 4; j++) {

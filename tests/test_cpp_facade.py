@@ -95,3 +95,30 @@ def test_cpp_facade_with_a_user_feature_matches_the_builtin(tmp_path):
         assert r.returncode == 0, r.stderr + r.stdout
         out[tag] = (xml.read_text(), post.read_bytes())
     assert out["user"] == out["builtin"]
+
+
+def test_cpp_sampler_facade_compiles(tmp_path):
+    _compile(CPP / "facade_sample.cpp", tmp_path / "facade_sample", link=True)
+
+
+@pytest.mark.gpu
+def test_cpp_sampler_facade_matches_the_oracle(tmp_path):
+    """CUDAUniformImageSampler / CUDAClassWeightedImageSampler (sample(), sampleBatch() and
+    sampledTrainingSet) return the oracle's samples."""
+    import oracle_bind as ob
+
+    exe = tmp_path / "facade_sample"
+    _compile(CPP / "facade_sample.cpp", exe, link=True)
+    r = subprocess.run([str(exe), str(tmp_path / "s.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + r.stdout
+    got = np.fromfile(tmp_path / "s.bin", np.uint32)
+    px, lb, _ = pg.synth_depth(4, 4, 160, 120, min_ellipses=1, max_ellipses=3, parts=0, samples_per_image=1)
+    w = np.array([0.5, 0.25, 0.3], np.float32)
+    want = [ob.sample_uniform(px[i], lb[i], 500, 3) for i in range(4)]
+    want += [ob.sample_class_weighted(px[i], lb[i], 400, 3, w, 7) for i in range(4)] * 2
+    pos = 0
+    for wv in want:
+        n = int(got[pos])
+        assert np.array_equal(got[pos + 1:pos + 1 + n], wv)
+        pos += 1 + n
+    assert pos == got.size
