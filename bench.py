@@ -246,6 +246,67 @@ def sampler_bench(a, pg, N, px, lb):
     return out
 
 
+def loader_bench(a, pg, N):
+    """The colour-to-class step of the label loader over 500 RGB label images of the training
+    size: device-resident (CUDA-event kernel time), from host buffers (wall clock), and the
+    oracle on all host cores."""
+    import concurrent.futures as cf
+
+    import torch
+
+    n, H, W = 500, a.height, a.width
+    colours = np.array([[255, 0, 0], [0, 0, 255], [0, 255, 0], [255, 255, 0], [0, 255, 255], [255, 0, 255],
+                        [128, 0, 0], [0, 128, 0], [0, 0, 128]], np.uint8)
+    _, lb, _ = pg.synth_depth(a.seed, n, W, H, first_image=3_000_000, parts=1, min_ellipses=2, max_ellipses=5,
+                              samples_per_image=1)
+    rgb = colours[np.maximum(lb.astype(np.int64) - 1, 0)]
+    h = pg._sampler_ctx(torch.cuda.current_device())
+    src = torch.from_numpy(rgb.reshape(-1)).cuda()
+    dst = torch.empty(n * H * W, dtype=torch.uint8, device="cuda")
+    cmap = np.ascontiguousarray(colours.reshape(-1))
+    ms = C.c_float()
+
+    def dstep():
+        N.check(N.lib().pd_rgb_to_labels_device(h, n * H * W, src.data_ptr(), 3, cmap.ctypes.data, len(colours),
+                                                dst.data_ptr(), C.byref(ms)))
+
+    torch.cuda.synchronize()
+    for _ in range(3):
+        dstep()
+    kms = []
+    for _ in range(5):
+        dstep()
+        kms.append(ms.value)
+    k_ms = float(np.median(kms))
+    peak, _ = measured_peaks()
+    nbytes = n * H * W * 4  # 3 bytes in, 1 out per pixel
+    loader = pg.RGBLabelsLoader(colours)
+    imgs = [rgb[i] for i in range(n)]
+    loader.convert_batch(imgs)
+    t0 = time.perf_counter()
+    loader.convert_batch(imgs)
+    e_ms = (time.perf_counter() - t0) * 1000
+    out = dict(metric="label images Mpix/s", value=n * H * W / (k_ms / 1000) / 1e6, unit="Mpix/s", images=n,
+               ms_kernel=k_ms,
+               roofline=dict(kernel="k_rgb_to_labels", bound="hbm", achieved=nbytes / (k_ms / 1000) / 1e9, peak=peak,
+                             unit="GB/s", frac=nbytes / (k_ms / 1000) / 1e9 / peak, algorithmic_bytes=nbytes),
+               e2e=dict(value=n * H * W / (e_ms / 1000) / 1e6, unit="Mpix/s", ms=e_ms))
+    del src, dst
+    if not a.no_cpu:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_bind as ob
+
+        m = n
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+            list(ex.map(lambda i: ob.rgb_to_labels(rgb[i], colours), range(m)))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = dict(value=m * H * W / dt / 1e6, unit="Mpix/s", cores=os.cpu_count() or 1, kind="port",
+                                   sample=f"{m} images, the oracle restatement of _rgb2label (per-pixel colour "
+                                          f"search) on all host cores; {dt:.1f} s")
+    return out
+
+
 def run_reference(a):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -467,6 +528,8 @@ def run_ours(a):
                                         "CUDA-graph replay of the batch kernel, posteriors out; wall clock")
 
     samp = sampler_bench(a, pg, N, px, lb) if a.sampler_images > 0 else None
+    if samp is not None:
+        samp["label_images"] = loader_bench(a, pg, N)
 
     if rank != 0:
         return

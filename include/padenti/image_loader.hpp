@@ -1,0 +1,160 @@
+// ImageLoader and the label loader, the reference's image loaders
+// (image_loader.hpp:35-59, cv_image_loader.hpp:28-52) without OpenCV: images are
+// binary netpbm files (PGM: 8- or 16-bit grey, PPM: 8-bit RGB) in place of the
+// PNG files cv::imread reads, and the colour-to-class step of
+// CVRGBLabelsLoader (_rgb2label, cv_image_loader_impl.hpp:233-266) runs on the
+// GPU (pd_rgb_to_labels).  loadTrainingSet() is the TrainingSet constructor over
+// a directory (training_set_impl.hpp:40-112).  Errors throw std::runtime_error.
+#ifndef PADENTI_GB300_IMAGE_LOADER_HPP
+#define PADENTI_GB300_IMAGE_LOADER_HPP
+
+#include <padenti/image_sampler.hpp>
+#include <padenti/training_set.hpp>
+#include <padenti_gb300.h>
+
+#include <algorithm>
+#include <cctype>
+#include <filesystem>
+#include <fstream>
+#include <iterator>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+template <typename type, unsigned int nChannels>
+class ImageLoader {
+ public:
+  virtual ~ImageLoader() {}
+  virtual void load(const std::string &imagePath, type *data, unsigned int *width, unsigned int *height) = 0;
+  virtual Image<type, nChannels> load(const std::string &imagePath) = 0;
+};
+
+namespace padenti_gb300 {
+
+// A binary netpbm file: its size, channel count (1 for P5, 3 for P6), bytes per
+// sample (1, or 2 stored big-endian) and samples.
+struct Pnm {
+  unsigned int width = 0, height = 0, channels = 0, bytes = 0;
+  std::vector<unsigned char> raw;
+};
+
+inline Pnm read_pnm(const std::string &path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw std::runtime_error("padenti_gb300: cannot read " + path);
+  std::string magic;
+  f >> magic;
+  unsigned long v[3];
+  for (unsigned long &x : v) {
+    while (f >> std::ws && f.peek() == '#') f.ignore(1 << 20, '\n');
+    f >> x;
+  }
+  f.get();
+  if ((magic != "P5" && magic != "P6") || !f) throw std::runtime_error("padenti_gb300: " + path + " is not a binary PGM/PPM");
+  Pnm p;
+  p.width = (unsigned int)v[0];
+  p.height = (unsigned int)v[1];
+  p.channels = magic == "P5" ? 1 : 3;
+  p.bytes = v[2] < 256 ? 1 : 2;
+  p.raw.resize((size_t)p.width * p.height * p.channels * p.bytes);
+  f.read(reinterpret_cast<char *>(p.raw.data()), (std::streamsize)p.raw.size());
+  if (!f) throw std::runtime_error("padenti_gb300: " + path + " is truncated");
+  return p;
+}
+
+}  // namespace padenti_gb300
+
+// CVImageLoader (cv_image_loader_impl.hpp:37-73) for PGM/PPM files.
+template <typename type, unsigned int nChannels>
+class PNMImageLoader : public ImageLoader<type, nChannels> {
+ public:
+  void load(const std::string &imagePath, type *data, unsigned int *width, unsigned int *height) override {
+    const padenti_gb300::Pnm p = padenti_gb300::read_pnm(imagePath);
+    if (p.channels != nChannels || p.bytes != sizeof(type)) throw "Image type different from expected one";
+    *width = p.width;
+    *height = p.height;
+    const size_t n = (size_t)p.width * p.height * nChannels;
+    for (size_t i = 0; i < n; i++)
+      data[i] = p.bytes == 1 ? (type)p.raw[i] : (type)((p.raw[2 * i] << 8) | p.raw[2 * i + 1]);
+  }
+  Image<type, nChannels> load(const std::string &imagePath) override {
+    const padenti_gb300::Pnm p = padenti_gb300::read_pnm(imagePath);
+    Image<type, nChannels> img(p.width, p.height);
+    unsigned int w, h;
+    load(imagePath, img.getData(), &w, &h);
+    return img;
+  }
+};
+
+// CVRGBLabelsLoader (cv_image_loader.hpp:37-52) for PPM label images; the
+// colour-to-class mapping runs on the GPU.
+class CUDARGBLabelsLoader : public ImageLoader<unsigned char, 1> {
+  std::vector<unsigned char> m_map;
+  pd_ctx *m_ctx = nullptr;
+
+  static void check(int rc) {
+    if (rc != PD_OK) throw std::runtime_error(std::string("padenti_gb300: ") + pd_last_error());
+  }
+
+ public:
+  CUDARGBLabelsLoader(const unsigned char (*rgb2labelMap)[3], unsigned int nClasses, int device = 0)
+      : m_map(&rgb2labelMap[0][0], &rgb2labelMap[0][0] + 3 * nClasses) {
+    const pd_config cfg{PD_PLUGIN_DEPTH_DIFF2, PD_IMG_U16, 1, PD_FEAT_I32, 4, 2};  // any valid configuration
+    check(pd_ctx_create(&cfg, device, &m_ctx));
+  }
+  CUDARGBLabelsLoader(const CUDARGBLabelsLoader &) = delete;
+  CUDARGBLabelsLoader &operator=(const CUDARGBLabelsLoader &) = delete;
+  ~CUDARGBLabelsLoader() override { pd_ctx_destroy(m_ctx); }
+
+  // labels of an RGB (channels 3) or RGBA (4) image in memory
+  void convert(const unsigned char *rgb, unsigned int width, unsigned int height, unsigned int channels,
+               unsigned char *labels) const {
+    uint8_t *out[1] = {labels};
+    const uint8_t *in[1] = {rgb};
+    check(pd_rgb_to_labels(m_ctx, 1, in, &width, &height, channels, m_map.data(), (uint32_t)(m_map.size() / 3), out));
+  }
+  void load(const std::string &imagePath, unsigned char *data, unsigned int *width, unsigned int *height) override {
+    const padenti_gb300::Pnm p = padenti_gb300::read_pnm(imagePath);
+    if (p.channels != 3 || p.bytes != 1) throw "Labels image type must be 8-bit RGB";
+    *width = p.width;
+    *height = p.height;
+    convert(p.raw.data(), p.width, p.height, 3, data);
+  }
+  Image<unsigned char, 1> load(const std::string &imagePath) override {
+    const padenti_gb300::Pnm p = padenti_gb300::read_pnm(imagePath);
+    Image<unsigned char, 1> img(p.width, p.height);
+    unsigned int w, h;
+    load(imagePath, img.getData(), &w, &h);
+    return img;
+  }
+};
+
+// TrainingSet(tsPath, dataSuffix, labelsSuffix, nClasses, dataLoader,
+// labelsLoader, sampler) (training_set_impl.hpp:40-112): files in name order
+// (the reference takes the directory's order), pairs of different sizes skipped.
+template <typename type, unsigned int nChannels>
+TrainingSet<type, nChannels> loadTrainingSet(const std::string &tsPath, const std::string &dataSuffix,
+                                             const std::string &labelsSuffix, unsigned int nClasses,
+                                             ImageLoader<type, nChannels> &dataLoader,
+                                             ImageLoader<unsigned char, 1> &labelsLoader,
+                                             const ImageSampler<type, nChannels> &sampler, unsigned int maxSamples) {
+  namespace fs = std::filesystem;
+  std::vector<std::string> names;
+  for (const auto &e : fs::directory_iterator(tsPath)) {
+    const std::string n = e.path().filename().string();
+    if (!e.is_directory() && n.size() >= dataSuffix.size() &&
+        n.compare(n.size() - dataSuffix.size(), dataSuffix.size(), dataSuffix) == 0)
+      names.push_back(n);
+  }
+  std::sort(names.begin(), names.end());
+  std::vector<Image<type, nChannels>> images;
+  std::vector<Image<unsigned char, 1>> labels;
+  for (const std::string &n : names) {
+    const std::string lp = tsPath + "/" + n.substr(0, n.size() - dataSuffix.size()) + labelsSuffix;
+    if (!fs::exists(lp)) continue;
+    images.push_back(dataLoader.load(tsPath + "/" + n));
+    labels.push_back(labelsLoader.load(lp));
+  }
+  return sampledTrainingSet(nClasses, images, labels, sampler, maxSamples);
+}
+
+#endif

@@ -310,6 +310,21 @@ int pd_sample_device(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, const 
                      uint32_t *samples_device, uint32_t *counts_device);
 int pd_sample_get_stats(pd_ctx *ctx, pd_sample_stats *out);
 
+/* Label images (CVRGBLabelsLoader, cv_image_loader.hpp:37-52) ------------------ */
+/* The colour-to-class step of CVRGBLabelsLoader::load (_rgb2label,
+ * cv_image_loader_impl.hpp:233-266) for a batch of host label images:
+ * images[i] holds widths[i] x heights[i] pixels of `channels` bytes (3: R, G, B;
+ * 4: R, G, B, A -- the reference converts OpenCV's BGR(A) to RGB(A) first),
+ * map[3k..3k+2] is the colour of class k (k < n_classes <= 255).  out[i] gets,
+ * per pixel, 1 + the first class with the pixel's colour, or 0 (unlabelled). */
+int pd_rgb_to_labels(pd_ctx *ctx, uint32_t n_images, const uint8_t *const *images, const uint32_t *widths,
+                     const uint32_t *heights, uint32_t channels, const uint8_t *map, uint32_t n_classes,
+                     uint8_t *const *out);
+/* The same over n_pixels pixels already in device memory (16-byte aligned
+ * buffers); *ms (may be NULL) gets the kernel's CUDA-event time. */
+int pd_rgb_to_labels_device(pd_ctx *ctx, uint64_t n_pixels, const uint8_t *src_device, uint32_t channels,
+                            const uint8_t *map, uint32_t n_classes, uint8_t *dst_device, float *ms);
+
 /* Synthetic data (seeded, bit-identical on every host) ------------------------ */
 /* Depth maps: background plane U(3000,4000) mm + N(0,5^2) noise, ellipses at
  * U(800,2500) mm.  parts=0: 3 classes (bg, left half, right half of each

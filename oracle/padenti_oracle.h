@@ -155,6 +155,10 @@ void or_sample_batch(int kind, const void *images, uint64_t data_bytes, const ui
                      uint32_t n_images, uint32_t n_samples, uint32_t n_classes, const uint32_t *sizes,
                      uint32_t seed, uint32_t stride, uint32_t *out, int64_t *counts);
 
+/* Label images (image_loader.c): _rgb2label. */
+void or_rgb_to_labels(const uint8_t *src, uint64_t n_pix, uint32_t channels, const uint8_t *map, uint32_t n_classes,
+                      uint8_t *dst);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,6 +24,7 @@ __all__ = [
     "ForestConfig", "TreeTrainerParameters", "TrainingSetImage", "TrainingSet", "Tree", "TreeTrainer",
     "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS", "USER_SHAPES", "check_plugin",
     "ImageSampler", "UniformImageSampler", "ClassWeightedImageSampler", "sampled_training_set",
+    "read_pnm", "write_pnm", "PNMImageLoader", "RGBLabelsLoader", "load_training_set",
 ]
 
 FEAT_DTYPE = {N.PD_FEAT_I16: np.int16, N.PD_FEAT_I32: np.int32}
@@ -536,6 +537,114 @@ def sampled_training_set(n_classes: int, images: list, labels: list, sampler: Im
     samples = sampler.sample_batch([images[i] for i in keep], [labels[i] for i in keep])
     return TrainingSet(n_classes, [TrainingSetImage(images[i], labels[i], n_classes, sm)
                                    for i, sm in zip(keep, samples)])
+
+
+def read_pnm(path) -> np.ndarray:
+    """A binary netpbm image: P5 (grey) as [H][W], P6 (RGB) as [H][W][3]; maxval < 256 gives
+    uint8, else uint16 (stored big-endian, as the format says).  Stands in for the reference's
+    OpenCV loaders (cv::imread), which are absent here."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    fields, pos = [], 0
+    while len(fields) < 4:
+        while raw[pos:pos + 1].isspace():
+            pos += 1
+        if raw[pos:pos + 1] == b"#":
+            pos = raw.index(b"\n", pos) + 1
+            continue
+        end = pos
+        while not raw[end:end + 1].isspace():
+            end += 1
+        fields.append(raw[pos:end])
+        pos = end
+    pos += 1  # the single whitespace byte before the pixels
+    magic, w, h, maxval = fields[0], int(fields[1]), int(fields[2]), int(fields[3])
+    if magic not in (b"P5", b"P6"):
+        raise ValueError(f"{path}: not a binary PGM/PPM file")
+    ch = 1 if magic == b"P5" else 3
+    dt = np.dtype(np.uint8) if maxval < 256 else np.dtype(">u2")
+    a = np.frombuffer(raw, dt, count=w * h * ch, offset=pos).astype(dt.newbyteorder("="))
+    return a.reshape((h, w) if ch == 1 else (h, w, 3))
+
+
+def write_pnm(path, image: np.ndarray) -> None:
+    """Writes [H][W] (P5) or [H][W][3] (P6) uint8/uint16 as binary netpbm."""
+    a = np.asarray(image)
+    magic = b"P5" if a.ndim == 2 else b"P6"
+    maxval = 255 if a.dtype == np.uint8 else 65535
+    with open(path, "wb") as f:
+        f.write(magic + b"\n%d %d\n%d\n" % (a.shape[1], a.shape[0], maxval))
+        f.write(np.ascontiguousarray(a.astype(">u2") if maxval > 255 else a).tobytes())
+
+
+class PNMImageLoader:
+    """CVImageLoader (cv_image_loader_impl.hpp:37-73) for binary PGM/PPM files: ``load(path)``
+    returns the image; its dtype and channel count must be the expected ones."""
+
+    def __init__(self, dtype=np.uint16, n_channels: int = 1):
+        self.dtype, self.n_channels = np.dtype(dtype), n_channels
+
+    def load(self, path) -> np.ndarray:
+        a = read_pnm(path)
+        if a.dtype != self.dtype or (a.shape[2] if a.ndim == 3 else 1) != self.n_channels:
+            raise ValueError(f"{path}: image type different from the expected one")
+        return a
+
+
+class RGBLabelsLoader:
+    """CVRGBLabelsLoader (cv_image_loader.hpp:37-52): label images whose colours name the
+    classes (``rgb2label[k]`` is the colour of class k).  ``convert`` maps an [H][W][3|4] RGB(A)
+    image to labels (class k -> k+1, unknown colours -> 0) on the GPU; ``load`` reads a PPM file
+    first."""
+
+    def __init__(self, rgb2label, device: int = 0):
+        self.map = np.ascontiguousarray(rgb2label, np.uint8).reshape(-1, 3)
+        if not 1 <= len(self.map) <= 255:
+            raise ValueError(f"{len(self.map)} colours (1 to 255 classes)")
+        self.device = device
+
+    def convert_batch(self, images: list) -> list:
+        imgs = [np.ascontiguousarray(a, np.uint8) for a in images]
+        if not imgs:
+            return []
+        ch = {a.shape[2] for a in imgs}
+        if len(ch) != 1 or not ch <= {3, 4}:
+            raise ValueError("label images of one batch need 3 or 4 channels, all the same")
+        outs = [np.zeros(a.shape[:2], np.uint8) for a in imgs]
+        n = len(imgs)
+        ip = (C.c_void_p * n)(*[a.ctypes.data for a in imgs])
+        op = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+        w = np.array([a.shape[1] for a in imgs], np.uint32)
+        h = np.array([a.shape[0] for a in imgs], np.uint32)
+        check(lib().pd_rgb_to_labels(_sampler_ctx(self.device), n, ip, _ptr(w), _ptr(h), ch.pop(), _ptr(self.map),
+                                     len(self.map), op))
+        return outs
+
+    def convert(self, image: np.ndarray) -> np.ndarray:
+        return self.convert_batch([image])[0]
+
+    def load(self, path) -> np.ndarray:
+        return self.convert(read_pnm(path))
+
+
+def load_training_set(path, data_suffix: str, labels_suffix: str, n_classes: int, data_loader: PNMImageLoader,
+                      labels_loader: RGBLabelsLoader, sampler: ImageSampler) -> TrainingSet:
+    """TrainingSet(tsPath, dataSuffix, labelsSuffix, nClasses, dataLoader, labelsLoader, sampler)
+    (training_set_impl.hpp:40-112): every file ending in data_suffix with a labels file of the
+    same stem; pairs of different sizes are skipped.  Files are taken in name order (the
+    reference takes the directory's order).  Labels are converted and pixels sampled on the GPU,
+    one batch each."""
+    import os
+
+    names = sorted(n for n in os.listdir(path) if n.endswith(data_suffix) and os.path.isfile(os.path.join(path, n)))
+    datas, rgbs = [], []
+    for n in names:
+        lp = os.path.join(path, n[:len(n) - len(data_suffix)] + labels_suffix)
+        if os.path.exists(lp):
+            datas.append(data_loader.load(os.path.join(path, n)))
+            rgbs.append(read_pnm(lp))
+    labels = labels_loader.convert_batch(rgbs) if rgbs else []
+    return sampled_training_set(n_classes, datas, labels, sampler)
 
 
 def synth_depth(seed: int, n_images: int, width: int, height: int, *, first_image: int = 0, min_ellipses: int = 1,

@@ -136,6 +136,9 @@ _SIGS = {
     "pd_sample_device": (C.c_int, [_P, C.POINTER(Sampler), C.c_uint32, _P, _P, C.c_uint32, C.c_uint32, C.c_uint32,
                                    _P, _P]),
     "pd_sample_get_stats": (C.c_int, [_P, C.POINTER(SampleStats)]),
+    "pd_rgb_to_labels": (C.c_int, [_P, C.c_uint32, _P, _P, _P, C.c_uint32, _P, C.c_uint32, _P]),
+    "pd_rgb_to_labels_device": (C.c_int, [_P, C.c_uint64, _P, C.c_uint32, _P, C.c_uint32, _P,
+                                          C.POINTER(C.c_float)]),
     "pd_synth_depth": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "pd_synth_rgb": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,

@@ -98,6 +98,10 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
   ctx->sm_out.release();
   ctx->h_sm.release();
   ctx->h_sm_desc.release();
+  ctx->lab_tab.release();
+  ctx->lab_src.release();
+  ctx->lab_dst.release();
+  ctx->h_lab.release();
   ctx->h_stage.release();
   ctx->h_items.release();
   for (auto &ev : ctx->ev)

@@ -86,6 +86,9 @@ struct pd_ctx {
   pd::DevBuf sm_out;             // samples and counts of a host batch
   pd::HostBuf h_sm, h_sm_desc;   // pinned staging of a host batch and of its descriptors
   pd_sample_stats sample_stats{};
+  // ---- label images (pd_rgb_to_labels*) ----
+  pd::DevBuf lab_tab, lab_src, lab_dst;
+  pd::HostBuf h_lab;
 
   cudaEvent_t ev[8] = {};
   uint64_t bytes_h2d = 0, bytes_d2h = 0, launches = 0;

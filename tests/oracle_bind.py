@@ -299,3 +299,13 @@ def ref_sample_class_weighted(img_type: int, data, labels, n_samples: int, n_cla
     r.ref_sample_class_weighted.restype = C.c_uint
     n = r.ref_sample_class_weighted(img_type, P(d), P(lb), w, h, n_samples, n_classes, P(wt), C.c_uint(seed), P(out))
     return out[:n]
+
+
+def rgb_to_labels(image, colours) -> np.ndarray:
+    """_rgb2label on an [H][W][3|4] uint8 image; colours [K][3]."""
+    img = np.ascontiguousarray(image, np.uint8)
+    cmap = np.ascontiguousarray(colours, np.uint8).reshape(-1)
+    out = np.zeros(img.shape[:2], np.uint8)
+    lib().or_rgb_to_labels(P(img), C.c_uint64(out.size), C.c_uint32(img.shape[2]), P(cmap),
+                           C.c_uint32(cmap.size // 3), P(out))
+    return out

@@ -1,0 +1,164 @@
+"""Label images and the directory constructor of TrainingSet: the colour-to-class step of
+CVRGBLabelsLoader (_rgb2label) on the GPU against the oracle, binary PGM/PPM files standing in
+for the OpenCV loaders, and TrainingSet(dir, …, loaders, sampler)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle_bind as ob
+import padenti_gb300 as pg
+from padenti_gb300 import _native as N
+
+
+def _numpy_rgb2label(img, colours):
+    """An independent restatement: the first matching colour wins."""
+    out = np.zeros(img.shape[:2], np.uint8)
+    done = np.zeros(img.shape[:2], bool)
+    for k, c in enumerate(np.asarray(colours, np.uint8)):
+        m = (img[..., 0] == c[0]) & (img[..., 1] == c[1]) & (img[..., 2] == c[2]) & ~done
+        out[m] = k + 1
+        done |= m
+    return out
+
+
+def _label_image(rng, h, w, colours, channels=3, unknown=0.1):
+    idx = rng.integers(0, len(colours), (h, w))
+    img = np.asarray(colours, np.uint8)[idx]
+    off = rng.random((h, w)) < unknown
+    img[off] = rng.integers(0, 256, (int(off.sum()), 3), dtype=np.uint8)
+    if channels == 4:
+        img = np.concatenate([img, rng.integers(0, 256, (h, w, 1), dtype=np.uint8)], axis=2)
+    return img
+
+
+COLOURS = [(255, 0, 0), (0, 0, 255), (0, 255, 0), (255, 0, 0), (10, 20, 30)]  # class 3 repeats class 0
+
+
+def test_oracle_rgb2label_matches_numpy_restatement():
+    rng = np.random.default_rng(0)
+    for ch in (3, 4):
+        img = _label_image(rng, 37, 53, COLOURS, ch)
+        got = ob.rgb_to_labels(img, COLOURS)
+        assert np.array_equal(got, _numpy_rgb2label(img, COLOURS))
+        assert set(np.unique(got)) <= {0, 1, 2, 3, 5}  # the repeated colour keeps its first class
+
+
+def test_pnm_round_trip_and_loader_types(tmp_path):
+    a = (np.arange(6 * 11, dtype=np.uint16) * 997).reshape(6, 11)
+    pg.write_pnm(tmp_path / "d.pgm", a)
+    raw = (tmp_path / "d.pgm").read_bytes()
+    (tmp_path / "c.pgm").write_bytes(raw.replace(b"P5\n", b"P5\n# a comment\n", 1))
+    assert np.array_equal(pg.read_pnm(tmp_path / "c.pgm"), a)
+    assert np.array_equal(pg.PNMImageLoader(np.uint16, 1).load(tmp_path / "d.pgm"), a)
+    with pytest.raises(ValueError, match="different from the expected"):
+        pg.PNMImageLoader(np.uint8, 3).load(tmp_path / "d.pgm")
+    rgb = np.random.default_rng(1).integers(0, 256, (4, 5, 3), dtype=np.uint8)
+    pg.write_pnm(tmp_path / "l.ppm", rgb)
+    assert np.array_equal(pg.read_pnm(tmp_path / "l.ppm"), rgb)
+
+
+def test_rgb_to_labels_rejects_bad_maps():
+    with pytest.raises(ValueError, match="1 to 255"):
+        pg.RGBLabelsLoader(np.zeros((0, 3), np.uint8))
+    with pytest.raises(ValueError):
+        pg.RGBLabelsLoader(COLOURS).convert_batch([np.zeros((4, 4, 2), np.uint8)])
+
+
+@pytest.mark.gpu
+def test_gpu_rgb_to_labels_matches_the_oracle():
+    rng = np.random.default_rng(2)
+    many = [tuple(int(x) for x in rng.integers(0, 256, 3)) for _ in range(250)] + [(7, 7, 7)] * 5
+    for colours in (COLOURS, many):
+        for ch in (3, 4):
+            imgs = [_label_image(rng, h, w, colours, ch) for (h, w) in [(37, 53), (1, 1), (120, 160), (3, 17)]]
+            got = pg.RGBLabelsLoader(colours).convert_batch(imgs)
+            for im, g in zip(imgs, got):
+                assert np.array_equal(g, ob.rgb_to_labels(im, colours))
+
+
+@pytest.mark.gpu
+def test_gpu_rgb_to_labels_device_entry():
+    import torch
+
+    rng = np.random.default_rng(3)
+    img = _label_image(rng, 480, 640, COLOURS, 3)
+    src = torch.from_numpy(img.reshape(-1)).cuda()
+    dst = torch.zeros(480 * 640, dtype=torch.uint8, device="cuda")
+    cmap = np.ascontiguousarray(COLOURS, np.uint8).reshape(-1)
+    ms = C.c_float()
+    torch.cuda.synchronize()
+    N.check(N.lib().pd_rgb_to_labels_device(pg._sampler_ctx(0), 480 * 640, src.data_ptr(), 3, cmap.ctypes.data,
+                                            len(COLOURS), dst.data_ptr(), C.byref(ms)))
+    assert np.array_equal(dst.cpu().numpy().reshape(480, 640), ob.rgb_to_labels(img, COLOURS))
+    assert ms.value > 0
+
+
+@pytest.mark.gpu
+def test_training_set_from_a_directory(tmp_path):
+    """load_training_set = TrainingSet(dir, "_depth.pgm", "_labels.ppm", K, loaders, sampler):
+    labels and samples are those of the oracle; a pair of different sizes is skipped."""
+    colours = [(255, 0, 0), (0, 0, 255), (0, 255, 0)]
+    px, lb, _ = pg.synth_depth(9, 5, 96, 72, parts=0, samples_per_image=4)
+    for i in range(5):
+        pg.write_pnm(tmp_path / f"img{i}_depth.pgm", px[i])
+        rgb = np.zeros(lb[i].shape + (3,), np.uint8)
+        for k in range(3):
+            rgb[lb[i] == k + 1] = colours[k]
+        if i == 3:
+            rgb = rgb[:-1]  # a labels image of another size: skipped
+        pg.write_pnm(tmp_path / f"img{i}_labels.ppm", rgb)
+    (tmp_path / "img9_depth.pgm").write_bytes((tmp_path / "img0_depth.pgm").read_bytes())  # no labels: ignored
+    sampler = pg.ClassWeightedImageSampler(300, 3, seed=11)
+    ts = pg.load_training_set(tmp_path, "_depth.pgm", "_labels.ppm", 3, pg.PNMImageLoader(np.uint16, 1),
+                              pg.RGBLabelsLoader(colours), sampler)
+    assert len(ts.images) == 4
+    for im, i in zip(ts.images, [0, 1, 2, 4]):
+        assert np.array_equal(im.data, px[i]) and np.array_equal(im.labels, lb[i])
+        assert np.array_equal(im.samples, ob.sample_class_weighted(px[i], lb[i], 300, 3, None, 11))
+
+
+def _write_set(tmp_path):
+    colours = [(255, 0, 0), (0, 0, 255), (0, 255, 0)]
+    px, lb, _ = pg.synth_depth(9, 5, 96, 72, parts=0, samples_per_image=4)
+    for i in range(5):
+        pg.write_pnm(tmp_path / f"img{i}_depth.pgm", px[i])
+        rgb = np.zeros(lb[i].shape + (3,), np.uint8)
+        for k in range(3):
+            rgb[lb[i] == k + 1] = colours[k]
+        if i == 3:
+            rgb = rgb[:-1]
+        pg.write_pnm(tmp_path / f"img{i}_labels.ppm", rgb)
+    return px, lb
+
+
+def test_cpp_loader_facade_compiles(tmp_path):
+    from test_cpp_facade import CPP, _compile
+
+    _compile(CPP / "facade_load.cpp", tmp_path / "facade_load", link=True)
+
+
+@pytest.mark.gpu
+def test_cpp_loader_facade_matches_python(tmp_path):
+    import subprocess
+
+    from test_cpp_facade import CPP, _compile
+
+    exe = tmp_path / "facade_load"
+    _compile(CPP / "facade_load.cpp", exe, link=True)
+    d = tmp_path / "set"
+    d.mkdir()
+    px, lb = _write_set(d)
+    r = subprocess.run([str(exe), str(d), str(tmp_path / "out.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr + r.stdout
+    got = np.fromfile(tmp_path / "out.bin", np.uint32)
+    pos = 0
+    for i in [0, 1, 2, 4]:
+        w, h = int(got[pos]), int(got[pos + 1])
+        assert (w, h) == (96, 72)
+        assert np.array_equal(got[pos + 2:pos + 2 + w * h].astype(np.uint8).reshape(h, w), lb[i])
+        pos += 2 + w * h
+        n = int(got[pos])
+        assert np.array_equal(got[pos + 1:pos + 1 + n], ob.sample_class_weighted(px[i], lb[i], 300, 3, None, 11))
+        pos += 1 + n
+    assert pos == got.size
