@@ -545,6 +545,20 @@ def run_ours(a):
                 evals_per_s_in_kernel=evals / hist_s if hist_s > 0 else None,
                 note="the histogram kernel is bound by instruction issue and the L1 data pipe (probe gathers, "
                      "threshold search), not by HBM")
+    # the histogram kernel's own bound: instruction issue (lane slots of warp instructions)
+    issue_roof = None
+    ip = ROOT / "profiles" / "k_hist_issue_300x640x480.json"
+    clk_sum = clk.summary()
+    if ip.exists() and hist_s > 0 and clk_sum.get("sm_mhz"):
+        ipe = json.loads(ip.read_text())["thread_instr_per_eval"]
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        ach = evals / hist_s * ipe
+        pk = sms * 4 * 32 * clk_sum["sm_mhz"] * 1e6
+        issue_roof = dict(bound="issue", kernel="k_hist", achieved=ach, peak=pk, unit="thread-instr/s", frac=ach / pk,
+                          thread_instr_per_eval=ipe,
+                          note="achieved = live evaluations/s x instruction slots per evaluation from "
+                               "profiles/k_hist_issue_300x640x480.json; peak = SMs x 4 schedulers x 32 lanes x the "
+                               "median SM clock sampled during the timed region")
     base = None
     if not a.no_cpu:
         base, _ = cpu_sample(a, cfg, ts, tp, a.cpu_seconds)
@@ -558,7 +572,7 @@ def run_ours(a):
                             cand_order=1 if a.cand_order is None else a.cand_order,
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
-                roofline=roof, cpu_baseline=base, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
+                roofline=roof, roofline_issue=issue_roof, cpu_baseline=base, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
                 predict=pred, sampler=samp, phases_per_step={k: v / a.steps for k, v in phases.items()}, impl="ours")
     print(json.dumps(line), flush=True)
 
