@@ -33,6 +33,51 @@ PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
   return node;
 }
 
+// The leaves of trees t0 .. t0+G-1 (those below n_trees) for one pixel, the G
+// walks interleaved level by level so that their loads overlap; each walk is
+// the one walk() does.
+template <class P, int G>
+PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ lc,
+                     const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+                     const TreeMeta *__restrict__ meta, uint32_t t0, uint32_t n_trees, int32_t *leaf_s,
+                     uint32_t tid) {
+  using FeatT = typename P::feat_t;
+  constexpr int D = P::kFeatDim;
+  int32_t node[G];
+  size_t off[G];
+  uint32_t depth[G];
+#pragma unroll
+  for (int g = 0; g < G; g++) {
+    node[g] = 0;
+    const bool have = t0 + g < n_trees;
+    off[g] = have ? meta[t0 + g].off : 0;
+    depth[g] = have ? meta[t0 + g].depth : 0;  // depth 0: no step
+  }
+  uint32_t live = 0;
+#pragma unroll
+  for (int g = 0; g < G; g++) live |= (depth[g] > 1 ? 1u : 0u) << g;
+  for (uint32_t d = 1; live; d++) {
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+      if (!((live >> g) & 1u)) continue;
+      const int32_t c = ldg(lc + off[g] + node[g]);
+      if (c < 0) {  // leaf (-1); an untrained root (-2) also stops
+        live &= ~(1u << g);
+        continue;
+      }
+      FeatT fv[D];
+#pragma unroll
+      for (int k = 0; k < D; k++) fv[k] = ldg(feat + (off[g] + (size_t)node[g]) * D + k);
+      const FeatT r = P::eval(prep, fv);
+      node[g] = c + (r <= ldg(thr + off[g] + node[g]) ? 0 : 1);
+      if (d + 1 >= depth[g]) live &= ~(1u << g);
+    }
+  }
+#pragma unroll
+  for (int g = 0; g < G; g++)
+    if (t0 + g < n_trees) leaf_s[(t0 + g) * kPredThreads + tid] = node[g];
+}
+
 // The forest posterior of pixel (x, y): the leaf of every tree (kept in the
 // CTA's leaf_s, [tree][thread]), then the leaf posteriors summed in tree order
 // and divided by the tree count, written planar with stride plane.
@@ -42,16 +87,12 @@ PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint3
                         const typename P::feat_t *__restrict__ thr, const float *__restrict__ post,
                         const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K, int32_t *leaf_s,
                         uint32_t tid) {
-  constexpr int D = P::kFeatDim;
   if (masked_out) {
     for (uint32_t l = 0; l < K; l++) o[l * plane] = 0.0f;
     return;
   }
   const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
-  for (uint32_t t = 0; t < n_trees; t++) {
-    const size_t off = meta[t].off;
-    leaf_s[t * kPredThreads + tid] = walk<P>(prep, lc + off, feat + off * D, thr + off, meta[t].depth);
-  }
+  for (uint32_t t = 0; t < n_trees; t += 4) walk_group<P, 4>(prep, lc, feat, thr, meta, t, n_trees, leaf_s, tid);
   const float nt = (float)n_trees;
   for (uint32_t l = 0; l < K; l++) {
     float acc = 0.0f;
