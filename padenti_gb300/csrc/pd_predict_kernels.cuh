@@ -13,6 +13,13 @@ struct TreeMeta {
 };
 
 constexpr int kPredX = 32, kPredY = 8, kPredThreads = kPredX * kPredY;
+// Tree walks interleaved per pixel.  On the 3-tree, depth-16 forest of 640x480
+// depth maps, 1 measures fastest (5.72e9 pixels/s; 2: 5.53e9, 3: 5.55e9, 4:
+// 5.19e9): the wider walks cost registers and occupancy.
+#ifndef PD_PRED_GROUP
+#define PD_PRED_GROUP 1
+#endif
+constexpr int kPredGroup = PD_PRED_GROUP;
 
 template <class P>
 PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
@@ -92,7 +99,8 @@ PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint3
     return;
   }
   const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
-  for (uint32_t t = 0; t < n_trees; t += 4) walk_group<P, 4>(prep, lc, feat, thr, meta, t, n_trees, leaf_s, tid);
+  for (uint32_t t = 0; t < n_trees; t += kPredGroup)
+    walk_group<P, kPredGroup>(prep, lc, feat, thr, meta, t, n_trees, leaf_s, tid);
   const float nt = (float)n_trees;
   for (uint32_t l = 0; l < K; l++) {
     float acc = 0.0f;
