@@ -84,7 +84,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
                     &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->cand_ord, &ctx->parent, &ctx->xlog2_tab, &ctx->split_par, &ctx->hist, &ctx->g32, &ctx->items,
                     &ctx->zero_slots, &ctx->split_out, &ctx->split_cl, &ctx->recheck, &ctx->split_scratch, &ctx->fused_scratch, &ctx->t_lc,
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
-                    &ctx->f_post, &ctx->f_meta, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
+                    &ctx->f_post, &ctx->f_meta, &ctx->f_cand, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
   for (DevBuf *b : bufs) b->release();
   if (ctx->batch_graph) cudaGraphExecDestroy(ctx->batch_graph);
   ctx->b_img.release();

@@ -130,7 +130,7 @@ struct DepthDiff2 {
     int32_t x, y;
     RoundDiv div;
   };
-  struct Cand {
+  struct __align__(16) Cand {  // one 16-byte-aligned record per tree node in prediction
     OffsetConst o[4];
   };
   static constexpr int kPreWords = 2;  // centre depth, its RoundDiv multiplier
@@ -211,7 +211,7 @@ struct DepthDiff1 {
     int16_t depth;
     RoundDiv div;
   };
-  struct Cand {
+  struct __align__(16) Cand {  // one 16-byte-aligned record per tree node in prediction
     OffsetConst o[2];
     int16_t f[2];
   };
@@ -285,7 +285,7 @@ struct ChannelDiff {
     uint32_t w, h;
     int32_t x, y;
   };
-  struct Cand {
+  struct __align__(16) Cand {  // one 16-byte-aligned record per tree node in prediction
     int32_t c1, c2, ux, uy, vx, vy;
   };
   static constexpr int kPreWords = 1;

@@ -46,6 +46,39 @@ static int upload_forest(pd_ctx *ctx) {
   return PD_OK;
 }
 
+// Bytes of one node's candidate record: P::Cand, or for a user feature the
+// UserPlugin::Cand compiled at run time (its feature values, 16-byte aligned).
+template <class P>
+static size_t cand_record(const pd_ctx *ctx) {
+  if (is_user_plugin(ctx)) return ((size_t)ctx->cfg.feat_dim * feat_size(ctx->cfg.feat_type) + 15) / 16 * 16;
+  return sizeof(typename P::Cand);
+}
+
+// The candidate record of every forest node (k_forest_cands), rebuilt when the
+// forest changes, so that a tree walk loads each node's constants.
+template <class P>
+static int ensure_forest_cands(pd_ctx *ctx) {
+  if (ctx->cand_version == ctx->forest_version) return PD_OK;
+  using FeatT = typename P::feat_t;
+  unsigned long long nodes = ctx->h_lc.size();
+  PD_TRY(ctx->f_cand.ensure(nodes * cand_record<P>(ctx) + 16));
+  const FeatT *ft = ctx->f_feat.as<FeatT>();
+  const dim3 grid((unsigned)((nodes + 255) / 256 + (nodes == 0)));
+  if (is_user_plugin(ctx)) {
+    const RtcKernels *rk = nullptr;
+    PD_TRY(rtc_kernels(ctx, &rk));
+    void *out = ctx->f_cand.ptr;
+    void *args[] = {&ft, &nodes, &out};
+    PD_TRY(rtc_launch(ctx, rk->forest_cands, grid, dim3(256), 0, args));
+  } else {
+    k_forest_cands<P><<<grid, 256, 0, ctx->stream>>>(ft, nodes, ctx->f_cand.as<typename P::Cand>());
+    PD_CUDA(cudaGetLastError());
+    ctx->launches++;
+  }
+  ctx->cand_version = ctx->forest_version;
+  return PD_OK;
+}
+
 template <class P>
 static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_t W, uint32_t H,
                             const uint8_t *masks, float *out) {
@@ -54,6 +87,7 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
   const size_t smem = (size_t)nt * kPredThreads * 4;
   dim3 grid((W + kPredX - 1) / kPredX, (H + kPredY - 1) / kPredY, n);
   const uint64_t img_bytes = (uint64_t)W * H * P::kChannels * sizeof(typename P::img_t);
+  PD_TRY(ensure_forest_cands<P>(ctx));
   if (is_user_plugin(ctx)) {
     const RtcKernels *rk = nullptr;
     PD_TRY(rtc_kernels(ctx, &rk));
@@ -62,18 +96,19 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
     uint64_t ib = img_bytes;
     uint32_t w_ = W, h_ = H, nt_ = nt, k_ = (uint32_t)ctx->cfg.n_classes;
     const int32_t *lc = ctx->f_lc.as<int32_t>();
-    const FeatT *ft = ctx->f_feat.as<FeatT>(), *th = ctx->f_thr.as<FeatT>();
+    const void *cd = ctx->f_cand.ptr;
+    const FeatT *th = ctx->f_thr.as<FeatT>();
     const float *po = ctx->f_post.as<float>();
     const TreeMeta *me = ctx->f_meta.as<TreeMeta>();
     const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
-    void *args[] = {&im, &ib, &w_, &h_, &masks, &out, &lc, &ft, &th, &po, &me, &nt_, &k_, &mg};
+    void *args[] = {&im, &ib, &w_, &h_, &masks, &out, &lc, &cd, &th, &po, &me, &nt_, &k_, &mg};
     return rtc_launch(ctx, rk->predict_posterior, grid, dim3(kPredX, kPredY), smem, args);
   }
   PD_CUDA(cudaFuncSetAttribute(k_predict_posterior<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_predict_posterior<P><<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
       static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_lc.as<int32_t>(),
-      ctx->f_feat.as<FeatT>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(), ctx->f_meta.as<TreeMeta>(), nt,
-      (uint32_t)ctx->cfg.n_classes, ctx->magic_tab.as<uint32_t>());
+      ctx->f_cand.as<typename P::Cand>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(),
+      ctx->f_meta.as<TreeMeta>(), nt, (uint32_t)ctx->cfg.n_classes, ctx->magic_tab.as<uint32_t>());
   PD_CUDA(cudaGetLastError());
   ctx->launches++;
   return PD_OK;
@@ -159,7 +194,7 @@ extern "C" int pd_predict_posterior(pd_ctx *ctx, const void *image, uint32_t wid
   return PD_OK;
 }
 
-// Config 3's serving form: a batch of images of mixed sizes in one launch of
+// A serving batch: images of mixed sizes in one launch of
 // k_predict_batch (one CTA per 32x8 tile of any image), captured in a CUDA graph
 // that is replayed while the batch layout (sizes, masks) and the forest stay the
 // same.  Inputs and outputs are the caller's host buffers, copied per image.
@@ -213,16 +248,19 @@ extern "C" int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *c
     const size_t smem = (size_t)nt * kPredThreads * 4;
     const int rc = dispatch_config(ctx->cfg, [&]<class P>() -> int {
       using FeatT = typename P::feat_t;
+      PD_TRY(ensure_forest_cands<P>(ctx));
+      PD_CUDA(cudaStreamSynchronize(st));
       const uint8_t *im = ctx->b_img.as<uint8_t>(), *mk = ctx->b_mask.as<uint8_t>();
       uint8_t *o = ctx->b_out.as<uint8_t>();
       const BatchImage *bd = ctx->b_desc.as<BatchImage>();
       uint32_t n_ = n, nt_ = nt, k_ = K;
       const int32_t *lc = ctx->f_lc.as<int32_t>();
-      const FeatT *ft = ctx->f_feat.as<FeatT>(), *th = ctx->f_thr.as<FeatT>();
+      const void *cd = ctx->f_cand.ptr;
+      const FeatT *th = ctx->f_thr.as<FeatT>();
       const float *po = ctx->f_post.as<float>();
       const TreeMeta *me = ctx->f_meta.as<TreeMeta>();
       const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
-      void *args[] = {&im, &mk, &o, &bd, &n_, &lc, &ft, &th, &po, &me, &nt_, &k_, &mg};
+      void *args[] = {&im, &mk, &o, &bd, &n_, &lc, &cd, &th, &po, &me, &nt_, &k_, &mg};
       const void *fn = (const void *)k_predict_batch<P>;
       if (is_user_plugin(ctx)) {
         const RtcKernels *rk = nullptr;
@@ -281,6 +319,7 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
   PD_TRY(dispatch_config(ctx->cfg, [&]<class P>() {
     using FeatT = typename P::feat_t;
     dim3 grid((width + kPredX - 1) / kPredX, (height + kPredY - 1) / kPredY, 1);
+    PD_TRY(ensure_forest_cands<P>(ctx));
     if (is_user_plugin(ctx)) {
       const RtcKernels *rk = nullptr;
       PD_TRY(rtc_kernels(ctx, &rk));
@@ -288,14 +327,15 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
       uint32_t w_ = width, h_ = height, dp = depth;
       int32_t *o = ctx->p_out.as<int32_t>();
       const int32_t *lc = ctx->f_lc.as<int32_t>() + off;
-      const FeatT *ft = ctx->f_feat.as<FeatT>() + off * P::kFeatDim, *th = ctx->f_thr.as<FeatT>() + off;
+      const void *cd = ctx->f_cand.as<uint8_t>() + off * cand_record<P>(ctx);
+      const FeatT *th = ctx->f_thr.as<FeatT>() + off;
       const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
-      void *args[] = {&im, &w_, &h_, &mk, &o, &lc, &ft, &th, &dp, &mg};
+      void *args[] = {&im, &w_, &h_, &mk, &o, &lc, &cd, &th, &dp, &mg};
       return rtc_launch(ctx, rk->predict_leaf, grid, dim3(kPredX, kPredY), 0, args);
     }
     k_predict_leaf<P><<<grid, dim3(kPredX, kPredY), 0, st>>>(
         ctx->p_img.as<uint8_t>(), width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
-        ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_feat.as<FeatT>() + off * P::kFeatDim,
+        ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_cand.as<typename P::Cand>() + off,
         ctx->f_thr.as<FeatT>() + off, depth, ctx->magic_tab.as<uint32_t>());
     PD_CUDA(cudaGetLastError());
     return PD_OK;

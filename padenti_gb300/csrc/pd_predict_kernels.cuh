@@ -21,23 +21,31 @@ constexpr int kPredX = 32, kPredY = 8, kPredThreads = kPredX * kPredY;
 #endif
 constexpr int kPredGroup = PD_PRED_GROUP;
 
+// Leaf reached by one tree from the root; cand holds P::candidate of every
+// node's features (k_forest_cands), so a visit loads the node's constants
+// instead of deriving them.
 template <class P>
 PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
-                  const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+                  const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
                   uint32_t depth) {
   using FeatT = typename P::feat_t;
-  constexpr int D = P::kFeatDim;
   int32_t node = 0;
   for (uint32_t d = 1; d < depth; d++) {
     const int32_t c = ldg(lc + node);
     if (c < 0) break;  // leaf (-1); an untrained root (-2) also stops
-    FeatT fv[D];
-#pragma unroll
-    for (int k = 0; k < D; k++) fv[k] = ldg(feat + (size_t)node * D + k);
-    const FeatT r = P::eval(prep, fv);
+    const typename P::Cand cd = cand[node];
+    const FeatT r = P::fast(cd) ? P::template eval<true>(prep, cd) : P::template eval<false>(prep, cd);
     node = c + (r <= ldg(thr + node) ? 0 : 1);
   }
   return node;
+}
+
+// P::candidate of every node's features, for the prediction kernels.
+template <class P>
+__global__ void k_forest_cands(const typename P::feat_t *__restrict__ feat, unsigned long long n_nodes,
+                               typename P::Cand *__restrict__ cand) {
+  const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  if (i < n_nodes) cand[i] = P::candidate(feat + i * P::kFeatDim);
 }
 
 // The leaves of trees t0 .. t0+G-1 (those below n_trees) for one pixel, the G
@@ -45,11 +53,10 @@ PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
 // the one walk() does.
 template <class P, int G>
 PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ lc,
-                     const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+                     const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
                      const TreeMeta *__restrict__ meta, uint32_t t0, uint32_t n_trees, int32_t *leaf_s,
                      uint32_t tid) {
   using FeatT = typename P::feat_t;
-  constexpr int D = P::kFeatDim;
   int32_t node[G];
   size_t off[G];
   uint32_t depth[G];
@@ -72,10 +79,8 @@ PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ l
         live &= ~(1u << g);
         continue;
       }
-      FeatT fv[D];
-#pragma unroll
-      for (int k = 0; k < D; k++) fv[k] = ldg(feat + (off[g] + (size_t)node[g]) * D + k);
-      const FeatT r = P::eval(prep, fv);
+      const typename P::Cand cd = cand[off[g] + node[g]];
+      const FeatT r = P::fast(cd) ? P::template eval<true>(prep, cd) : P::template eval<false>(prep, cd);
       node[g] = c + (r <= ldg(thr + off[g] + node[g]) ? 0 : 1);
       if (d + 1 >= depth[g]) live &= ~(1u << g);
     }
@@ -90,7 +95,7 @@ PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ l
 // and divided by the tree count, written planar with stride plane.
 template <class P>
 PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint32_t y, bool masked_out, float *o,
-                        size_t plane, const int32_t *__restrict__ lc, const typename P::feat_t *__restrict__ feat,
+                        size_t plane, const int32_t *__restrict__ lc, const typename P::Cand *__restrict__ cand,
                         const typename P::feat_t *__restrict__ thr, const float *__restrict__ post,
                         const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K, int32_t *leaf_s,
                         uint32_t tid) {
@@ -100,7 +105,7 @@ PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint3
   }
   const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
   for (uint32_t t = 0; t < n_trees; t += kPredGroup)
-    walk_group<P, kPredGroup>(prep, lc, feat, thr, meta, t, n_trees, leaf_s, tid);
+    walk_group<P, kPredGroup>(prep, lc, cand, thr, meta, t, n_trees, leaf_s, tid);
   const float nt = (float)n_trees;
   for (uint32_t l = 0; l < K; l++) {
     float acc = 0.0f;
@@ -115,7 +120,7 @@ template <class P>
 __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
     const uint8_t *__restrict__ images, uint64_t img_bytes, uint32_t W, uint32_t H,
     const uint8_t *__restrict__ masks, float *__restrict__ out, const int32_t *__restrict__ lc,
-    const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+    const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
     const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
     const uint32_t *__restrict__ magic) {
   using ImgT = typename P::img_t;
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
   im.w = (int32_t)W;
   im.h = (int32_t)H;
   im.magic = magic;
-  predict_pixel<P>(im, x, y, masks && !masks[(size_t)z * P_ + pix], out + (size_t)z * K * P_ + pix, P_, lc, feat,
+  predict_pixel<P>(im, x, y, masks && !masks[(size_t)z * P_ + pix], out + (size_t)z * K * P_ + pix, P_, lc, cand,
                    thr, post, meta, n_trees, K, leaf_s, tid);
 }
 
@@ -147,7 +152,7 @@ template <class P>
 __global__ void __launch_bounds__(kPredThreads) k_predict_batch(
     const uint8_t *__restrict__ images, const uint8_t *__restrict__ masks, uint8_t *__restrict__ out,
     const BatchImage *__restrict__ batch, uint32_t n, const int32_t *__restrict__ lc,
-    const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+    const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
     const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
     const uint32_t *__restrict__ magic) {
   using ImgT = typename P::img_t;
@@ -170,7 +175,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_batch(
   im.h = (int32_t)b.h;
   im.magic = magic;
   const bool masked_out = b.has_mask && !masks[b.mask_off + pix];
-  predict_pixel<P>(im, x, y, masked_out, reinterpret_cast<float *>(out + b.out_off) + pix, P_, lc, feat, thr, post,
+  predict_pixel<P>(im, x, y, masked_out, reinterpret_cast<float *>(out + b.out_off) + pix, P_, lc, cand, thr, post,
                    meta, n_trees, K, leaf_s, tid);
 }
 
@@ -179,7 +184,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__
                                                                uint32_t H, const uint8_t *__restrict__ mask,
                                                                int32_t *__restrict__ out,
                                                                const int32_t *__restrict__ lc,
-                                                               const typename P::feat_t *__restrict__ feat,
+                                                               const typename P::Cand *__restrict__ cand,
                                                                const typename P::feat_t *__restrict__ thr,
                                                                uint32_t depth, const uint32_t *__restrict__ magic) {
   using ImgT = typename P::img_t;
@@ -195,7 +200,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__
   im.w = (int32_t)W;
   im.h = (int32_t)H;
   im.magic = magic;
-  out[pix] = walk<P>(P::prepare(im, (int32_t)x, (int32_t)y), lc, feat, thr, depth);
+  out[pix] = walk<P>(P::prepare(im, (int32_t)x, (int32_t)y), lc, cand, thr, depth);
 }
 
 }  // namespace pd

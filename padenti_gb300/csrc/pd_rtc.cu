@@ -190,7 +190,7 @@ extern "C" int pd_plugin_compile(pd_ctx *ctx, const char *source) {
   const std::vector<std::string> exprs = {
       "pd::k_reassign<pd::UserPlugin>", "pd::k_build_rec<pd::UserPlugin>", "pd::k_cand_order<pd::UserPlugin>",
       "pd::k_predict_posterior<pd::UserPlugin>", "pd::k_predict_leaf<pd::UserPlugin>",
-      "pd::k_predict_batch<pd::UserPlugin>"};
+      "pd::k_predict_batch<pd::UserPlugin>", "pd::k_forest_cands<pd::UserPlugin>"};
   std::string cubin;
   std::vector<std::string> low;
   int rc = compile_unit(ctx->cfg, p->source, p->arch, exprs, &cubin, &low, nullptr);
@@ -209,6 +209,7 @@ extern "C" int pd_plugin_compile(pd_ctx *ctx, const char *source) {
   p->base.predict_posterior = ks[3];
   p->base.predict_leaf = ks[4];
   p->base.predict_batch = ks[5];
+  p->base.forest_cands = ks[6];
   rtc_release(ctx);  // a previous plugin of this context
   ctx->rtc = p;
   ctx->have_dataset = false;  // the sample records depend on the plugin: upload again

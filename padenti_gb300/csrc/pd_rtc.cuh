@@ -12,6 +12,7 @@ namespace pd {
 struct RtcKernels {
   cudaKernel_t reassign = nullptr, build_rec = nullptr, cand_order = nullptr;
   cudaKernel_t predict_posterior = nullptr, predict_leaf = nullptr, predict_batch = nullptr;
+  cudaKernel_t forest_cands = nullptr;
 };
 
 // The compiled base kernels; PD_ERR_STATE when pd_plugin_compile has not run.

@@ -18,7 +18,7 @@ struct UserPlugin {
     ImageView im;
     int32_t x, y;
   };
-  struct Cand {
+  struct __align__(16) Cand {  // one 16-byte-aligned record per tree node in prediction
     feat_t f[kFeatDim];
   };
   static PD_D void preload(const ImageRef<img_t> &, int32_t, int32_t, uint32_t *pre) { pre[0] = 0u; }
