@@ -14,8 +14,8 @@ struct TreeMeta {
 
 constexpr int kPredX = 32, kPredY = 8, kPredThreads = kPredX * kPredY;
 // Tree walks interleaved per pixel.  On the 3-tree, depth-16 forest of 640x480
-// depth maps, 1 measures fastest (5.72e9 pixels/s; 2: 5.53e9, 3: 5.55e9, 4:
-// 5.19e9): the wider walks cost registers and occupancy.
+// depth maps, 1 measures fastest (7.07e9 pixels/s; 2: 6.91e9, 3: 7.08e9): the
+// wider walks cost registers and occupancy.
 #ifndef PD_PRED_GROUP
 #define PD_PRED_GROUP 1
 #endif
