@@ -157,3 +157,21 @@ def test_sampled_training_set_trains_like_the_oracle():
     o = ob.train_tree(ob.params(cfg, tp), ob.OracleSet(ts, cfg), 2, 6, ts.priors)
     assert np.array_equal(tree.left_child, o["left_child"])
     assert np.array_equal(tree.thresholds, o["thresholds"])
+
+
+@pytest.mark.gpu
+def test_gpu_samplers_tiny_and_ragged_images():
+    """Images of 1, 6, 17 and 255 pixels (shorter than one checksum block or label vector)
+    beside a normal one, in one batch."""
+    rng = np.random.default_rng(5)
+    shapes = [(1, 1), (2, 3), (1, 17), (15, 17), (48, 64)]
+    images = [rng.integers(0, 65536, s, dtype=np.uint16) for s in shapes]
+    labels = [rng.integers(0, 4, s, dtype=np.uint8) for s in shapes]
+    labels[0][:] = 2
+    labels[1][:] = 0  # nothing labelled
+    for s in [pg.UniformImageSampler(40, 9), pg.ClassWeightedImageSampler(60, 3, seed=4)]:
+        got = s.sample_batch(images, labels)
+        for d, lab, g in zip(images, labels, got):
+            want = (ob.sample_uniform(d, lab, 40, 9) if s.kind == 1
+                    else ob.sample_class_weighted(d, lab, 60, 3, None, 4))
+            assert np.array_equal(g, want)
