@@ -5,7 +5,6 @@
 // open-addressing table from colour to first class (512 entries, in shared
 // memory) and each thread maps 16 pixels with 16-byte loads and one 16-byte store.
 #include <algorithm>
-#include <chrono>
 #include <cstring>
 #include <thread>
 #include <vector>

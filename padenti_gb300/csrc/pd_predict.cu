@@ -18,7 +18,6 @@ namespace pd {
 
 static int upload_forest(pd_ctx *ctx) {
   if (!ctx->forest_dirty) return PD_OK;
-  const size_t fs = feat_size(ctx->cfg.feat_type);
   const size_t nodes = ctx->h_lc.size();
   const uint32_t nt = (uint32_t)ctx->tree_depth.size();
   std::vector<TreeMeta> meta(nt);
@@ -32,7 +31,6 @@ static int upload_forest(pd_ctx *ctx) {
   PD_TRY(ctx->f_thr.ensure(ctx->h_thr.size() + 4));
   PD_TRY(ctx->f_post.ensure(ctx->h_post.size() * 4 + 4));
   PD_TRY(ctx->f_meta.ensure(nt * sizeof(TreeMeta) + 16));
-  cudaStream_t st = ctx->stream;
   if (nodes) {
     PD_CUDA(h2d(ctx, ctx->f_lc.ptr, ctx->h_lc.data(), nodes * 4));
     PD_CUDA(h2d(ctx, ctx->f_feat.ptr, ctx->h_feat.data(), ctx->h_feat.size()));
@@ -40,7 +38,6 @@ static int upload_forest(pd_ctx *ctx) {
     PD_CUDA(h2d(ctx, ctx->f_post.ptr, ctx->h_post.data(), ctx->h_post.size() * 4));
     PD_CUDA(h2d(ctx, ctx->f_meta.ptr, meta.data(), nt * sizeof(TreeMeta)));
   }
-  (void)fs;
   ctx->forest_dirty = false;
   ctx->forest_version++;
   return PD_OK;
