@@ -12,6 +12,7 @@ kernels behind the C ABI of include/padenti_gb300.h).
 from __future__ import annotations
 
 import ctypes as C
+import threading
 import xml.etree.ElementTree as ET
 from dataclasses import dataclass, field
 
@@ -432,16 +433,19 @@ class Classifier(_Ctx):
 
 
 _SAMPLER_CTX: dict = {}
+_SAMPLER_LOCK = threading.RLock()  # calls on one context are serialised (one stream, shared staging)
 
 
 def _sampler_ctx(device: int):
-    """A context per device for the samplers (their own arguments fix the image type)."""
-    h = _SAMPLER_CTX.get(device)
-    if h is None:
-        h = C.c_void_p()
-        check(lib().pd_ctx_create(C.byref(ForestConfig("depth_diff2", 2).c()), device, C.byref(h)))
-        _SAMPLER_CTX[device] = h
-    return h
+    """A context per device for the samplers and the label loader (their own arguments fix
+    the image type).  Callers hold _SAMPLER_LOCK while they use it."""
+    with _SAMPLER_LOCK:
+        h = _SAMPLER_CTX.get(device)
+        if h is None:
+            h = C.c_void_p()
+            check(lib().pd_ctx_create(C.byref(ForestConfig("depth_diff2", 2).c()), device, C.byref(h)))
+            _SAMPLER_CTX[device] = h
+        return h
 
 
 class ImageSampler:
@@ -497,14 +501,20 @@ class ImageSampler:
         lptr = (C.c_void_p * n)(*[a.ctypes.data for a in lbs])
         w = np.array([a.shape[1] for a in lbs], np.uint32)
         h = np.array([a.shape[0] for a in lbs], np.uint32)
-        check(lib().pd_sample(_sampler_ctx(self.device), C.byref(self._c(pb.pop())), n, iptr, lptr, _ptr(w), _ptr(h),
-                              max(stride, 1), _ptr(out), _ptr(counts)))
+        with _SAMPLER_LOCK:
+            check(lib().pd_sample(_sampler_ctx(self.device), C.byref(self._c(pb.pop())), n, iptr, lptr, _ptr(w),
+                                  _ptr(h), max(stride, 1), _ptr(out), _ptr(counts)))
         return [out[i, :counts[i]].copy() for i in range(n)]
 
-    def stats(self) -> dict:
+    def _read_stats(self) -> dict:
         st = N.SampleStats()
         check(lib().pd_sample_get_stats(_sampler_ctx(self.device), C.byref(st)))
         return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def stats(self) -> dict:
+        """Counters and kernel times of the last call through this device's sampler context."""
+        with _SAMPLER_LOCK:
+            return self._read_stats()
 
 
 class UniformImageSampler(ImageSampler):
@@ -616,8 +626,9 @@ class RGBLabelsLoader:
         op = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
         w = np.array([a.shape[1] for a in imgs], np.uint32)
         h = np.array([a.shape[0] for a in imgs], np.uint32)
-        check(lib().pd_rgb_to_labels(_sampler_ctx(self.device), n, ip, _ptr(w), _ptr(h), ch.pop(), _ptr(self.map),
-                                     len(self.map), op))
+        with _SAMPLER_LOCK:
+            check(lib().pd_rgb_to_labels(_sampler_ctx(self.device), n, ip, _ptr(w), _ptr(h), ch.pop(),
+                                         _ptr(self.map), len(self.map), op))
         return outs
 
     def convert(self, image: np.ndarray) -> np.ndarray:
