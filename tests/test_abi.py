@@ -68,3 +68,26 @@ def test_python_api_fails_loudly_when_the_library_is_missing(monkeypatch, tmp_pa
     monkeypatch.setattr(N, "LIB_PATH", tmp_path / "missing.so")
     with pytest.raises(RuntimeError, match="missing"):
         N.lib()
+
+
+def test_headers_compile_cleanly_as_c_and_cpp(tmp_path):
+    """padenti_gb300.h is plain C (C99, pedantic); the C++ façade headers build without
+    warnings under -Wall -Wextra -Wpedantic."""
+    import shutil
+    import subprocess
+
+    inc = str(HEADER.parent)
+    if shutil.which("gcc"):
+        c = tmp_path / "h.c"
+        c.write_text("#include <padenti_gb300.h>\nint main(void) { pd_sampler s; (void)s; return 0; }\n")
+        r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Wpedantic", "-Werror", f"-I{inc}",
+                            "-fsyntax-only", str(c)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    if shutil.which("g++"):
+        cpp = tmp_path / "h.cpp"
+        cpp.write_text("".join(f"#include <padenti/{h}>\n" for h in
+                               ["cuda_tree_trainer.hpp", "image_sampler.hpp", "image_loader.hpp", "classifier.hpp",
+                                "tree_trainer.hpp", "training_set.hpp", "tree.hpp", "image.hpp"]) + "int main() {}\n")
+        r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Wpedantic", "-Werror", f"-I{inc}",
+                            "-fsyntax-only", str(cpp)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
