@@ -3,8 +3,10 @@
 // binary netpbm files (PGM: 8- or 16-bit grey, PPM: 8-bit RGB) in place of the
 // PNG files cv::imread reads, and the colour-to-class step of
 // CVRGBLabelsLoader (_rgb2label, cv_image_loader_impl.hpp:233-266) runs on the
-// GPU (pd_rgb_to_labels).  loadTrainingSet() is the TrainingSet constructor over
-// a directory (training_set_impl.hpp:40-112).  Errors throw std::runtime_error.
+// GPU (pd_rgb_to_labels).  The ROI loaders crop to the largest bounding
+// rectangle of the nonzero pixels' components (pd_image_roi).  loadTrainingSet()
+// is the TrainingSet constructor over a directory (training_set_impl.hpp:40-112).
+// Errors throw std::runtime_error.
 #ifndef PADENTI_GB300_IMAGE_LOADER_HPP
 #define PADENTI_GB300_IMAGE_LOADER_HPP
 
@@ -14,6 +16,7 @@
 
 #include <algorithm>
 #include <cctype>
+#include <cstring>
 #include <filesystem>
 #include <fstream>
 #include <iterator>
@@ -80,7 +83,7 @@ class PNMImageLoader : public ImageLoader<type, nChannels> {
     const padenti_gb300::Pnm p = padenti_gb300::read_pnm(imagePath);
     Image<type, nChannels> img(p.width, p.height);
     unsigned int w, h;
-    load(imagePath, img.getData(), &w, &h);
+    PNMImageLoader::load(imagePath, img.getData(), &w, &h);  // this class's, not an override's
     return img;
   }
 };
@@ -123,9 +126,76 @@ class CUDARGBLabelsLoader : public ImageLoader<unsigned char, 1> {
     const padenti_gb300::Pnm p = padenti_gb300::read_pnm(imagePath);
     Image<unsigned char, 1> img(p.width, p.height);
     unsigned int w, h;
-    load(imagePath, img.getData(), &w, &h);
+    CUDARGBLabelsLoader::load(imagePath, img.getData(), &w, &h);  // this class's, not an override's
     return img;
   }
+};
+
+namespace padenti_gb300 {
+// Crops data (width x height pixels of `channels` values) in place to the ROI
+// of its nonzero pixels (pd_image_roi); returns {x, y, width, height}.
+template <typename type>
+std::vector<unsigned int> crop_to_roi(type *data, unsigned int *width, unsigned int *height, unsigned int channels) {
+  uint32_t roi[4];
+  const int rc = pd_image_roi(data, *width, *height, (uint32_t)(sizeof(type) * channels), roi);
+  if (rc != PD_OK) throw std::runtime_error(std::string("padenti_gb300: ") + pd_last_error());
+  const size_t row = (size_t)roi[2] * channels;
+  for (unsigned int y = 0; y < roi[3]; y++)
+    std::memmove(data + y * row, data + ((size_t)(roi[1] + y) * *width + roi[0]) * channels, row * sizeof(type));
+  *width = roi[2];
+  *height = roi[3];
+  return {roi[0], roi[1], roi[2], roi[3]};
+}
+}  // namespace padenti_gb300
+
+// CVImageROILoader (cv_image_loader.hpp:52-65): the image cropped to the ROI of
+// its nonzero pixels.
+template <typename type, unsigned int nChannels>
+class PNMImageROILoader : public PNMImageLoader<type, nChannels> {
+  unsigned int m_roiX = 0, m_roiY = 0;
+
+ public:
+  void load(const std::string &imagePath, type *data, unsigned int *width, unsigned int *height) override {
+    PNMImageLoader<type, nChannels>::load(imagePath, data, width, height);
+    const std::vector<unsigned int> r = padenti_gb300::crop_to_roi(data, width, height, nChannels);
+    m_roiX = r[0];
+    m_roiY = r[1];
+  }
+  Image<type, nChannels> load(const std::string &imagePath) override {
+    Image<type, nChannels> full = PNMImageLoader<type, nChannels>::load(imagePath);
+    unsigned int w = full.getWidth(), h = full.getHeight();
+    const std::vector<unsigned int> r = padenti_gb300::crop_to_roi(full.getData(), &w, &h, nChannels);
+    m_roiX = r[0];
+    m_roiY = r[1];
+    return Image<type, nChannels>(full.getData(), w, h);
+  }
+  unsigned int getRoiX() const { return m_roiX; }
+  unsigned int getRoiY() const { return m_roiY; }
+};
+
+// CVRGBLabelsROILoader (cv_image_loader.hpp:69-82): the labels cropped to the ROI
+// of the labelled pixels.
+class CUDARGBLabelsROILoader : public CUDARGBLabelsLoader {
+  unsigned int m_roiX = 0, m_roiY = 0;
+
+ public:
+  using CUDARGBLabelsLoader::CUDARGBLabelsLoader;
+  void load(const std::string &imagePath, unsigned char *data, unsigned int *width, unsigned int *height) override {
+    CUDARGBLabelsLoader::load(imagePath, data, width, height);
+    const std::vector<unsigned int> r = padenti_gb300::crop_to_roi(data, width, height, 1u);
+    m_roiX = r[0];
+    m_roiY = r[1];
+  }
+  Image<unsigned char, 1> load(const std::string &imagePath) override {
+    Image<unsigned char, 1> full = CUDARGBLabelsLoader::load(imagePath);
+    unsigned int w = full.getWidth(), h = full.getHeight();
+    const std::vector<unsigned int> r = padenti_gb300::crop_to_roi(full.getData(), &w, &h, 1u);
+    m_roiX = r[0];
+    m_roiY = r[1];
+    return Image<unsigned char, 1>(full.getData(), w, h);
+  }
+  unsigned int getRoiX() const { return m_roiX; }
+  unsigned int getRoiY() const { return m_roiY; }
 };
 
 // TrainingSet(tsPath, dataSuffix, labelsSuffix, nClasses, dataLoader,

@@ -325,6 +325,15 @@ int pd_rgb_to_labels(pd_ctx *ctx, uint32_t n_images, const uint8_t *const *image
 int pd_rgb_to_labels_device(pd_ctx *ctx, uint64_t n_pixels, const uint8_t *src_device, uint32_t channels,
                             const uint8_t *map, uint32_t n_classes, uint8_t *dst_device, float *ms);
 
+/* The crop of the ROI loaders (CVImageROILoader, CVRGBLabelsROILoader;
+ * _extractROI at cv_image_loader_impl.hpp:268-289), on the host: the bounding
+ * rectangle of largest area among the 8-connected components of the pixels with
+ * a nonzero byte (pixel_bytes bytes each), the one-pixel image border counting
+ * as zero; ties go to the component met first in raster order.  roi = {x, y,
+ * width, height}.  No such pixel is an error (the reference indexes an empty
+ * contour list then). */
+int pd_image_roi(const void *image, uint32_t width, uint32_t height, uint32_t pixel_bytes, uint32_t roi[4]);
+
 /* Synthetic data (seeded, bit-identical on every host) ------------------------ */
 /* Depth maps: background plane U(3000,4000) mm + N(0,5^2) noise, ellipses at
  * U(800,2500) mm.  parts=0: 3 classes (bg, left half, right half of each

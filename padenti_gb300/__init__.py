@@ -25,7 +25,8 @@ __all__ = [
     "ForestConfig", "TreeTrainerParameters", "TrainingSetImage", "TrainingSet", "Tree", "TreeTrainer",
     "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS", "USER_SHAPES", "check_plugin",
     "ImageSampler", "UniformImageSampler", "ClassWeightedImageSampler", "sampled_training_set",
-    "read_pnm", "write_pnm", "PNMImageLoader", "RGBLabelsLoader", "load_training_set",
+    "read_pnm", "write_pnm", "PNMImageLoader", "RGBLabelsLoader", "load_training_set", "image_roi",
+    "PNMImageROILoader", "RGBLabelsROILoader",
 ]
 
 FEAT_DTYPE = {N.PD_FEAT_I16: np.int16, N.PD_FEAT_I32: np.int32}
@@ -636,6 +637,46 @@ class RGBLabelsLoader:
 
     def load(self, path) -> np.ndarray:
         return self.convert(read_pnm(path))
+
+
+def image_roi(image: np.ndarray) -> tuple:
+    """_extractROI (cv_image_loader_impl.hpp:268-289): (x, y, width, height) of the largest
+    bounding rectangle among the 8-connected components of the nonzero pixels, the one-pixel
+    border counting as zero (pd_image_roi)."""
+    a = np.ascontiguousarray(image)
+    h, w = a.shape[:2]
+    roi = np.zeros(4, np.uint32)
+    check(lib().pd_image_roi(_ptr(a), w, h, a.nbytes // max(w * h, 1), _ptr(roi)))
+    return tuple(int(v) for v in roi)
+
+
+class PNMImageROILoader(PNMImageLoader):
+    """CVImageROILoader (cv_image_loader_impl.hpp:139-186): the image cropped to the ROI of its
+    nonzero pixels; ``roi_x``, ``roi_y`` (getRoiX, getRoiY) give the crop's corner."""
+
+    roi_x = roi_y = 0
+
+    def load(self, path) -> np.ndarray:
+        a = super().load(path)
+        x, y, w, h = image_roi(a)
+        self.roi_x, self.roi_y = x, y
+        return np.ascontiguousarray(a[y:y + h, x:x + w])
+
+
+class RGBLabelsROILoader(RGBLabelsLoader):
+    """CVRGBLabelsROILoader (cv_image_loader_impl.hpp:190-230): the labels (colours mapped on the
+    GPU) cropped to the ROI of the labelled pixels; ``roi_x``, ``roi_y`` give the corner."""
+
+    roi_x = roi_y = 0
+
+    def convert(self, image: np.ndarray) -> np.ndarray:
+        lab = RGBLabelsLoader.convert_batch(self, [image])[0]
+        x, y, w, h = image_roi(lab)
+        self.roi_x, self.roi_y = x, y
+        return np.ascontiguousarray(lab[y:y + h, x:x + w])
+
+    def convert_batch(self, images: list) -> list:
+        return [self.convert(im) for im in images]
 
 
 def load_training_set(path, data_suffix: str, labels_suffix: str, n_classes: int, data_loader: PNMImageLoader,

@@ -139,6 +139,7 @@ _SIGS = {
     "pd_rgb_to_labels": (C.c_int, [_P, C.c_uint32, _P, _P, _P, C.c_uint32, _P, C.c_uint32, _P]),
     "pd_rgb_to_labels_device": (C.c_int, [_P, C.c_uint64, _P, C.c_uint32, _P, C.c_uint32, _P,
                                           C.POINTER(C.c_float)]),
+    "pd_image_roi": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
     "pd_synth_depth": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "pd_synth_rgb": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,

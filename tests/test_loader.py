@@ -162,3 +162,103 @@ def test_cpp_loader_facade_matches_python(tmp_path):
         assert np.array_equal(got[pos + 1:pos + 1 + n], ob.sample_class_weighted(px[i], lb[i], 300, 3, None, 11))
         pos += 1 + n
     assert pos == got.size
+
+
+def _roi_by_flood_fill(mask):
+    """An independent restatement: 8-connected components by breadth-first search, the
+    one-pixel border counting as zero, the largest bounding rectangle, first in raster order."""
+    from collections import deque
+
+    h, w = mask.shape
+    m = mask.copy()
+    m[0, :] = m[-1, :] = False
+    m[:, 0] = m[:, -1] = False
+    seen = np.zeros_like(m)
+    best, best_area = None, 0
+    for y in range(h):
+        for x in range(w):
+            if not m[y, x] or seen[y, x]:
+                continue
+            q = deque([(y, x)])
+            seen[y, x] = True
+            y0 = y1 = y
+            x0 = x1 = x
+            while q:
+                cy, cx = q.popleft()
+                y0, y1, x0, x1 = min(y0, cy), max(y1, cy), min(x0, cx), max(x1, cx)
+                for dy in (-1, 0, 1):
+                    for dx in (-1, 0, 1):
+                        ny, nx = cy + dy, cx + dx
+                        if 0 <= ny < h and 0 <= nx < w and m[ny, nx] and not seen[ny, nx]:
+                            seen[ny, nx] = True
+                            q.append((ny, nx))
+            area = (x1 - x0 + 1) * (y1 - y0 + 1)
+            if area > best_area:
+                best, best_area = (x0, y0, x1 - x0 + 1, y1 - y0 + 1), area
+    return best
+
+
+def test_image_roi_matches_flood_fill():
+    rng = np.random.default_rng(4)
+    for trial in range(30):
+        h, w = int(rng.integers(3, 40)), int(rng.integers(3, 40))
+        img = (rng.random((h, w)) < rng.uniform(0.05, 0.5)).astype(np.uint16) * rng.integers(1, 5000, (h, w))
+        img = img.astype(np.uint16)
+        if not (img[1:-1, 1:-1] != 0).any():
+            with pytest.raises(pg.PadentiError, match="no nonzero pixel"):
+                pg.image_roi(img)
+            continue
+        assert pg.image_roi(img) == _roi_by_flood_fill(img != 0), trial
+    # two components with equal rectangles: the first in raster order wins
+    img = np.zeros((10, 12), np.uint8)
+    img[2:4, 2:4] = 1
+    img[6:8, 7:9] = 1
+    assert pg.image_roi(img) == (2, 2, 2, 2)
+
+
+def test_roi_loaders_crop(tmp_path):
+    depth = np.zeros((30, 40), np.uint16)
+    depth[5:12, 6:20] = 900
+    depth[20:22, 30:32] = 800  # a smaller component
+    pg.write_pnm(tmp_path / "d.pgm", depth)
+    ld = pg.PNMImageROILoader(np.uint16, 1)
+    crop = ld.load(tmp_path / "d.pgm")
+    assert (ld.roi_x, ld.roi_y) == (6, 5) and crop.shape == (7, 14) and np.all(crop == 900)
+
+
+def test_cpp_roi_loader(tmp_path):
+    """PNMImageROILoader of the C++ facade crops as the Python loader does (host code, no GPU)."""
+    import subprocess
+
+    from test_cpp_facade import CPP, _compile
+
+    exe = tmp_path / "facade_roi"
+    _compile(CPP / "facade_roi.cpp", exe, link=True)
+    depth = np.zeros((30, 40), np.uint16)
+    depth[5:12, 6:20] = 900
+    depth[6, 7] = 901
+    depth[20:22, 30:32] = 800
+    pg.write_pnm(tmp_path / "d.pgm", depth)
+    r = subprocess.run([str(exe), str(tmp_path / "d.pgm")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    ld = pg.PNMImageROILoader(np.uint16, 1)
+    crop = ld.load(tmp_path / "d.pgm")
+    want = f"{crop.shape[1]} {crop.shape[0]} {ld.roi_x} {ld.roi_y} {crop[0, 0]}"
+    assert r.stdout.split("\n")[:2] == [want, want]
+
+
+@pytest.mark.gpu
+def test_rgb_labels_roi_loader(tmp_path):
+    colours = [(255, 0, 0), (0, 0, 255)]
+    rgb = np.zeros((40, 50, 3), np.uint8)
+    rgb[8:30, 10:22] = colours[0]
+    rgb[12:16, 12:18] = colours[1]
+    rgb[33:35, 40:45] = colours[1]  # a smaller component
+    rgb[2, 2] = (9, 9, 9)           # an unknown colour: unlabelled
+    pg.write_pnm(tmp_path / "l.ppm", rgb)
+    ld = pg.RGBLabelsROILoader(colours)
+    lab = ld.load(tmp_path / "l.ppm")
+    full = ob.rgb_to_labels(rgb, colours)
+    x, y, w, h = _roi_by_flood_fill(full != 0)
+    assert (ld.roi_x, ld.roi_y, lab.shape[1], lab.shape[0]) == (x, y, w, h) == (10, 8, 12, 22)
+    assert np.array_equal(lab, full[y:y + h, x:x + w])
