@@ -43,6 +43,20 @@ def test_oracle_reproduces_reference_fixture():
     assert n == len(GOLDEN.files) - 1
 
 
+def test_reference_sources_reproduce_the_fixture():
+    """The fixture is what the reference's sampler sources return (where they were built)."""
+    if ob.ref("sampler") is None:
+        pytest.skip("reference sampler not built (Padenti sources absent at build time)")
+    for name, img_type, data, labels, k in sampler_images():
+        for cname, kind, ns, seed, rule in SAMPLER_CONFIGS:
+            key = f"{cname}/{name}"
+            if key not in GOLDEN:
+                continue
+            got = (ob.ref_sample_uniform(img_type, data, labels, ns, seed) if kind == 1 else
+                   ob.ref_sample_class_weighted(img_type, data, labels, ns, k, sampler_weights(rule, k), seed))
+            assert np.array_equal(got, GOLDEN[key]), key
+
+
 def test_sampler_stride_and_argument_errors():
     assert pg.UniformImageSampler(500).stride == 500
     # ceil(float(1/9) * 2000) = 223 per class
