@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(kSmThreads) k_sample_class_weighted(
     for (uint32_t j = 0; j < 4; j++) {
       const uint32_t k = cls[j] - 1u;
       valid[j] = cls[j] != 0 && k < n_classes;
-      if (cls[j] != 0 && k >= n_classes) bad = 1;
+      if (cls[j] != 0 && k >= n_classes) atomicOr(&bad, 1u);
       cls[j] = valid[j] ? k : 0xFFFFFFFFu;
       const uint32_t peers = __match_any_sync(0xFFFFFFFFu, cls[j]);
       rank[j] = valid[j] ? wcnt[warp][cls[j]] + __popc(peers & lt) : 0u;
