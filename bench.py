@@ -176,6 +176,17 @@ def cpu_sample(a, cfg, ts, tp, seconds: float):
                        f"(sample, candidate) as the reference kernel does; {dt:.1f} s"), m
 
 
+def profile_dram_per_image(kernel: str):
+    """DRAM bytes per 640x480 image of a sampler or label kernel launch, from the committed
+    ncu summary profiles/sampler_dram_640x480.json (None when absent)."""
+    p = ROOT / "profiles" / "sampler_dram_640x480.json"
+    try:
+        d = json.loads(p.read_text())[kernel]
+        return d["dram_bytes"] / d["images"]
+    except Exception:
+        return None
+
+
 def sampler_bench(a, pg, N, px, lb):
     """UniformImageSampler / ClassWeightedImageSampler over the training images (2000 samples per
     image, 9 classes): device-resident (pd_sample_device, CUDA-event kernel times) and from host
@@ -226,7 +237,9 @@ def sampler_bench(a, pg, N, px, lb):
             ms_kernels=ms_scan + ms_draw, ms_scan=ms_scan, ms_draw=ms_draw, ms_call=wall,
             roofline=dict(kernel="k_sample_scan", bound="hbm", achieved=scan_bytes / (ms_scan / 1000) / 1e9,
                           peak=peak, unit="GB/s", frac=scan_bytes / (ms_scan / 1000) / 1e9 / peak,
-                          algorithmic_bytes=scan_bytes),
+                          algorithmic_bytes=scan_bytes,
+                          traffic=(lambda v: None if v is None else v * n)(profile_dram_per_image("k_sample_scan")),
+                          traffic_note="DRAM bytes of a 300-image ncu capture, scaled by the images"),
             e2e=dict(value=n / (e2e_ms / 1000), unit="images/s", ms=e2e_ms, h2d_bytes=est["h2d_bytes"],
                      d2h_bytes=est["d2h_bytes"]))
         del dout, dcnt
@@ -289,7 +302,10 @@ def loader_bench(a, pg, N):
     out = dict(metric="label images Mpix/s", value=n * H * W / (k_ms / 1000) / 1e6, unit="Mpix/s", images=n,
                ms_kernel=k_ms,
                roofline=dict(kernel="k_rgb_to_labels", bound="hbm", achieved=nbytes / (k_ms / 1000) / 1e9, peak=peak,
-                             unit="GB/s", frac=nbytes / (k_ms / 1000) / 1e9 / peak, algorithmic_bytes=nbytes),
+                             unit="GB/s", frac=nbytes / (k_ms / 1000) / 1e9 / peak, algorithmic_bytes=nbytes,
+                             traffic=(lambda v: None if v is None else v * n)(profile_dram_per_image("k_rgb_to_labels")),
+                             traffic_note="DRAM bytes of a 200-image ncu capture, scaled by the images (writes "
+                                          "still in L2 at the end of that short launch are not counted)"),
                e2e=dict(value=n * H * W / (e_ms / 1000) / 1e6, unit="Mpix/s", ms=e_ms))
     del src, dst
     if not a.no_cpu:

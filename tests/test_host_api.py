@@ -73,3 +73,18 @@ def test_config_and_params():
     tp = pg.TreeTrainerParameters(10, 5, [0, 0, -30, -30, -30, -30], [3, 3, 30, 30, 30, 30], -255, 255, 7)
     c = tp.c()
     assert c.n_features == 10 and list(c.feat_up)[:6] == [3, 3, 30, 30, 30, 30] and c.per_leaf_samples_thr == 7
+
+
+def test_bench_reads_the_committed_profile_figures():
+    """bench.py's roofline objects take traffic and instruction figures from profiles/."""
+    import importlib.util
+    import pathlib
+
+    root = pathlib.Path(__file__).resolve().parent.parent
+    spec = importlib.util.spec_from_file_location("bench_mod", root / "bench.py")
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    assert b.profile_traffic()["dram_bytes_per_launch"] > 1e9
+    for k in ("k_sample_scan", "k_rgb_to_labels"):
+        assert 0.5e6 < b.profile_dram_per_image(k) < 2e6
+    assert b.profile_dram_per_image("no_such_kernel") is None
