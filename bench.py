@@ -62,6 +62,10 @@ def args_():
     a.add_argument("--fuse-max", type=int, default=None, help="largest node (samples) with the fused split")
     a.add_argument("--cand-order", type=int, default=None, choices=(0, 1),
                    help="1: candidate columns ordered by first-probe offset (default), 0: index order")
+    a.add_argument("--only", default=None, choices=["sampler_uniform", "sampler_class_weighted", "labels"],
+                   help="run one kernel family alone on --images synthetic images already in device memory "
+                        "(--reps times) and print its times: the workload of the sampler and label profiles")
+    a.add_argument("--reps", type=int, default=3)
     return a.parse_args()
 
 
@@ -321,6 +325,46 @@ def loader_bench(a, pg, N):
                                    sample=f"{m} images, the oracle restatement of _rgb2label (per-pixel colour "
                                           f"search) on all host cores; {dt:.1f} s")
     return out
+
+
+def run_only(a):
+    """One kernel family alone (the pixel samplers through pd_sample_device, or the colour-to-class
+    mapping through pd_rgb_to_labels_device) on a.images synthetic depth-map images already in
+    device memory, a.reps times: the command the sampler and label-image profiles run."""
+    import torch
+
+    import padenti_gb300 as pg
+    from padenti_gb300 import _native as N
+
+    px, lb, _ = pg.synth_depth(a.seed, a.images, a.width, a.height, parts=1, min_ellipses=2, max_ellipses=5,
+                               samples_per_image=1)
+    h = pg._sampler_ctx(0)
+    if a.only == "labels":
+        colours = np.array([[255, 0, 0], [0, 0, 255], [0, 255, 0], [255, 255, 0], [0, 255, 255], [255, 0, 255],
+                            [128, 0, 0], [0, 128, 0], [0, 0, 128]], np.uint8)
+        src = torch.from_numpy(colours[np.maximum(lb.astype(np.int64) - 1, 0)].reshape(-1)).cuda()
+        dst = torch.empty(lb.size, dtype=torch.uint8, device="cuda")
+        cmap = np.ascontiguousarray(colours.reshape(-1))
+        ms = C.c_float()
+        torch.cuda.synchronize()
+        for _ in range(a.reps):
+            N.check(N.lib().pd_rgb_to_labels_device(h, lb.size, src.data_ptr(), 3, cmap.ctypes.data, len(colours),
+                                                    dst.data_ptr(), C.byref(ms)))
+            print(json.dumps(dict(kernel="k_rgb_to_labels", ms=ms.value, gbs=lb.size * 4 / ms.value / 1e6)))
+        return
+    sm = (pg.UniformImageSampler(a.samples) if a.only == "sampler_uniform"
+          else pg.ClassWeightedImageSampler(a.samples, 9))
+    dpx = torch.from_numpy(px.view(np.int16)).cuda()
+    dlb = torch.from_numpy(lb).cuda()
+    out = torch.zeros((a.images, sm.stride), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(a.images, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(a.reps):
+        N.check(N.lib().pd_sample_device(h, C.byref(sm._c(2)), a.images, dpx.data_ptr(), dlb.data_ptr(), a.width,
+                                         a.height, sm.stride, out.data_ptr(), cnt.data_ptr()))
+        st = sm.stats()
+        print(json.dumps(dict(sampler=a.only, ms_scan=st["ms_scan"], ms_draw=st["ms_draw"],
+                              scan_gbs=(st["data_bytes"] + st["label_bytes"]) / st["ms_scan"] / 1e6)))
 
 
 def run_reference(a):
@@ -595,7 +639,9 @@ def run_ours(a):
 
 def main():
     a = args_()
-    if a.impl == "reference":
+    if a.only:
+        run_only(a)
+    elif a.impl == "reference":
         run_reference(a)
     else:
         run_ours(a)

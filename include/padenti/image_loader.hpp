@@ -4,7 +4,7 @@
 // PNG files cv::imread reads, and the colour-to-class step of
 // CVRGBLabelsLoader (_rgb2label, cv_image_loader_impl.hpp:233-266) runs on the
 // GPU (pd_rgb_to_labels).  The ROI loaders crop to the largest bounding
-// rectangle of the nonzero pixels' components (pd_image_roi).  loadTrainingSet()
+// rectangle of the components of the pixels > 0 (pd_image_roi).  loadTrainingSet()
 // is the TrainingSet constructor over a directory (training_set_impl.hpp:40-112).
 // Errors throw std::runtime_error.
 #ifndef PADENTI_GB300_IMAGE_LOADER_HPP
@@ -22,6 +22,7 @@
 #include <iterator>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 template <typename type, unsigned int nChannels>
@@ -133,11 +134,23 @@ class CUDARGBLabelsLoader : public ImageLoader<unsigned char, 1> {
 
 namespace padenti_gb300 {
 // Crops data (width x height pixels of `channels` values) in place to the ROI
-// of its nonzero pixels (pd_image_roi); returns {x, y, width, height}.
+// of its pixels > 0 (pd_image_roi); returns {x, y, width, height}.
+template <typename type>
+constexpr int32_t roi_img_type() {
+  if constexpr (std::is_same_v<type, unsigned char>) return PD_IMG_U8;
+  else if constexpr (std::is_same_v<type, unsigned short>) return PD_IMG_U16;
+  else if constexpr (std::is_same_v<type, short>) return PD_IMG_I16;
+  else if constexpr (std::is_same_v<type, int>) return PD_IMG_I32;
+  else {
+    static_assert(std::is_same_v<type, float>, "ROI loaders take uint8, uint16, int16, int32 or float images");
+    return PD_IMG_F32;
+  }
+}
+
 template <typename type>
 std::vector<unsigned int> crop_to_roi(type *data, unsigned int *width, unsigned int *height, unsigned int channels) {
   uint32_t roi[4];
-  const int rc = pd_image_roi(data, *width, *height, (uint32_t)(sizeof(type) * channels), roi);
+  const int rc = pd_image_roi(data, *width, *height, roi_img_type<type>(), channels, roi);
   if (rc != PD_OK) throw std::runtime_error(std::string("padenti_gb300: ") + pd_last_error());
   const size_t row = (size_t)roi[2] * channels;
   for (unsigned int y = 0; y < roi[3]; y++)
@@ -149,7 +162,7 @@ std::vector<unsigned int> crop_to_roi(type *data, unsigned int *width, unsigned 
 }  // namespace padenti_gb300
 
 // CVImageROILoader (cv_image_loader.hpp:52-65): the image cropped to the ROI of
-// its nonzero pixels.
+// its pixels > 0.
 template <typename type, unsigned int nChannels>
 class PNMImageROILoader : public PNMImageLoader<type, nChannels> {
   unsigned int m_roiX = 0, m_roiY = 0;

@@ -39,8 +39,12 @@ extern "C" {
 #define PD_ERR_UNSUPPORTED (-4)  /* configuration outside the built kernels */
 #define PD_ERR_STATE (-5)        /* call out of order (e.g. no dataset uploaded) */
 
+/* Image element types (ImgType). */
 #define PD_IMG_U8 1
 #define PD_IMG_U16 2
+#define PD_IMG_I16 3
+#define PD_IMG_I32 4
+#define PD_IMG_F32 5
 
 #define PD_FEAT_I16 1
 #define PD_FEAT_I32 2
@@ -209,20 +213,21 @@ int pd_split(pd_ctx *ctx, const pd_train_params *params, const uint32_t *hist,
              const uint32_t *class_tot, uint32_t n_nodes, int32_t *out_t, int32_t *out_f,
              double *out_gain);
 /* pd_split for callers that cannot allocate device memory.  It has no
- * counterpart in the reference.  Code running inside a CUDA graph capture, or a
- * host that only hands out memory from its own pre-allocated pool, cannot call
- * cudaMalloc; this entry point takes DEVICE pointers for its inputs
- * (hist_device: [n_nodes][K][T][F] cumulative counts as pd_split takes them,
- * class_tot_device: [n_nodes][K]) and outputs (out_t/out_f int32, out_gain
- * double, n_nodes each), needs no context, and keeps every intermediate result
- * in one fixed 32 MiB device array inside the library (held by every GPU that
- * loads it until the process exits).  Limits: the working set must fit the
- * array (PD_ERR_UNSUPPORTED otherwise: about n_nodes*T*F*4 bytes plus 8 MiB of
- * log2 table), and every node must hold fewer than 2^20 - 1 samples.  The first
- * call on a device sets the array up and synchronises `stream`: make it before
- * any stream capture.  Calls share the array, so calls that overlap on the GPU
- * race; serialise them.  Each call synchronises `stream` (a cudaStream_t, NULL
- * for the default stream) before returning. */
+ * counterpart in the reference.  A host that only hands out memory from its own
+ * pre-allocated pool, or a runtime whose allocator must not be bypassed, cannot
+ * let a library call cudaMalloc; this entry point takes DEVICE pointers for its
+ * inputs (hist_device: [n_nodes][K][T][F] cumulative counts as pd_split takes
+ * them, class_tot_device: [n_nodes][K]) and outputs (out_t/out_f int32,
+ * out_gain double, n_nodes each), needs no context, and keeps every
+ * intermediate result in one fixed 32 MiB device array inside the library
+ * (held by every GPU that loads it until the process exits).  Limits: the
+ * working set must fit the array (PD_ERR_UNSUPPORTED otherwise: about
+ * n_nodes*T*F*4 bytes plus 8 MiB of log2 table), and every node must hold
+ * fewer than 2^20 samples.  The first call on a device sets the array up and
+ * synchronises `stream`: make it before any stream capture; cudaDeviceReset on
+ * that device afterwards is not supported.  Calls share the array, so calls
+ * that overlap on the GPU race; serialise them.  Each call synchronises
+ * `stream` (a cudaStream_t, NULL for the default stream) before returning. */
 int pd_split_noalloc(const pd_train_params *params, uint32_t n_classes, const uint32_t *hist_device,
                      const uint32_t *class_tot_device, uint32_t n_nodes, int32_t *out_t_device,
                      int32_t *out_f_device, double *out_gain_device, void *stream);
@@ -327,12 +332,15 @@ int pd_rgb_to_labels_device(pd_ctx *ctx, uint64_t n_pixels, const uint8_t *src_d
 
 /* The crop of the ROI loaders (CVImageROILoader, CVRGBLabelsROILoader;
  * _extractROI at cv_image_loader_impl.hpp:268-289), on the host: the bounding
- * rectangle of largest area among the 8-connected components of the pixels with
- * a nonzero byte (pixel_bytes bytes each), the one-pixel image border counting
- * as zero; ties go to the component met first in raster order.  roi = {x, y,
- * width, height}.  No such pixel is an error (the reference indexes an empty
- * contour list then). */
-int pd_image_roi(const void *image, uint32_t width, uint32_t height, uint32_t pixel_bytes, uint32_t roi[4]);
+ * rectangle of largest area among the 8-connected components of the pixels
+ * whose value is > 0 in the image's element type img_type (PD_IMG_*; the
+ * reference's mask img > 0: negative values and -0.0f are background), the
+ * one-pixel image border counting as zero; ties go to the component met first
+ * in raster order.  The reference takes single-channel images; with channels > 1
+ * a pixel counts when any of its channels is > 0.  roi = {x, y, width, height}.
+ * No such pixel is an error (the reference indexes an empty contour list then). */
+int pd_image_roi(const void *image, uint32_t width, uint32_t height, int32_t img_type, uint32_t channels,
+                 uint32_t roi[4]);
 
 /* Synthetic data (seeded, bit-identical on every host) ------------------------ */
 /* Depth maps: background plane U(3000,4000) mm + N(0,5^2) noise, ellipses at

@@ -639,20 +639,28 @@ class RGBLabelsLoader:
         return self.convert(read_pnm(path))
 
 
+_ROI_TYPES = {np.dtype(np.uint8): N.PD_IMG_U8, np.dtype(np.uint16): N.PD_IMG_U16, np.dtype(np.int16): N.PD_IMG_I16,
+              np.dtype(np.int32): N.PD_IMG_I32, np.dtype(np.float32): N.PD_IMG_F32}
+
+
 def image_roi(image: np.ndarray) -> tuple:
     """_extractROI (cv_image_loader_impl.hpp:268-289): (x, y, width, height) of the largest
-    bounding rectangle among the 8-connected components of the nonzero pixels, the one-pixel
-    border counting as zero (pd_image_roi)."""
+    bounding rectangle among the 8-connected components of the pixels whose value is > 0 (the
+    reference's mask img > 0, compared in the image's own type), the one-pixel border counting
+    as zero (pd_image_roi)."""
     a = np.ascontiguousarray(image)
+    if a.dtype not in _ROI_TYPES:
+        raise ValueError(f"image_roi: element type {a.dtype} (supported: {sorted(map(str, _ROI_TYPES))})")
     h, w = a.shape[:2]
+    ch = a.size // max(w * h, 1)
     roi = np.zeros(4, np.uint32)
-    check(lib().pd_image_roi(_ptr(a), w, h, a.nbytes // max(w * h, 1), _ptr(roi)))
+    check(lib().pd_image_roi(_ptr(a), w, h, _ROI_TYPES[a.dtype], ch, _ptr(roi)))
     return tuple(int(v) for v in roi)
 
 
 class PNMImageROILoader(PNMImageLoader):
     """CVImageROILoader (cv_image_loader_impl.hpp:139-186): the image cropped to the ROI of its
-    nonzero pixels; ``roi_x``, ``roi_y`` (getRoiX, getRoiY) give the crop's corner."""
+    pixels > 0; ``roi_x``, ``roi_y`` (getRoiX, getRoiY) give the crop's corner."""
 
     roi_x = roi_y = 0
 

@@ -14,7 +14,7 @@ LIB_PATH = pathlib.Path(os.environ.get("PADENTI_GB300_LIB") or
                         pathlib.Path(__file__).resolve().parent / "_build" / "libpadenti_gb300.so")
 
 PD_OK = 0
-PD_IMG_U8, PD_IMG_U16 = 1, 2
+PD_IMG_U8, PD_IMG_U16, PD_IMG_I16, PD_IMG_I32, PD_IMG_F32 = 1, 2, 3, 4, 5
 PD_FEAT_I16, PD_FEAT_I32 = 1, 2
 PD_PLUGIN_DEPTH_DIFF2, PD_PLUGIN_DEPTH_DIFF1, PD_PLUGIN_CHANNEL_DIFF = 1, 2, 3
 PD_PLUGIN_USER = 100
@@ -139,7 +139,7 @@ _SIGS = {
     "pd_rgb_to_labels": (C.c_int, [_P, C.c_uint32, _P, _P, _P, C.c_uint32, _P, C.c_uint32, _P]),
     "pd_rgb_to_labels_device": (C.c_int, [_P, C.c_uint64, _P, C.c_uint32, _P, C.c_uint32, _P,
                                           C.POINTER(C.c_float)]),
-    "pd_image_roi": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
+    "pd_image_roi": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_int32, C.c_uint32, _P]),
     "pd_synth_depth": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "pd_synth_rgb": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,

@@ -1,10 +1,10 @@
 // pd_split_noalloc: the best-split computation for callers that cannot
 // allocate device memory.
 //
-// Some callers cannot call cudaMalloc at all: code running inside a CUDA graph
-// that is being captured or replayed, a host that hands out only memory it
-// pre-allocated from its own pool, or an embedding runtime whose allocator must
-// not be bypassed.  This entry point takes device pointers for its inputs and
+// Some callers cannot call cudaMalloc at all: a host that hands out only memory
+// it pre-allocated from its own pool, or an embedding runtime whose allocator
+// must not be bypassed (allocating behind its back would break its accounting or
+// its memory limit).  This entry point takes device pointers for its inputs and
 // outputs from the caller and does all its intermediate work in one fixed,
 // file-scope device array, kSplitScratchBytes (32 MiB) in size, which every GPU
 // that loads this library holds until the process exits.
@@ -12,12 +12,18 @@
 // Set-up: the first call on a device (with that device current) looks up the
 // device address of the array with cudaGetSymbolAddress and fills the part of it
 // that holds the exact log2 table; it synchronises the stream it is given.  Make
-// that first call before any stream capture begins.
+// that first call before any stream capture begins.  The address is kept per
+// device for the life of the process, so cudaDeviceReset on a device after its
+// first call is not supported (the array would be reloaded without the table).
+//
+// Limits: every node must hold fewer than 2^20 samples (the log2 table of the
+// array has 2^20 entries), and the per-call working set must fit the array.
 //
 // The array is shared by every call: each call clears the parts that must start
 // at zero, and two calls whose work overlaps on the GPU (for example on two
 // streams, or from two threads) race on it and give wrong results.  Serialise
-// them.
+// them.  Each call reads its error flag back and synchronises its stream before
+// returning.
 #include <cstring>
 #include <mutex>
 
@@ -27,7 +33,7 @@
 namespace pd {
 
 constexpr size_t kSplitScratchBytes = 32ull << 20;
-constexpr uint32_t kNoallocLog2Len = 1u << 20;  // node sample totals below 2^20 - 1
+constexpr uint32_t kNoallocLog2Len = 1u << 20;  // nodes of fewer than 2^20 samples
 constexpr size_t kNoallocLog2Bytes = (size_t)kNoallocLog2Len * sizeof(double);
 
 static __device__ __align__(256) unsigned char g_split_scratch[kSplitScratchBytes];
@@ -167,7 +173,8 @@ extern "C" int pd_split_noalloc(const pd_train_params *params, uint32_t n_classe
   PD_CUDA(cudaMemcpyAsync(&h_err, err, 4, cudaMemcpyDeviceToHost, st));
   PD_CUDA(cudaStreamSynchronize(st));
   PD_CHECK(h_err == 0, PD_ERR_UNSUPPORTED,
-           "pd_split_noalloc: a node holds %u or more samples, beyond the fixed log2 table of the working memory",
-           kNoallocLog2Len - 1);
+           "pd_split_noalloc: a node holds %u (2^20) or more samples; nodes must hold fewer (the fixed log2 table "
+           "of the working memory has %u entries)",
+           kNoallocLog2Len, kNoallocLog2Len);
   return PD_OK;
 }

@@ -1,7 +1,8 @@
 // The crop of the reference's ROI loaders (CVImageROILoader,
 // CVRGBLabelsROILoader; _extractROI at cv_image_loader_impl.hpp:268-289): of the
-// outer contours of the nonzero pixels, the one whose bounding rectangle has
-// the largest area gives the crop.  The outer contours are those of the
+// outer contours of the pixels whose value is > 0 (the reference's mask img > 0,
+// a numeric comparison in the image's element type), the one whose bounding
+// rectangle has the largest area gives the crop.  The outer contours are those of the
 // 8-connected components of the nonzero pixels (a component inside another's
 // hole has a smaller rectangle and never wins), so the rectangle is found here
 // by union-find over the components.  As OpenCV 2's contour tracing does, the
@@ -37,19 +38,32 @@ void unite(std::vector<uint32_t> &p, uint32_t a, uint32_t b) {
 
 }  // namespace
 
-extern "C" int pd_image_roi(const void *image, uint32_t width, uint32_t height, uint32_t pixel_bytes,
-                            uint32_t roi[4]) {
+// Whether element i of the image is > 0 in its own type (a negative value or a
+// negative zero is background).
+static bool positive(const void *px, int img_type, uint64_t i) {
+  switch (img_type) {
+    case PD_IMG_U8: return static_cast<const uint8_t *>(px)[i] > 0;
+    case PD_IMG_U16: return static_cast<const uint16_t *>(px)[i] > 0;
+    case PD_IMG_I16: return static_cast<const int16_t *>(px)[i] > 0;
+    case PD_IMG_I32: return static_cast<const int32_t *>(px)[i] > 0;
+    default: return static_cast<const float *>(px)[i] > 0.0f;
+  }
+}
+
+extern "C" int pd_image_roi(const void *image, uint32_t width, uint32_t height, int32_t img_type,
+                            uint32_t channels, uint32_t roi[4]) {
   if (!image || !roi) return pd::set_error(PD_ERR_INVALID, "null argument");
-  if (width == 0 || height == 0 || pixel_bytes == 0) return pd::set_error(PD_ERR_INVALID, "empty image");
+  if (width == 0 || height == 0 || channels == 0) return pd::set_error(PD_ERR_INVALID, "empty image");
+  if (img_type < PD_IMG_U8 || img_type > PD_IMG_F32)
+    return pd::set_error(PD_ERR_INVALID, "unknown image element type %d", img_type);
   const uint64_t n = (uint64_t)width * height;
   if (n >= (1ull << 32) - 1) return pd::set_error(PD_ERR_UNSUPPORTED, "image of %llu pixels", (unsigned long long)n);
-  const uint8_t *px = static_cast<const uint8_t *>(image);
   const uint32_t none = 0xFFFFFFFFu;
   auto on = [&](uint32_t x, uint32_t y) {
     if (x == 0 || y == 0 || x + 1 >= width || y + 1 >= height) return false;  // the zero border
-    const uint8_t *q = px + ((uint64_t)y * width + x) * pixel_bytes;
-    for (uint32_t b = 0; b < pixel_bytes; b++)
-      if (q[b]) return true;
+    const uint64_t e = ((uint64_t)y * width + x) * channels;
+    for (uint32_t c = 0; c < channels; c++)
+      if (positive(image, img_type, e + c)) return true;
     return false;
   };
   std::vector<uint32_t> parent(n, none);
@@ -85,7 +99,7 @@ extern "C" int pd_image_roi(const void *image, uint32_t width, uint32_t height, 
         if (y > b.y1) b.y1 = y;
       }
     }
-  if (roots.empty()) return pd::set_error(PD_ERR_INVALID, "no nonzero pixel inside the image border");
+  if (roots.empty()) return pd::set_error(PD_ERR_INVALID, "no pixel > 0 inside the image border");
   uint64_t best_area = 0;
   Box best{};
   for (uint32_t r : roots) {  // raster order of the components' first pixels

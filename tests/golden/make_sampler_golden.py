@@ -2,7 +2,7 @@
 UniformImageSampler and ClassWeightedImageSampler return on the images of
 tests/cases.py:sampler_images(), for each configuration of SAMPLER_CONFIGS.
 
-    make -C oracle ref REF=/root/reference && python tests/golden/make_sampler_golden.py
+    make -C oracle ref REF=<Padenti source tree> && python tests/golden/make_sampler_golden.py
 
 The samplers come from the Padenti sources compiled in place
 (oracle/ref_shim/ref_sampler.cpp, over libstdc++'s mt19937, zlib's CRC-32 and

@@ -91,3 +91,64 @@ def test_headers_compile_cleanly_as_c_and_cpp(tmp_path):
         r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Wpedantic", "-Werror", f"-I{inc}",
                             "-fsyntax-only", str(cpp)], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def _compile_cpp(tmp_path, body: str, link: bool = False):
+    import subprocess
+
+    inc = str(HEADER.parent)
+    src = tmp_path / "t.cpp"
+    src.write_text("#include <padenti/cuda_tree_trainer.hpp>\n" + body)
+    cmd = ["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", f"-I{inc}"]
+    if link:
+        lib = N.LIB_PATH
+        cmd += [str(src), "-o", str(tmp_path / "t"), f"-L{lib.parent}", "-lpadenti_gb300",
+                f"-Wl,-rpath,{lib.parent}"]
+    else:
+        cmd += ["-fsyntax-only", str(src)]
+    return subprocess.run(cmd, capture_output=True, text=True)
+
+
+def test_facade_refuses_types_without_kernels(tmp_path):
+    """A float image or feature type does not compile (the reference would throw at run time);
+    the supported types do."""
+    import shutil
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    ok = _compile_cpp(tmp_path, "void f() { CUDATreeTrainer<unsigned short, 1, int, 4, 3> t(1); (void)t; }\n")
+    assert ok.returncode == 0, ok.stderr
+    for img, feat in (("float", "int"), ("unsigned short", "float"), ("int", "int")):
+        r = _compile_cpp(tmp_path, f"void f() {{ CUDATreeTrainer<{img}, 1, {feat}, 4, 3> t(1); (void)t; }}\n")
+        assert r.returncode != 0 and "padenti_gb300:" in r.stderr, (img, feat)
+
+
+def test_facade_use_cpu_overload(tmp_path):
+    """CUDATreeTrainer(path, bool useCPU) is the reference's constructor (cl_tree_trainer.hpp:115):
+    useCPU=true is refused with an error (there is no CPU path), never read as device 1."""
+    import shutil
+    import subprocess
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    body = """#include <cstdio>
+int main() {
+  try {
+    CUDATreeTrainer<unsigned short, 1, int, 4, 3> t(std::string("/nonexistent"), true);
+    return 1;
+  } catch (const std::exception &e) {
+    std::puts(e.what());
+  }
+  try {
+    CUDAClassifier<unsigned short, 1, int, 4, 3> c(std::string("/nonexistent"), true);
+    return 1;
+  } catch (const std::exception &e) {
+    std::puts(e.what());
+  }
+  return 0;
+}
+"""
+    r = _compile_cpp(tmp_path, body, link=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(tmp_path / "t")], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.count("useCPU=true") == 2, out.stdout + out.stderr

@@ -205,7 +205,7 @@ def test_image_roi_matches_flood_fill():
         img = (rng.random((h, w)) < rng.uniform(0.05, 0.5)).astype(np.uint16) * rng.integers(1, 5000, (h, w))
         img = img.astype(np.uint16)
         if not (img[1:-1, 1:-1] != 0).any():
-            with pytest.raises(pg.PadentiError, match="no nonzero pixel"):
+            with pytest.raises(pg.PadentiError, match="no pixel > 0"):
                 pg.image_roi(img)
             continue
         assert pg.image_roi(img) == _roi_by_flood_fill(img != 0), trial
@@ -214,6 +214,28 @@ def test_image_roi_matches_flood_fill():
     img[2:4, 2:4] = 1
     img[6:8, 7:9] = 1
     assert pg.image_roi(img) == (2, 2, 2, 2)
+
+
+def test_image_roi_compares_in_the_element_type():
+    """The reference's mask is img > 0: negative pixels (int16 depth, float) and -0.0f are
+    background, not foreground."""
+    rng = np.random.default_rng(5)
+    for dtype in (np.int16, np.int32, np.float32):
+        for trial in range(10):
+            h, w = int(rng.integers(5, 30)), int(rng.integers(5, 30))
+            img = rng.integers(-3, 3, (h, w)).astype(dtype)
+            if dtype == np.float32:
+                img[img == 0] = -0.0
+            if not (img[1:-1, 1:-1] > 0).any():
+                continue
+            assert pg.image_roi(img) == _roi_by_flood_fill(img > 0), (dtype, trial)
+    # a large negative region beside a small positive one: only the positive one counts
+    img = np.full((12, 12), -5, np.int16)
+    img[0, :] = img[-1, :] = img[:, 0] = img[:, -1] = 0
+    img[3:5, 6:9] = 7
+    assert pg.image_roi(img) == (6, 3, 3, 2)
+    with pytest.raises(ValueError):
+        pg.image_roi(np.ones((4, 4), np.float64))
 
 
 def test_roi_loaders_crop(tmp_path):

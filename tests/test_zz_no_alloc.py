@@ -1,6 +1,6 @@
 """pd_split_noalloc -- the best split for callers that cannot allocate device
-memory (a CUDA graph being captured, a host that only lends memory from its own
-pool).  It works in a fixed array inside the library instead of allocating, and
+memory (a host that only lends memory from its own pool, a runtime whose
+allocator must not be bypassed).  It works in a fixed array inside the library instead of allocating, and
 must give exactly what pd_split gives.  Two calls in a row check that the shared
 array is reset between calls.  This file is collected last on purpose."""
 import ctypes as C
