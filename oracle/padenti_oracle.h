@@ -7,20 +7,26 @@
  * baseline (and its reference arm) may load it.  Nothing in the product
  * links, calls or falls back to it.
  *
- * Parity status:
- *   - MD5 counter RNG (candidate and threshold generation) is pinned against
- *     RFC-1321 known answers (Python hashlib) and against the reference's own
- *     src/padenti/prng.hpp compiled from its source (oracle/ref_shim).
- *   - The split rule is cross-checked against the reference's own
- *     learnBestFeature kernel (kernels/learn_best_feature.cl) compiled as C
- *     from its source (oracle/ref_shim) on the same histograms.
- *   - The single-offset depth plugin is checked against the reference's own
- *     test/feature.cl compiled as C (oracle/ref_shim).
- *   - Everything else (histogram accumulation, finalize, traversal, forest
- *     posterior) is "parity unpinned": the reference needs OpenCL, Boost and
- *     OpenCV, none of which exist here, and its tests hold no golden vectors.
- *     The restatement follows the reference line by line; the cited
- *     file:line of each function names what it follows.
+ * Parity status (each pin compiles the reference's own source here and
+ * compares on the same inputs; oracle/Makefile "ref", oracle/ref_shim):
+ *   - MD5 counter RNG (candidate and threshold generation): RFC-1321 known
+ *     answers (Python hashlib) and the reference's src/padenti/prng.hpp.
+ *   - Histograms (indicator writes + host accumulation), traversal and
+ *     reassignment, split finalize (stored split, child posteriors) and the
+ *     forest posterior: the reference's kernels/hist_update.cl and
+ *     kernels/predict.cl compiled as C through an OpenCL shim and run over
+ *     their NDRanges, with the host steps around them restated from
+ *     cl_tree_trainer_impl_traverse_ts.hpp and cl_classifier_impl.hpp, at
+ *     every depth of trained trees for three features
+ *     (tests/test_reference_kernels.py).
+ *   - The split rule: the reference's learnBestFeature kernel
+ *     (kernels/learn_best_feature.cl) compiled as C, on the same histograms;
+ *     winners agree except at FP32 near-ties of the reference's float gains.
+ *   - The single-offset depth plugin: the reference's test/feature.cl.
+ *   - Arithmetic: IEEE single precision with correctly rounded division,
+ *     where OpenCL allows a less accurate divide and log2.
+ * tests/golden/ref_kernels.npz carries outputs of those reference kernels to
+ * machines without the Padenti sources.
  */
 #ifndef PADENTI_ORACLE_H
 #define PADENTI_ORACLE_H

@@ -309,3 +309,17 @@ def rgb_to_labels(image, colours) -> np.ndarray:
     lib().or_rgb_to_labels(P(img), C.c_uint64(out.size), C.c_uint32(img.shape[2]), P(cmap),
                            C.c_uint32(cmap.size // 3), P(out))
     return out
+
+
+# ------------------------------------------------- reference kernels as C ----
+REF_KERNEL_LIBS = {"depth_diff1": "kernels_dd1", "depth_diff2": "kernels_dd2", "channel_diff": "kernels_chd"}
+
+
+def ref_kernels(plugin: str):
+    """The reference's hist_update.cl and predict.cl compiled as C with the plugin's
+    feature.cl (oracle/ref_shim/ref_hist.c, ref_predict.c); None when absent."""
+    r = ref(REF_KERNEL_LIBS[plugin])
+    if r is not None:
+        r.ref_per_image_hist.restype = C.c_int
+        r.ref_predict_step.restype = C.c_int
+    return r
