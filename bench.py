@@ -66,6 +66,8 @@ def args_():
                    help="run one kernel family alone on --images synthetic images already in device memory "
                         "(--reps times) and print its times: the workload of the sampler and label profiles")
     a.add_argument("--reps", type=int, default=3)
+    a.add_argument("--rgb-images", type=int, default=1000,
+                   help="images of the RGB channel-difference configuration timed beside the headline (0: skip)")
     return a.parse_args()
 
 
@@ -150,34 +152,84 @@ def make_workload(a, rank: int):
     return pg, cfg, ts, tp, (px, lb, sm)
 
 
-def cpu_sample(a, cfg, ts, tp, seconds: float):
-    """Root-depth histogram + split of the first m images, reference-cost oracle on all host cores."""
-    sys.path.insert(0, str(ROOT / "tests"))
-    import oracle_bind as ob
+def root_sample_set(a, m: int, lib_free: bool):
+    """The first m images of the workload as a TrainingSet: from the library's generator, or
+    (lib_free, for the reference arm) from the oracle's byte-identical restatement."""
     import padenti_gb300 as pg
 
+    if lib_free:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_bind as ob
+
+        px, lb, sm = ob.synth_depth(a.seed, m, a.width, a.height, parts=1, min_ellipses=2, max_ellipses=5,
+                                    samples_per_image=a.samples, bg_permille=100)
+    else:
+        px, lb, sm = pg.synth_depth(a.seed, m, a.width, a.height, parts=1, min_ellipses=2, max_ellipses=5,
+                                    samples_per_image=a.samples, bg_permille=100)
+    return pg.TrainingSet(9, [pg.TrainingSetImage(px[i], lb[i], 9, sm[i]) for i in range(m)])
+
+
+def cpu_root(a, cfg, tp, sub, threads):
+    """Root depth (histogram + split) of a training set on the host cores: the oracle in
+    reference-cost mode (MD5 candidates regenerated per (sample, candidate), T comparisons per
+    evaluation, as kernels/hist_update.cl does).  Returns (evals/s, seconds, samples)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_bind as ob
+
+    p = ob.params(cfg, tp)
+    ds = ob.OracleSet(sub, cfg)
+    node = np.zeros(ds.n_samples, np.int32)
+    t0 = time.perf_counter()
+    h = ob.hist(p, ds, 0, node, [0], reference_cost=True, threads=threads)
+    labels = np.concatenate([im.labels.reshape(-1)[im.samples] for im in sub.images]).astype(np.int64) - 1
+    ctot = np.bincount(labels, minlength=9).astype(np.uint32)[None, :]
+    ob.split(p, h, ctot)
+    dt = time.perf_counter() - t0
+    return ds.n_samples * tp.n_features / dt, dt, ds.n_samples
+
+
+def root_sample_text(m, n, tp, dt):
+    return (f"root depth (histogram + split) of the first {m} images ({n} samples x {tp.n_features} candidates x "
+            f"{tp.n_thresholds} thresholds), MD5 candidates regenerated per (sample, candidate) as the reference "
+            f"kernel does; {dt:.1f} s")
+
+
+def cpu_sample(a, cfg, tp, seconds: float, lib_free: bool = False):
+    """The CPU baseline sample: the root depth of as many leading images as fill about `seconds`
+    on all host cores."""
     threads = os.cpu_count() or 1
+    _, dt, _ = cpu_root(a, cfg, tp, root_sample_set(a, 1, lib_free), threads)
+    m = int(max(1, min(a.images, round(seconds / max(dt, 1e-3)))))
+    rate, dt, n = cpu_root(a, cfg, tp, root_sample_set(a, m, lib_free), threads)
+    return dict(value=rate, unit=UNIT, cores=threads, kind="port", sample=root_sample_text(m, n, tp, dt)), m
 
-    def run(m):
-        sub = pg.TrainingSet(9, ts.images[:m])
-        p = ob.params(cfg, tp)
-        ds = ob.OracleSet(sub, cfg)
-        node = np.zeros(ds.n_samples, np.int32)
-        t0 = time.perf_counter()
-        h = ob.hist(p, ds, 0, node, [0], reference_cost=True, threads=threads)
-        labels = np.concatenate([im.labels.reshape(-1)[im.samples] for im in sub.images]).astype(np.int64) - 1
-        ctot = np.bincount(labels, minlength=9).astype(np.uint32)[None, :]
-        ob.split(p, h, ctot)
-        dt = time.perf_counter() - t0
-        return ds.n_samples * tp.n_features / dt, dt, ds.n_samples
 
-    rate, dt, n = run(1)
-    m = int(max(1, min(len(ts.images), round(seconds / max(dt, 1e-3)))))
-    rate, dt, n = run(m)
-    return dict(value=rate, unit=UNIT, cores=threads, kind="port",
-                sample=f"root depth (histogram + split) of the first {m} images ({n} samples x {tp.n_features} "
-                       f"candidates x {tp.n_thresholds} thresholds), MD5 candidates regenerated per "
-                       f"(sample, candidate) as the reference kernel does; {dt:.1f} s"), m
+def gpu_root_sample(a, pg, cfg, tp, m: int, device: int):
+    """The GPU on exactly the CPU baseline's sample: root depth (histogram + split) of the first
+    m images through pd_train_tree with end_depth 2, inputs resident, median of 5 calls (CUDA
+    events around the call on the context's stream)."""
+    import torch
+    from padenti_gb300 import _native as N
+
+    sub = root_sample_set(a, m, False)
+    tr = pg.TreeTrainer(cfg, device=device)
+    tr.upload(sub)
+    stream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(tr.h))
+    times = []
+    for r in range(7):
+        tree = pg.Tree(cfg, 0, 2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        tr.train(tree, sub, tp, 1, 2)
+        e1.record(stream)
+        e1.synchronize()
+        if r >= 2:
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    evals = sub.n_samples * tp.n_features
+    return dict(value=evals / (ms / 1000), unit=UNIT, ms=ms, sample=f"root depth (histogram + split) of the "
+                f"first {m} images ({sub.n_samples} samples x {tp.n_features} candidates x {tp.n_thresholds} "
+                f"thresholds): the cpu_baseline's own sample; pd_train_tree with end_depth 2, median of 5 calls")
 
 
 def profile_dram_per_image(kernel: str):
@@ -367,34 +419,138 @@ def run_only(a):
                               scan_gbs=(st["data_bytes"] + st["label_bytes"]) / st["ms_scan"] / 1e6)))
 
 
-def run_reference(a):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
-    pg, cfg, ts, tp, _ = make_workload(a, 0)
-    base, m = cpu_sample(a, cfg, ts, tp, a.cpu_seconds)
-    times, evals = [], 0
+def rgb_bench(a, pg, device: int):
+    """The RGB configuration: 1000 synthetic 320x240 RGB Voronoi images (21 classes, 2000 samples
+    per image), channel-difference feature, F=1000 x T=30, 5 trees of depth 18 (min 20 samples
+    per leaf), inputs resident; then the 5-tree forest predicts 200 held-out images.  Training
+    evals/s over the forest (CUDA events on the context stream) and prediction Mpix/s, with the
+    oracle's reference-cost root depth on the host cores beside the training rate."""
+    import torch
+    from padenti_gb300 import _native as N
+
+    W, H, n = 320, 240, a.rgb_images
+    px, lb, sm = pg.synth_rgb(a.seed, n, W, H, n_classes=21, samples_per_image=2000)
+    cfg = pg.ForestConfig("channel_diff", 21)
+    ts = pg.training_set(21, px, lb, sm)
+    tp = pg.TreeTrainerParameters(1000, 30, [0, 0, -30, -30, -30, -30], [3, 3, 30, 30, 30, 30], -255, 255, 20)
+    tr = pg.TreeTrainer(cfg, device=device)
+    tr.upload(ts)
+    stream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(tr.h))
+    tr.train(pg.Tree(cfg, 100, 18), ts, tp)  # warm-up
+    trees, evals = [], 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(5):
+        tree = pg.Tree(cfg, k, 18)
+        tr.train(tree, ts, tp)
+        evals += tr.stats()["evals"]
+        trees.append(tree)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = dict(workload="RGB Voronoi forest, 1000x320x240 uint8x3, 21 classes, 2000 samples/image, F=1000, "
+                        "T=30, 5 trees of depth 18, min 20", metric=METRIC, value=evals / (ms / 1000), unit=UNIT,
+               ms_forest=ms, trees=5, evals=evals)
+    clf = pg.Classifier(cfg, device=device)
+    for tr_ in trees:
+        clf << tr_
+    hx, _, _ = pg.synth_rgb(a.seed, 200, W, H, first_image=1_000_000, n_classes=21, samples_per_image=1)
+    dimg = torch.from_numpy(hx.reshape(-1)).cuda()
+    dout = torch.empty((200, 21, H, W), dtype=torch.float32, device="cuda")
+    cstream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(clf.h))
+
+    def pstep():
+        N.check(N.lib().pd_predict_posterior_device(clf.h, 200, dimg.data_ptr(), W, H, None, dout.data_ptr()))
+
+    pstep()
+    N.check(N.lib().pd_ctx_sync(clf.h))
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(cstream)
+    for _ in range(3):
+        pstep()
+    p1.record(cstream)
+    N.check(N.lib().pd_ctx_sync(clf.h))
+    pms = p0.elapsed_time(p1) / 3
+    peak, _ = measured_peaks()
+    bytes_alg = 200 * W * H * (3 + 21 * 4)
+    out["predict"] = dict(metric="predict Mpix/s", value=200 * W * H / (pms / 1000) / 1e6, unit="Mpix/s",
+                          images=200, ms_per_batch=pms,
+                          roofline=dict(kernel="k_predict_posterior", bound="hbm",
+                                        achieved=bytes_alg / (pms / 1000) / 1e9, peak=peak, unit="GB/s",
+                                        frac=bytes_alg / (pms / 1000) / 1e9 / peak,
+                                        algorithmic_bytes_per_launch=bytes_alg,
+                                        note="87 algorithmic B/px: 3 RGB bytes in, 21 float posteriors out"))
+    del dimg, dout
+    if not a.no_cpu:
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_bind as ob
+
+        m = 4
+        sub = pg.TrainingSet(21, ts.images[:m])
+        p = ob.params(cfg, tp)
+        ds = ob.OracleSet(sub, cfg)
+        node = np.zeros(ds.n_samples, np.int32)
+        t0 = time.perf_counter()
+        ob.hist(p, ds, 0, node, [0], reference_cost=True, threads=os.cpu_count() or 1)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = dict(value=ds.n_samples * tp.n_features / dt, unit=UNIT, cores=os.cpu_count() or 1,
+                                   kind="port", sample=f"root histogram of the first {m} images ({ds.n_samples} "
+                                   f"samples x 1000 candidates x 30 thresholds), reference-cost oracle; {dt:.1f} s")
+    return out
+
+
+def cpu_predict(a, cfg, trees, hx):
+    """The oracle's forest posterior (cl_classifier_impl.hpp:356-557 restated) on all host cores
+    over the first held-out images, about 10 s of work: Mpix/s."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_bind as ob
 
-    sub = pg.TrainingSet(9, ts.images[:m])
+    import padenti_gb300 as pg
+
+    tp = pg.TreeTrainerParameters(a.features, a.thresholds, [-60000] * 4, [60000] * 4, -500, 500, a.min_leaf)
     p = ob.params(cfg, tp)
-    ds = ob.OracleSet(sub, cfg)
-    node = np.zeros(ds.n_samples, np.int32)
-    labels = np.concatenate([im.labels.reshape(-1)[im.samples] for im in sub.images]).astype(np.int64) - 1
-    ctot = np.bincount(labels, minlength=9).astype(np.uint32)[None, :]
+    tt = [(t.depth, t.left_child, np.asarray(t.features, np.int32), np.asarray(t.thresholds, np.int32), t.posteriors)
+          for t in trees]
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ob.predict_posterior(p, hx[0], None, tt, threads=threads)
+    one = time.perf_counter() - t0
+    m = int(max(1, min(len(hx), round(10.0 / max(one, 1e-3)))))
+    t0 = time.perf_counter()
+    for i in range(m):
+        ob.predict_posterior(p, hx[i], None, tt, threads=threads)
+    dt = time.perf_counter() - t0
+    px = m * hx.shape[1] * hx.shape[2]
+    return dict(value=px / dt / 1e6, unit="Mpix/s", cores=threads, kind="port",
+                sample=f"the first {m} held-out images through the {len(tt)}-tree forest, oracle restatement of "
+                       f"the reference's per-tree traversal and posterior sum on all host cores; {dt:.1f} s")
+
+
+def run_reference(a):
+    """The reference algorithm on the host cores (the oracle port in reference-cost mode), on a
+    bounded sample of the workload: the root depth of the first m images.  Its inputs come from
+    the oracle's restatement of the synthetic generator, so the CUDA library is never loaded."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import padenti_gb300 as pg
+
+    cfg = pg.ForestConfig("depth_diff2", 9)
+    tp = pg.TreeTrainerParameters(a.features, a.thresholds, [-60000] * 4, [60000] * 4, -500, 500, a.min_leaf)
+    base, m = cpu_sample(a, cfg, tp, a.cpu_seconds, lib_free=True)
+    sub = root_sample_set(a, m, True)
+    times, evals, n = [], 0, 0
     for _ in range(a.steps):
-        t0 = time.perf_counter()
-        h = ob.hist(p, ds, 0, node, [0], reference_cost=True, threads=base["cores"])
-        ob.split(p, h, ctot)
-        times.append(time.perf_counter() - t0)
-        evals += ds.n_samples * tp.n_features
+        rate, dt, n = cpu_root(a, cfg, tp, sub, base["cores"])
+        times.append(dt)
+        evals += n * tp.n_features
     value = evals / sum(times)
     base["value"] = value
+    base["sample"] = root_sample_text(m, n, tp, sum(times) / len(times))
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=a.gpus, steps=a.steps, warmup=a.warmup,
                 ms_per_step=1000 * sum(times) / len(times), higher_is_better=True, scaling="weak", vs_baseline=None,
-                dtype="int32", data="synthetic", impl="reference",
-                config=dict(workload=WORKLOAD, sample=base["sample"]), cpu_baseline=base,
+                dtype="int32", data="synthetic (the oracle's restatement of the seeded generator)", impl="reference",
+                config=dict(workload=WORKLOAD, sample=base["sample"], sample_images=m), cpu_baseline=base,
                 e2e=dict(value=value, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line), flush=True)
 
@@ -549,10 +705,20 @@ def run_ours(a):
         pms = pe0.elapsed_time(pe1) / reps
         px_total = n_p * a.width * a.height
         bytes_alg = px_total * (2 + 9 * 4)
+        peak_p, peak_kind_p = measured_peaks()
         pred = dict(metric="predict Mpix/s", value=px_total / (pms / 1000) / 1e6, unit="Mpix/s",
                     images=n_p, trees=len(trees), ms_per_batch=pms,
-                    hbm_gbs=bytes_alg / (pms / 1000) / 1e9,
+                    roofline=dict(kernel="k_predict_posterior", bound="hbm",
+                                  achieved=bytes_alg / (pms / 1000) / 1e9, peak=peak_p, unit="GB/s",
+                                  frac=bytes_alg / (pms / 1000) / 1e9 / peak_p,
+                                  algorithmic_bytes_per_launch=bytes_alg,
+                                  traffic=None, peak_source=f"{peak_kind_p} (hbm_gbs)",
+                                  note="38 algorithmic B/px: the 2-byte depth read once and 9 float posteriors "
+                                       "written once; the forest's nodes stay in L2; the kernel is bound by "
+                                       "instruction issue (tree walks), not HBM"),
                     note="500 held-out 640x480 images in one launch, forest of the timed trees, 38 algorithmic B/px")
+        if not a.no_cpu:
+            pred["cpu_baseline"] = cpu_predict(a, cfg, trees, hx)
         del dimg, dout
         # mixed-size serving batch: 256 images, a third each of 160x120,
         # 320x240 and 640x480, host buffers in and out, one graph-replayed launch per batch
@@ -588,6 +754,7 @@ def run_ours(a):
                                         "CUDA-graph replay of the batch kernel, posteriors out; wall clock")
 
     samp = sampler_bench(a, pg, N, px, lb) if a.sampler_images > 0 else None
+    rgb = rgb_bench(a, pg, local) if a.rgb_images > 0 else None
     if samp is not None:
         samp["label_images"] = loader_bench(a, pg, N)
 
@@ -619,9 +786,21 @@ def run_ours(a):
                           note="achieved = live evaluations/s x instruction slots per evaluation from "
                                "profiles/k_hist_issue_300x640x480.json; peak = SMs x 4 schedulers x 32 lanes x the "
                                "median SM clock sampled during the timed region")
-    base = None
+    atomic_roof = None
+    if hist_s > 0:
+        rate = C.c_double()
+        ctas = C.c_int32()
+        if N.lib().pd_measure_smem_atomics(local, C.byref(rate), C.byref(ctas)) == 0 and rate.value > 0:
+            ach = evals / hist_s
+            atomic_roof = dict(bound="smem_atomic", kernel="k_hist", achieved=ach, peak=rate.value, unit="adds/s",
+                               frac=ach / rate.value, adds_per_eval=1, peak_ctas_per_sm=ctas.value,
+                               note="one conflict-free shared-memory atomic add per evaluation; peak = "
+                                    "pd_measure_smem_atomics (the same add in the same [class][rank][lane] "
+                                    "layout, 8 in flight per thread, best of 2/4/8 CTAs per SM), CUDA events")
+    base = same = None
     if not a.no_cpu:
-        base, _ = cpu_sample(a, cfg, ts, tp, a.cpu_seconds)
+        base, m = cpu_sample(a, cfg, tp, a.cpu_seconds)
+        same = gpu_root_sample(a, pg, cfg, tp, m, local)
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=a.steps, warmup=a.warmup,
                 ms_per_step=ms / a.steps, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="int32",
                 data="synthetic (seeded depth maps generated on the host; see config)",
@@ -632,7 +811,8 @@ def run_ours(a):
                             cand_order=1 if a.cand_order is None else a.cand_order,
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
-                roofline=roof, roofline_issue=issue_roof, cpu_baseline=base, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
+                roofline=roof, roofline_issue=issue_roof, roofline_atomic=atomic_roof, cpu_baseline=base,
+                gpu_on_cpu_sample=same, rgb_config=rgb, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
                 predict=pred, sampler=samp, phases_per_step={k: v / a.steps for k, v in phases.items()}, impl="ours")
     print(json.dumps(line), flush=True)
 

@@ -342,6 +342,15 @@ int pd_rgb_to_labels_device(pd_ctx *ctx, uint64_t n_pixels, const uint8_t *src_d
 int pd_image_roi(const void *image, uint32_t width, uint32_t height, int32_t img_type, uint32_t channels,
                  uint32_t roi[4]);
 
+/* Measurement ------------------------------------------------------------------ */
+/* The rate (adds/s) at which GPU `device` retires conflict-free shared-memory
+ * atomic adds -- the histogram kernel's one add per evaluation, in its
+ * [class][rank][lane] layout -- measured with CUDA events at 2, 4 and 8 CTAs of
+ * 256 threads per SM; the best rate and its CTAs per SM are returned.  No
+ * counterpart in the reference (it is the ceiling the histogram kernel is
+ * reported against). */
+int pd_measure_smem_atomics(int device, double *adds_per_s, int32_t *best_ctas_per_sm);
+
 /* Synthetic data (seeded, bit-identical on every host) ------------------------ */
 /* Depth maps: background plane U(3000,4000) mm + N(0,5^2) noise, ellipses at
  * U(800,2500) mm.  parts=0: 3 classes (bg, left half, right half of each

@@ -349,32 +349,53 @@ int or_hist(const or_params *p, const or_dataset *ds, uint32_t tree_id,
       or_candidate(p, tree_id, (uint32_t)nodes[q / F], (uint32_t)(q % F), cf + (size_t)q * D, ct + (size_t)q * T);
   }
 
+  /* the active samples grouped by slot (stable counting sort): one (slot, f)
+   * work item then counts its samples into a private K x T block and writes
+   * the column once (no writes shared between threads) */
+  uint64_t *slot_off = (uint64_t *)calloc((size_t)n_nodes + 1, sizeof(uint64_t));
+  uint64_t *by_slot = (uint64_t *)malloc(sizeof(uint64_t) * (n_act ? n_act : 1));
+  for (uint64_t a = 0; a < n_act; a++) slot_off[act_slot[a] + 1]++;
+  for (uint32_t i = 0; i < n_nodes; i++) slot_off[i + 1] += slot_off[i];
+  {
+    uint64_t *pos = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)n_nodes + 1));
+    memcpy(pos, slot_off, sizeof(uint64_t) * ((size_t)n_nodes + 1));
+    for (uint64_t a = 0; a < n_act; a++) by_slot[pos[act_slot[a]]++] = act[a];
+    free(pos);
+  }
 #pragma omp parallel NT(n_threads)
   {
     int32_t feat[OR_MAX_FEAT_DIM];
     int32_t *thr = (int32_t *)malloc(sizeof(int32_t) * (T ? T : 1));
-#pragma omp for schedule(dynamic, 4)
-    for (int64_t f = 0; f < (int64_t)F; f++) {
-      for (uint64_t a = 0; a < n_act; a++) {
-        const sample_t *sm = &smp[act[a]];
-        uint32_t slot = act_slot[a];
-        const int32_t *fv, *tv;
+    uint32_t *loc = (uint32_t *)malloc(sizeof(uint32_t) * ((size_t)K * T + 1));
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t q = 0; q < (int64_t)n_nodes * F; q++) {
+      const uint32_t slot = (uint32_t)(q / F), f = (uint32_t)(q % F);
+      if (slot_off[slot] == slot_off[slot + 1]) continue;
+      memset(loc, 0, sizeof(uint32_t) * (size_t)K * T);
+      const int32_t *fv = NULL, *tv = NULL;
+      if (!reference_cost) {
+        fv = cf + ((size_t)slot * F + (size_t)f) * D;
+        tv = ct + ((size_t)slot * F + (size_t)f) * T;
+      }
+      for (uint64_t a = slot_off[slot]; a < slot_off[slot + 1]; a++) {
+        const sample_t *sm = &smp[by_slot[a]];
         if (reference_cost) {
           /* the reference kernel regenerates both MD5 chains per (sample, f) */
-          or_candidate(p, tree_id, (uint32_t)nodes[slot], (uint32_t)f, feat, thr);
+          or_candidate(p, tree_id, (uint32_t)nodes[slot], f, feat, thr);
           fv = feat; tv = thr;
-        } else {
-          fv = cf + ((size_t)slot * F + (size_t)f) * D;
-          tv = ct + ((size_t)slot * F + (size_t)f) * T;
         }
         int32_t r = or_feature(p->plugin, p->feat_type, image_ptr(ds, sm->img), ds->width[sm->img],
                                ds->height[sm->img], ds->n_channels, sm->x, sm->y, fv);
-        uint32_t *hp = hist + (((size_t)slot * K + sm->label) * T) * F + (size_t)f;
-        for (uint32_t t = 0; t < T; t++) hp[(size_t)t * F] += (uint32_t)(r <= tv[t]);
+        uint32_t *lp = loc + (size_t)sm->label * T;
+        for (uint32_t t = 0; t < T; t++) lp[t] += (uint32_t)(r <= tv[t]);
       }
+      uint32_t *hp = hist + ((size_t)slot * K * T) * F + (size_t)f;
+      for (size_t i = 0; i < (size_t)K * T; i++) hp[i * F] = loc[i];
     }
     free(thr);
+    free(loc);
   }
+  free(slot_off); free(by_slot);
   free(cf); free(ct);
   free(act); free(act_slot); free(map); free(smp);
   return 0;
@@ -430,8 +451,14 @@ int or_split(const or_params *p, const uint32_t *hist, const uint32_t *class_tot
              int32_t *out_t, int32_t *out_f, double *out_gain,
              float *out_gain32_max, double *out_max_abs_err) {
   const uint32_t F = p->n_features, T = p->n_thresholds, K = (uint32_t)p->n_classes;
+  /* the FP32 reference formula only when its maximum or error is asked for */
+  const int fp32 = out_gain32_max != NULL || out_max_abs_err != NULL;
   int rc = 0;
-  for (uint32_t i = 0; i < n_nodes; i++) {
+  double maxerr_all = 0.0;
+  /* nodes are independent; the per-node results do not depend on the schedule */
+#pragma omp parallel for schedule(dynamic, 1) reduction(min : rc) reduction(max : maxerr_all)
+  for (int64_t ii = 0; ii < (int64_t)n_nodes; ii++) {
+    const uint32_t i = (uint32_t)ii;
     const uint32_t *tot = class_tot + (size_t)i * K;
     uint64_t N = 0;
     for (uint32_t l = 0; l < K; l++) N += tot[l];
@@ -440,7 +467,7 @@ int or_split(const or_params *p, const uint32_t *hist, const uint32_t *class_tot
     if (N == 0) continue;
     if (N >= table_len) { rc = -1; continue; }
     double hp = sum64(tot, K, N, L) / (double)N;
-    float hp32 = ent32(tot, K, N);
+    float hp32 = fp32 ? ent32(tot, K, N) : 0.0f;
     double best = 0.0;
     float best32 = 0.0f;
     double maxerr = 0.0;
@@ -455,18 +482,21 @@ int or_split(const or_params *p, const uint32_t *hist, const uint32_t *class_tot
           nL += cl[l]; nR += cr[l];
         }
         double g = gain64(cl, cr, K, N, nL, nR, hp, L);
-        float hl32 = ent32(cl, K, nL), hr32 = ent32(cr, K, nR);
-        float g32 = hp32 - ((float)nL / (float)N * hl32 + (float)nR / (float)N * hr32);
-        double err = fabs((double)g32 - g);
-        if (err > maxerr) maxerr = err;
+        if (fp32) {
+          float hl32 = ent32(cl, K, nL), hr32 = ent32(cr, K, nR);
+          float g32 = hp32 - ((float)nL / (float)N * hl32 + (float)nR / (float)N * hr32);
+          double err = fabs((double)g32 - g);
+          if (err > maxerr) maxerr = err;
+          if ((t == 0 && f == 0) || g32 > best32) best32 = g32;
+        }
         if (!have || g > best) { best = g; out_t[i] = (int32_t)t; out_f[i] = (int32_t)f; have = 1; }
-        if ((t == 0 && f == 0) || g32 > best32) best32 = g32;
       }
     }
     out_gain[i] = best;
     if (out_gain32_max) out_gain32_max[i] = best32;
-    if (out_max_abs_err && maxerr > *out_max_abs_err) *out_max_abs_err = maxerr;
+    if (maxerr > maxerr_all) maxerr_all = maxerr;
   }
+  if (out_max_abs_err && maxerr_all > *out_max_abs_err) *out_max_abs_err = maxerr_all;
   return rc;
 }
 

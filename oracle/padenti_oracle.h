@@ -161,6 +161,12 @@ void or_sample_batch(int kind, const void *images, uint64_t data_bytes, const ui
                      uint32_t n_images, uint32_t n_samples, uint32_t n_classes, const uint32_t *sizes,
                      uint32_t seed, uint32_t stride, uint32_t *out, int64_t *counts);
 
+/* The benchmark's seeded synthetic depth maps (synth.c): the same bytes as the
+ * library's pd_synth_depth, for callers that must not load the library. */
+int or_synth_depth(uint64_t seed, uint32_t first_image, uint32_t n_images, uint32_t width, uint32_t height,
+                   uint32_t min_ellipses, uint32_t max_ellipses, uint32_t parts, uint32_t samples_per_image,
+                   uint32_t bg_permille, uint16_t *pixels, uint8_t *labels, uint32_t *samples);
+
 /* Label images (image_loader.c): _rgb2label. */
 void or_rgb_to_labels(const uint8_t *src, uint64_t n_pix, uint32_t channels, const uint8_t *map, uint32_t n_classes,
                       uint8_t *dst);

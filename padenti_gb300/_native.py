@@ -140,6 +140,7 @@ _SIGS = {
     "pd_rgb_to_labels_device": (C.c_int, [_P, C.c_uint64, _P, C.c_uint32, _P, C.c_uint32, _P,
                                           C.POINTER(C.c_float)]),
     "pd_image_roi": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_int32, C.c_uint32, _P]),
+    "pd_measure_smem_atomics": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
     "pd_synth_depth": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P]),
     "pd_synth_rgb": (C.c_int, [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32,

@@ -323,3 +323,18 @@ def ref_kernels(plugin: str):
         r.ref_per_image_hist.restype = C.c_int
         r.ref_predict_step.restype = C.c_int
     return r
+
+
+def synth_depth(seed: int, n_images: int, width: int, height: int, *, first_image: int = 0, min_ellipses: int = 1,
+                max_ellipses: int = 3, parts: int = 0, samples_per_image: int = 500, bg_permille: int = 100):
+    """The benchmark's seeded depth maps from the oracle's restatement (synth.c), without the
+    CUDA library: the same bytes as padenti_gb300.synth_depth."""
+    px = np.zeros((n_images, height, width), np.uint16)
+    lb = np.zeros((n_images, height, width), np.uint8)
+    sm = np.zeros((n_images, samples_per_image), np.uint32)
+    rc = lib().or_synth_depth(C.c_uint64(seed), C.c_uint32(first_image), C.c_uint32(n_images), C.c_uint32(width),
+                              C.c_uint32(height), C.c_uint32(min_ellipses), C.c_uint32(max_ellipses),
+                              C.c_uint32(parts), C.c_uint32(samples_per_image), C.c_uint32(bg_permille), P(px),
+                              P(lb), P(sm))
+    assert rc == 0
+    return px, lb, sm

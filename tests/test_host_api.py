@@ -88,3 +88,17 @@ def test_bench_reads_the_committed_profile_figures():
     for k in ("k_sample_scan", "k_rgb_to_labels"):
         assert 0.5e6 < b.profile_dram_per_image(k) < 2e6
     assert b.profile_dram_per_image("no_such_kernel") is None
+
+
+def test_oracle_synth_equals_library_synth():
+    """The oracle's restatement of the synthetic depth maps (used where the CUDA library must not
+    be loaded) gives the library's bytes."""
+    import oracle_bind as ob
+
+    for kw in (dict(parts=1, min_ellipses=2, max_ellipses=5, samples_per_image=2000, bg_permille=100),
+               dict(parts=0, samples_per_image=500, first_image=7), dict(parts=1, samples_per_image=37,
+                                                                          bg_permille=0)):
+        a = pg.synth_depth(3, 4, 97, 61, **kw)
+        b = ob.synth_depth(3, 4, 97, 61, **kw)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), kw
