@@ -62,7 +62,12 @@ def args_():
     a.add_argument("--fuse-max", type=int, default=None, help="largest node (samples) with the fused split")
     a.add_argument("--cand-order", type=int, default=None, choices=(0, 1),
                    help="1: candidate columns ordered by first-probe offset (default), 0: index order")
-    a.add_argument("--only", default=None, choices=["sampler_uniform", "sampler_class_weighted", "labels"],
+    a.add_argument("--learned", type=int, default=1, help="1: time the learned-proposal forest beside the plain one")
+    a.add_argument("--fit-steps", type=int, default=400)
+    a.add_argument("--fit-batch", type=int, default=4096)
+    a.add_argument("--fit-lr", type=float, default=2e-3)
+    a.add_argument("--only", default=None,
+                   choices=["sampler_uniform", "sampler_class_weighted", "labels", "learned"],
                    help="run one kernel family alone on --images synthetic images already in device memory "
                         "(--reps times) and print its times: the workload of the sampler and label profiles")
     a.add_argument("--reps", type=int, default=3)
@@ -499,6 +504,99 @@ def rgb_bench(a, pg, device: int):
     return out
 
 
+def forest_accuracy(pg, cfg, trees, device, hx, hl):
+    """Held-out per-pixel accuracy of a forest (argmax of the posterior against the labels):
+    over all pixels, and over the object (non-background) pixels."""
+    clf = pg.Classifier(cfg, device=device)
+    for t in trees:
+        clf << t
+    ok = fg_ok = fg = tot = 0
+    for i in range(len(hx)):
+        post = clf.predict(hx[i])
+        pred = np.argmax(post, axis=0) + 1
+        lab = hl[i]
+        ok += int((pred == lab).sum())
+        tot += lab.size
+        m = lab > 1
+        fg_ok += int((pred[m] == lab[m]).sum())
+        fg += int(m.sum())
+    return ok / tot, fg_ok / max(fg, 1)
+
+
+def learned_bench(a, pg, cfg, ts, tp, device):
+    """Learned candidate proposals on the depth configuration (no reference counterpart):
+    the plain 3-tree forest (2000 uniform candidates per node) against the learned one -- tree 0
+    plain with records, the proposal network fitted to them on the GPU, trees 1 and 2 with 250
+    proposed + 50 uniform candidates per node -- and, as the method without the network, trees 1
+    and 2 with 300 uniform candidates.  Training time is the GPU time of each forest (trees and
+    fit, CUDA events on the context stream); accuracy is per pixel over held-out images."""
+    import torch
+    from padenti_gb300 import _native as N
+
+    tr = pg.TreeTrainer(cfg, device=device)
+    tr.upload(ts)
+    stream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(tr.h))
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return r, e0.elapsed_time(e1)
+
+    tr.train(pg.Tree(cfg, 90, a.depth), ts, tp)  # warm-up
+    plain, ms_plain = [], 0.0
+    for k in range(3):
+        t = pg.Tree(cfg, k, a.depth)
+        if k == 0:
+            tr.set_tuning("records", 1)
+        _, ms = timed(lambda: tr.train(t, ts, tp))
+        if k == 0:
+            tr.set_tuning("records", 0)
+            rec = tr.records()
+            ms_tree0 = ms
+        plain.append(t)
+        ms_plain += ms
+    tp300 = pg.TreeTrainerParameters(300, tp.n_thresholds, tp.feat_low_bounds, tp.feat_up_bounds, tp.thr_low_bound,
+                                     tp.thr_up_bound, tp.per_leaf_samples_thr)
+    net = pg.ProposalNetwork(tr, tp300, seed=a.seed)
+    fit = net.fit(rec[:1], steps=1, batch=a.fit_batch, lr=a.fit_lr)  # warm-up (graph capture)
+    net = pg.ProposalNetwork(tr, tp300, seed=a.seed)
+    fit, ms_fit = timed(lambda: net.fit(rec, steps=a.fit_steps, batch=a.fit_batch, lr=a.fit_lr))
+    learned, ms_learned = [plain[0]], ms_tree0 + ms_fit
+    for k in (1, 2):
+        t = pg.Tree(cfg, k, a.depth)
+        _, ms = timed(lambda: tr.train_proposed(t, ts, tp300, net, 250))
+        learned.append(t)
+        ms_learned += ms
+    uni, ms_uni = [plain[0]], ms_tree0
+    for k in (1, 2):
+        t = pg.Tree(cfg, k, a.depth)
+        _, ms = timed(lambda: tr.train(t, ts, tp300))
+        uni.append(t)
+        ms_uni += ms
+    hx, hl, _ = pg.synth_depth(a.seed, 100, a.width, a.height, first_image=5_000_000, parts=1, min_ellipses=2,
+                               max_ellipses=5, samples_per_image=1)
+    acc = {name: forest_accuracy(pg, cfg, f, device, hx, hl) for name, f in
+           (("plain", plain), ("learned", learned), ("uniform300", uni))}
+    return dict(
+        metric="learned vs plain time at same accuracy", unit="ratio of GPU training times",
+        value=ms_learned / ms_plain, higher_is_better=False,
+        plain=dict(ms=ms_plain, accuracy=acc["plain"][0], object_accuracy=acc["plain"][1], candidates=tp.n_features),
+        learned=dict(ms=ms_learned, ms_tree0=ms_tree0, ms_fit=ms_fit, accuracy=acc["learned"][0],
+                     object_accuracy=acc["learned"][1], records=int(len(rec)), proposed=250, uniform=50,
+                     fit_steps=a.fit_steps, fit_batch=a.fit_batch, first_loss=float(fit["loss"][0]),
+                     last_loss=float(fit["loss"][-10:].mean())),
+        uniform300=dict(ms=ms_uni, accuracy=acc["uniform300"][0], object_accuracy=acc["uniform300"][1]),
+        accuracy_gap_pt=100 * (acc["plain"][0] - acc["learned"][0]),
+        network_gain_pt=100 * (acc["learned"][0] - acc["uniform300"][0]),
+        held_out="100 synthetic 640x480 images of the same generator (not trained on)",
+        note="tree 0 is the plain tree in both forests; the learned forest's time counts it, the fit and "
+             "trees 1-2")
+
+
 def cpu_predict(a, cfg, trees, hx):
     """The oracle's forest posterior (cl_classifier_impl.hpp:356-557 restated) on all host cores
     over the first held-out images, about 10 s of work: Mpix/s."""
@@ -753,6 +851,7 @@ def run_ours(a):
                                         "pd_predict_posterior_batch from host buffers: per-image copies in, one "
                                         "CUDA-graph replay of the batch kernel, posteriors out; wall clock")
 
+    learned = learned_bench(a, pg, cfg, ts, tp, local) if a.learned and world == 1 else None
     samp = sampler_bench(a, pg, N, px, lb) if a.sampler_images > 0 else None
     rgb = rgb_bench(a, pg, local) if a.rgb_images > 0 else None
     if samp is not None:
@@ -812,14 +911,19 @@ def run_ours(a):
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
                 roofline=roof, roofline_issue=issue_roof, roofline_atomic=atomic_roof, cpu_baseline=base,
-                gpu_on_cpu_sample=same, rgb_config=rgb, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
+                gpu_on_cpu_sample=same, rgb_config=rgb, learned_proposals=learned, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
                 predict=pred, sampler=samp, phases_per_step={k: v / a.steps for k, v in phases.items()}, impl="ours")
     print(json.dumps(line), flush=True)
 
 
 def main():
     a = args_()
-    if a.only:
+    if a.only == "learned":
+        import padenti_gb300 as pg
+
+        pg_, cfg, ts, tp, _ = make_workload(a, 0)
+        print(json.dumps(learned_bench(a, pg, cfg, ts, tp, 0)), flush=True)
+    elif a.only:
         run_only(a)
     elif a.impl == "reference":
         run_reference(a)

@@ -169,7 +169,8 @@ int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
  *               order of the candidates' first probe offsets (n_features <= 8192),
  *               so that neighbouring lanes probe neighbouring pixels; 0: index order;
  *   "sample_group" bytes of images and labels pd_sample stages per round trip,
- *               >= 4096 (default 512 MiB). */
+ *               >= 4096 (default 512 MiB);
+ *   "records"   1: training calls keep one pd_record per split node (pd_train_records); 0 (default): none. */
 int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value);
 /* Synchronises the context's stream. */
 int pd_ctx_sync(pd_ctx *ctx);
@@ -233,6 +234,65 @@ int pd_split_noalloc(const pd_train_params *params, uint32_t n_classes, const ui
                      int32_t *out_f_device, double *out_gain_device, void *stream);
 /* Exact per-integer log2 table used by the split: out[n] = log2(n), out[0]=0. */
 int pd_log2_table(pd_ctx *ctx, uint32_t n, double *out);
+
+/* Learned candidate proposals ------------------------------------------------
+ * No counterpart in the reference, which draws every candidate uniformly
+ * (kernels/hist_update.cl:62-184).  The plain trainer emits one record per
+ * node it splits; a proposal network (a BF16 MLP: the node's depth, log-count
+ * and class frequencies in, three hidden layers of 256 with GELU, a
+ * 16-component Gaussian mixture over the normalised feature values and
+ * threshold out) is fitted to them on the GPU; a tree trained with it draws
+ * the first n_proposed of each node's n_features candidates (and each one's
+ * thresholds) from the mixture and the rest uniformly as the reference does.
+ * Every candidate is still scored by the exact histogram and split kernels. */
+typedef struct pd_record {
+  uint32_t depth;      /* level of the node (root = 1) */
+  uint32_t count;      /* samples at the node */
+  uint32_t node;       /* heap index */
+  uint32_t tree;
+  double gain;         /* exact gain of the winning split */
+  int32_t feat[PD_MAX_FEAT_DIM];  /* the winner's feature values */
+  int32_t thr;         /* the winner's threshold */
+  uint32_t class_count[PD_MAX_CLASSES];
+} pd_record;
+
+/* Records of the last pd_train_tree / pd_train_tree_proposed call of a context
+ * whose tuning "records" is 1: one per split node, in training order.  Writes
+ * min(cap, available) records to out (may be NULL to query) and the number
+ * available to *n. */
+int pd_train_records(pd_ctx *ctx, pd_record *out, uint64_t cap, uint64_t *n);
+
+typedef struct pd_proposer pd_proposer;
+/* A proposal network for the context's configuration (classes, FeatDim) and the
+ * value ranges of `bounds` (feature and threshold bounds), with parameters
+ * initialised from `seed`.  It runs on the context's GPU and stream. */
+int pd_proposer_create(pd_ctx *ctx, const pd_train_params *bounds, uint64_t seed, pd_proposer **out);
+int pd_proposer_destroy(pd_proposer *p);
+/* dims = {input width, hidden width, hidden layers, output width, mixture
+ * components, drawn dimensions}; *n_params = length of the parameter vector. */
+int pd_proposer_dims(pd_proposer *p, uint32_t dims[6], uint64_t *n_params);
+/* The FP32 parameter vector (W1 [H][IN], b1, W2 [H][H], b2, W3 [H][H], b3,
+ * Wo [OUT][H], bo); setting it resets the optimiser state. */
+int pd_proposer_get_params(pd_proposer *p, float *out);
+int pd_proposer_set_params(pd_proposer *p, const float *in);
+/* Network outputs of n input rows (host buffers: x [n][IN], out [n][OUT]). */
+int pd_proposer_forward(pd_proposer *p, const float *x, uint32_t n, float *out);
+/* Weighted mean mixture negative log-likelihood of targets y [n][DY] (w [n] or
+ * NULL for equal weights) and its gradient with respect to the parameter
+ * vector (grad: n_params floats); the parameters do not change. */
+int pd_proposer_loss_grad(pd_proposer *p, const float *x, const float *y, const float *w, uint32_t n, float *loss,
+                          float *grad);
+/* Fits the network to n records with Adam (steps steps of `batch` records drawn
+ * with replacement, learning rate lr); loss (steps floats, may be NULL) gets
+ * the batch loss of every step, *ms (may be NULL) the GPU time of the fit. */
+int pd_proposer_fit(pd_proposer *p, const pd_record *records, uint64_t n, uint32_t steps, uint32_t batch, float lr,
+                    float *loss, float *ms);
+/* pd_train_tree with learned proposals: candidates f < n_proposed of every node
+ * are drawn from the network's mixture for that node, f >= n_proposed are the
+ * reference's uniform MD5 candidates (params->n_features in total). */
+int pd_train_tree_proposed(pd_ctx *ctx, pd_proposer *p, const pd_train_params *params, uint32_t n_proposed,
+                           uint32_t tree_id, uint32_t start_depth, uint32_t end_depth, const float *root_prior,
+                           int32_t *left_child, void *features, void *thresholds, float *posteriors);
 
 /* Classifier (cl_classifier_impl.hpp) ---------------------------------------- */
 int pd_forest_clear(pd_ctx *ctx);

@@ -167,6 +167,15 @@ int or_synth_depth(uint64_t seed, uint32_t first_image, uint32_t n_images, uint3
                    uint32_t min_ellipses, uint32_t max_ellipses, uint32_t parts, uint32_t samples_per_image,
                    uint32_t bg_permille, uint16_t *pixels, uint8_t *labels, uint32_t *samples);
 
+/* The proposal network of learned proposals (proposal.c): network outputs of
+ * n rows, and the weighted-mean mixture loss with its gradient with respect to
+ * the FP32 parameter vector (grad: double, one per parameter).  bf16 = 1
+ * rounds to BF16 where the GPU stores BF16. */
+int or_prop_forward(const float *params, uint32_t IN, uint32_t H, uint32_t OUT, const float *x, uint32_t n,
+                    int bf16, float *out);
+int or_prop_loss_grad(const float *params, uint32_t IN, uint32_t H, uint32_t OUT, uint32_t DY, const float *x,
+                      const float *y, const float *w, uint32_t n, int bf16, double *loss, double *grad);
+
 /* Label images (image_loader.c): _rgb2label. */
 void or_rgb_to_labels(const uint8_t *src, uint64_t n_pix, uint32_t channels, const uint8_t *map, uint32_t n_classes,
                       uint8_t *dst);

@@ -25,7 +25,7 @@ __all__ = [
     "ForestConfig", "TreeTrainerParameters", "TrainingSetImage", "TrainingSet", "Tree", "TreeTrainer",
     "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS", "USER_SHAPES", "check_plugin",
     "ImageSampler", "UniformImageSampler", "ClassWeightedImageSampler", "sampled_training_set",
-    "read_pnm", "write_pnm", "PNMImageLoader", "RGBLabelsLoader", "load_training_set", "image_roi",
+    "ProposalNetwork", "RECORD_DTYPE", "read_pnm", "write_pnm", "PNMImageLoader", "RGBLabelsLoader", "load_training_set", "image_roi",
     "PNMImageROILoader", "RGBLabelsROILoader",
 ]
 
@@ -335,6 +335,31 @@ class TreeTrainer(_Ctx):
                                   _ptr(lc), _ptr(ft), _ptr(th), _ptr(po)))
         tree.left_child[:n], tree.features[:n], tree.thresholds[:n], tree.posteriors[:n] = lc, ft, th, po
 
+    def train_proposed(self, tree: Tree, ts: TrainingSet, params: TreeTrainerParameters, proposer: "ProposalNetwork",
+                       n_proposed: int, end_depth: int | None = None) -> None:
+        """train() with learned proposals: candidates f < n_proposed of every node are drawn from
+        the proposal network's mixture, the others are the reference's uniform candidates."""
+        end_depth = tree.depth if end_depth is None else end_depth
+        self.upload(ts)
+        n = (1 << end_depth) - 1
+        lc = np.ascontiguousarray(tree.left_child[:n])
+        ft = np.ascontiguousarray(tree.features[:n])
+        th = np.ascontiguousarray(tree.thresholds[:n])
+        po = np.ascontiguousarray(tree.posteriors[:n])
+        prior = np.ascontiguousarray(ts.priors, np.float32)
+        check(lib().pd_train_tree_proposed(self.h, proposer.h, C.byref(params.c()), n_proposed, tree.id, 1, end_depth,
+                                           _ptr(prior), _ptr(lc), _ptr(ft), _ptr(th), _ptr(po)))
+        tree.left_child[:n], tree.features[:n], tree.thresholds[:n], tree.posteriors[:n] = lc, ft, th, po
+
+    def records(self) -> np.ndarray:
+        """The records (one per split node) of the last training call; set_tuning("records", 1)
+        before training to keep them."""
+        n = C.c_uint64()
+        check(lib().pd_train_records(self.h, None, 0, C.byref(n)))
+        out = (N.Record * max(1, n.value))()
+        check(lib().pd_train_records(self.h, C.cast(out, C.c_void_p), n.value, C.byref(n)))
+        return np.ctypeslib.as_array(out)[: n.value].copy() if n.value else np.zeros(0, RECORD_DTYPE)
+
     def stats(self) -> dict:
         s = N.TrainStats()
         check(lib().pd_train_get_stats(self.h, C.byref(s)))
@@ -378,6 +403,71 @@ class TreeTrainer(_Ctx):
         out = np.zeros(n, np.float64)
         check(lib().pd_log2_table(self.h, n, _ptr(out)))
         return out
+
+
+RECORD_DTYPE = np.dtype([("depth", np.uint32), ("count", np.uint32), ("node", np.uint32), ("tree", np.uint32),
+                         ("gain", np.float64), ("feat", np.int32, (8,)), ("thr", np.int32),
+                         ("class_count", np.uint32, (64,))], align=True)
+
+
+class ProposalNetwork:
+    """The proposal network of learned candidate proposals (pd_proposer; no reference
+    counterpart): a BF16 MLP on the trainer's GPU mapping a node's depth, log-count and class
+    frequencies to a 16-component Gaussian mixture over the normalised feature values and
+    threshold, fitted to the records of the plain trainer."""
+
+    def __init__(self, trainer: TreeTrainer, bounds: TreeTrainerParameters, seed: int = 0):
+        self.trainer = trainer  # keeps the context alive
+        h = C.c_void_p()
+        check(lib().pd_proposer_create(trainer.h, C.byref(bounds.c()), seed, C.byref(h)))
+        self.h = h
+        d = (C.c_uint32 * 6)()
+        n = C.c_uint64()
+        check(lib().pd_proposer_dims(h, d, C.byref(n)))
+        self.in_dim, self.hidden, self.layers, self.out_dim, self.components, self.drawn = list(d)
+        self.n_params = n.value
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            lib().pd_proposer_destroy(h)
+            self.h = None
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, np.float32)
+        check(lib().pd_proposer_get_params(self.h, _ptr(out)))
+        return out
+
+    @params.setter
+    def params(self, v: np.ndarray) -> None:
+        v = np.ascontiguousarray(v, np.float32)
+        if v.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters")
+        check(lib().pd_proposer_set_params(self.h, _ptr(v)))
+
+    def forward(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32)
+        out = np.zeros((x.shape[0], self.out_dim), np.float32)
+        check(lib().pd_proposer_forward(self.h, _ptr(x), x.shape[0], _ptr(out)))
+        return out
+
+    def loss_grad(self, x: np.ndarray, y: np.ndarray, w: np.ndarray | None = None) -> tuple[float, np.ndarray]:
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        w = None if w is None else np.ascontiguousarray(w, np.float32)
+        grad = np.zeros(self.n_params, np.float32)
+        loss = C.c_float()
+        check(lib().pd_proposer_loss_grad(self.h, _ptr(x), _ptr(y), _ptr(w), x.shape[0], C.byref(loss), _ptr(grad)))
+        return loss.value, grad
+
+    def fit(self, records: np.ndarray, steps: int = 400, batch: int = 4096, lr: float = 1e-3) -> dict:
+        rec = np.ascontiguousarray(records, RECORD_DTYPE)
+        loss = np.zeros(steps, np.float32)
+        ms = C.c_float()
+        check(lib().pd_proposer_fit(self.h, _ptr(rec), rec.size, steps, batch, C.c_float(lr), _ptr(loss),
+                                    C.byref(ms)))
+        return dict(loss=loss, ms=ms.value)
 
 
 class Classifier(_Ctx):

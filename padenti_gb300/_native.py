@@ -83,6 +83,12 @@ class Sampler(C.Structure):
     ]
 
 
+class Record(C.Structure):
+    """pd_record: one split node of a trained tree (learned proposals)."""
+    _fields_ = [("depth", C.c_uint32), ("count", C.c_uint32), ("node", C.c_uint32), ("tree", C.c_uint32),
+                ("gain", C.c_double), ("feat", C.c_int32 * 8), ("thr", C.c_int32), ("class_count", C.c_uint32 * 64)]
+
+
 class SampleStats(C.Structure):
     _fields_ = [
         ("images", C.c_uint64),
@@ -123,6 +129,18 @@ _SIGS = {
     "pd_hist": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, _P, _P, C.c_uint32, _P]),
     "pd_split": (C.c_int, [_P, C.POINTER(TrainParams), _P, _P, C.c_uint32, _P, _P, _P]),
     "pd_log2_table": (C.c_int, [_P, C.c_uint32, _P]),
+    "pd_train_records": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "pd_proposer_create": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint64, C.POINTER(_P)]),
+    "pd_proposer_destroy": (C.c_int, [_P]),
+    "pd_proposer_dims": (C.c_int, [_P, _P, C.POINTER(C.c_uint64)]),
+    "pd_proposer_get_params": (C.c_int, [_P, _P]),
+    "pd_proposer_set_params": (C.c_int, [_P, _P]),
+    "pd_proposer_forward": (C.c_int, [_P, _P, C.c_uint32, _P]),
+    "pd_proposer_loss_grad": (C.c_int, [_P, _P, _P, _P, C.c_uint32, C.POINTER(C.c_float), _P]),
+    "pd_proposer_fit": (C.c_int, [_P, _P, C.c_uint64, C.c_uint32, C.c_uint32, C.c_float, _P,
+                                  C.POINTER(C.c_float)]),
+    "pd_train_tree_proposed": (C.c_int, [_P, _P, C.POINTER(TrainParams), C.c_uint32, C.c_uint32, C.c_uint32,
+                                         C.c_uint32, _P, _P, _P, _P, _P]),
     "pd_split_noalloc": (C.c_int, [C.POINTER(TrainParams), C.c_uint32, _P, _P, C.c_uint32, _P, _P, _P, _P]),
     "pd_forest_clear": (C.c_int, [_P]),
     "pd_forest_add_tree": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P]),

@@ -43,7 +43,7 @@ def _stale(obj: pathlib.Path, src: pathlib.Path, deps: list[pathlib.Path]) -> bo
 
 # Headers compiled again at run time by NVRTC for user feature plugins; they are
 # embedded into the library as raw string literals (_build/pd_rtc_sources.inc).
-RTC_HEADERS = ["padenti_gb300.h", "pd_common.cuh", "pd_log2.cuh", "pd_rng.cuh", "pd_plugins.cuh",
+RTC_HEADERS = ["padenti_gb300.h", "pd_common.cuh", "pd_log2.cuh", "pd_rng.cuh", "pd_propose.cuh", "pd_plugins.cuh",
                "pd_train_kernels.cuh", "pd_predict_kernels.cuh", "pd_user_plugin.cuh", "pd_user_plugin_impl.cuh"]
 
 

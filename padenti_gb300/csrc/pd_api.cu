@@ -136,6 +136,9 @@ extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
   } else if (n == "sample_group") {
     PD_CHECK(value >= 4096, PD_ERR_INVALID, "sample_group %lld below 4096 bytes", (long long)value);
     ctx->sample_group = (uint64_t)value;
+  } else if (n == "records") {
+    PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "records must be 0 or 1");
+    ctx->collect_records = value != 0;
   } else {
     return set_error(PD_ERR_INVALID, "unknown tuning knob '%s'", name);
   }

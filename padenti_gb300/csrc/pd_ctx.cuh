@@ -24,6 +24,8 @@ struct pd_ctx {
   uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
   bool cand_order = true;    // order each node's candidate columns by first-probe offset
   uint64_t sample_group = 512ull << 20;  // bytes of images + labels pd_sample stages per round trip
+  bool collect_records = false;          // keep a pd_record per split node (learned proposals)
+  std::vector<pd_record> records;        // of the last training call
 
   // ---- training set in HBM (cl_tree_trainer_impl_init.hpp:99-154 streams it
   // image by image; here it stays resident) ----
@@ -109,6 +111,10 @@ inline cudaError_t d2h(pd_ctx *c, void *dst, const void *src, size_t n) {
 }  // namespace pd
 
 namespace pd {
+struct PropSrc;
+// The proposal network's mixture for n frontier nodes of depth `depth` (class
+// totals d_ctot [n][K] on the device), on the context's stream (pd_propose.cu).
+int proposer_infer(pd_proposer *p, const uint32_t *d_ctot, uint32_t n, uint32_t depth, uint32_t n_prop, PropSrc *src);
 int ensure_log2_table(pd_ctx *ctx, uint64_t n);
 int init_tables(pd_ctx *ctx);
 // Prepares the uploaded images for the plugin's eval_train (zero depths).

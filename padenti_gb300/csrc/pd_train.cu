@@ -155,7 +155,8 @@ static uint64_t slot_bytes(const pd_ctx *ctx, const pd_train_params *p) {
 // *ord_out is null.
 template <class P>
 static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tree, const int32_t *d_nodes,
-                             uint32_t n, bool ordered = false, const uint32_t **ord_out = nullptr) {
+                             uint32_t n, bool ordered = false, const uint32_t **ord_out = nullptr,
+                             const PropSrc *prop = nullptr) {
   using FeatT = typename P::feat_t;
   const uint32_t F = p->n_features;
   const uint64_t total = (uint64_t)n * F;
@@ -193,7 +194,7 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
   PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)((total + kCandThreads - 1) / kCandThreads), kCandThreads, smem, ctx->stream>>>(
       d_nodes, n, tree, F, p->n_thresholds, P::kFeatDim, b, ord, ctx->cand_feat.as<FeatT>(),
-      ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>());
+      ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>(), prop ? *prop : PropSrc{});
   PD_CUDA(cudaGetLastError());
   ctx->launches++;
   if (ord_out) *ord_out = ord;
@@ -392,10 +393,14 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 // ------------------------------------------------------------- one tree ----
+// With `prop`, candidates f < n_prop of every node come from the proposal
+// network (learned proposals); with ctx->collect_records, one pd_record per
+// split node is kept.
 template <class P>
 static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_id, uint32_t end_depth,
                            const float *root_prior, int32_t *lc, typename P::feat_t *feats,
-                           typename P::feat_t *thrs, float *posts) {
+                           typename P::feat_t *thrs, float *posts, pd_proposer *prop = nullptr,
+                           uint32_t n_prop = 0) {
   using FeatT = typename P::feat_t;
   constexpr int D = P::kFeatDim;
   const auto t_start = std::chrono::steady_clock::now();
@@ -407,6 +412,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   memset(&stats, 0, sizeof(stats));
   const uint64_t h2d0 = ctx->bytes_h2d, d2h0 = ctx->bytes_d2h, launches0 = ctx->launches;
   const uint64_t image_bytes = ctx->pixels_bytes;
+  ctx->records.clear();
 
   PD_TRY(ensure_log2_table(ctx, S + 2));
   PD_TRY(ctx->t_lc.ensure(n_nodes * 4));
@@ -479,7 +485,14 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       std::vector<uint64_t> off(cur_off.begin() + s0, cur_off.begin() + s0 + ns + 1);
       PD_CUDA(cudaEventRecord(ev[0], st));
       const uint32_t *d_ord = nullptr;
-      PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, ctx->cand_order, &d_ord));
+      if (prop) {
+        // the network's mixture for every node of the slice, then the table drawn from it
+        PropSrc src;
+        PD_TRY(proposer_infer(prop, d_ctot.as<uint32_t>(), ns, depth, n_prop, &src));
+        PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, false, &d_ord, &src));
+      } else {
+        PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, ctx->cand_order, &d_ord));
+      }
       PD_CUDA(cudaEventRecord(ev[1], st));
       uint64_t n_items = 0;
       std::vector<uint32_t> split_slots;
@@ -544,6 +557,19 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
         lc[n] = (int32_t)L;
         split_now[s0 + i] = 1;
         stats.nodes_split++;
+        if (ctx->collect_records) {
+          pd_record r;
+          memset(&r, 0, sizeof(r));
+          r.depth = depth;
+          r.count = node_tot[n];
+          r.node = n;
+          r.tree = tree_id;
+          r.gain = o.gain;
+          for (int d = 0; d < D; d++) r.feat[d] = (int32_t)feats[(size_t)n * D + d];
+          r.thr = (int32_t)thrs[n];
+          for (uint32_t l = 0; l < K; l++) r.class_count[l] = class_tot[(size_t)n * K + l];
+          ctx->records.push_back(r);
+        }
       }
     }
 
@@ -672,6 +698,34 @@ extern "C" int pd_train_tree(pd_ctx *ctx, const pd_train_params *params, uint32_
     return train_tree_impl<P>(ctx, params, tree_id, end_depth, root_prior, left_child,
                               static_cast<FeatT *>(features), static_cast<FeatT *>(thresholds), posteriors);
   });
+}
+
+extern "C" int pd_train_tree_proposed(pd_ctx *ctx, pd_proposer *prop, const pd_train_params *params,
+                                      uint32_t n_proposed, uint32_t tree_id, uint32_t start_depth, uint32_t end_depth,
+                                      const float *root_prior, int32_t *left_child, void *features, void *thresholds,
+                                      float *posteriors) {
+  PD_CHECK(ctx && prop, PD_ERR_INVALID, "null context or proposer");
+  PD_CHECK(ctx->have_dataset, PD_ERR_STATE, "no dataset uploaded");
+  PD_CHECK(start_depth == 1, PD_ERR_INVALID, "Starting depth must be equal to 1");
+  PD_CHECK(end_depth >= 1 && end_depth <= 24, PD_ERR_UNSUPPORTED, "end_depth %u outside [1,24]", end_depth);
+  PD_CHECK(root_prior && left_child && features && thresholds && posteriors, PD_ERR_INVALID, "null tree array");
+  PD_TRY(check_params(ctx, params));
+  PD_CHECK(n_proposed <= params->n_features, PD_ERR_INVALID, "n_proposed %u above n_features %u", n_proposed,
+           params->n_features);
+  PD_CUDA(cudaSetDevice(ctx->device));
+  return dispatch_config(ctx->cfg, [&]<class P>() {
+    using FeatT = typename P::feat_t;
+    return train_tree_impl<P>(ctx, params, tree_id, end_depth, root_prior, left_child,
+                              static_cast<FeatT *>(features), static_cast<FeatT *>(thresholds), posteriors, prop,
+                              n_proposed);
+  });
+}
+
+extern "C" int pd_train_records(pd_ctx *ctx, pd_record *out, uint64_t cap, uint64_t *n) {
+  PD_CHECK(ctx && n, PD_ERR_INVALID, "null argument");
+  *n = ctx->records.size();
+  if (out) memcpy(out, ctx->records.data(), std::min<uint64_t>(cap, ctx->records.size()) * sizeof(pd_record));
+  return PD_OK;
 }
 
 extern "C" int pd_train_get_stats(pd_ctx *ctx, pd_train_stats *out) {

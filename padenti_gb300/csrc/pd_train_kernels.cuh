@@ -15,6 +15,7 @@
 
 #include "pd_log2.cuh"
 #include "pd_plugins.cuh"
+#include "pd_propose.cuh"
 #include "pd_rng.cuh"
 
 namespace pd {
@@ -102,13 +103,15 @@ constexpr int kCandThreads = 128;
 // PACKED (threshold range below 2^24): value and original index sort as one
 // word (v - lo) << 8 | t, whose order is the stable order of the values; else
 // two shared-memory columns.
+// With prop.out set, candidates f < prop.n_prop of slot n are drawn from the
+// proposal network's mixture for that slot (pd_propose.cuh) instead of MD5.
 template <typename FeatT, bool PACKED>
 __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__restrict__ nodes, uint32_t n_nodes,
                                                              uint32_t tree, uint32_t F, uint32_t T, int D,
                                                              CandBounds b, const uint32_t *__restrict__ ord,
                                                              FeatT *__restrict__ feat,
                                                              FeatT *__restrict__ thr_sorted,
-                                                             uint8_t *__restrict__ perm) {
+                                                             uint8_t *__restrict__ perm, PropSrc prop) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   uint32_t *sk = reinterpret_cast<uint32_t *>(smem_raw);                         // PACKED: [T][128]
   FeatT *sv = reinterpret_cast<FeatT *>(smem_raw);                               // [T][128]
@@ -119,22 +122,32 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
   if (active) {
     const uint32_t node = (uint32_t)nodes[n];
     const uint32_t f = ord ? ord[(size_t)n * F + c] : c;
+    const bool net = prop.out != nullptr && f < prop.n_prop;
+    uint64_t stream = 0;
+    uint32_t g = 0;
     FeatT fv[PD_MAX_FEAT_DIM];
-    candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
+    if (net) {
+      stream = prop_stream(prop.seed, tree, node, f);
+      g = prop_component(prop, n, stream);
+      for (int d = 0; d < D; d++) fv[d] = (FeatT)prop_draw(prop, n, g, (uint32_t)d, stream, (uint32_t)d);
+    } else {
+      candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
+    }
     for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + c] = fv[d];
     uint32_t *k = sk + threadIdx.x;
     FeatT *v = sv + threadIdx.x;
     uint8_t *id = si + threadIdx.x;
     uint32_t seed[4] = {tree, node, f, 1u}, st[4] = {0u, 0u, 0u, 0u};
     for (uint32_t t = 0; t < T; t++) {
-      if ((t & 3u) == 0) {
+      if (!net && (t & 3u) == 0) {
         md5_block(seed, st);
         seed[0] = st[0];
         seed[1] = st[1];
         seed[2] = st[2];
         seed[3] = st[3];
       }
-      const FeatT x = draw<FeatT>(st[t & 3u], b.thr_lo, b.thr_hi);
+      const FeatT x = net ? (FeatT)prop_draw(prop, n, g, (uint32_t)D, stream, (uint32_t)D + 1u + t)
+                          : draw<FeatT>(st[t & 3u], b.thr_lo, b.thr_hi);
       // stable insertion
       uint32_t j = t;
       if (PACKED) {

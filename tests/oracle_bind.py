@@ -338,3 +338,25 @@ def synth_depth(seed: int, n_images: int, width: int, height: int, *, first_imag
                               P(lb), P(sm))
     assert rc == 0
     return px, lb, sm
+
+
+def prop_forward(params, IN, H, OUT, x, bf16=True):
+    x = np.ascontiguousarray(x, np.float32)
+    out = np.zeros((x.shape[0], OUT), np.float32)
+    rc = lib().or_prop_forward(P(np.ascontiguousarray(params, np.float32)), C.c_uint32(IN), C.c_uint32(H),
+                               C.c_uint32(OUT), P(x), C.c_uint32(x.shape[0]), C.c_int(int(bf16)), P(out))
+    assert rc == 0
+    return out
+
+
+def prop_loss_grad(params, IN, H, OUT, DY, x, y, w=None, bf16=True):
+    params = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    w = None if w is None else np.ascontiguousarray(w, np.float32)
+    grad = np.zeros(params.size, np.float64)
+    loss = C.c_double()
+    rc = lib().or_prop_loss_grad(P(params), C.c_uint32(IN), C.c_uint32(H), C.c_uint32(OUT), C.c_uint32(DY), P(x),
+                                 P(y), P(w), C.c_uint32(x.shape[0]), C.c_int(int(bf16)), C.byref(loss), P(grad))
+    assert rc == 0
+    return loss.value, grad
