@@ -63,8 +63,8 @@ def args_():
     a.add_argument("--cand-order", type=int, default=None, choices=(0, 1),
                    help="1: candidate columns ordered by first-probe offset (default), 0: index order")
     a.add_argument("--learned", type=int, default=1, help="1: time the learned-proposal forest beside the plain one")
-    a.add_argument("--fit-steps", type=int, default=400)
-    a.add_argument("--fit-batch", type=int, default=4096)
+    a.add_argument("--fit-steps", type=int, default=200)
+    a.add_argument("--fit-batch", type=int, default=2048)
     a.add_argument("--fit-lr", type=float, default=2e-3)
     a.add_argument("--only", default=None,
                    choices=["sampler_uniform", "sampler_class_weighted", "labels", "learned"],
@@ -577,10 +577,19 @@ def learned_bench(a, pg, cfg, ts, tp, device):
         _, ms = timed(lambda: tr.train(t, ts, tp300))
         uni.append(t)
         ms_uni += ms
+    # what the network gains at a small budget: one tree, 25 proposed + 5 uniform against 30 uniform
+    tp30 = pg.TreeTrainerParameters(30, tp.n_thresholds, tp.feat_low_bounds, tp.feat_up_bounds, tp.thr_low_bound,
+                                    tp.thr_up_bound, tp.per_leaf_samples_thr)
+    net30 = pg.ProposalNetwork(tr, tp30, seed=a.seed)
+    net30.params = net.params
+    small_l, small_u = pg.Tree(cfg, 1, a.depth), pg.Tree(cfg, 1, a.depth)
+    tr.train_proposed(small_l, ts, tp30, net30, 25)
+    tr.train(small_u, ts, tp30)
     hx, hl, _ = pg.synth_depth(a.seed, 100, a.width, a.height, first_image=5_000_000, parts=1, min_ellipses=2,
                                max_ellipses=5, samples_per_image=1)
     acc = {name: forest_accuracy(pg, cfg, f, device, hx, hl) for name, f in
-           (("plain", plain), ("learned", learned), ("uniform300", uni))}
+           (("plain", plain), ("learned", learned), ("uniform300", uni), ("tree30_learned", [small_l]),
+            ("tree30_uniform", [small_u]))}
     return dict(
         metric="learned vs plain time at same accuracy", unit="ratio of GPU training times",
         value=ms_learned / ms_plain, higher_is_better=False,
@@ -590,6 +599,11 @@ def learned_bench(a, pg, cfg, ts, tp, device):
                      fit_steps=a.fit_steps, fit_batch=a.fit_batch, first_loss=float(fit["loss"][0]),
                      last_loss=float(fit["loss"][-10:].mean())),
         uniform300=dict(ms=ms_uni, accuracy=acc["uniform300"][0], object_accuracy=acc["uniform300"][1]),
+        single_tree_30_candidates=dict(learned=dict(accuracy=acc["tree30_learned"][0],
+                                                    object_accuracy=acc["tree30_learned"][1]),
+                                       uniform=dict(accuracy=acc["tree30_uniform"][0],
+                                                    object_accuracy=acc["tree30_uniform"][1]),
+                                       note="tree 1 alone, 25 proposed + 5 uniform against 30 uniform candidates"),
         accuracy_gap_pt=100 * (acc["plain"][0] - acc["learned"][0]),
         network_gain_pt=100 * (acc["learned"][0] - acc["uniform300"][0]),
         held_out="100 synthetic 640x480 images of the same generator (not trained on)",

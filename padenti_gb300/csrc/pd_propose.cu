@@ -49,6 +49,10 @@ struct GemmArgs {
   const float *zin;    // z of the layer (EPI_DGELU)
   int64_t ldo;         // row pitch of outf / outb / zin
   int64_t split_stride;  // EPI_PARTIAL: floats between the partials of two splits
+  // 16-byte loads of 8 elements along the contiguous index of A / B (set by
+  // gemm() when that index's extent, the other stride, the split length and
+  // the base pointer allow it)
+  int vec_a, vec_b;
 };
 
 PD_D float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
@@ -85,7 +89,25 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
 #pragma unroll
       for (int c = 0; c < 4; c++) acc[a][b][c] = 0.0f;
   for (int k0 = kb; k0 < ke; k0 += kGemmTK) {
-    if (g.a_k == 1) {
+    if (g.vec_a && g.a_k == 1) {
+      // rows contiguous in k: one 16-byte load per 8 elements
+      for (int e = tid; e < kGemmTM * kGemmTK / 8; e += 128) {
+        const int r = e / (kGemmTK / 8), c = (e % (kGemmTK / 8)) * 8, gi = i0 + r, gk = k0 + c;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (gi < g.M && gk < ke) v = *reinterpret_cast<const uint4 *>(g.A + (int64_t)gi * g.a_i + gk);
+        *reinterpret_cast<uint4 *>(&As[r][c]) = v;
+      }
+    } else if (g.vec_a) {
+      // columns contiguous in i: 16-byte loads of 8 rows, spread over the tile's rows
+      for (int e = tid; e < kGemmTM / 8 * kGemmTK; e += 128) {
+        const int r = (e % (kGemmTM / 8)) * 8, c = e / (kGemmTM / 8), gi = i0 + r, gk = k0 + c;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (gi < g.M && gk < ke) v = *reinterpret_cast<const uint4 *>(g.A + gi + (int64_t)gk * g.a_k);
+        const bf16 *pv = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+        for (int q = 0; q < 8; q++) As[r + q][c] = pv[q];
+      }
+    } else if (g.a_k == 1) {
       for (int e = tid; e < kGemmTM * kGemmTK; e += 128) {
         const int r = e / kGemmTK, c = e % kGemmTK, gi = i0 + r, gk = k0 + c;
         As[r][c] = (gi < g.M && gk < ke) ? g.A[(int64_t)gi * g.a_i + gk] : zero;
@@ -96,7 +118,23 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
         As[r][c] = (gi < g.M && gk < ke) ? g.A[(int64_t)gi * g.a_i + (int64_t)gk * g.a_k] : zero;
       }
     }
-    if (g.b_k == 1) {
+    if (g.vec_b && g.b_k == 1) {
+      for (int e = tid; e < kGemmTN * kGemmTK / 8; e += 128) {
+        const int r = e / (kGemmTK / 8), c = (e % (kGemmTK / 8)) * 8, gj = j0 + r, gk = k0 + c;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (gj < g.N && gk < ke) v = *reinterpret_cast<const uint4 *>(g.B + gk + (int64_t)gj * g.b_j);
+        *reinterpret_cast<uint4 *>(&Bs[r][c]) = v;
+      }
+    } else if (g.vec_b) {
+      for (int e = tid; e < kGemmTN / 8 * kGemmTK; e += 128) {
+        const int r = (e % (kGemmTN / 8)) * 8, c = e / (kGemmTN / 8), gj = j0 + r, gk = k0 + c;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (gj < g.N && gk < ke) v = *reinterpret_cast<const uint4 *>(g.B + (int64_t)gk * g.b_k + gj);
+        const bf16 *pv = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+        for (int q = 0; q < 8; q++) Bs[r + q][c] = pv[q];
+      }
+    } else if (g.b_k == 1) {
       for (int e = tid; e < kGemmTN * kGemmTK; e += 128) {
         const int r = e / kGemmTK, c = e % kGemmTK, gj = j0 + r, gk = k0 + c;
         Bs[r][c] = (gj < g.N && gk < ke) ? g.B[gk + (int64_t)gj * g.b_j] : zero;
@@ -159,66 +197,85 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
 }
 
 // Mixture negative log-likelihood of each row's target and its gradient with
-// respect to the network output (thread per row).  Rows are weighted by
-// w[i] * inv_wsum (the loss is the weighted mean); a log-sd outside the clamp
-// gets no gradient.
-__global__ void k_prop_mdn(const float *__restrict__ out, uint32_t ldo, const float *__restrict__ y,
-                           const float *__restrict__ w, uint32_t B, uint32_t DY, const float *__restrict__ inv_wsum,
-                           bf16 *__restrict__ dout, float *__restrict__ loss_rows) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= B) return;
-  const float *o = out + (size_t)i * ldo;
-  const float *yi = y + (size_t)i * DY;
-  bf16 *d = dout + (size_t)i * ldo;
-  float lmax = o[0];
-  for (int gk = 1; gk < kPropG; gk++) lmax = fmaxf(lmax, o[gk]);
-  float lsum = 0.0f;
-  for (int gk = 0; gk < kPropG; gk++) lsum += expf(o[gk] - lmax);
+// respect to the network output.  Half a warp per row, one lane per mixture
+// component (log-sum-exps by shuffles within the 16 lanes).  Rows are weighted
+// by w[i] * inv_wsum (the loss is the weighted mean); a log-sd outside the
+// clamp gets no gradient.
+__global__ void __launch_bounds__(128) k_prop_mdn(const float *__restrict__ out, uint32_t ldo,
+                                                  const float *__restrict__ y, const float *__restrict__ w,
+                                                  uint32_t B, uint32_t DY, const float *__restrict__ inv_wsum,
+                                                  bf16 *__restrict__ dout, float *__restrict__ loss_rows) {
+  static_assert(kPropG == 16, "one half-warp lane per component");
+  const uint32_t lane = threadIdx.x & 31u, gk = lane & 15u;
+  const uint32_t i = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2u + (lane >> 4);
+  const bool live = i < B;
+  const uint32_t ii = live ? i : 0u;  // every lane takes part in the shuffles
+  const float *o = out + (size_t)ii * ldo;
+  const float *yi = y + (size_t)ii * DY;
+  const float logit = o[gk];
+  float lmax = logit;
+#pragma unroll
+  for (int off = 8; off > 0; off >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, off));
+  float lsum = expf(logit - lmax);
+#pragma unroll
+  for (int off = 8; off > 0; off >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, off);
   const float lse_logits = lmax + logf(lsum);
-  float a[kPropG];
-  float amax = -INFINITY;
-  for (int gk = 0; gk < kPropG; gk++) {
-    float ll = 0.0f;
-    for (uint32_t dd = 0; dd < DY; dd++) {
-      const float mu = o[kPropG + gk * DY + dd];
-      const float s = fminf(fmaxf(o[kPropG + kPropG * DY + gk * DY + dd], kPropSMin), kPropSMax);
-      const float q = (yi[dd] - mu) * expf(-s);
-      ll += -0.5f * q * q - s - 0.91893853320467274f;
-    }
-    a[gk] = o[gk] - lse_logits + ll;
-    amax = fmaxf(amax, a[gk]);
+  float ll = 0.0f;
+  for (uint32_t dd = 0; dd < DY; dd++) {
+    const float mu = o[kPropG + gk * DY + dd];
+    const float s = fminf(fmaxf(o[kPropG + kPropG * DY + gk * DY + dd], kPropSMin), kPropSMax);
+    const float q = (yi[dd] - mu) * expf(-s);
+    ll += -0.5f * q * q - s - 0.91893853320467274f;
   }
-  float asum = 0.0f;
-  for (int gk = 0; gk < kPropG; gk++) asum += expf(a[gk] - amax);
+  const float a = logit - lse_logits + ll;
+  float amax = a;
+#pragma unroll
+  for (int off = 8; off > 0; off >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, off));
+  float asum = expf(a - amax);
+#pragma unroll
+  for (int off = 8; off > 0; off >>= 1) asum += __shfl_xor_sync(0xffffffffu, asum, off);
+  if (!live) return;
   const float lse = amax + logf(asum);
   const float ws = (w ? w[i] : 1.0f) * inv_wsum[0];
-  loss_rows[i] = -lse * ws;
-  for (int gk = 0; gk < kPropG; gk++) {
-    const float r = expf(a[gk] - lse), pi = expf(o[gk] - lse_logits);
-    d[gk] = __float2bfloat16(ws * (pi - r));
-    for (uint32_t dd = 0; dd < DY; dd++) {
-      const float mu = o[kPropG + gk * DY + dd];
-      const float sraw = o[kPropG + kPropG * DY + gk * DY + dd];
-      const float s = fminf(fmaxf(sraw, kPropSMin), kPropSMax);
-      const float inv = expf(-s), q = (yi[dd] - mu) * inv;
-      d[kPropG + gk * DY + dd] = __float2bfloat16(-ws * r * q * inv);
-      const bool live = sraw > kPropSMin && sraw < kPropSMax;
-      d[kPropG + kPropG * DY + gk * DY + dd] = __float2bfloat16(live ? -ws * r * (q * q - 1.0f) : 0.0f);
-    }
+  if (gk == 0) loss_rows[i] = -lse * ws;
+  bf16 *d = dout + (size_t)i * ldo;
+  const float r = expf(a - lse), pi = expf(logit - lse_logits);
+  d[gk] = __float2bfloat16(ws * (pi - r));
+  for (uint32_t dd = 0; dd < DY; dd++) {
+    const float mu = o[kPropG + gk * DY + dd];
+    const float sraw = o[kPropG + kPropG * DY + gk * DY + dd];
+    const float s = fminf(fmaxf(sraw, kPropSMin), kPropSMax);
+    const float inv = expf(-s), q = (yi[dd] - mu) * inv;
+    d[kPropG + gk * DY + dd] = __float2bfloat16(-ws * r * q * inv);
+    const bool grad_s = sraw > kPropSMin && sraw < kPropSMax;
+    d[kPropG + kPropG * DY + gk * DY + dd] = __float2bfloat16(grad_s ? -ws * r * (q * q - 1.0f) : 0.0f);
   }
-  for (uint32_t j = (uint32_t)kPropG * (1u + 2u * DY); j < ldo; j++) d[j] = __float2bfloat16(0.0f);
+  for (uint32_t j = (uint32_t)kPropG * (1u + 2u * DY) + gk; j < ldo; j += 16u) d[j] = __float2bfloat16(0.0f);
 }
 
 // Bias gradients: per split, column sums of a BF16 [rows][n] matrix over the
-// split's rows (fixed order).
-__global__ void k_prop_colsum(const bf16 *__restrict__ m, uint32_t rows, uint32_t n, uint32_t rows_per_split,
-                              float *__restrict__ part, uint64_t split_stride) {
-  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
+// split's rows.  A block covers 32 columns with 8 row groups (rows r, r + 8,
+// ... of the split, several loads in flight per thread), and the groups are
+// added in a fixed order, so the sums do not depend on scheduling.
+__global__ void __launch_bounds__(256) k_prop_colsum(const bf16 *__restrict__ m, uint32_t rows, uint32_t n,
+                                                     uint32_t rows_per_split, float *__restrict__ part,
+                                                     uint64_t split_stride) {
+  __shared__ float acc[8][33];
+  const uint32_t j = blockIdx.x * 32u + threadIdx.x, grp = threadIdx.y;
   const uint32_t r0 = blockIdx.y * rows_per_split, r1 = min(rows, r0 + rows_per_split);
   float s = 0.0f;
-  for (uint32_t r = r0; r < r1; r++) s += __bfloat162float(m[(size_t)r * n + j]);
-  part[blockIdx.y * split_stride + j] = s;
+  if (j < n) {
+#pragma unroll 8
+    for (uint32_t r = r0 + grp; r < r1; r += 8u) s += __bfloat162float(m[(size_t)r * n + j]);
+  }
+  acc[grp][threadIdx.x] = s;
+  __syncthreads();
+  if (grp == 0 && j < n) {
+    float t = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 8; q++) t += acc[q][threadIdx.x];
+    part[blockIdx.y * split_stride + j] = t;
+  }
 }
 
 // Sums the split partials of every parameter in split order (the gradient).
@@ -371,7 +428,12 @@ static int prop_ensure_rows(pd_proposer *p, uint32_t rows) {
 }
 
 template <int EPI>
-static int gemm(cudaStream_t st, const GemmArgs &g, int splits = 1) {
+static int gemm(cudaStream_t st, GemmArgs g, int splits = 1) {
+  auto al16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+  // along k: every row start and every k-range start (k0 steps by 32 from a split start) is a multiple of 8
+  const bool kfit = g.K % 8 == 0 && g.k_split % 8 == 0;
+  g.vec_a = al16(g.A) && ((g.a_k == 1 && g.a_i % 8 == 0 && kfit) || (g.a_i == 1 && g.a_k % 8 == 0 && g.M % 8 == 0));
+  g.vec_b = al16(g.B) && ((g.b_k == 1 && g.b_j % 8 == 0 && kfit) || (g.b_j == 1 && g.b_k % 8 == 0 && g.N % 8 == 0));
   const dim3 grid((unsigned)((g.N + kGemmTN - 1) / kGemmTN), (unsigned)((g.M + kGemmTM - 1) / kGemmTM),
                   (unsigned)splits);
   k_prop_gemm<EPI><<<grid, 128, 0, st>>>(g);
@@ -438,7 +500,7 @@ static int prop_backward(pd_proposer *p, uint32_t n, cudaStream_t st) {
     g.ldo = di;
     g.split_stride = (int64_t)p->P;
     PD_TRY(gemm<EPI_PARTIAL>(st, g, kSplits));
-    k_prop_colsum<<<dim3((dn + 127) / 128, kSplits), 128, 0, st>>>(d, n, dn, per, part + p->off_b[l], p->P);
+    k_prop_colsum<<<dim3((dn + 31) / 32, kSplits), dim3(32, 8), 0, st>>>(d, n, dn, per, part + p->off_b[l], p->P);
     PD_CUDA(cudaGetLastError());
     if (l == 0) break;
     // d(in)(i, k) = sum_j d(i, j) W[j][k], times GELU'(z of layer l - 1)
@@ -456,9 +518,9 @@ static int prop_backward(pd_proposer *p, uint32_t n, cudaStream_t st) {
 // Loss and gradient partials of the batch already in x / y / w.
 static int prop_loss_grad(pd_proposer *p, uint32_t n, cudaStream_t st) {
   PD_TRY(prop_forward(p, n, st));
-  k_prop_mdn<<<(n + 127) / 128, 128, 0, st>>>(p->out.as<float>(), p->OUT, p->y.as<float>(), p->w.as<float>(), n,
-                                              p->DY, p->wsum.as<float>(), p->dout_b.as<bf16>(),
-                                              p->loss_rows.as<float>());
+  k_prop_mdn<<<(n + 7) / 8, 128, 0, st>>>(p->out.as<float>(), p->OUT, p->y.as<float>(), p->w.as<float>(), n,
+                                          p->DY, p->wsum.as<float>(), p->dout_b.as<bf16>(),
+                                          p->loss_rows.as<float>());
   PD_CUDA(cudaGetLastError());
   return prop_backward(p, n, st);
 }

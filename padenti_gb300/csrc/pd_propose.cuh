@@ -57,12 +57,12 @@ PD_D uint32_t prop_component(const PropSrc &p, uint32_t slot, uint64_t stream) {
   float m = o[0];
   for (int g = 1; g < kPropG; g++) m = fmaxf(m, o[g]);
   float tot = 0.0f;
-  for (int g = 0; g < kPropG; g++) tot += expf(o[g] - m);
+  for (int g = 0; g < kPropG; g++) tot += __expf(o[g] - m);
   const float u = prop_unit(prop_mix(stream)) * tot;
   float acc = 0.0f;
   uint32_t pick = kPropG - 1;
   for (int g = 0; g < kPropG; g++) {
-    acc += expf(o[g] - m);
+    acc += __expf(o[g] - m);
     if (u < acc) {
       pick = (uint32_t)g;
       break;
@@ -71,16 +71,18 @@ PD_D uint32_t prop_component(const PropSrc &p, uint32_t slot, uint64_t stream) {
   return pick;
 }
 
-// Draw k of dimension d of component g (Box-Muller on two hash uniforms),
-// mapped back to the value range and rounded to the nearest integer, clamped.
+// Draw k of dimension d of component g (Box-Muller on two hash uniforms, with
+// the fast exp / log / cos intrinsics: the draws need not match any other
+// implementation, only be reproducible), mapped back to the value range,
+// rounded to the nearest integer and clamped.
 PD_D int32_t prop_draw(const PropSrc &p, uint32_t slot, uint32_t g, uint32_t d, uint64_t stream, uint32_t k) {
   const float *o = p.out + (size_t)slot * p.ldo;
   const float mu = o[kPropG + g * p.DY + d];
   const float s = fminf(fmaxf(o[kPropG + kPropG * p.DY + g * p.DY + d], kPropSMin), kPropSMax);
   const uint64_t h1 = prop_mix(stream ^ (0x51ED27ull + 2ull * k + 1ull) * 0x2545F4914F6CDD1Dull);
   const uint64_t h2 = prop_mix(h1 + 0x632BE59BD9B4E019ull);
-  const float z = sqrtf(-2.0f * logf(prop_unit(h1))) * cosf(6.283185307f * prop_unit(h2));
-  const float y = mu + expf(s) * z;
+  const float z = sqrtf(-2.0f * __logf(prop_unit(h1))) * __cosf(6.283185307f * prop_unit(h2));
+  const float y = mu + __expf(s) * z;
   float v = p.lo[d] + (y + 1.0f) * 0.5f * p.span[d];
   v = fminf(fmaxf(v, p.lo[d]), p.lo[d] + p.span[d]);
   return (int32_t)rintf(v);

@@ -175,11 +175,13 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
       uint32_t tr = tree, f_ = F;
       CandBounds bb = b;
       uint32_t *o = ctx->cand_ord.as<uint32_t>();
-      void *args[] = {&d_nodes, &tr, &f_, &bb, &o};
+      PropSrc ps = prop ? *prop : PropSrc{};
+      void *args[] = {&d_nodes, &tr, &f_, &bb, &o, &ps};
       PD_TRY(rtc_launch(ctx, rk->cand_order, dim3(n), dim3(kOrderThreads), osmem, args));
     } else {
       PD_CUDA(cudaFuncSetAttribute(k_cand_order<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)osmem));
-      k_cand_order<P><<<n, kOrderThreads, osmem, ctx->stream>>>(d_nodes, tree, F, b, ctx->cand_ord.as<uint32_t>());
+      k_cand_order<P><<<n, kOrderThreads, osmem, ctx->stream>>>(d_nodes, tree, F, b, ctx->cand_ord.as<uint32_t>(),
+                                                                prop ? *prop : PropSrc{});
       PD_CUDA(cudaGetLastError());
       ctx->launches++;
     }
@@ -489,7 +491,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
         // the network's mixture for every node of the slice, then the table drawn from it
         PropSrc src;
         PD_TRY(proposer_infer(prop, d_ctot.as<uint32_t>(), ns, depth, n_prop, &src));
-        PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, false, &d_ord, &src));
+        PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, ctx->cand_order, &d_ord, &src));
       } else {
         PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, ctx->cand_order, &d_ord));
       }

@@ -199,9 +199,12 @@ PD_D uint32_t order_quant10(int32_t v, int32_t lo, int32_t up) {
   const int64_t q = span > 0 ? x * 1024 / span : 0;
   return (uint32_t)(q < 0 ? 0 : (q > 1023 ? 1023 : q));
 }
+// With prop.out set, candidates f < prop.n_prop are the proposal network's
+// draws (the same values k_candidates puts in the table).
 template <class P>
 __global__ void __launch_bounds__(kOrderThreads) k_cand_order(const int32_t *__restrict__ nodes, uint32_t tree,
-                                                              uint32_t F, CandBounds b, uint32_t *__restrict__ ord) {
+                                                              uint32_t F, CandBounds b, uint32_t *__restrict__ ord,
+                                                              PropSrc prop) {
   using FeatT = typename P::feat_t;
   constexpr int D = P::kFeatDim, X = P::kOrderDim;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -212,10 +215,20 @@ __global__ void __launch_bounds__(kOrderThreads) k_cand_order(const int32_t *__r
   for (uint32_t f = threadIdx.x; f < N; f += blockDim.x) {
     unsigned long long k = ~0ull;  // padding sorts last
     if (f < F) {
-      FeatT fv[D];
-      candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
-      const uint32_t qx = order_quant10((int32_t)fv[X], b.low[X], b.up[X]);
-      const uint32_t qy = order_quant10((int32_t)fv[X + 1], b.low[X + 1], b.up[X + 1]);
+      int32_t vx, vy;
+      if (prop.out != nullptr && f < prop.n_prop) {
+        const uint64_t stream = prop_stream(prop.seed, tree, node, f);
+        const uint32_t g = prop_component(prop, n, stream);
+        vx = (int32_t)(FeatT)prop_draw(prop, n, g, (uint32_t)X, stream, (uint32_t)X);
+        vy = (int32_t)(FeatT)prop_draw(prop, n, g, (uint32_t)X + 1u, stream, (uint32_t)X + 1u);
+      } else {
+        FeatT fv[D];
+        candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
+        vx = (int32_t)fv[X];
+        vy = (int32_t)fv[X + 1];
+      }
+      const uint32_t qx = order_quant10(vx, b.low[X], b.up[X]);
+      const uint32_t qy = order_quant10(vy, b.low[X + 1], b.up[X + 1]);
       k = ((unsigned long long)((qy << 10) | qx) << 32) | f;
     }
     key[f] = k;
