@@ -30,7 +30,7 @@ using bf16 = __nv_bfloat16;
 
 namespace pd {
 
-constexpr int kGemmTM = 64, kGemmTN = 64, kGemmTK = 32, kGemmPad = 8;
+constexpr int kGemmTM = 64, kGemmTN = 64, kGemmMaxStage = 256, kGemmPad = 8;
 constexpr int kSplits = 8;  // batch splits of the weight-gradient products
 
 enum { EPI_GELU = 0, EPI_LINEAR = 1, EPI_DGELU = 2, EPI_PARTIAL = 3 };
@@ -53,6 +53,7 @@ struct GemmArgs {
   // gemm() when that index's extent, the other stride, the split length and
   // the base pointer allow it)
   int vec_a, vec_b;
+  int kstage;  // reduction columns staged in shared memory at a time (a multiple of 32, <= 256)
 };
 
 PD_D float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
@@ -68,14 +69,19 @@ PD_D void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// 64 x 64 output tile per CTA, 4 warps of 32 x 32 (2 x 4 mma tiles each); the
-// A tile is staged as [i][k] and the B tile as [j][k] in shared memory (k
-// contiguous, so every fragment register is one aligned 32-bit load), from
-// global memory along whichever index is contiguous there.
+// 64 x 64 output tile per CTA, 4 warps of 32 x 32 (2 x 4 mma tiles each).  The
+// reduction range is staged in shared memory kstage (<= 256) at a time -- for
+// every product of the network one stage holds it all, so each CTA issues all
+// its loads before its single barrier -- as an A tile [i][k] and a B tile
+// [j][k] (k contiguous, so every fragment register is one aligned 32-bit
+// load), read from global memory along whichever index is contiguous there
+// (16-byte loads where the layout allows).
 template <int EPI>
 __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
-  __shared__ __align__(16) bf16 As[kGemmTM][kGemmTK + kGemmPad];
-  __shared__ __align__(16) bf16 Bs[kGemmTN][kGemmTK + kGemmPad];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ks = g.kstage, ld = ks + kGemmPad;  // row pitch in elements (a multiple of 8)
+  bf16 *As = reinterpret_cast<bf16 *>(smem_raw);
+  bf16 *Bs = As + kGemmTM * ld;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = warp >> 1, wn = warp & 1, gq = lane >> 2, tq = lane & 3;
   const int i0 = blockIdx.y * kGemmTM, j0 = blockIdx.x * kGemmTN;
@@ -88,80 +94,72 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
     for (int b = 0; b < 4; b++)
 #pragma unroll
       for (int c = 0; c < 4; c++) acc[a][b][c] = 0.0f;
-  for (int k0 = kb; k0 < ke; k0 += kGemmTK) {
+  for (int k0 = kb; k0 < ke; k0 += ks) {
+    const int kn = min(ks, ke - k0 + 31) / 32 * 32;  // columns of this stage, a multiple of 32
     if (g.vec_a && g.a_k == 1) {
       // rows contiguous in k: one 16-byte load per 8 elements
-      for (int e = tid; e < kGemmTM * kGemmTK / 8; e += 128) {
-        const int r = e / (kGemmTK / 8), c = (e % (kGemmTK / 8)) * 8, gi = i0 + r, gk = k0 + c;
+      for (int e = tid; e < kGemmTM * kn / 8; e += 128) {
+        const int r = e / (kn / 8), c = (e % (kn / 8)) * 8, gi = i0 + r, gk = k0 + c;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (gi < g.M && gk < ke) v = *reinterpret_cast<const uint4 *>(g.A + (int64_t)gi * g.a_i + gk);
-        *reinterpret_cast<uint4 *>(&As[r][c]) = v;
+        *reinterpret_cast<uint4 *>(As + r * ld + c) = v;
       }
     } else if (g.vec_a) {
       // columns contiguous in i: 16-byte loads of 8 rows, spread over the tile's rows
-      for (int e = tid; e < kGemmTM / 8 * kGemmTK; e += 128) {
+      for (int e = tid; e < kGemmTM / 8 * kn; e += 128) {
         const int r = (e % (kGemmTM / 8)) * 8, c = e / (kGemmTM / 8), gi = i0 + r, gk = k0 + c;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (gi < g.M && gk < ke) v = *reinterpret_cast<const uint4 *>(g.A + gi + (int64_t)gk * g.a_k);
         const bf16 *pv = reinterpret_cast<const bf16 *>(&v);
 #pragma unroll
-        for (int q = 0; q < 8; q++) As[r + q][c] = pv[q];
-      }
-    } else if (g.a_k == 1) {
-      for (int e = tid; e < kGemmTM * kGemmTK; e += 128) {
-        const int r = e / kGemmTK, c = e % kGemmTK, gi = i0 + r, gk = k0 + c;
-        As[r][c] = (gi < g.M && gk < ke) ? g.A[(int64_t)gi * g.a_i + gk] : zero;
+        for (int q = 0; q < 8; q++) As[(r + q) * ld + c] = pv[q];
       }
     } else {
-      for (int e = tid; e < kGemmTM * kGemmTK; e += 128) {
-        const int r = e % kGemmTM, c = e / kGemmTM, gi = i0 + r, gk = k0 + c;
-        As[r][c] = (gi < g.M && gk < ke) ? g.A[(int64_t)gi * g.a_i + (int64_t)gk * g.a_k] : zero;
+      for (int e = tid; e < kGemmTM * kn; e += 128) {
+        const int r = g.a_k == 1 ? e / kn : e % kGemmTM, c = g.a_k == 1 ? e % kn : e / kGemmTM;
+        const int gi = i0 + r, gk = k0 + c;
+        As[r * ld + c] = (gi < g.M && gk < ke) ? g.A[(int64_t)gi * g.a_i + (int64_t)gk * g.a_k] : zero;
       }
     }
     if (g.vec_b && g.b_k == 1) {
-      for (int e = tid; e < kGemmTN * kGemmTK / 8; e += 128) {
-        const int r = e / (kGemmTK / 8), c = (e % (kGemmTK / 8)) * 8, gj = j0 + r, gk = k0 + c;
+      for (int e = tid; e < kGemmTN * kn / 8; e += 128) {
+        const int r = e / (kn / 8), c = (e % (kn / 8)) * 8, gj = j0 + r, gk = k0 + c;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (gj < g.N && gk < ke) v = *reinterpret_cast<const uint4 *>(g.B + gk + (int64_t)gj * g.b_j);
-        *reinterpret_cast<uint4 *>(&Bs[r][c]) = v;
+        *reinterpret_cast<uint4 *>(Bs + r * ld + c) = v;
       }
     } else if (g.vec_b) {
-      for (int e = tid; e < kGemmTN / 8 * kGemmTK; e += 128) {
+      for (int e = tid; e < kGemmTN / 8 * kn; e += 128) {
         const int r = (e % (kGemmTN / 8)) * 8, c = e / (kGemmTN / 8), gj = j0 + r, gk = k0 + c;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (gj < g.N && gk < ke) v = *reinterpret_cast<const uint4 *>(g.B + (int64_t)gk * g.b_k + gj);
         const bf16 *pv = reinterpret_cast<const bf16 *>(&v);
 #pragma unroll
-        for (int q = 0; q < 8; q++) Bs[r + q][c] = pv[q];
-      }
-    } else if (g.b_k == 1) {
-      for (int e = tid; e < kGemmTN * kGemmTK; e += 128) {
-        const int r = e / kGemmTK, c = e % kGemmTK, gj = j0 + r, gk = k0 + c;
-        Bs[r][c] = (gj < g.N && gk < ke) ? g.B[gk + (int64_t)gj * g.b_j] : zero;
+        for (int q = 0; q < 8; q++) Bs[(r + q) * ld + c] = pv[q];
       }
     } else {
-      for (int e = tid; e < kGemmTN * kGemmTK; e += 128) {
-        const int r = e % kGemmTN, c = e / kGemmTN, gj = j0 + r, gk = k0 + c;
-        Bs[r][c] = (gj < g.N && gk < ke) ? g.B[(int64_t)gk * g.b_k + (int64_t)gj * g.b_j] : zero;
+      for (int e = tid; e < kGemmTN * kn; e += 128) {
+        const int r = g.b_k == 1 ? e / kn : e % kGemmTN, c = g.b_k == 1 ? e % kn : e / kGemmTN;
+        const int gj = j0 + r, gk = k0 + c;
+        Bs[r * ld + c] = (gj < g.N && gk < ke) ? g.B[(int64_t)gk * g.b_k + (int64_t)gj * g.b_j] : zero;
       }
     }
     __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < kGemmTK; kk += 16) {
+    for (int kk = 0; kk < kn; kk += 16) {
       uint32_t a[2][4], b[4][2];
 #pragma unroll
       for (int mt = 0; mt < 2; mt++) {
-        const int r = wm * 32 + mt * 16 + gq;
-        a[mt][0] = *reinterpret_cast<const uint32_t *>(&As[r][kk + tq * 2]);
-        a[mt][1] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + tq * 2]);
-        a[mt][2] = *reinterpret_cast<const uint32_t *>(&As[r][kk + tq * 2 + 8]);
-        a[mt][3] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + tq * 2 + 8]);
+        const bf16 *r0 = As + (wm * 32 + mt * 16 + gq) * ld + kk + tq * 2;
+        a[mt][0] = *reinterpret_cast<const uint32_t *>(r0);
+        a[mt][1] = *reinterpret_cast<const uint32_t *>(r0 + 8 * ld);
+        a[mt][2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
+        a[mt][3] = *reinterpret_cast<const uint32_t *>(r0 + 8 * ld + 8);
       }
 #pragma unroll
       for (int nt = 0; nt < 4; nt++) {
-        const int c = wn * 32 + nt * 8 + gq;
-        b[nt][0] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + tq * 2]);
-        b[nt][1] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + tq * 2 + 8]);
+        const bf16 *c0 = Bs + (wn * 32 + nt * 8 + gq) * ld + kk + tq * 2;
+        b[nt][0] = *reinterpret_cast<const uint32_t *>(c0);
+        b[nt][1] = *reinterpret_cast<const uint32_t *>(c0 + 8);
       }
 #pragma unroll
       for (int mt = 0; mt < 2; mt++)
@@ -434,10 +432,24 @@ static int gemm(cudaStream_t st, GemmArgs g, int splits = 1) {
   const bool kfit = g.K % 8 == 0 && g.k_split % 8 == 0;
   g.vec_a = al16(g.A) && ((g.a_k == 1 && g.a_i % 8 == 0 && kfit) || (g.a_i == 1 && g.a_k % 8 == 0 && g.M % 8 == 0));
   g.vec_b = al16(g.B) && ((g.b_k == 1 && g.b_j % 8 == 0 && kfit) || (g.b_j == 1 && g.b_k % 8 == 0 && g.N % 8 == 0));
+  const int krange = std::min(g.K, g.k_split);
+  g.kstage = std::min(kGemmMaxStage, (krange + 31) / 32 * 32);
+  const size_t smem = (size_t)(kGemmTM + kGemmTN) * (g.kstage + kGemmPad) * sizeof(bf16);
   const dim3 grid((unsigned)((g.N + kGemmTN - 1) / kGemmTN), (unsigned)((g.M + kGemmTM - 1) / kGemmTM),
                   (unsigned)splits);
-  k_prop_gemm<EPI><<<grid, 128, 0, st>>>(g);
+  k_prop_gemm<EPI><<<grid, 128, smem, st>>>(g);
   PD_CUDA(cudaGetLastError());
+  return PD_OK;
+}
+
+// Opts the product kernels into the shared memory of a full stage (done when a
+// network is created on a device, before any capture of a training step).
+static int gemm_setup() {
+  const int bytes = (int)((kGemmTM + kGemmTN) * (kGemmMaxStage + kGemmPad) * sizeof(bf16));
+  PD_CUDA(cudaFuncSetAttribute(k_prop_gemm<EPI_GELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  PD_CUDA(cudaFuncSetAttribute(k_prop_gemm<EPI_LINEAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  PD_CUDA(cudaFuncSetAttribute(k_prop_gemm<EPI_DGELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  PD_CUDA(cudaFuncSetAttribute(k_prop_gemm<EPI_PARTIAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   return PD_OK;
 }
 
@@ -613,7 +625,7 @@ extern "C" int pd_proposer_create(pd_ctx *ctx, const pd_train_params *bounds, ui
     o += dn[l];
   }
   p->P = o;
-  int rc = PD_OK;
+  int rc = gemm_setup();
   if (rc == PD_OK) rc = p->master.ensure(p->P * 4);
   if (rc == PD_OK) rc = p->m.ensure(p->P * 4);
   if (rc == PD_OK) rc = p->v.ensure(p->P * 4);

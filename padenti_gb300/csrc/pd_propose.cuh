@@ -71,17 +71,19 @@ PD_D uint32_t prop_component(const PropSrc &p, uint32_t slot, uint64_t stream) {
   return pick;
 }
 
-// Draw k of dimension d of component g (Box-Muller on two hash uniforms, with
-// the fast exp / log / cos intrinsics: the draws need not match any other
-// implementation, only be reproducible), mapped back to the value range,
-// rounded to the nearest integer and clamped.
+// Draw k of dimension d of component g, mapped back to the value range,
+// rounded to the nearest integer and clamped.  The standard normal variate is
+// an Irwin-Hall sum of four 16-bit uniforms of one hash, scaled to unit
+// variance (support +-3.46 sd): no transcendental function per draw, and the
+// same value on every device.
 PD_D int32_t prop_draw(const PropSrc &p, uint32_t slot, uint32_t g, uint32_t d, uint64_t stream, uint32_t k) {
   const float *o = p.out + (size_t)slot * p.ldo;
   const float mu = o[kPropG + g * p.DY + d];
   const float s = fminf(fmaxf(o[kPropG + kPropG * p.DY + g * p.DY + d], kPropSMin), kPropSMax);
-  const uint64_t h1 = prop_mix(stream ^ (0x51ED27ull + 2ull * k + 1ull) * 0x2545F4914F6CDD1Dull);
-  const uint64_t h2 = prop_mix(h1 + 0x632BE59BD9B4E019ull);
-  const float z = sqrtf(-2.0f * __logf(prop_unit(h1))) * __cosf(6.283185307f * prop_unit(h2));
+  const uint64_t h = prop_mix(stream ^ (0x51ED27ull + 2ull * k + 1ull) * 0x2545F4914F6CDD1Dull);
+  const uint32_t u = (uint32_t)(h & 0xffffu) + (uint32_t)((h >> 16) & 0xffffu) + (uint32_t)((h >> 32) & 0xffffu) +
+                     (uint32_t)(h >> 48);
+  const float z = ((float)u - 131070.0f) * (1.7320508f / 65536.0f);
   const float y = mu + __expf(s) * z;
   float v = p.lo[d] + (y + 1.0f) * 0.5f * p.span[d];
   v = fminf(fmaxf(v, p.lo[d]), p.lo[d] + p.span[d]);

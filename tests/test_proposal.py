@@ -194,3 +194,37 @@ def test_proposed_tree_is_valid_deterministic_and_records_match():
             continue
         c = np.bincount(labels[on], minlength=9).astype(np.float32)
         assert np.array_equal(t1.posteriors[node].view(np.uint32), (c / np.float32(c.sum())).view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_network_gain_over_uniform_candidates():
+    """What the trained network gains over the method without it: one tree with 25 proposed + 5
+    uniform candidates per node against 30 uniform ones, on 150 synthetic 640x480 depth maps
+    (9 classes, 2000 samples each), depth 12; the network is fitted to the records of a plain
+    2000-candidate tree.  Held-out per-pixel accuracy on the object (non-background) pixels of
+    30 unseen images must be at least 0.5 pt higher with the network (measured: about +2 pt)."""
+    import padenti_gb300 as pg
+    from bench import forest_accuracy
+
+    px, lb, sm = pg.synth_depth(0, 150, 640, 480, parts=1, min_ellipses=2, max_ellipses=5, samples_per_image=2000,
+                                bg_permille=100)
+    cfg = pg.ForestConfig("depth_diff2", 9)
+    ts = pg.training_set(9, px, lb, sm)
+    tp = pg.TreeTrainerParameters(2000, 50, [-60000] * 4, [60000] * 4, -500, 500, 20)
+    tr = pg.TreeTrainer(cfg)
+    tr.set_tuning("records", 1)
+    tr.train(pg.Tree(cfg, 0, 12), ts, tp)
+    rec = tr.records()
+    tr.set_tuning("records", 0)
+    tp30 = pg.TreeTrainerParameters(30, 50, [-60000] * 4, [60000] * 4, -500, 500, 20)
+    net = pg.ProposalNetwork(tr, tp30, seed=0)
+    fit = net.fit(rec, steps=200, batch=2048, lr=2e-3)
+    assert fit["loss"][-10:].mean() < fit["loss"][:10].mean() - 0.5
+    hx, hl, _ = pg.synth_depth(0, 30, 640, 480, first_image=5_000_000, parts=1, min_ellipses=2, max_ellipses=5,
+                               samples_per_image=1)
+    learned, uniform = pg.Tree(cfg, 1, 12), pg.Tree(cfg, 1, 12)
+    tr.train_proposed(learned, ts, tp30, net, 25)
+    tr.train(uniform, ts, tp30)
+    acc_l = forest_accuracy(pg, cfg, [learned], 0, hx, hl)
+    acc_u = forest_accuracy(pg, cfg, [uniform], 0, hx, hl)
+    assert acc_l[1] >= acc_u[1] + 0.005, (acc_l, acc_u)
