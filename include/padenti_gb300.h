@@ -170,6 +170,8 @@ int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
  *               so that neighbouring lanes probe neighbouring pixels; 0: index order;
  *   "sample_group" bytes of images and labels pd_sample stages per round trip,
  *               >= 4096 (default 512 MiB);
+ *   "persist"   1 (default): one persistent histogram grid per launch (a few CTAs per SM) pulling the
+ *               work items from a device counter, largest first; 0: one CTA per work item;
  *   "records"   1: training calls keep one pd_record per split node (pd_train_records); 0 (default): none. */
 int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value);
 /* Synchronises the context's stream. */
@@ -234,6 +236,30 @@ int pd_split_noalloc(const pd_train_params *params, uint32_t n_classes, const ui
                      int32_t *out_f_device, double *out_gain_device, void *stream);
 /* Exact per-integer log2 table used by the split: out[n] = log2(n), out[0]=0. */
 int pd_log2_table(pd_ctx *ctx, uint32_t n, double *out);
+
+/* Candidate-sharded training ---------------------------------------------------
+ * Several ranks (one GPU each) train one tree together: rank r evaluates the
+ * candidates [f_begin, f_end) of every node (candidate f of a node is drawn
+ * from its own MD5 seed (tree, node, f), hist_update.cl:62-65,127-130, so no
+ * rank needs another's candidates), and after the split of each frontier slice
+ * `exchange` is called with this rank's best split of every node of the slice:
+ * gain_key[i] (an int64 whose order is the order of the exact gains; INT64_MIN
+ * when the rank has none), cand_index[i] = t * F + f (-1: none) and
+ * left_counts[i * n_classes ...] (its left class counts).  It must return 0 and
+ * leave in cand_index / left_counts the global winner of every node: the
+ * largest key, ties to the lowest index (the single-GPU rule; for example an
+ * all-reduce MAX of the keys, MIN of the indices holding the maximum, and a sum
+ * of the owner's counts).  Every rank then applies the same splits and
+ * reassignment, so all ranks end with the same tree -- the unsharded one.  The
+ * exchange replaces the host argmax of learn_best_featthr.hpp:101-112 across
+ * GPUs.  Slices are cut for all params->n_features candidates, the same on
+ * every rank. */
+typedef int (*pd_exchange_fn)(void *user, uint32_t n_nodes, uint32_t n_classes, int64_t *gain_key,
+                              int64_t *cand_index, uint32_t *left_counts);
+int pd_train_tree_sharded(pd_ctx *ctx, const pd_train_params *params, uint32_t f_begin, uint32_t f_end,
+                          pd_exchange_fn exchange, void *user, uint32_t tree_id, uint32_t start_depth,
+                          uint32_t end_depth, const float *root_prior, int32_t *left_child, void *features,
+                          void *thresholds, float *posteriors);
 
 /* Learned candidate proposals ------------------------------------------------
  * No counterpart in the reference, which draws every candidate uniformly

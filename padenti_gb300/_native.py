@@ -83,6 +83,11 @@ class Sampler(C.Structure):
     ]
 
 
+# int exchange(void *user, uint32 n_nodes, uint32 n_classes, int64 *gain_key, int64 *cand_index, uint32 *left_counts)
+EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                          C.POINTER(C.c_uint32))
+
+
 class Record(C.Structure):
     """pd_record: one split node of a trained tree (learned proposals)."""
     _fields_ = [("depth", C.c_uint32), ("count", C.c_uint32), ("node", C.c_uint32), ("tree", C.c_uint32),
@@ -130,6 +135,8 @@ _SIGS = {
     "pd_split": (C.c_int, [_P, C.POINTER(TrainParams), _P, _P, C.c_uint32, _P, _P, _P]),
     "pd_log2_table": (C.c_int, [_P, C.c_uint32, _P]),
     "pd_train_records": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "pd_train_tree_sharded": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, C.c_uint32, _P, _P, C.c_uint32,
+                                        C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]),
     "pd_proposer_create": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint64, C.POINTER(_P)]),
     "pd_proposer_destroy": (C.c_int, [_P]),
     "pd_proposer_dims": (C.c_int, [_P, _P, C.POINTER(C.c_uint64)]),

@@ -59,6 +59,8 @@ extern "C" int pd_ctx_create(const pd_config *cfg, int device, pd_ctx **out) {
   pd_ctx *c = new pd_ctx();
   c->cfg = *cfg;
   c->device = device;
+  cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, device);
+  if (c->n_sms <= 0) c->n_sms = 1;
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
@@ -81,7 +83,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
   DevBuf *bufs[] = {&ctx->pixels, &ctx->img_off, &ctx->img_wh, &ctx->s_xy, &ctx->s_img, &ctx->s_label,
                     &ctx->log2_tab, &ctx->magic_tab, &ctx->snode, &ctx->act[0], &ctx->act[1], &ctx->act_rec[0], &ctx->act_rec[1], &ctx->s_rec, &ctx->act_slot[0],
                     &ctx->act_slot[1], &ctx->flags, &ctx->scan_blocks, &ctx->slot_adj, &ctx->scatter_err,
-                    &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->cand_ord, &ctx->parent, &ctx->xlog2_tab, &ctx->split_par, &ctx->hist, &ctx->g32, &ctx->items,
+                    &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->cand_ord, &ctx->parent, &ctx->xlog2_tab, &ctx->split_par, &ctx->hist, &ctx->g32, &ctx->items, &ctx->hist_queue,
                     &ctx->zero_slots, &ctx->split_out, &ctx->split_cl, &ctx->recheck, &ctx->split_scratch, &ctx->fused_scratch, &ctx->t_lc,
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
                     &ctx->f_post, &ctx->f_meta, &ctx->f_cand, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
@@ -136,6 +138,9 @@ extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
   } else if (n == "sample_group") {
     PD_CHECK(value >= 4096, PD_ERR_INVALID, "sample_group %lld below 4096 bytes", (long long)value);
     ctx->sample_group = (uint64_t)value;
+  } else if (n == "persist") {
+    PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "persist must be 0 or 1");
+    ctx->persist = value != 0;
   } else if (n == "records") {
     PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "records must be 0 or 1");
     ctx->collect_records = value != 0;

@@ -23,6 +23,8 @@ struct pd_ctx {
   uint32_t hist_spi = 8;  // samples per iteration of the histogram kernel (2, 4 or 8)
   uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
   bool cand_order = true;    // order each node's candidate columns by first-probe offset
+  bool persist = true;       // one persistent histogram grid per launch, items pulled largest first
+  int n_sms = 0;             // multiprocessors of the context's GPU
   uint64_t sample_group = 512ull << 20;  // bytes of images + labels pd_sample stages per round trip
   bool collect_records = false;          // keep a pd_record per split node (learned proposals)
   std::vector<pd_record> records;        // of the last training call
@@ -61,7 +63,7 @@ struct pd_ctx {
   pd::DevBuf cand_feat, cand_thr, cand_perm;
   pd::DevBuf cand_ord;       // [slots][F] original candidate index of each column
   pd::DevBuf hist, g32;
-  pd::DevBuf items, zero_slots;
+  pd::DevBuf items, zero_slots, hist_queue;
   pd::DevBuf split_out, split_cl, recheck, split_scratch, fused_scratch;
   pd::DevBuf t_lc, t_feat, t_thr, t_post;  // device copy of the tree being trained
   pd_train_stats stats{};

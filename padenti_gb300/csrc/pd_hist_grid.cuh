@@ -20,6 +20,7 @@ struct HistGrid {
   size_t smem;            // dynamic shared memory per CTA
   FusedSplit fs;
   cudaEvent_t ev_before;  // recorded just before the first launch (may be null)
+  unsigned *queue;        // persistent launch: the work counter (zeroed here), null: one CTA per item
 };
 
 template <class P>

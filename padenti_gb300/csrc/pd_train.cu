@@ -102,9 +102,10 @@ int init_tables(pd_ctx *ctx) {
   return PD_OK;
 }
 
-static CandBounds bounds(const pd_train_params *p, int D) {
+static CandBounds bounds(const pd_train_params *p, int D, uint32_t f_base = 0) {
   CandBounds b;
   memset(&b, 0, sizeof(b));
+  b.f_base = f_base;
   for (int d = 0; d < D; d++) {
     b.low[d] = p->feat_low[d];
     b.up[d] = p->feat_up[d];
@@ -156,14 +157,14 @@ static uint64_t slot_bytes(const pd_ctx *ctx, const pd_train_params *p) {
 template <class P>
 static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tree, const int32_t *d_nodes,
                              uint32_t n, bool ordered = false, const uint32_t **ord_out = nullptr,
-                             const PropSrc *prop = nullptr) {
+                             const PropSrc *prop = nullptr, uint32_t f_base = 0) {
   using FeatT = typename P::feat_t;
   const uint32_t F = p->n_features;
   const uint64_t total = (uint64_t)n * F;
   const uint32_t *ord = nullptr;
   if (ord_out) *ord_out = nullptr;
   if (!total) return PD_OK;
-  const CandBounds b = bounds(p, P::kFeatDim);
+  const CandBounds b = bounds(p, P::kFeatDim, f_base);
   if (ordered && F <= kOrderMaxF) {
     uint32_t N = 1;
     while (N < F) N <<= 1;
@@ -217,9 +218,26 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   const uint32_t F = p->n_features, T = p->n_thresholds, K = ctx->cfg.n_classes;
   const uint32_t tiles = (F + kTileF - 1) / kTileF;
   PD_CHECK(ctx->chunk >= 1 && ctx->chunk <= kMaxChunk, PD_ERR_INVALID, "chunk %u outside [1,%u]", ctx->chunk, kMaxChunk);
-  // the work list is written straight into pinned staging (sized by a first pass)
-  uint64_t n_items = 0;
-  for (uint32_t i = 0; i < n; i++) n_items += (off[i + 1] - off[i] + ctx->chunk - 1) / ctx->chunk * tiles;
+  // the work list is written straight into pinned staging (sized by a first
+  // pass); for a persistent launch it is ordered largest item first (by the
+  // power of two of its sample count, stable), so the last items to start are
+  // the short ones
+  const bool persist = ctx->persist;
+  auto bucket = [](uint64_t cnt) { return cnt ? 63 - __builtin_clzll(cnt) : 0; };  // floor(log2), <= 15
+  uint64_t n_items = 0, pos[17] = {};
+  for (uint32_t i = 0; i < n; i++) {
+    const uint64_t cnt = off[i + 1] - off[i];
+    const uint64_t chunks = (cnt + ctx->chunk - 1) / ctx->chunk;
+    n_items += chunks * tiles;
+    for (uint64_t c = 0; persist && c < chunks; c++)
+      pos[bucket(std::min<uint64_t>(cnt - c * ctx->chunk, ctx->chunk))] += tiles;
+  }
+  uint64_t acc = 0;
+  for (int b = 15; persist && b >= 0; b--) {  // start of each bucket, largest first
+    const uint64_t c = pos[b];
+    pos[b] = acc;
+    acc += c;
+  }
   PD_TRY(ctx->h_items.ensure(std::max<uint64_t>(1, n_items) * sizeof(WorkItem)));
   WorkItem *items = ctx->h_items.as<WorkItem>();
   uint64_t ni = 0;
@@ -247,7 +265,8 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
         w.begin = cb;
         w.end = ce;
         w.multi = chunks > 1 ? 1u : (fused ? 2u : 0u);
-        items[ni++] = w;
+        items[persist ? pos[bucket(ce - cb)]++ : ni] = w;
+        ni++;
       }
     }
   }
@@ -311,6 +330,11 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
   g.smem = smem;
   g.fs = fs;
   g.ev_before = ev_before;
+  g.queue = nullptr;
+  if (persist && ni < 0x7fffffffull) {
+    PD_TRY(ctx->hist_queue.ensure(16));
+    g.queue = ctx->hist_queue.as<unsigned>();
+  }
   PD_TRY(launch_hist_grid<P>(ctx, g));
   if (ev_after) PD_CUDA(cudaEventRecord(ev_after, ctx->stream));
   return PD_OK;
@@ -395,14 +419,31 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 // ------------------------------------------------------------- one tree ----
+// A rank of candidate-sharded training: it evaluates candidates
+// [f_base, f_base + params->n_features) of F_total, and `exchange` turns the
+// ranks' best splits of a slice into the global ones.
+struct Shard {
+  uint32_t f_base, F_total;
+  pd_exchange_fn exchange;
+  void *user;
+};
+
+// Order key of a double (the device's gain_order_key).
+static int64_t gain_key_host(double g) {
+  int64_t b;
+  memcpy(&b, &g, 8);
+  return b < 0 ? (INT64_MIN - b - 1) : b;
+}
+
 // With `prop`, candidates f < n_prop of every node come from the proposal
 // network (learned proposals); with ctx->collect_records, one pd_record per
-// split node is kept.
+// split node is kept; with `shard`, this rank's candidates are a range of the
+// node's and each slice's winners are exchanged with the other ranks.
 template <class P>
 static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_id, uint32_t end_depth,
                            const float *root_prior, int32_t *lc, typename P::feat_t *feats,
                            typename P::feat_t *thrs, float *posts, pd_proposer *prop = nullptr,
-                           uint32_t n_prop = 0) {
+                           uint32_t n_prop = 0, const Shard *shard = nullptr) {
   using FeatT = typename P::feat_t;
   constexpr int D = P::kFeatDim;
   const auto t_start = std::chrono::steady_clock::now();
@@ -452,7 +493,10 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   std::vector<uint64_t> cur_off{0, S};
   int cur = 0;
   uint64_t n_act = S;
-  const uint64_t per_slot = slot_bytes(ctx, p);
+  // slices are sized for all F_total candidates when sharded, so every rank cuts the same slices
+  pd_train_params p_all = *p;
+  if (shard) p_all.n_features = shard->F_total;
+  const uint64_t per_slot = slot_bytes(ctx, &p_all);
   const uint32_t max_slots = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ctx->hist_budget / per_slot, 1u << 30));
   DevBuf d_nodes, d_ctot, d_next, d_split_list;
   std::vector<SplitOut> h_out;
@@ -493,7 +537,8 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
         PD_TRY(proposer_infer(prop, d_ctot.as<uint32_t>(), ns, depth, n_prop, &src));
         PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, ctx->cand_order, &d_ord, &src));
       } else {
-        PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, ctx->cand_order, &d_ord));
+        PD_TRY(launch_candidates<P>(ctx, p, tree_id, d_nodes.as<int32_t>(), ns, ctx->cand_order, &d_ord, nullptr,
+                                    shard ? shard->f_base : 0u));
       }
       PD_CUDA(cudaEventRecord(ev[1], st));
       uint64_t n_items = 0;
@@ -528,6 +573,38 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       stats.ms_hist += elapsed(ev[6], ev[2]);
       stats.ms_split += elapsed(ev[2], ev[3]);
       stats.split_rechecked += rechecked;
+
+      if (shard) {
+        // the ranks' best splits -> the global ones: largest exact gain, ties to the lowest t * F + f
+        std::vector<int64_t> key(ns), idx(ns);
+        for (uint32_t i = 0; i < ns; i++) {
+          const SplitOut &o = h_out[i];
+          key[i] = o.t < 0 ? INT64_MIN : gain_key_host(o.gain);
+          idx[i] = o.t < 0 ? -1 : (int64_t)o.t * shard->F_total + (int64_t)(shard->f_base + (uint32_t)o.f);
+          if (o.t < 0) memset(&h_cl[(size_t)i * K], 0, K * 4);
+        }
+        PD_CHECK(shard->exchange(shard->user, ns, K, key.data(), idx.data(), h_cl.data()) == 0, PD_ERR_STATE,
+                 "the exchange of the ranks' best splits failed at depth %u", depth);
+        for (uint32_t i = 0; i < ns; i++) {
+          SplitOut &o = h_out[i];
+          if (idx[i] < 0) {
+            o.t = -1;
+            continue;
+          }
+          const uint32_t t_g = (uint32_t)(idx[i] / shard->F_total), f_g = (uint32_t)(idx[i] % shard->F_total);
+          const bool mine = o.t >= 0 && (uint32_t)o.t == t_g && shard->f_base + (uint32_t)o.f == f_g;
+          o.t = (int32_t)t_g;
+          o.gain = 0.0;
+          if (!mine) {
+            // the winner lives on another rank: its values from its seeds (hist_update.cl:62-184)
+            const uint32_t node = (uint32_t)frontier[s0 + i];
+            FeatT fv[PD_MAX_FEAT_DIM];
+            candidate_feature<FeatT>(tree_id, node, f_g, D, p->feat_low, p->feat_up, fv);
+            for (int d = 0; d < D; d++) h_par[(size_t)i * (D + 1) + d] = fv[d];
+            h_par[(size_t)i * (D + 1) + D] = candidate_threshold<FeatT>(tree_id, node, f_g, t_g, p->thr_low, p->thr_up);
+          }
+        }
+      }
 
       // finalize (learn_best_featthr.hpp:117-243)
       for (uint32_t i = 0; i < ns; i++) {
@@ -720,6 +797,29 @@ extern "C" int pd_train_tree_proposed(pd_ctx *ctx, pd_proposer *prop, const pd_t
     return train_tree_impl<P>(ctx, params, tree_id, end_depth, root_prior, left_child,
                               static_cast<FeatT *>(features), static_cast<FeatT *>(thresholds), posteriors, prop,
                               n_proposed);
+  });
+}
+
+extern "C" int pd_train_tree_sharded(pd_ctx *ctx, const pd_train_params *params, uint32_t f_begin, uint32_t f_end,
+                                     pd_exchange_fn exchange, void *user, uint32_t tree_id, uint32_t start_depth,
+                                     uint32_t end_depth, const float *root_prior, int32_t *left_child, void *features,
+                                     void *thresholds, float *posteriors) {
+  PD_CHECK(ctx && exchange, PD_ERR_INVALID, "null context or exchange function");
+  PD_CHECK(ctx->have_dataset, PD_ERR_STATE, "no dataset uploaded");
+  PD_CHECK(start_depth == 1, PD_ERR_INVALID, "Starting depth must be equal to 1");
+  PD_CHECK(end_depth >= 1 && end_depth <= 24, PD_ERR_UNSUPPORTED, "end_depth %u outside [1,24]", end_depth);
+  PD_CHECK(root_prior && left_child && features && thresholds && posteriors, PD_ERR_INVALID, "null tree array");
+  PD_TRY(check_params(ctx, params));
+  PD_CHECK(f_begin < f_end && f_end <= params->n_features, PD_ERR_INVALID,
+           "candidate range [%u, %u) outside [0, %u)", f_begin, f_end, params->n_features);
+  PD_CUDA(cudaSetDevice(ctx->device));
+  pd_train_params local = *params;
+  local.n_features = f_end - f_begin;
+  const Shard shard{f_begin, params->n_features, exchange, user};
+  return dispatch_config(ctx->cfg, [&]<class P>() {
+    using FeatT = typename P::feat_t;
+    return train_tree_impl<P>(ctx, &local, tree_id, end_depth, root_prior, left_child, static_cast<FeatT *>(features),
+                              static_cast<FeatT *>(thresholds), posteriors, nullptr, 0, &shard);
   });
 }
 

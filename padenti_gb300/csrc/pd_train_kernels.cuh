@@ -48,6 +48,7 @@ struct CandBounds {
   int32_t low[PD_MAX_FEAT_DIM];
   int32_t up[PD_MAX_FEAT_DIM];
   int32_t thr_lo, thr_hi;
+  uint32_t f_base;  // candidate f of a table is the node's candidate f_base + f (candidate-sharded training)
 };
 
 // One histogram work item: candidates [tile*64, tile*64+64) of frontier slot
@@ -122,6 +123,7 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
   if (active) {
     const uint32_t node = (uint32_t)nodes[n];
     const uint32_t f = ord ? ord[(size_t)n * F + c] : c;
+    const uint32_t fg = b.f_base + f;  // the candidate's index among all of the node's candidates
     const bool net = prop.out != nullptr && f < prop.n_prop;
     uint64_t stream = 0;
     uint32_t g = 0;
@@ -131,13 +133,13 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
       g = prop_component(prop, n, stream);
       for (int d = 0; d < D; d++) fv[d] = (FeatT)prop_draw(prop, n, g, (uint32_t)d, stream, (uint32_t)d);
     } else {
-      candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
+      candidate_feature<FeatT>(tree, node, fg, D, b.low, b.up, fv);
     }
     for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + c] = fv[d];
     uint32_t *k = sk + threadIdx.x;
     FeatT *v = sv + threadIdx.x;
     uint8_t *id = si + threadIdx.x;
-    uint32_t seed[4] = {tree, node, f, 1u}, st[4] = {0u, 0u, 0u, 0u};
+    uint32_t seed[4] = {tree, node, fg, 1u}, st[4] = {0u, 0u, 0u, 0u};
     for (uint32_t t = 0; t < T; t++) {
       if (!net && (t & 3u) == 0) {
         md5_block(seed, st);
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(kOrderThreads) k_cand_order(const int32_t *__r
         vy = (int32_t)(FeatT)prop_draw(prop, n, g, (uint32_t)X + 1u, stream, (uint32_t)X + 1u);
       } else {
         FeatT fv[D];
-        candidate_feature<FeatT>(tree, node, f, D, b.low, b.up, fv);
+        candidate_feature<FeatT>(tree, node, b.f_base + f, D, b.low, b.up, fv);
         vx = (int32_t)fv[X];
         vy = (int32_t)fv[X + 1];
       }
@@ -742,13 +744,13 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   fs.out[slot] = o;
 }
 
+// One work item of the histogram kernel (the whole CTA).
 template <class P, uint32_t TP, int SPI>
-__global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet ds, const SampleRec *__restrict__ rec,
-                                                       const WorkItem *__restrict__ items,
-                                                       const typename P::feat_t *__restrict__ cand_feat,
-                                                       const typename P::feat_t *__restrict__ cand_thr,
-                                                       uint32_t *__restrict__ hist, uint32_t F,
-                                                       uint32_t T, uint32_t K, FusedSplit fs) {
+__device__ __forceinline__ void hist_item(const DevSet &ds, const SampleRec *__restrict__ rec, const WorkItem w,
+                                          const typename P::feat_t *__restrict__ cand_feat,
+                                          const typename P::feat_t *__restrict__ cand_thr,
+                                          uint32_t *__restrict__ hist, uint32_t F, uint32_t T, uint32_t K,
+                                          const FusedSplit &fs) {
   using FeatT = typename P::feat_t;
   using ImgT = typename P::img_t;
   constexpr int D = P::kFeatDim;
@@ -759,7 +761,6 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
   // sh_g [T][64] gains, sh_nl [T][32] packed left totals
   float *sh_g = reinterpret_cast<float *>(sh_thr);
   uint32_t *sh_nl = reinterpret_cast<uint32_t *>(sh_g + (size_t)T * kTileF);
-  const WorkItem w = items[blockIdx.x];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t f0 = w.tile * kTileF;
   const uint32_t fa = f0 + lane, fb = f0 + 32 + lane;
@@ -826,6 +827,34 @@ __global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet 
         }
       }
     }
+  }
+}
+
+// The histogram kernel over a work list.  queue == null: one CTA per item
+// (blockIdx.x).  Otherwise a persistent grid (a few CTAs per SM) whose CTAs
+// take items k = 0, 1, ... in list order from the counter *queue (an atomic
+// add, no wait), so a list sorted largest first keeps every SM busy to the end.
+template <class P, uint32_t TP, int SPI>
+__global__ void __launch_bounds__(kHistThreads, SPI <= 2 ? 3 : 2) k_hist(DevSet ds, const SampleRec *__restrict__ rec,
+                                                       const WorkItem *__restrict__ items, uint32_t n_items,
+                                                       unsigned *__restrict__ queue,
+                                                       const typename P::feat_t *__restrict__ cand_feat,
+                                                       const typename P::feat_t *__restrict__ cand_thr,
+                                                       uint32_t *__restrict__ hist, uint32_t F,
+                                                       uint32_t T, uint32_t K, FusedSplit fs) {
+  if (queue == nullptr) {
+    hist_item<P, TP, SPI>(ds, rec, items[blockIdx.x], cand_feat, cand_thr, hist, F, T, K, fs);
+    return;
+  }
+  __shared__ uint32_t s_next;
+  for (;;) {
+    if (threadIdx.x == 0) s_next = atomicAdd(queue, 1u);
+    __syncthreads();
+    const uint32_t k = s_next;
+    __syncthreads();  // read by every thread before thread 0 takes the next item
+    if (k >= n_items) return;
+    hist_item<P, TP, SPI>(ds, rec, items[k], cand_feat, cand_thr, hist, F, T, K, fs);
+    __syncthreads();  // the item's shared memory is free again
   }
 }
 

@@ -70,6 +70,7 @@ def test_full_size_tree_properties():
     tr.set_tuning("chunk", 4096)
     tr.set_tuning("hist_spi", 4)
     tr.set_tuning("cand_order", 0)
+    tr.set_tuning("persist", 0)
     again = pg.Tree(cfg, 0, 16)
     tr.train(again, ts, tp)
     assert np.array_equal(again.left_child, lc)

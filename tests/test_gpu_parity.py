@@ -258,12 +258,14 @@ def test_launch_shape_knobs_do_not_change_the_tree():
     cfg, ts, tp, _ = depth_case(n_images=16, n_features=96, n_thresholds=20)
     a = pg.Tree(cfg, 5, 7)
     pg.TreeTrainer(cfg).train(a, ts, tp)
-    for chunk, spi, fuse, order in [(256, 4, 0, 1), (1000, 2, 300, 0), (65535, 8, 65535, 1), (4096, 8, 0, 0)]:
+    for chunk, spi, fuse, order, persist in [(256, 4, 0, 1, 1), (1000, 2, 300, 0, 0), (65535, 8, 65535, 1, 1),
+                                             (4096, 8, 0, 0, 0), (16384, 8, 4096, 1, 0)]:
         tr = pg.TreeTrainer(cfg)
         tr.set_tuning("chunk", chunk)
         tr.set_tuning("hist_spi", spi)
         tr.set_tuning("fuse_max", fuse)
         tr.set_tuning("cand_order", order)
+        tr.set_tuning("persist", persist)
         b = pg.Tree(cfg, 5, 7)
         tr.train(b, ts, tp)
         assert np.array_equal(a.left_child, b.left_child)
