@@ -528,10 +528,48 @@ void or_priors(const or_dataset *ds, uint32_t K, float *out) {
 /* cl_tree_trainer_impl_init.hpp:333-365 (frontier), learn_best_featthr.hpp: */
 /* 117-243 (finalize) and kernels/predict.cl:36-85 (reassignment).           */
 /* ------------------------------------------------------------------------ */
+/* A rank of candidate-sharded training: it splits on candidates [f0, f1) only
+ * and `exchange` turns the ranks' best splits into the global ones (the
+ * library's pd_train_tree_sharded protocol). */
+typedef struct {
+  uint32_t f0, f1;
+  or_exchange_fn exchange;
+  void *user;
+} or_shard;
+
+static int64_t gain_key64(double g) {
+  int64_t b;
+  memcpy(&b, &g, 8);
+  return b < 0 ? (INT64_MIN - b - 1) : b;
+}
+
+static int train_tree_impl(const or_params *p, const or_dataset *ds, uint32_t tree_id, uint32_t end_depth,
+                           const float *root_prior, int32_t *lc, int32_t *feats, int32_t *thrs, float *posts,
+                           int32_t *sample_leaf, int reference_cost, int n_threads, or_stats *stats,
+                           const or_shard *sh);
+
 int or_train_tree(const or_params *p, const or_dataset *ds, uint32_t tree_id, uint32_t end_depth,
                   const float *root_prior, int32_t *lc, int32_t *feats, int32_t *thrs,
                   float *posts, int32_t *sample_leaf, int reference_cost, int n_threads,
                   or_stats *stats) {
+  return train_tree_impl(p, ds, tree_id, end_depth, root_prior, lc, feats, thrs, posts, sample_leaf, reference_cost,
+                         n_threads, stats, NULL);
+}
+
+int or_train_tree_sharded(const or_params *p, const or_dataset *ds, uint32_t tree_id, uint32_t end_depth,
+                          const float *root_prior, uint32_t f0, uint32_t f1, or_exchange_fn exchange, void *user,
+                          int32_t *lc, int32_t *feats, int32_t *thrs, float *posts, int32_t *sample_leaf,
+                          int n_threads) {
+  if (f0 >= f1 || f1 > p->n_features || !exchange) return -1;
+  or_shard sh = {f0, f1, exchange, user};
+  return train_tree_impl(p, ds, tree_id, end_depth, root_prior, lc, feats, thrs, posts, sample_leaf, 0, n_threads,
+                         NULL, &sh);
+}
+
+static int train_tree_impl(const or_params *p, const or_dataset *ds, uint32_t tree_id, uint32_t end_depth,
+                           const float *root_prior, int32_t *lc, int32_t *feats, int32_t *thrs, float *posts,
+                           int32_t *sample_leaf, int reference_cost, int n_threads, or_stats *stats,
+                           const or_shard *sh) {
   const uint32_t F = p->n_features, T = p->n_thresholds, K = (uint32_t)p->n_classes;
   const int D = p->feat_dim;
   if (end_depth < 1 || end_depth > 24 || K > 64 || D > OR_MAX_FEAT_DIM || T > 256) return -1;
@@ -578,7 +616,38 @@ int or_train_tree(const or_params *p, const or_dataset *ds, uint32_t tree_id, ui
       for (uint32_t i = 0; i < ns; i++) memcpy(ctot + (size_t)i * K, class_tot + (size_t)sl[i] * K, sizeof(uint32_t) * K);
       int32_t *bt = (int32_t *)malloc(sizeof(int32_t) * ns), *bf = (int32_t *)malloc(sizeof(int32_t) * ns);
       double *bg = (double *)malloc(sizeof(double) * ns);
-      or_split(p, hist, ctot, ns, L, S + 2, bt, bf, bg, NULL, NULL);
+      uint32_t *xcl = NULL; /* sharded: the global winners' left class counts */
+      if (sh) {
+        /* this rank's candidates only: the split over columns [f0, f1) */
+        const uint32_t Fl = sh->f1 - sh->f0;
+        uint32_t *sub = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)ns * K * T * Fl);
+        for (size_t r = 0; r < (size_t)ns * K * T; r++)
+          memcpy(sub + r * Fl, hist + r * F + sh->f0, sizeof(uint32_t) * Fl);
+        or_params pl = *p;
+        pl.n_features = Fl;
+        or_split(&pl, sub, ctot, ns, L, S + 2, bt, bf, bg, NULL, NULL);
+        int64_t *key = (int64_t *)malloc(sizeof(int64_t) * ns), *idx = (int64_t *)malloc(sizeof(int64_t) * ns);
+        xcl = (uint32_t *)calloc((size_t)ns * K, sizeof(uint32_t));
+        for (uint32_t i = 0; i < ns; i++) {
+          key[i] = bt[i] < 0 ? INT64_MIN : gain_key64(bg[i]);
+          idx[i] = bt[i] < 0 ? -1 : (int64_t)bt[i] * F + sh->f0 + (uint32_t)bf[i];
+          for (uint32_t l = 0; bt[i] >= 0 && l < K; l++)
+            xcl[(size_t)i * K + l] = sub[(((size_t)i * K + l) * T + (uint32_t)bt[i]) * Fl + (uint32_t)bf[i]];
+        }
+        const int xr = sh->exchange(sh->user, ns, K, key, idx, xcl);
+        for (uint32_t i = 0; i < ns; i++) {
+          bt[i] = idx[i] < 0 ? -1 : (int32_t)(idx[i] / F);
+          bf[i] = idx[i] < 0 ? -1 : (int32_t)(idx[i] % F);
+        }
+        free(key); free(idx); free(sub);
+        if (xr != 0) {
+          free(xcl); free(hist); free(ctot); free(bt); free(bf); free(bg);
+          free(frontier); free(split_now); free(L); free(class_tot); free(node_tot); free(snode); free(smp);
+          return -2;
+        }
+      } else {
+        or_split(p, hist, ctot, ns, L, S + 2, bt, bf, bg, NULL, NULL);
+      }
       st.seconds_hist += t1 - t0;
       st.seconds_split += now_s() - t1;
       for (uint32_t i = 0; i < ns; i++) st.evals += (uint64_t)node_tot[sl[i]] * F;
@@ -589,7 +658,7 @@ int or_train_tree(const or_params *p, const or_dataset *ds, uint32_t tree_id, ui
         if (bt[i] < 0) continue;
         uint32_t cl[64], cr[64], lsum = 0, rsum = 0;
         for (uint32_t l = 0; l < K; l++) {
-          cl[l] = hist[(((size_t)i * K + l) * T + (uint32_t)bt[i]) * F + (uint32_t)bf[i]];
+          cl[l] = xcl ? xcl[(size_t)i * K + l] : hist[(((size_t)i * K + l) * T + (uint32_t)bt[i]) * F + (uint32_t)bf[i]];
           cr[l] = class_tot[(size_t)n * K + l] - cl[l];
           lsum += cl[l]; rsum += cr[l];
         }
@@ -610,7 +679,7 @@ int or_train_tree(const or_params *p, const or_dataset *ds, uint32_t tree_id, ui
         split_now[n] = 1;
         st.nodes_split++;
       }
-      free(hist); free(ctot); free(bt); free(bf); free(bg);
+      free(xcl); free(hist); free(ctot); free(bt); free(bf); free(bg);
     }
     /* reassignment of every sample that sits on a node split at this depth */
 #pragma omp parallel for schedule(static) NT(n_threads)

@@ -125,6 +125,18 @@ int or_train_tree(const or_params *p, const or_dataset *ds, uint32_t tree_id, ui
                   int32_t *thresholds, float *posteriors, int32_t *sample_leaf,
                   int reference_cost, int n_threads, or_stats *stats);
 
+/* Candidate-sharded training (the library's pd_train_tree_sharded protocol):
+ * this rank splits on candidates [f0, f1) of every node and, per frontier
+ * slice, `exchange` receives its best splits -- gain_key (order key of the exact
+ * gain, INT64_MIN for none), cand_index (t * F + f, -1 for none), left_counts
+ * [n][K] -- and must leave the global winners in cand_index / left_counts. */
+typedef int (*or_exchange_fn)(void *user, uint32_t n_nodes, uint32_t n_classes, int64_t *gain_key,
+                              int64_t *cand_index, uint32_t *left_counts);
+int or_train_tree_sharded(const or_params *p, const or_dataset *ds, uint32_t tree_id, uint32_t end_depth,
+                          const float *root_prior, uint32_t f0, uint32_t f1, or_exchange_fn exchange, void *user,
+                          int32_t *lc, int32_t *feats, int32_t *thrs, float *posts, int32_t *sample_leaf,
+                          int n_threads);
+
 /* a11: forest posterior, planar [K][H][W]; masked-out pixels are 0.
  * Trees are given as concatenated SoA arrays; tree t has 2^depth[t]-1 nodes
  * starting at node_off[t]. */

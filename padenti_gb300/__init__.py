@@ -351,6 +351,29 @@ class TreeTrainer(_Ctx):
                                            _ptr(prior), _ptr(lc), _ptr(ft), _ptr(th), _ptr(po)))
         tree.left_child[:n], tree.features[:n], tree.thresholds[:n], tree.posteriors[:n] = lc, ft, th, po
 
+    def train_sharded(self, tree: Tree, ts: TrainingSet, params: TreeTrainerParameters, f_begin: int, f_end: int,
+                      exchange, end_depth: int | None = None) -> None:
+        """This rank's part of candidate-sharded training (pd_train_tree_sharded): it evaluates
+        candidates [f_begin, f_end) of params.n_features, and exchange(key, idx, counts) ->
+        (idx, counts) gives the global best split of every node of a slice (see
+        padenti_gb300.dist: torch_exchange, LocalExchange).  Every rank ends with the same,
+        unsharded tree."""
+        from padenti_gb300 import dist as pdist
+
+        end_depth = tree.depth if end_depth is None else end_depth
+        self.upload(ts)
+        n = (1 << end_depth) - 1
+        lc = np.ascontiguousarray(tree.left_child[:n])
+        ft = np.ascontiguousarray(tree.features[:n])
+        th = np.ascontiguousarray(tree.thresholds[:n])
+        po = np.ascontiguousarray(tree.posteriors[:n])
+        prior = np.ascontiguousarray(ts.priors, np.float32)
+        cb = pdist.c_exchange(exchange)
+        check(lib().pd_train_tree_sharded(self.h, C.byref(params.c()), f_begin, f_end, C.cast(cb, C.c_void_p), None,
+                                          tree.id, 1, end_depth, _ptr(prior), _ptr(lc), _ptr(ft), _ptr(th),
+                                          _ptr(po)))
+        tree.left_child[:n], tree.features[:n], tree.thresholds[:n], tree.posteriors[:n] = lc, ft, th, po
+
     def records(self) -> np.ndarray:
         """The records (one per split node) of the last training call; set_tuning("records", 1)
         before training to keep them."""

@@ -360,3 +360,23 @@ def prop_loss_grad(params, IN, H, OUT, DY, x, y, w=None, bf16=True):
                                  P(y), P(w), C.c_uint32(x.shape[0]), C.c_int(int(bf16)), C.byref(loss), P(grad))
     assert rc == 0
     return loss.value, grad
+
+
+
+def train_tree_sharded(p: Params, ds: OracleSet, tree_id: int, depth: int, root_prior, f0: int, f1: int, exchange,
+                       threads=0):
+    """or_train_tree_sharded with a Python exchange(key, idx, counts) -> (idx, counts)."""
+    from padenti_gb300 import dist as pdist
+
+    n = (1 << depth) - 1
+    lc = np.full(n, -2, np.int32)
+    feats = np.zeros((n, p.feat_dim), np.int32)
+    thrs = np.zeros(n, np.int32)
+    posts = np.zeros((n, p.n_classes), np.float32)
+    leaf = np.zeros(ds.n_samples, np.int32)
+    prior = np.ascontiguousarray(root_prior, np.float32)
+    cb = pdist.c_exchange(exchange)  # kept alive for the call
+    rc = lib().or_train_tree_sharded(C.byref(p), C.byref(ds.c), tree_id, depth, P(prior), C.c_uint32(f0),
+                                     C.c_uint32(f1), cb, None, P(lc), P(feats), P(thrs), P(posts), P(leaf), threads)
+    assert rc == 0, rc
+    return dict(left_child=lc, features=feats, thresholds=thrs, posteriors=posts, sample_leaf=leaf)

@@ -79,3 +79,54 @@ def test_gain_keys_preserve_order():
     k = pdist.gain_key(g)
     assert np.array_equal(np.argsort(k, kind="stable"), np.argsort(g, kind="stable"))
     assert pdist.shard_range(2000, 1, 3) == (667, 1334) and pdist.shard_range(10, 3, 4) == (9, 10)
+
+
+def _tree_worker(rank, world, port, out):
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path.insert(0, here)
+    sys.path.insert(0, os.path.dirname(here))
+    import oracle_bind as ob
+    from cases import depth_case
+    from padenti_gb300 import dist as pdist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    cfg, ts, tp, _ = depth_case(n_images=8, n_features=96, n_thresholds=20, parts=1)
+    f0, f1 = pdist.shard_range(tp.n_features, rank, world)
+    o = ob.train_tree_sharded(ob.params(cfg, tp), ob.OracleSet(ts, cfg), 3, 7, ts.priors, f0, f1,
+                              pdist.torch_exchange(), threads=1)
+    out[rank] = {k: o[k] for k in ("left_child", "features", "thresholds", "posteriors", "sample_leaf")}
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_sharded_whole_tree_equals_unsharded(world):
+    """Candidate-sharded training of a whole tree over gloo ranks (each evaluates its range of the
+    96 candidates; uneven ranges with 3 ranks), the per-slice exchange of padenti_gb300.dist, on
+    the oracle: every rank ends with the unsharded tree, bit for bit."""
+    import oracle_bind as ob
+    from cases import depth_case
+
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_tree_worker, args=(world, _free_port(), out), nprocs=world, join=True)
+    cfg, ts, tp, _ = depth_case(n_images=8, n_features=96, n_thresholds=20, parts=1)
+    ref = ob.train_tree(ob.params(cfg, tp), ob.OracleSet(ts, cfg), 3, 7, ts.priors)
+    assert ref["nodes_split"] >= 10
+    for r in range(world):
+        for k in ("left_child", "features", "thresholds", "sample_leaf"):
+            assert np.array_equal(out[r][k], ref[k]), (r, k)
+        assert np.array_equal(out[r]["posteriors"].view(np.uint32), ref["posteriors"].view(np.uint32))
+
+
+def test_local_exchange_picks_the_global_winner():
+    from padenti_gb300 import dist as pdist
+
+    keys = [np.array([5, 7, np.iinfo(np.int64).min], np.int64), np.array([5, 3, np.iinfo(np.int64).min], np.int64)]
+    idxs = [np.array([40, 2, -1], np.int64), np.array([12, 9, -1], np.int64)]
+    cnts = [np.array([[1, 2], [3, 4], [0, 0]], np.uint32), np.array([[5, 6], [7, 8], [0, 0]], np.uint32)]
+    best, cnt = pdist.global_winners(keys, idxs, cnts)
+    assert best.tolist() == [12, 2, -1]  # tie on node 0 -> lowest index (rank 1); node 1 -> rank 0
+    assert cnt.tolist() == [[5, 6], [3, 4], [0, 0]]
