@@ -170,10 +170,30 @@ int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
  *               so that neighbouring lanes probe neighbouring pixels; 0: index order;
  *   "sample_group" bytes of images and labels pd_sample stages per round trip,
  *               >= 4096 (default 512 MiB);
- *   "persist"   1 (default): one persistent histogram grid per launch (a few CTAs per SM) pulling the
- *               work items from a device counter, largest first; 0: one CTA per work item;
+ *   "persist"   1: one persistent histogram grid per launch (a few CTAs per SM) pulling the work
+ *               items from a device counter, largest first; 0 (default): one CTA per work item;
  *   "records"   1: training calls keep one pd_record per split node (pd_train_records); 0 (default): none. */
 int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value);
+/* The launch shape chosen by pd_autotune. */
+typedef struct {
+  int32_t chunk, hist_spi, fuse_max, cand_order, persist;
+  double ms_start;   /* tree time with the settings the call started from */
+  double ms_best;    /* tree time with the chosen settings */
+  int32_t trials;    /* settings timed (0 when the cache had the key) */
+  int32_t from_cache;
+} pd_tuning;
+/* Autotuner of the launch-shape knobs above (no counterpart in the reference,
+ * whose tunables are compile-time constants, cl_tree_trainer_impl.hpp:47-68):
+ * coordinate descent over chunk {4096..32768}, persist, hist_spi {4, 8},
+ * fuse_max {1024..8192} and cand_order, each setting timed as the best of two
+ * trees of end_depth levels with `params` on the uploaded training set (at
+ * most max_trials settings; 0 = no limit), every tree checked equal to the
+ * first.  The winner is applied to the context and, with cache_path, appended
+ * to that text file under a key of (GPU, SM count, configuration, F, T,
+ * training-set size class, depth, min samples per leaf); a later call with the
+ * same key applies the cached setting without timing. */
+int pd_autotune(pd_ctx *ctx, const pd_train_params *params, uint32_t end_depth, uint32_t max_trials,
+                const char *cache_path, pd_tuning *out);
 /* Synchronises the context's stream. */
 int pd_ctx_sync(pd_ctx *ctx);
 /* The CUDA stream (cudaStream_t) the context launches on. */

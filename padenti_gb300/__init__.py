@@ -311,6 +311,16 @@ class TreeTrainer(_Ctx):
         """Launch-shape knob of the histogram kernel ("chunk", "hist_spi", "fuse_max", "cand_order"); results do not change."""
         check(lib().pd_ctx_set_tuning(self.h, name.encode(), int(value)))
 
+    def autotune(self, ts: TrainingSet, params: TreeTrainerParameters, end_depth: int, cache: str | None = None,
+                 max_trials: int = 0) -> dict:
+        """pd_autotune: searches the launch-shape knobs by timing trees of end_depth levels on `ts`
+        (results never change), applies the best and caches it in the text file `cache`."""
+        self.upload(ts)
+        out = N.Tuning()
+        check(lib().pd_autotune(self.h, C.byref(params.c()), end_depth, max_trials,
+                                None if cache is None else str(cache).encode(), C.byref(out)))
+        return {k: getattr(out, k) for k, _ in out._fields_}
+
     def upload(self, ts: TrainingSet) -> None:
         key = (id(ts), ts._version, len(ts.images))
         if self._uploaded == key:

@@ -88,6 +88,12 @@ EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER
                           C.POINTER(C.c_uint32))
 
 
+class Tuning(C.Structure):
+    _fields_ = [("chunk", C.c_int32), ("hist_spi", C.c_int32), ("fuse_max", C.c_int32), ("cand_order", C.c_int32),
+                ("persist", C.c_int32), ("ms_start", C.c_double), ("ms_best", C.c_double), ("trials", C.c_int32),
+                ("from_cache", C.c_int32)]
+
+
 class Record(C.Structure):
     """pd_record: one split node of a trained tree (learned proposals)."""
     _fields_ = [("depth", C.c_uint32), ("count", C.c_uint32), ("node", C.c_uint32), ("tree", C.c_uint32),
@@ -135,6 +141,7 @@ _SIGS = {
     "pd_split": (C.c_int, [_P, C.POINTER(TrainParams), _P, _P, C.c_uint32, _P, _P, _P]),
     "pd_log2_table": (C.c_int, [_P, C.c_uint32, _P]),
     "pd_train_records": (C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "pd_autotune": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, C.c_uint32, C.c_char_p, C.POINTER(Tuning)]),
     "pd_train_tree_sharded": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, C.c_uint32, _P, _P, C.c_uint32,
                                         C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]),
     "pd_proposer_create": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint64, C.POINTER(_P)]),
