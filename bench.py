@@ -63,6 +63,7 @@ def args_():
     a.add_argument("--cand-order", type=int, default=None, choices=(0, 1),
                    help="1: candidate columns ordered by first-probe offset (default), 0: index order")
     a.add_argument("--learned", type=int, default=1, help="1: time the learned-proposal forest beside the plain one")
+    a.add_argument("--autotune", type=int, default=1, help="1: launch shapes from pd_autotune before timing")
     a.add_argument("--fit-steps", type=int, default=200)
     a.add_argument("--fit-batch", type=int, default=2048)
     a.add_argument("--fit-lr", type=float, default=2e-3)
@@ -546,6 +547,17 @@ def learned_bench(a, pg, cfg, ts, tp, device):
         e1.synchronize()
         return r, e0.elapsed_time(e1)
 
+    import tempfile
+
+    cache = os.path.join(tempfile.mkdtemp(), "tune.txt")
+    tp300 = pg.TreeTrainerParameters(300, tp.n_thresholds, tp.feat_low_bounds, tp.feat_up_bounds, tp.thr_low_bound,
+                                     tp.thr_up_bound, tp.per_leaf_samples_thr)
+    # launch shapes tuned once per candidate count (pd_autotune), outside the timed regions
+    tuned = {}
+    if a.autotune:
+        tuned["F2000"] = tr.autotune(ts, tp, a.depth, cache=cache, max_trials=10)
+        tuned["F300"] = tr.autotune(ts, tp300, a.depth, cache=cache, max_trials=10)
+        tr.autotune(ts, tp, a.depth, cache=cache)
     tr.train(pg.Tree(cfg, 90, a.depth), ts, tp)  # warm-up
     plain, ms_plain = [], 0.0
     for k in range(3):
@@ -559,8 +571,8 @@ def learned_bench(a, pg, cfg, ts, tp, device):
             ms_tree0 = ms
         plain.append(t)
         ms_plain += ms
-    tp300 = pg.TreeTrainerParameters(300, tp.n_thresholds, tp.feat_low_bounds, tp.feat_up_bounds, tp.thr_low_bound,
-                                     tp.thr_up_bound, tp.per_leaf_samples_thr)
+    if a.autotune:
+        tr.autotune(ts, tp300, a.depth, cache=cache)  # the F=300 setting, from the cache
     net = pg.ProposalNetwork(tr, tp300, seed=a.seed)
     fit = net.fit(rec[:1], steps=1, batch=a.fit_batch, lr=a.fit_lr)  # warm-up (graph capture)
     net = pg.ProposalNetwork(tr, tp300, seed=a.seed)
@@ -607,6 +619,8 @@ def learned_bench(a, pg, cfg, ts, tp, device):
         accuracy_gap_pt=100 * (acc["plain"][0] - acc["learned"][0]),
         network_gain_pt=100 * (acc["learned"][0] - acc["uniform300"][0]),
         held_out="100 synthetic 640x480 images of the same generator (not trained on)",
+        launch_shapes={k: {q: v[q] for q in ("chunk", "hist_spi", "fuse_max", "cand_order", "persist", "ms_start",
+                                            "ms_best", "trials")} for k, v in tuned.items()},
         note="tree 0 is the plain tree in both forests; the learned forest's time counts it, the fit and "
              "trees 1-2")
 
@@ -716,6 +730,10 @@ def run_ours(a):
         tr.set_tuning("cand_order", a.cand_order)
     tr.upload(ts)
     stream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(tr.h))
+    tune = None
+    if a.autotune and not (a.chunk or a.spi or a.fuse_max is not None or a.cand_order is not None):
+        # launch shapes from the autotuner (whole trees timed on this training set; results never change)
+        tune = tr.autotune(ts, tp, a.depth, max_trials=10)
 
     def tree_step(tid):
         tree = pg.Tree(cfg, tid, a.depth)
@@ -920,8 +938,12 @@ def run_ours(a):
                 config=dict(workload=WORKLOAD, images=a.images, width=a.width, height=a.height,
                             samples_per_image=a.samples, features=a.features, thresholds=a.thresholds,
                             depth=a.depth, min_leaf=a.min_leaf, trees_per_step=1,
-                            chunk=a.chunk or 16384, fuse_max=4096 if a.fuse_max is None else a.fuse_max, hist_spi=a.spi or 8,
-                            cand_order=1 if a.cand_order is None else a.cand_order,
+                            chunk=(tune or {}).get("chunk", a.chunk or 16384),
+                            fuse_max=(tune or {}).get("fuse_max", 4096 if a.fuse_max is None else a.fuse_max),
+                            hist_spi=(tune or {}).get("hist_spi", a.spi or 8),
+                            cand_order=(tune or {}).get("cand_order", 1 if a.cand_order is None else a.cand_order),
+                            persist=(tune or {}).get("persist", 0),
+                            launch_shape="pd_autotune (%d settings timed)" % tune["trials"] if tune else "fixed",
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
                 roofline=roof, roofline_issue=issue_roof, roofline_atomic=atomic_roof, cpu_baseline=base,
