@@ -23,14 +23,15 @@ from ._native import PadentiError, check, lib
 
 __all__ = [
     "ForestConfig", "TreeTrainerParameters", "TrainingSetImage", "TrainingSet", "Tree", "TreeTrainer",
-    "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS", "USER_SHAPES", "check_plugin",
+    "Classifier", "PadentiError", "synth_depth", "synth_rgb", "PLUGINS", "USER_SHAPES", "user_shape", "check_plugin",
     "ImageSampler", "UniformImageSampler", "ClassWeightedImageSampler", "sampled_training_set",
     "ProposalNetwork", "RECORD_DTYPE", "read_pnm", "write_pnm", "PNMImageLoader", "RGBLabelsLoader", "load_training_set", "image_roi",
     "PNMImageROILoader", "RGBLabelsROILoader",
 ]
 
 FEAT_DTYPE = {N.PD_FEAT_I16: np.int16, N.PD_FEAT_I32: np.int32}
-IMG_DTYPE = {N.PD_IMG_U8: np.uint8, N.PD_IMG_U16: np.uint16}
+IMG_DTYPE = {N.PD_IMG_U8: np.uint8, N.PD_IMG_U16: np.uint16, N.PD_IMG_I16: np.int16, N.PD_IMG_I32: np.int32,
+             N.PD_IMG_F32: np.float32}
 
 # Built-in feature plugins and the template parameters they are compiled for.
 PLUGINS = {
@@ -44,11 +45,24 @@ PLUGINS = {
 
 # Types and dimensions a user feature (plugin "user", compiled at run time from
 # CUDA source defining computeFeature) may have: those of the built-in plugins.
-USER_SHAPES = {
-    "u16x1_i32x4": dict(img_type=N.PD_IMG_U16, n_channels=1, feat_type=N.PD_FEAT_I32, feat_dim=4),
-    "u16x1_i16x2": dict(img_type=N.PD_IMG_U16, n_channels=1, feat_type=N.PD_FEAT_I16, feat_dim=2),
-    "u8x3_i32x6": dict(img_type=N.PD_IMG_U8, n_channels=3, feat_type=N.PD_FEAT_I32, feat_dim=6),
-}
+_IMG_CODES = {"u8": N.PD_IMG_U8, "u16": N.PD_IMG_U16, "i16": N.PD_IMG_I16, "i32": N.PD_IMG_I32, "f32": N.PD_IMG_F32}
+_FEAT_CODES = {"i16": N.PD_FEAT_I16, "i32": N.PD_FEAT_I32}
+
+
+def user_shape(shape: str) -> dict:
+    """The template parameters of a user plugin from "<img><C>_<feat>x<D>": img in u8, u16, i16,
+    i32, f32; C channels in 1..4; feat in i16, i32; FeatDim D in 1..8 (e.g. "u16x1_i32x4",
+    "f32x1_i32x4", "u8x4_i32x6")."""
+    import re
+
+    m = re.fullmatch(r"(u8|u16|i16|i32|f32)x([1-4])_(i16|i32)x([1-8])", shape or "")
+    if not m:
+        raise ValueError(f"user plugin shape {shape!r}: expected <u8|u16|i16|i32|f32>x<1-4>_<i16|i32>x<1-8>")
+    return dict(img_type=_IMG_CODES[m[1]], n_channels=int(m[2]), feat_type=_FEAT_CODES[m[3]], feat_dim=int(m[4]))
+
+
+# the shapes of the built-in plugins, kept as names
+USER_SHAPES = {s: user_shape(s) for s in ("u16x1_i32x4", "u16x1_i16x2", "u8x3_i32x6")}
 
 
 def _ptr(a: np.ndarray | None) -> int | None:
@@ -58,8 +72,8 @@ def _ptr(a: np.ndarray | None) -> int | None:
 @dataclass(frozen=True)
 class ForestConfig:
     """<ImgType, nChannels, FeatType, FeatDim, nClasses> for one plugin: a built-in one, or
-    plugin="user" with the CUDA `source` of computeFeature (the reference's feature.cl) and one
-    of the USER_SHAPES."""
+    plugin="user" with the CUDA `source` of computeFeature (the reference's feature.cl) and a
+    shape "<img><C>_<feat>x<D>" (user_shape)."""
 
     plugin: str
     n_classes: int
@@ -68,15 +82,16 @@ class ForestConfig:
 
     def __post_init__(self):
         if self.plugin == "user":
-            if self.shape not in USER_SHAPES or not self.source:
-                raise ValueError(f"a user plugin needs source and a shape in {sorted(USER_SHAPES)}")
+            if not self.source:
+                raise ValueError("a user plugin needs its computeFeature source")
+            user_shape(self.shape)
         elif self.plugin not in PLUGINS:
             raise ValueError(f"unknown plugin {self.plugin!r}; built-in: {sorted(PLUGINS)} or 'user'")
 
     @property
     def spec(self) -> dict:
         if self.plugin == "user":
-            return dict(plugin=N.PD_PLUGIN_USER, **USER_SHAPES[self.shape])
+            return dict(plugin=N.PD_PLUGIN_USER, **user_shape(self.shape))
         return PLUGINS[self.plugin]
 
     @property

@@ -29,6 +29,18 @@ static int check_config(const pd_config *c) {
   PD_CHECK(c, PD_ERR_INVALID, "null config");
   PD_CHECK(c->n_classes >= 1 && c->n_classes <= PD_MAX_CLASSES, PD_ERR_UNSUPPORTED, "nClasses %d outside [1,%d]",
            c->n_classes, PD_MAX_CLASSES);
+  if (c->plugin == PD_PLUGIN_USER) {
+    // a run-time compiled feature: any FeatDim 1..8, int16 / int32 features, and
+    // uint8 / uint16 / int16 / int32 / float images of 1..4 channels
+    PD_CHECK(c->feat_dim >= 1 && c->feat_dim <= PD_MAX_FEAT_DIM, PD_ERR_UNSUPPORTED, "FeatDim %d outside [1,%d]",
+             c->feat_dim, PD_MAX_FEAT_DIM);
+    PD_CHECK(c->feat_type == PD_FEAT_I16 || c->feat_type == PD_FEAT_I32, PD_ERR_UNSUPPORTED,
+             "feat_type %d (supported: PD_FEAT_I16, PD_FEAT_I32)", c->feat_type);
+    PD_CHECK(c->img_type >= PD_IMG_U8 && c->img_type <= PD_IMG_F32, PD_ERR_UNSUPPORTED, "img_type %d", c->img_type);
+    PD_CHECK(c->n_channels >= 1 && c->n_channels <= 4, PD_ERR_UNSUPPORTED, "%d channels outside [1,4]",
+             c->n_channels);
+    return PD_OK;
+  }
   return dispatch_config(*c, [&]<class P>() {
     const int img = sizeof(typename P::img_t) == 1 ? PD_IMG_U8 : PD_IMG_U16;
     const int ft = sizeof(typename P::feat_t) == 2 ? PD_FEAT_I16 : PD_FEAT_I32;

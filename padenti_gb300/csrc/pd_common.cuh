@@ -170,7 +170,9 @@ struct HostBuf {
 };
 
 inline size_t feat_size(int feat_type) { return feat_type == PD_FEAT_I16 ? 2 : 4; }
-inline size_t img_size(int img_type) { return img_type == PD_IMG_U8 ? 1 : 2; }
+inline size_t img_size(int img_type) {
+  return img_type == PD_IMG_U8 ? 1 : (img_type == PD_IMG_U16 || img_type == PD_IMG_I16 ? 2 : 4);
+}
 
 #endif
 

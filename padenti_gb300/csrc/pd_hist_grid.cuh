@@ -25,6 +25,8 @@ struct HistGrid {
 
 template <class P>
 int launch_hist_grid(pd_ctx *ctx, const HistGrid &g);
+// The run-time compiled histogram kernel of a user feature (pd_rtc.cu).
+int launch_hist_grid_rtc(pd_ctx *ctx, const HistGrid &g);
 
 extern template int launch_hist_grid<DepthDiff2>(pd_ctx *, const HistGrid &);
 extern template int launch_hist_grid<DepthDiff1>(pd_ctx *, const HistGrid &);

@@ -20,32 +20,6 @@ static int launch_hist_grid_as(pd_ctx *ctx, const HistGrid &g) {
   PD_CUDA(cudaFuncGetAttributes(&fa, kern));
   const size_t per_cta = g.smem + fa.sharedSizeBytes + 1024;  // dynamic + static + reserved
   const int pct = (int)std::min<size_t>(100, (resident * per_cta * 100 + 233471) / 233472);
-  if (is_user_plugin(ctx)) {
-    // the same kernel compiled with the user's feature (same shared memory)
-    cudaKernel_t uk = nullptr;
-    PD_TRY(rtc_hist_kernel(ctx, TP, SPI, &uk));
-    PD_TRY(rtc_set_smem(ctx, uk, g.smem, pct));
-    if (g.queue) PD_CUDA(cudaMemsetAsync(g.queue, 0, 4, ctx->stream));
-    if (g.ev_before) PD_CUDA(cudaEventRecord(g.ev_before, ctx->stream));
-    for (uint64_t b = 0; b < g.n_items; b += 0x7fffffffull) {
-      const uint64_t cnt = std::min<uint64_t>(g.n_items - b, 0x7fffffffull);
-      DevSet ds = g.ds;
-      const SampleRec *rec = g.rec;
-      const WorkItem *items = g.items + b;
-      uint32_t n = (uint32_t)cnt;
-      unsigned *queue = g.queue;
-      const FeatT *cf = static_cast<const FeatT *>(g.cand_feat), *ct = static_cast<const FeatT *>(g.cand_thr);
-      uint32_t *hist = g.hist;
-      uint32_t F = g.F, T = g.T, K = g.K;
-      FusedSplit fs = g.fs;
-      void *args[] = {&ds, &rec, &items, &n, &queue, &cf, &ct, &hist, &F, &T, &K, &fs};
-      const unsigned grid = g.queue ? (unsigned)std::min<uint64_t>(cnt, (uint64_t)ctx->n_sms * resident)
-                                    : (unsigned)cnt;
-      PD_TRY(rtc_launch(ctx, uk, dim3(grid), dim3(kHistThreads), g.smem, args));
-      if (g.queue) break;  // a persistent list holds fewer than 2^31 items
-    }
-    return PD_OK;
-  }
   PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
   if (g.queue) PD_CUDA(cudaMemsetAsync(g.queue, 0, 4, ctx->stream));
   if (g.ev_before) PD_CUDA(cudaEventRecord(g.ev_before, ctx->stream));

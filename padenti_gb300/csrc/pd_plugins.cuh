@@ -124,6 +124,7 @@ struct DepthDiff2 {
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF2;
   static constexpr int kOrderDim = 0;  // feature dims (0, 1): the first probe offset
   static constexpr bool kTrainMapsZero = true;  // 0 and 10000 read alike everywhere
+  static constexpr bool kRtcOnly = false;     // kernels compiled into the library
   struct Prep {
     const uint16_t *im;
     uint32_t w, h;
@@ -204,6 +205,7 @@ struct DepthDiff1 {
   static constexpr int kId = PD_PLUGIN_DEPTH_DIFF1;
   static constexpr int kOrderDim = 0;  // feature dims (0, 1): the probe offset
   static constexpr bool kTrainMapsZero = false;  // the centre depth is used as read
+  static constexpr bool kRtcOnly = false;     // kernels compiled into the library
   struct Prep {
     const uint16_t *im;
     uint32_t w, h;
@@ -280,6 +282,7 @@ struct ChannelDiff {
   static constexpr int kId = PD_PLUGIN_CHANNEL_DIFF;
   static constexpr int kOrderDim = 2;  // feature dims (2, 3): the first probe offset
   static constexpr bool kTrainMapsZero = false;
+  static constexpr bool kRtcOnly = false;     // kernels compiled into the library
   struct Prep {
     const uint8_t *im;
     uint32_t w, h;
@@ -338,22 +341,49 @@ int dispatch_plugin(int plugin, Fn &&fn) {
   }
 }
 
+#if !defined(__CUDACC_RTC__)
+// The host-side stand-in of a feature compiled at run time (PD_PLUGIN_USER):
+// the feature type and dimension the host paths need.  Every kernel of such a
+// context is the run-time compiled one (the compiled-in kernels are never
+// instantiated for it); image sizes come from the configuration.
+template <typename FeatT, int D>
+struct UserHost {
+  using feat_t = FeatT;
+  using img_t = uint8_t;  // unused: sizes come from the configuration
+  static constexpr int kFeatDim = D;
+  static constexpr int kChannels = 0;
+  static constexpr int kId = PD_PLUGIN_USER;
+  static constexpr bool kTrainMapsZero = false;
+  static constexpr bool kRtcOnly = true;
+  struct __align__(16) Cand {
+    FeatT f[D];
+  };
+};
+
+template <typename FeatT, typename Fn>
+int dispatch_user_dim(int D, Fn &&fn) {
+  switch (D) {
+    case 1: return fn.template operator()<UserHost<FeatT, 1>>();
+    case 2: return fn.template operator()<UserHost<FeatT, 2>>();
+    case 3: return fn.template operator()<UserHost<FeatT, 3>>();
+    case 4: return fn.template operator()<UserHost<FeatT, 4>>();
+    case 5: return fn.template operator()<UserHost<FeatT, 5>>();
+    case 6: return fn.template operator()<UserHost<FeatT, 6>>();
+    case 7: return fn.template operator()<UserHost<FeatT, 7>>();
+    case 8: return fn.template operator()<UserHost<FeatT, 8>>();
+    default: return set_error(PD_ERR_UNSUPPORTED, "FeatDim %d outside [1,%d]", D, PD_MAX_FEAT_DIM);
+  }
+}
+
 // The plugin whose host paths serve a configuration: the built-in plugin, or
-// for PD_PLUGIN_USER the built-in plugin with the same types and dimensions
-// (its kernels are then the run-time compiled ones).
+// for PD_PLUGIN_USER the stand-in of its feature type and dimension.
 template <typename Fn>
 int dispatch_config(const pd_config &c, Fn &&fn) {
   if (c.plugin != PD_PLUGIN_USER) return dispatch_plugin(c.plugin, fn);
-  if (c.img_type == PD_IMG_U16 && c.n_channels == 1 && c.feat_type == PD_FEAT_I32 && c.feat_dim == 4)
-    return fn.template operator()<DepthDiff2>();
-  if (c.img_type == PD_IMG_U16 && c.n_channels == 1 && c.feat_type == PD_FEAT_I16 && c.feat_dim == 2)
-    return fn.template operator()<DepthDiff1>();
-  if (c.img_type == PD_IMG_U8 && c.n_channels == 3 && c.feat_type == PD_FEAT_I32 && c.feat_dim == 6)
-    return fn.template operator()<ChannelDiff>();
-  return set_error(PD_ERR_UNSUPPORTED,
-                   "user plugin with img_type %d, %d channel(s), feat_type %d, FeatDim %d: supported are "
-                   "(uint16, 1, int32, 4), (uint16, 1, int16, 2) and (uint8, 3, int32, 6)",
-                   c.img_type, c.n_channels, c.feat_type, c.feat_dim);
+  if (c.feat_type == PD_FEAT_I16) return dispatch_user_dim<int16_t>(c.feat_dim, fn);
+  if (c.feat_type == PD_FEAT_I32) return dispatch_user_dim<int32_t>(c.feat_dim, fn);
+  return set_error(PD_ERR_UNSUPPORTED, "feat_type %d (supported: PD_FEAT_I16, PD_FEAT_I32)", c.feat_type);
 }
+#endif
 
 }  // namespace pd

@@ -67,7 +67,7 @@ static int ensure_forest_cands(pd_ctx *ctx) {
     void *out = ctx->f_cand.ptr;
     void *args[] = {&ft, &nodes, &out};
     PD_TRY(rtc_launch(ctx, rk->forest_cands, grid, dim3(256), 0, args));
-  } else {
+  } else if constexpr (!P::kRtcOnly) {
     k_forest_cands<P><<<grid, 256, 0, ctx->stream>>>(ft, nodes, ctx->f_cand.as<typename P::Cand>());
     PD_CUDA(cudaGetLastError());
     ctx->launches++;
@@ -83,7 +83,7 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
   const uint32_t nt = (uint32_t)ctx->tree_depth.size();
   const size_t smem = (size_t)nt * kPredThreads * 4;
   dim3 grid((W + kPredX - 1) / kPredX, (H + kPredY - 1) / kPredY, n);
-  const uint64_t img_bytes = (uint64_t)W * H * P::kChannels * sizeof(typename P::img_t);
+  const uint64_t img_bytes = (uint64_t)W * H * ctx->cfg.n_channels * img_size(ctx->cfg.img_type);
   PD_TRY(ensure_forest_cands<P>(ctx));
   if (is_user_plugin(ctx)) {
     const RtcKernels *rk = nullptr;
@@ -101,13 +101,15 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
     void *args[] = {&im, &ib, &w_, &h_, &masks, &out, &lc, &cd, &th, &po, &me, &nt_, &k_, &mg};
     return rtc_launch(ctx, rk->predict_posterior, grid, dim3(kPredX, kPredY), smem, args);
   }
-  PD_CUDA(cudaFuncSetAttribute(k_predict_posterior<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_predict_posterior<P><<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
-      static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_lc.as<int32_t>(),
-      ctx->f_cand.as<typename P::Cand>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(),
-      ctx->f_meta.as<TreeMeta>(), nt, (uint32_t)ctx->cfg.n_classes, ctx->magic_tab.as<uint32_t>());
-  PD_CUDA(cudaGetLastError());
-  ctx->launches++;
+  if constexpr (!P::kRtcOnly) {
+    PD_CUDA(cudaFuncSetAttribute(k_predict_posterior<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_predict_posterior<P><<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
+        static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_lc.as<int32_t>(),
+        ctx->f_cand.as<typename P::Cand>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(),
+        ctx->f_meta.as<TreeMeta>(), nt, (uint32_t)ctx->cfg.n_classes, ctx->magic_tab.as<uint32_t>());
+    PD_CUDA(cudaGetLastError());
+    ctx->launches++;
+  }
   return PD_OK;
 }
 
@@ -258,13 +260,14 @@ extern "C" int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *c
       const TreeMeta *me = ctx->f_meta.as<TreeMeta>();
       const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
       void *args[] = {&im, &mk, &o, &bd, &n_, &lc, &cd, &th, &po, &me, &nt_, &k_, &mg};
-      const void *fn = (const void *)k_predict_batch<P>;
+      const void *fn = nullptr;
       if (is_user_plugin(ctx)) {
         const RtcKernels *rk = nullptr;
         PD_TRY(rtc_kernels(ctx, &rk));
         PD_TRY(rtc_set_smem(ctx, rk->predict_batch, smem));
         fn = (const void *)rk->predict_batch;
-      } else {
+      } else if constexpr (!P::kRtcOnly) {
+        fn = (const void *)k_predict_batch<P>;
         PD_CUDA(cudaFuncSetAttribute(k_predict_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       }
       cudaGraph_t g = nullptr;
@@ -330,11 +333,13 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
       void *args[] = {&im, &w_, &h_, &mk, &o, &lc, &cd, &th, &dp, &mg};
       return rtc_launch(ctx, rk->predict_leaf, grid, dim3(kPredX, kPredY), 0, args);
     }
-    k_predict_leaf<P><<<grid, dim3(kPredX, kPredY), 0, st>>>(
-        ctx->p_img.as<uint8_t>(), width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
-        ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_cand.as<typename P::Cand>() + off,
-        ctx->f_thr.as<FeatT>() + off, depth, ctx->magic_tab.as<uint32_t>());
-    PD_CUDA(cudaGetLastError());
+    if constexpr (!P::kRtcOnly) {
+      k_predict_leaf<P><<<grid, dim3(kPredX, kPredY), 0, st>>>(
+          ctx->p_img.as<uint8_t>(), width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
+          ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_cand.as<typename P::Cand>() + off,
+          ctx->f_thr.as<FeatT>() + off, depth, ctx->magic_tab.as<uint32_t>());
+      PD_CUDA(cudaGetLastError());
+    }
     return PD_OK;
   }));
   PD_CUDA(d2h(ctx, out, ctx->p_out.ptr, P_ * 4));

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "pd_hist_grid.cuh"
 #include "pd_rtc.cuh"
 
 namespace pd {
@@ -27,7 +28,13 @@ const EmbeddedSource kSources[] = {
 
 std::string unit_source(const pd_config &c, const std::string &user) {
   std::string s;
-  s += c.img_type == PD_IMG_U8 ? "typedef unsigned char img_t;\n" : "typedef unsigned short img_t;\n";
+  switch (c.img_type) {
+    case PD_IMG_U8: s += "typedef unsigned char img_t;\n"; break;
+    case PD_IMG_U16: s += "typedef unsigned short img_t;\n"; break;
+    case PD_IMG_I16: s += "typedef short img_t;\n"; break;
+    case PD_IMG_I32: s += "typedef int img_t;\n"; break;
+    default: s += "typedef float img_t;\n"; break;
+  }
   s += c.feat_type == PD_FEAT_I16 ? "typedef short feat_t;\n" : "typedef int feat_t;\n";
   s += "#define PD_FEAT_DIM " + std::to_string(c.feat_dim) + "\n";
   s += "#define PD_CHANNELS " + std::to_string(c.n_channels) + "\n";
@@ -150,6 +157,39 @@ int rtc_set_smem(pd_ctx *ctx, cudaKernel_t k, size_t smem, int carveout_pct) {
 int rtc_launch(pd_ctx *ctx, cudaKernel_t k, dim3 grid, dim3 block, size_t smem, void **args) {
   PD_CUDA(cudaLaunchKernel((const void *)k, grid, block, args, smem, ctx->stream));
   ctx->launches++;
+  return PD_OK;
+}
+
+// The histogram launch of a user feature: the same work list, shared memory
+// and launch shapes as the compiled-in kernel (pd_hist_grid_impl.cuh), with
+// k_hist<UserPlugin, TP, SPI> compiled for the context's GPU.
+int launch_hist_grid_rtc(pd_ctx *ctx, const HistGrid &g) {
+  const int spi = (int)ctx->hist_spi;
+  const int resident = spi <= 2 ? 3 : 2;
+  cudaKernel_t uk = nullptr;
+  PD_TRY(rtc_hist_kernel(ctx, g.TP, spi, &uk));
+  // shared memory carve-out for the resident CTAs (dynamic + a static allowance + reserved)
+  const size_t per_cta = g.smem + 4096 + 1024;
+  const int pct = (int)std::min<size_t>(100, (resident * per_cta * 100 + 233471) / 233472);
+  PD_TRY(rtc_set_smem(ctx, uk, g.smem, pct));
+  if (g.queue) PD_CUDA(cudaMemsetAsync(g.queue, 0, 4, ctx->stream));
+  if (g.ev_before) PD_CUDA(cudaEventRecord(g.ev_before, ctx->stream));
+  for (uint64_t b = 0; b < g.n_items; b += 0x7fffffffull) {
+    const uint64_t cnt = std::min<uint64_t>(g.n_items - b, 0x7fffffffull);
+    DevSet ds = g.ds;
+    const SampleRec *rec = g.rec;
+    const WorkItem *items = g.items + b;
+    uint32_t n = (uint32_t)cnt;
+    unsigned *queue = g.queue;
+    const void *cf = g.cand_feat, *ct = g.cand_thr;
+    uint32_t *hist = g.hist;
+    uint32_t F = g.F, T = g.T, K = g.K;
+    FusedSplit fs = g.fs;
+    void *args[] = {&ds, &rec, &items, &n, &queue, &cf, &ct, &hist, &F, &T, &K, &fs};
+    const unsigned grid = g.queue ? (unsigned)std::min<uint64_t>(cnt, (uint64_t)ctx->n_sms * resident) : (unsigned)cnt;
+    PD_TRY(rtc_launch(ctx, uk, dim3(grid), dim3(kHistThreads), g.smem, args));
+    if (g.queue) break;
+  }
   return PD_OK;
 }
 

@@ -89,8 +89,10 @@ int build_sample_records(pd_ctx *ctx, uint64_t S) {
       void *args[] = {&ds, &n, &rec};
       return rtc_launch(ctx, rk->build_rec, grid, dim3(256), 0, args);
     }
-    k_build_rec<P><<<grid, 256, 0, ctx->stream>>>(devset(ctx), (uint32_t)S, ctx->s_rec.as<SampleRec>());
-    PD_CUDA(cudaGetLastError());
+    if constexpr (!P::kRtcOnly) {
+      k_build_rec<P><<<grid, 256, 0, ctx->stream>>>(devset(ctx), (uint32_t)S, ctx->s_rec.as<SampleRec>());
+      PD_CUDA(cudaGetLastError());
+    }
     return PD_OK;
   });
 }
@@ -179,7 +181,7 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
       PropSrc ps = prop ? *prop : PropSrc{};
       void *args[] = {&d_nodes, &tr, &f_, &bb, &o, &ps};
       PD_TRY(rtc_launch(ctx, rk->cand_order, dim3(n), dim3(kOrderThreads), osmem, args));
-    } else {
+    } else if constexpr (!P::kRtcOnly) {
       PD_CUDA(cudaFuncSetAttribute(k_cand_order<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)osmem));
       k_cand_order<P><<<n, kOrderThreads, osmem, ctx->stream>>>(d_nodes, tree, F, b, ctx->cand_ord.as<uint32_t>(),
                                                                 prop ? *prop : PropSrc{});
@@ -335,7 +337,11 @@ static int launch_hist(pd_ctx *ctx, const pd_train_params *p, const uint64_t *of
     PD_TRY(ctx->hist_queue.ensure(16));
     g.queue = ctx->hist_queue.as<unsigned>();
   }
-  PD_TRY(launch_hist_grid<P>(ctx, g));
+  if constexpr (P::kRtcOnly) {
+    PD_TRY(launch_hist_grid_rtc(ctx, g));
+  } else {
+    PD_TRY(launch_hist_grid<P>(ctx, g));
+  }
   if (ev_after) PD_CUDA(cudaEventRecord(ev_after, ctx->stream));
   return PD_OK;
 }
@@ -706,14 +712,16 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
       uint8_t *fl = ctx->flags.as<uint8_t>();
       void *args[] = {&ds, &a_, &r_, &as_, &na, &sn_, &lc_, &tf, &tt, &nx, &fl};
       PD_TRY(rtc_launch(ctx, rk->reassign, dim3((unsigned)((n_act + 255) / 256)), dim3(256), 0, args));
-    } else if (n_act) {
-      k_reassign<P><<<(unsigned)((n_act + 255) / 256), 256, 0, st>>>(
-          devset(ctx), ctx->act[cur].as<uint32_t>(), ctx->act_rec[cur].as<SampleRec>(),
-          ctx->act_slot[cur].as<uint32_t>(), (uint32_t)n_act,
-          ctx->snode.as<int32_t>(), ctx->t_lc.as<int32_t>(), ctx->t_feat.as<FeatT>(), ctx->t_thr.as<FeatT>(),
-          d_next.as<SlotNext>(), ctx->flags.as<uint8_t>());
-      PD_CUDA(cudaGetLastError());
-      ctx->launches++;
+    } else if constexpr (!P::kRtcOnly) {
+      if (n_act) {
+        k_reassign<P><<<(unsigned)((n_act + 255) / 256), 256, 0, st>>>(
+            devset(ctx), ctx->act[cur].as<uint32_t>(), ctx->act_rec[cur].as<SampleRec>(),
+            ctx->act_slot[cur].as<uint32_t>(), (uint32_t)n_act,
+            ctx->snode.as<int32_t>(), ctx->t_lc.as<int32_t>(), ctx->t_feat.as<FeatT>(), ctx->t_thr.as<FeatT>(),
+            d_next.as<SlotNext>(), ctx->flags.as<uint8_t>());
+        PD_CUDA(cudaGetLastError());
+        ctx->launches++;
+      }
     }
     const uint64_t n_next = next_off.back();
     if (!next.empty() && n_act) {

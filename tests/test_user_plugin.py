@@ -75,8 +75,10 @@ def test_user_plugin_compile_errors_carry_the_log():
 def test_user_plugin_config_needs_a_supported_shape():
     with pytest.raises(ValueError):
         pg.ForestConfig("user", 3, source="", shape="u16x1_i32x4")
-    with pytest.raises(ValueError):
-        pg.ForestConfig("user", 3, source="x", shape="u16x2_i32x4")
+    for bad in ("u16x5_i32x4", "u16x1_i32x9", "u16x1_i32x0", "f64x1_i32x4", "u16x1_f32x4"):
+        with pytest.raises(ValueError):
+            pg.ForestConfig("user", 3, source="x", shape=bad)
+    assert pg.user_shape("f32x2_i16x7")["feat_dim"] == 7
 
 
 @pytest.mark.gpu
@@ -116,3 +118,80 @@ def test_user_plugin_must_compile_before_use():
         assert rc != 0 and b"pd_plugin_compile" in N.lib().pd_last_error()
     finally:
         N.lib().pd_ctx_destroy(h)
+
+
+# Features of other types and dimensions than the built-in ones, each written so that it
+# computes a built-in feature exactly: its trees and predictions must equal the built-in
+# plugin's on the same data (which the parity tests pin to the oracle).
+GENERIC = {
+    # float images: the depth difference read from float32 depths
+    "f32x1_i32x4": ("depth_diff2", lambda px: px.astype(np.float32), r"""
+__device__ feat_t computeFeature(const pd::ImageView &img, int2 c, const feat_t *f, unsigned featDim) {
+  int d = (int)img.read(c.x, c.y, 0);
+  if (d == 0) d = 10000;
+  const float fd = (float)d;
+  const int x1 = c.x + (int)roundf(__fdiv_rn((float)f[0], fd)), y1 = c.y + (int)roundf(__fdiv_rn((float)f[1], fd));
+  const int x2 = c.x + (int)roundf(__fdiv_rn((float)f[2], fd)), y2 = c.y + (int)roundf(__fdiv_rn((float)f[3], fd));
+  int a = (int)img.read(x1, y1, 0), b = (int)img.read(x2, y2, 0);
+  if (a == 0) a = 10000;
+  if (b == 0) b = 10000;
+  return a - b;
+}
+"""),
+    # int16 images and FeatDim 3 (the third value unused): test/feature.cl
+    "i16x1_i16x3": ("depth_diff1", lambda px: px.astype(np.int16), r"""
+__device__ feat_t computeFeature(const pd::ImageView &img, int2 c, const feat_t *f, unsigned featDim) {
+  const short depth = img.read(c.x, c.y, 0);
+  int probe = 10000;
+  if (depth != 0) {
+    const int ox = c.x + (int)roundf(__fdiv_rn(__fmul_rn((float)f[0], 500.0f), (float)depth));
+    const int oy = c.y + (int)roundf(__fdiv_rn(__fmul_rn((float)f[1], 500.0f), (float)depth));
+    const short v = img.read(ox, oy, 0);
+    probe = v ? v : 10000;
+  }
+  return (feat_t)(depth - probe);
+}
+"""),
+    # four-channel images (RGBA, alpha unused): the RGB channel difference
+    "u8x4_i32x6": ("channel_diff",
+                   lambda px: np.concatenate([px, np.full(px.shape[:-1] + (1,), 255, np.uint8)], axis=-1), r"""
+__device__ feat_t computeFeature(const pd::ImageView &img, int2 c, const feat_t *f, unsigned featDim) {
+  const int c1 = min(max((int)f[0], 0), 2), c2 = min(max((int)f[1], 0), 2);
+  return (int)img.read(c.x + f[2], c.y + f[3], c1) - (int)img.read(c.x + f[4], c.y + f[5], c2);
+}
+"""),
+}
+
+
+@pytest.mark.parametrize("shape", sorted(GENERIC))
+def test_generic_user_plugin_compiles_without_a_gpu(shape):
+    base, _, src = GENERIC[shape]
+    assert isinstance(pg.check_plugin(pg.ForestConfig("user", 3, source=src, shape=shape)), str)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", sorted(GENERIC))
+def test_generic_user_plugin_equals_the_builtin(shape):
+    base, convert, src = GENERIC[shape]
+    cfg, ts, tp, (px, lb, sm) = CASES[base]()
+    ucfg = pg.ForestConfig("user", cfg.n_classes, source=src, shape=shape)
+    upx = convert(px)
+    uts = pg.training_set(cfg.n_classes, upx, lb, sm)
+    D = cfg.feat_dim
+    lo = list(tp.feat_low_bounds) + [0] * (ucfg.feat_dim - D)
+    up = list(tp.feat_up_bounds) + [1] * (ucfg.feat_dim - D)
+    utp = pg.TreeTrainerParameters(tp.n_features, tp.n_thresholds, lo, up, tp.thr_low_bound, tp.thr_up_bound,
+                                   tp.per_leaf_samples_thr)
+    a = pg.Tree(cfg, 3, 7)
+    pg.TreeTrainer(cfg).train(a, ts, tp)
+    b = pg.Tree(ucfg, 3, 7)
+    pg.TreeTrainer(ucfg).train(b, uts, utp)
+    assert (a.left_child >= 0).sum() > 3
+    assert np.array_equal(a.left_child, b.left_child)
+    assert np.array_equal(a.features, np.asarray(b.features)[:, :D]) and np.array_equal(a.thresholds, b.thresholds)
+    assert np.array_equal(a.posteriors.view(np.uint32), b.posteriors.view(np.uint32))
+    ca, cb = pg.Classifier(cfg), pg.Classifier(ucfg)
+    ca << a
+    cb << b
+    assert np.array_equal(ca.predict(px[0]).view(np.uint32), cb.predict(upx[0]).view(np.uint32))
+    assert np.array_equal(ca.predict_leaf(0, px[0]), cb.predict_leaf(0, upx[0]))
