@@ -69,6 +69,71 @@ PD_D void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// Stages rows [r0, r0 + 64) x columns [k0, k0 + kn) of a BF16 operand X(r, k) =
+// X[r * s_r + k * s_k] into S[r * ld + c] (zero outside r < R, k < ke).  Each
+// thread issues a batch of 8 loads before it stores any, so a batch's global
+// latencies overlap.  vec: 16-byte loads along whichever index is contiguous
+// (s_k == 1: along k, stored as 16 bytes; s_r == 1: along r, spread over 8 rows).
+constexpr int kStageBatch = 8;
+PD_D void stage_tile(bf16 *S, int ld, const bf16 *__restrict__ X, int64_t s_r, int64_t s_k, int r0, int R, int k0,
+                     int kn, int ke, bool vec, int tid) {
+  if (vec) {
+    const bool along_k = s_k == 1;
+    const int total = kGemmTM * kn / 8;
+    for (int e0 = tid; e0 < total; e0 += 128 * kStageBatch) {
+      uint4 v[kStageBatch];
+#pragma unroll
+      for (int b = 0; b < kStageBatch; b++) {
+        const int e = e0 + b * 128;
+        int r, c;
+        if (along_k) {
+          r = e / (kn / 8);
+          c = (e % (kn / 8)) * 8;
+        } else {
+          r = (e % (kGemmTM / 8)) * 8;
+          c = e / (kGemmTM / 8);
+        }
+        const int gr = r0 + r, gk = k0 + c;
+        v[b] = make_uint4(0u, 0u, 0u, 0u);
+        if (e < total && gr < R && gk < ke) v[b] = *reinterpret_cast<const uint4 *>(X + (int64_t)gr * s_r + (int64_t)gk * s_k);
+      }
+#pragma unroll
+      for (int b = 0; b < kStageBatch; b++) {
+        const int e = e0 + b * 128;
+        if (e >= total) break;
+        if (along_k) {
+          *reinterpret_cast<uint4 *>(S + (e / (kn / 8)) * ld + (e % (kn / 8)) * 8) = v[b];
+        } else {
+          const int r = (e % (kGemmTM / 8)) * 8, c = e / (kGemmTM / 8);
+          const bf16 *pv = reinterpret_cast<const bf16 *>(&v[b]);
+#pragma unroll
+          for (int q = 0; q < 8; q++) S[(r + q) * ld + c] = pv[q];
+        }
+      }
+    }
+    return;
+  }
+  const bf16 zero = __float2bfloat16(0.0f);
+  const int total = kGemmTM * kn;
+  for (int e0 = tid; e0 < total; e0 += 128 * kStageBatch) {
+    bf16 v[kStageBatch];
+#pragma unroll
+    for (int b = 0; b < kStageBatch; b++) {
+      const int e = e0 + b * 128;
+      const int r = s_k == 1 ? e / kn : e % kGemmTM, c = s_k == 1 ? e % kn : e / kGemmTM;
+      const int gr = r0 + r, gk = k0 + c;
+      v[b] = (e < total && gr < R && gk < ke) ? X[(int64_t)gr * s_r + (int64_t)gk * s_k] : zero;
+    }
+#pragma unroll
+    for (int b = 0; b < kStageBatch; b++) {
+      const int e = e0 + b * 128;
+      if (e >= total) break;
+      const int r = s_k == 1 ? e / kn : e % kGemmTM, c = s_k == 1 ? e % kn : e / kGemmTM;
+      S[r * ld + c] = v[b];
+    }
+  }
+}
+
 // 64 x 64 output tile per CTA, 4 warps of 32 x 32 (2 x 4 mma tiles each).  The
 // reduction range is staged in shared memory kstage (<= 256) at a time -- for
 // every product of the network one stage holds it all, so each CTA issues all
@@ -86,7 +151,6 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
   const int wm = warp >> 1, wn = warp & 1, gq = lane >> 2, tq = lane & 3;
   const int i0 = blockIdx.y * kGemmTM, j0 = blockIdx.x * kGemmTN;
   const int kb = blockIdx.z * g.k_split, ke = min(g.K, kb + g.k_split);
-  const bf16 zero = __float2bfloat16(0.0f);
   float acc[2][4][4];
 #pragma unroll
   for (int a = 0; a < 2; a++)
@@ -96,54 +160,9 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
       for (int c = 0; c < 4; c++) acc[a][b][c] = 0.0f;
   for (int k0 = kb; k0 < ke; k0 += ks) {
     const int kn = min(ks, ke - k0 + 31) / 32 * 32;  // columns of this stage, a multiple of 32
-    if (g.vec_a && g.a_k == 1) {
-      // rows contiguous in k: one 16-byte load per 8 elements
-      for (int e = tid; e < kGemmTM * kn / 8; e += 128) {
-        const int r = e / (kn / 8), c = (e % (kn / 8)) * 8, gi = i0 + r, gk = k0 + c;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gi < g.M && gk < ke) v = *reinterpret_cast<const uint4 *>(g.A + (int64_t)gi * g.a_i + gk);
-        *reinterpret_cast<uint4 *>(As + r * ld + c) = v;
-      }
-    } else if (g.vec_a) {
-      // columns contiguous in i: 16-byte loads of 8 rows, spread over the tile's rows
-      for (int e = tid; e < kGemmTM / 8 * kn; e += 128) {
-        const int r = (e % (kGemmTM / 8)) * 8, c = e / (kGemmTM / 8), gi = i0 + r, gk = k0 + c;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gi < g.M && gk < ke) v = *reinterpret_cast<const uint4 *>(g.A + gi + (int64_t)gk * g.a_k);
-        const bf16 *pv = reinterpret_cast<const bf16 *>(&v);
-#pragma unroll
-        for (int q = 0; q < 8; q++) As[(r + q) * ld + c] = pv[q];
-      }
-    } else {
-      for (int e = tid; e < kGemmTM * kn; e += 128) {
-        const int r = g.a_k == 1 ? e / kn : e % kGemmTM, c = g.a_k == 1 ? e % kn : e / kGemmTM;
-        const int gi = i0 + r, gk = k0 + c;
-        As[r * ld + c] = (gi < g.M && gk < ke) ? g.A[(int64_t)gi * g.a_i + (int64_t)gk * g.a_k] : zero;
-      }
-    }
-    if (g.vec_b && g.b_k == 1) {
-      for (int e = tid; e < kGemmTN * kn / 8; e += 128) {
-        const int r = e / (kn / 8), c = (e % (kn / 8)) * 8, gj = j0 + r, gk = k0 + c;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gj < g.N && gk < ke) v = *reinterpret_cast<const uint4 *>(g.B + gk + (int64_t)gj * g.b_j);
-        *reinterpret_cast<uint4 *>(Bs + r * ld + c) = v;
-      }
-    } else if (g.vec_b) {
-      for (int e = tid; e < kGemmTN / 8 * kn; e += 128) {
-        const int r = (e % (kGemmTN / 8)) * 8, c = e / (kGemmTN / 8), gj = j0 + r, gk = k0 + c;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gj < g.N && gk < ke) v = *reinterpret_cast<const uint4 *>(g.B + (int64_t)gk * g.b_k + gj);
-        const bf16 *pv = reinterpret_cast<const bf16 *>(&v);
-#pragma unroll
-        for (int q = 0; q < 8; q++) Bs[(r + q) * ld + c] = pv[q];
-      }
-    } else {
-      for (int e = tid; e < kGemmTN * kn; e += 128) {
-        const int r = g.b_k == 1 ? e / kn : e % kGemmTN, c = g.b_k == 1 ? e % kn : e / kGemmTN;
-        const int gj = j0 + r, gk = k0 + c;
-        Bs[r * ld + c] = (gj < g.N && gk < ke) ? g.B[(int64_t)gk * g.b_k + (int64_t)gj * g.b_j] : zero;
-      }
-    }
+    // A(i, k) for i in [i0, i0 + 64); B(k, j) staged as rows j in [j0, j0 + 64)
+    stage_tile(As, ld, g.A, g.a_i, g.a_k, i0, g.M, k0, kn, ke, g.vec_a != 0, tid);
+    stage_tile(Bs, ld, g.B, g.b_j, g.b_k, j0, g.N, k0, kn, ke, g.vec_b != 0, tid);
     __syncthreads();
     for (int kk = 0; kk < kn; kk += 16) {
       uint32_t a[2][4], b[4][2];
