@@ -49,6 +49,8 @@ struct GemmArgs {
   const float *zin;    // z of the layer (EPI_DGELU)
   int64_t ldo;         // row pitch of outf / outb / zin
   int64_t split_stride;  // EPI_PARTIAL: floats between the partials of two splits
+  float *bias_part;      // EPI_PARTIAL: row sums of A over the split (the bias gradient), written by the
+                         // CTAs of the first column tile (null: none)
   // 16-byte loads of 8 elements along the contiguous index of A / B (set by
   // gemm() when that index's extent, the other stride, the split length and
   // the base pointer allow it)
@@ -151,6 +153,7 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
   const int wm = warp >> 1, wn = warp & 1, gq = lane >> 2, tq = lane & 3;
   const int i0 = blockIdx.y * kGemmTM, j0 = blockIdx.x * kGemmTN;
   const int kb = blockIdx.z * g.k_split, ke = min(g.K, kb + g.k_split);
+  float bsum = 0.0f;  // EPI_PARTIAL with bias_part: this thread's row sum
   float acc[2][4][4];
 #pragma unroll
   for (int a = 0; a < 2; a++)
@@ -163,6 +166,11 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
     // A(i, k) for i in [i0, i0 + 64); B(k, j) staged as rows j in [j0, j0 + 64)
     stage_tile(As, ld, g.A, g.a_i, g.a_k, i0, g.M, k0, kn, ke, g.vec_a != 0, tid);
     stage_tile(Bs, ld, g.B, g.b_j, g.b_k, j0, g.N, k0, kn, ke, g.vec_b != 0, tid);
+    if (EPI == EPI_PARTIAL && g.bias_part && blockIdx.x == 0) {
+      __syncthreads();
+      if (tid < kGemmTM)  // row sums of the staged A tile, in column order
+        for (int c = 0; c < kn; c++) bsum += __bfloat162float(As[tid * ld + c]);
+    }
     __syncthreads();
     for (int kk = 0; kk < kn; kk += 16) {
       uint32_t a[2][4], b[4][2];
@@ -211,6 +219,8 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
             g.outf[(int64_t)blockIdx.z * g.split_stride + o] = v;
           }
         }
+  if (EPI == EPI_PARTIAL && g.bias_part && blockIdx.x == 0 && tid < kGemmTM && i0 + tid < g.M)
+    g.bias_part[(int64_t)blockIdx.z * g.split_stride + i0 + tid] = bsum;
 }
 
 // Mixture negative log-likelihood of each row's target and its gradient with
@@ -270,31 +280,6 @@ __global__ void __launch_bounds__(128) k_prop_mdn(const float *__restrict__ out,
   for (uint32_t j = (uint32_t)kPropG * (1u + 2u * DY) + gk; j < ldo; j += 16u) d[j] = __float2bfloat16(0.0f);
 }
 
-// Bias gradients: per split, column sums of a BF16 [rows][n] matrix over the
-// split's rows.  A block covers 32 columns with 8 row groups (rows r, r + 8,
-// ... of the split, several loads in flight per thread), and the groups are
-// added in a fixed order, so the sums do not depend on scheduling.
-__global__ void __launch_bounds__(256) k_prop_colsum(const bf16 *__restrict__ m, uint32_t rows, uint32_t n,
-                                                     uint32_t rows_per_split, float *__restrict__ part,
-                                                     uint64_t split_stride) {
-  __shared__ float acc[8][33];
-  const uint32_t j = blockIdx.x * 32u + threadIdx.x, grp = threadIdx.y;
-  const uint32_t r0 = blockIdx.y * rows_per_split, r1 = min(rows, r0 + rows_per_split);
-  float s = 0.0f;
-  if (j < n) {
-#pragma unroll 8
-    for (uint32_t r = r0 + grp; r < r1; r += 8u) s += __bfloat162float(m[(size_t)r * n + j]);
-  }
-  acc[grp][threadIdx.x] = s;
-  __syncthreads();
-  if (grp == 0 && j < n) {
-    float t = 0.0f;
-#pragma unroll
-    for (int q = 0; q < 8; q++) t += acc[q][threadIdx.x];
-    part[blockIdx.y * split_stride + j] = t;
-  }
-}
-
 // Sums the split partials of every parameter in split order (the gradient).
 __global__ void k_prop_grad_sum(const float *__restrict__ part, uint64_t P, float *__restrict__ grad) {
   const uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -313,7 +298,7 @@ __global__ void k_prop_adam(const float *__restrict__ part, uint64_t P, float *_
   float g = 0.0f;
   for (int s = 0; s < kSplits; s++) g += part[(uint64_t)s * P + p];
   const float b1 = 0.9f, b2 = 0.999f;
-  const float t = (float)step[0];
+  const float t = (float)(step[0] + 1u);  // this step's number (the loss kernel advances the counter)
   const float mm = b1 * m[p] + (1.0f - b1) * g, vv = b2 * v[p] + (1.0f - b2) * g * g;
   m[p] = mm;
   v[p] = vv;
@@ -323,16 +308,15 @@ __global__ void k_prop_adam(const float *__restrict__ part, uint64_t P, float *_
   wb[p] = __float2bfloat16(nw);
 }
 
-__global__ void k_prop_step(uint32_t *step) { step[0] += 1u; }
-
 __global__ void k_prop_to_bf16(const float *__restrict__ x, uint64_t n, bf16 *__restrict__ y) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) y[i] = __float2bfloat16(x[i]);
 }
 
-// The loss of one step: sum of the rows' weighted losses, in a fixed order.
+// The loss of one step: sum of the rows' weighted losses, in a fixed order;
+// the last kernel of a step, it advances the step counter.
 __global__ void __launch_bounds__(256) k_prop_loss(const float *__restrict__ rows, uint32_t B,
-                                                   const uint32_t *__restrict__ step, float *__restrict__ hist,
+                                                   uint32_t *__restrict__ step, float *__restrict__ hist,
                                                    uint32_t hist_len) {
   __shared__ float s[256];
   float a = 0.0f;
@@ -345,7 +329,8 @@ __global__ void __launch_bounds__(256) k_prop_loss(const float *__restrict__ row
   }
   if (threadIdx.x == 0) {
     const uint32_t t = step[0];
-    if (t >= 1 && t <= hist_len) hist[t - 1] = s[0];
+    if (t < hist_len) hist[t] = s[0];
+    step[0] = t + 1u;
   }
 }
 
@@ -372,7 +357,7 @@ __global__ void k_prop_gather(const bf16 *__restrict__ rx, const float *__restri
                               float *__restrict__ w) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B) return;
-  const uint32_t k = (uint32_t)(prop_mix(seed ^ prop_mix(((uint64_t)step[0] << 32) | i)) % n);
+  const uint32_t k = (uint32_t)(prop_mix(seed ^ prop_mix(((uint64_t)(step[0] + 1u) << 32) | i)) % n);
   for (uint32_t j = 0; j < IN; j++) x[(size_t)i * IN + j] = rx[(size_t)k * IN + j];
   for (uint32_t d = 0; d < DY; d++) y[(size_t)i * DY + d] = ry[(size_t)k * DY + d];
   w[i] = rw[k];
@@ -530,9 +515,8 @@ static int prop_backward(pd_proposer *p, uint32_t n, cudaStream_t st) {
     g.outf = part + p->off_w[l];
     g.ldo = di;
     g.split_stride = (int64_t)p->P;
+    g.bias_part = part + p->off_b[l];  // db[j] = sum_i d(i, j), from the same staged tiles
     PD_TRY(gemm<EPI_PARTIAL>(st, g, kSplits));
-    k_prop_colsum<<<dim3((dn + 31) / 32, kSplits), dim3(32, 8), 0, st>>>(d, n, dn, per, part + p->off_b[l], p->P);
-    PD_CUDA(cudaGetLastError());
     if (l == 0) break;
     // d(in)(i, k) = sum_j d(i, j) W[j][k], times GELU'(z of layer l - 1)
     GemmArgs h = gargs(d, dn, 1, wb + p->off_w[l], di, 1, (int)n, (int)di, (int)dn);
@@ -785,7 +769,6 @@ extern "C" int pd_proposer_fit(pd_proposer *p, const pd_record *records, uint64_
     cudaGraph_t g = nullptr;
     PD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     int rc = PD_OK;
-    k_prop_step<<<1, 1, 0, st>>>(p->step.as<uint32_t>());
     k_prop_gather<<<(batch + 127) / 128, 128, 0, st>>>(p->rec_x.as<bf16>(), p->rec_y.as<float>(),
                                                        p->rec_w.as<float>(), (uint32_t)n, p->IN, p->DY, batch,
                                                        p->seed, p->step.as<uint32_t>(), p->x.as<bf16>(),
@@ -817,6 +800,6 @@ extern "C" int pd_proposer_fit(pd_proposer *p, const pd_record *records, uint64_
     PD_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     *ms_out = ms;
   }
-  p->ctx->launches += (uint64_t)steps * 22;
+  p->ctx->launches += (uint64_t)steps * 15;  // gather, 4 forward and 7 backward products, loss, Adam, loss sum
   return PD_OK;
 }
