@@ -71,64 +71,63 @@ PD_D void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-// Stages rows [r0, r0 + 64) x columns [k0, k0 + kn) of a BF16 operand X(r, k) =
-// X[r * s_r + k * s_k] into S[r * ld + c] (zero outside r < R, k < ke).  Each
-// thread issues a batch of 8 loads before it stores any, so a batch's global
-// latencies overlap.  vec: 16-byte loads along whichever index is contiguous
-// (s_k == 1: along k, stored as 16 bytes; s_r == 1: along r, spread over 8 rows).
-constexpr int kStageBatch = 8;
-PD_D void stage_tile(bf16 *S, int ld, const bf16 *__restrict__ X, int64_t s_r, int64_t s_k, int r0, int R, int k0,
-                     int kn, int ke, bool vec, int tid) {
-  if (vec) {
-    const bool along_k = s_k == 1;
-    const int total = kGemmTM * kn / 8;
-    for (int e0 = tid; e0 < total; e0 += 128 * kStageBatch) {
-      uint4 v[kStageBatch];
+constexpr int kGemmThreads = 256;  // 8 warps: 4 x 2 warps of 16 x 32 outputs
+constexpr int kStageBatch = 8;     // 16-byte loads per thread per operand in flight
+
+// The 16-byte loads of one operand tile: rows [r0, r0 + 64) x columns
+// [k0, k0 + kn) of X(r, k) = X[r * s_r + k * s_k], 8 elements each along the
+// contiguous index (s_k == 1: along k; s_r == 1: along r); zero outside r < R,
+// k < ke.  Load and store are separate so that both operands' loads are in
+// flight before the first store.
+struct TileLoads {
+  uint4 v[kStageBatch];
+};
+PD_D void tile_load(TileLoads &L, int e0, const bf16 *__restrict__ X, int64_t s_r, int64_t s_k, int r0, int R,
+                    int k0, int kn, int ke) {
+  const bool along_k = s_k == 1;
+  const int total = kGemmTM * kn / 8;
 #pragma unroll
-      for (int b = 0; b < kStageBatch; b++) {
-        const int e = e0 + b * 128;
-        int r, c;
-        if (along_k) {
-          r = e / (kn / 8);
-          c = (e % (kn / 8)) * 8;
-        } else {
-          r = (e % (kGemmTM / 8)) * 8;
-          c = e / (kGemmTM / 8);
-        }
-        const int gr = r0 + r, gk = k0 + c;
-        v[b] = make_uint4(0u, 0u, 0u, 0u);
-        if (e < total && gr < R && gk < ke) v[b] = *reinterpret_cast<const uint4 *>(X + (int64_t)gr * s_r + (int64_t)gk * s_k);
-      }
-#pragma unroll
-      for (int b = 0; b < kStageBatch; b++) {
-        const int e = e0 + b * 128;
-        if (e >= total) break;
-        if (along_k) {
-          *reinterpret_cast<uint4 *>(S + (e / (kn / 8)) * ld + (e % (kn / 8)) * 8) = v[b];
-        } else {
-          const int r = (e % (kGemmTM / 8)) * 8, c = e / (kGemmTM / 8);
-          const bf16 *pv = reinterpret_cast<const bf16 *>(&v[b]);
-#pragma unroll
-          for (int q = 0; q < 8; q++) S[(r + q) * ld + c] = pv[q];
-        }
-      }
-    }
-    return;
+  for (int b = 0; b < kStageBatch; b++) {
+    const int e = e0 + b * kGemmThreads;
+    const int r = along_k ? e / (kn / 8) : (e % (kGemmTM / 8)) * 8, c = along_k ? (e % (kn / 8)) * 8 : e / (kGemmTM / 8);
+    const int gr = r0 + r, gk = k0 + c;
+    L.v[b] = make_uint4(0u, 0u, 0u, 0u);
+    if (e < total && gr < R && gk < ke) L.v[b] = *reinterpret_cast<const uint4 *>(X + (int64_t)gr * s_r + (int64_t)gk * s_k);
   }
+}
+PD_D void tile_store(const TileLoads &L, int e0, bf16 *S, int ld, bool along_k, int kn) {
+  const int total = kGemmTM * kn / 8;
+#pragma unroll
+  for (int b = 0; b < kStageBatch; b++) {
+    const int e = e0 + b * kGemmThreads;
+    if (e >= total) break;
+    if (along_k) {
+      *reinterpret_cast<uint4 *>(S + (e / (kn / 8)) * ld + (e % (kn / 8)) * 8) = L.v[b];
+    } else {
+      const int r = (e % (kGemmTM / 8)) * 8, c = e / (kGemmTM / 8);
+      const bf16 *pv = reinterpret_cast<const bf16 *>(&L.v[b]);
+#pragma unroll
+      for (int q = 0; q < 8; q++) S[(r + q) * ld + c] = pv[q];
+    }
+  }
+}
+// Element-wise staging for layouts that do not allow 16-byte loads.
+PD_D void tile_scalar(bf16 *S, int ld, const bf16 *__restrict__ X, int64_t s_r, int64_t s_k, int r0, int R, int k0,
+                      int kn, int ke, int tid) {
   const bf16 zero = __float2bfloat16(0.0f);
   const int total = kGemmTM * kn;
-  for (int e0 = tid; e0 < total; e0 += 128 * kStageBatch) {
+  for (int e0 = tid; e0 < total; e0 += kGemmThreads * kStageBatch) {
     bf16 v[kStageBatch];
 #pragma unroll
     for (int b = 0; b < kStageBatch; b++) {
-      const int e = e0 + b * 128;
+      const int e = e0 + b * kGemmThreads;
       const int r = s_k == 1 ? e / kn : e % kGemmTM, c = s_k == 1 ? e % kn : e / kGemmTM;
       const int gr = r0 + r, gk = k0 + c;
       v[b] = (e < total && gr < R && gk < ke) ? X[(int64_t)gr * s_r + (int64_t)gk * s_k] : zero;
     }
 #pragma unroll
     for (int b = 0; b < kStageBatch; b++) {
-      const int e = e0 + b * 128;
+      const int e = e0 + b * kGemmThreads;
       if (e >= total) break;
       const int r = s_k == 1 ? e / kn : e % kGemmTM, c = s_k == 1 ? e % kn : e / kGemmTM;
       S[r * ld + c] = v[b];
@@ -136,15 +135,14 @@ PD_D void stage_tile(bf16 *S, int ld, const bf16 *__restrict__ X, int64_t s_r, i
   }
 }
 
-// 64 x 64 output tile per CTA, 4 warps of 32 x 32 (2 x 4 mma tiles each).  The
+// 64 x 64 output tile per CTA, 8 warps of 16 x 32 (1 x 4 mma tiles each).  The
 // reduction range is staged in shared memory kstage (<= 256) at a time -- for
-// every product of the network one stage holds it all, so each CTA issues all
-// its loads before its single barrier -- as an A tile [i][k] and a B tile
-// [j][k] (k contiguous, so every fragment register is one aligned 32-bit
-// load), read from global memory along whichever index is contiguous there
-// (16-byte loads where the layout allows).
+// every product of the network one stage holds it all, and with 256 threads a
+// full stage is one batch of 8 loads per thread and operand, issued for both
+// operands before any store -- as an A tile [i][k] and a B tile [j][k] (k
+// contiguous, so every fragment register is one aligned 32-bit load).
 template <int EPI>
-__global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
+__global__ void __launch_bounds__(kGemmThreads) k_prop_gemm(GemmArgs g) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int ks = g.kstage, ld = ks + kGemmPad;  // row pitch in elements (a multiple of 8)
   bf16 *As = reinterpret_cast<bf16 *>(smem_raw);
@@ -154,34 +152,54 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
   const int i0 = blockIdx.y * kGemmTM, j0 = blockIdx.x * kGemmTN;
   const int kb = blockIdx.z * g.k_split, ke = min(g.K, kb + g.k_split);
   float bsum = 0.0f;  // EPI_PARTIAL with bias_part: this thread's row sum
-  float acc[2][4][4];
+  float acc[4][4];
 #pragma unroll
-  for (int a = 0; a < 2; a++)
+  for (int b = 0; b < 4; b++)
 #pragma unroll
-    for (int b = 0; b < 4; b++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) acc[a][b][c] = 0.0f;
+    for (int c = 0; c < 4; c++) acc[b][c] = 0.0f;
   for (int k0 = kb; k0 < ke; k0 += ks) {
     const int kn = min(ks, ke - k0 + 31) / 32 * 32;  // columns of this stage, a multiple of 32
     // A(i, k) for i in [i0, i0 + 64); B(k, j) staged as rows j in [j0, j0 + 64)
-    stage_tile(As, ld, g.A, g.a_i, g.a_k, i0, g.M, k0, kn, ke, g.vec_a != 0, tid);
-    stage_tile(Bs, ld, g.B, g.b_j, g.b_k, j0, g.N, k0, kn, ke, g.vec_b != 0, tid);
-    if (EPI == EPI_PARTIAL && g.bias_part && blockIdx.x == 0) {
-      __syncthreads();
-      if (tid < kGemmTM)  // row sums of the staged A tile, in column order
-        for (int c = 0; c < kn; c++) bsum += __bfloat162float(As[tid * ld + c]);
+    if (g.vec_a && g.vec_b) {
+      for (int e0 = tid; e0 < kGemmTM * kn / 8; e0 += kGemmThreads * kStageBatch) {
+        TileLoads la, lb;
+        tile_load(la, e0, g.A, g.a_i, g.a_k, i0, g.M, k0, kn, ke);
+        tile_load(lb, e0, g.B, g.b_j, g.b_k, j0, g.N, k0, kn, ke);
+        tile_store(la, e0, As, ld, g.a_k == 1, kn);
+        tile_store(lb, e0, Bs, ld, g.b_k == 1, kn);
+      }
+    } else {
+      if (g.vec_a) {
+        for (int e0 = tid; e0 < kGemmTM * kn / 8; e0 += kGemmThreads * kStageBatch) {
+          TileLoads la;
+          tile_load(la, e0, g.A, g.a_i, g.a_k, i0, g.M, k0, kn, ke);
+          tile_store(la, e0, As, ld, g.a_k == 1, kn);
+        }
+      } else {
+        tile_scalar(As, ld, g.A, g.a_i, g.a_k, i0, g.M, k0, kn, ke, tid);
+      }
+      if (g.vec_b) {
+        for (int e0 = tid; e0 < kGemmTN * kn / 8; e0 += kGemmThreads * kStageBatch) {
+          TileLoads lb;
+          tile_load(lb, e0, g.B, g.b_j, g.b_k, j0, g.N, k0, kn, ke);
+          tile_store(lb, e0, Bs, ld, g.b_k == 1, kn);
+        }
+      } else {
+        tile_scalar(Bs, ld, g.B, g.b_j, g.b_k, j0, g.N, k0, kn, ke, tid);
+      }
     }
     __syncthreads();
+    if (EPI == EPI_PARTIAL && g.bias_part && blockIdx.x == 0 && tid < kGemmTM) {
+      // row sums of the staged A tile, in column order
+      for (int c = 0; c < kn; c++) bsum += __bfloat162float(As[tid * ld + c]);
+    }
     for (int kk = 0; kk < kn; kk += 16) {
-      uint32_t a[2][4], b[4][2];
-#pragma unroll
-      for (int mt = 0; mt < 2; mt++) {
-        const bf16 *r0 = As + (wm * 32 + mt * 16 + gq) * ld + kk + tq * 2;
-        a[mt][0] = *reinterpret_cast<const uint32_t *>(r0);
-        a[mt][1] = *reinterpret_cast<const uint32_t *>(r0 + 8 * ld);
-        a[mt][2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
-        a[mt][3] = *reinterpret_cast<const uint32_t *>(r0 + 8 * ld + 8);
-      }
+      uint32_t a[4], b[4][2];
+      const bf16 *r0 = As + (wm * 16 + gq) * ld + kk + tq * 2;
+      a[0] = *reinterpret_cast<const uint32_t *>(r0);
+      a[1] = *reinterpret_cast<const uint32_t *>(r0 + 8 * ld);
+      a[2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
+      a[3] = *reinterpret_cast<const uint32_t *>(r0 + 8 * ld + 8);
 #pragma unroll
       for (int nt = 0; nt < 4; nt++) {
         const bf16 *c0 = Bs + (wn * 32 + nt * 8 + gq) * ld + kk + tq * 2;
@@ -189,36 +207,32 @@ __global__ void __launch_bounds__(128) k_prop_gemm(GemmArgs g) {
         b[nt][1] = *reinterpret_cast<const uint32_t *>(c0 + 8);
       }
 #pragma unroll
-      for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-        for (int nt = 0; nt < 4; nt++) mma_bf16(acc[mt][nt], a[mt], b[nt]);
+      for (int nt = 0; nt < 4; nt++) mma_bf16(acc[nt], a, b[nt]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int mt = 0; mt < 2; mt++)
+  for (int nt = 0; nt < 4; nt++)
 #pragma unroll
-    for (int nt = 0; nt < 4; nt++)
+    for (int h = 0; h < 2; h++)
 #pragma unroll
-      for (int h = 0; h < 2; h++)
-#pragma unroll
-        for (int e = 0; e < 2; e++) {
-          const int row = i0 + wm * 32 + mt * 16 + gq + h * 8, col = j0 + wn * 32 + nt * 8 + tq * 2 + e;
-          if (row >= g.M || col >= g.N) continue;
-          const float v = acc[mt][nt][h * 2 + e];
-          const int64_t o = (int64_t)row * g.ldo + col;
-          if (EPI == EPI_GELU) {
-            const float z = v + g.bias[col];
-            g.outf[o] = z;
-            g.outb[o] = __float2bfloat16(gelu_f(z));
-          } else if (EPI == EPI_LINEAR) {
-            g.outf[o] = v + g.bias[col];
-          } else if (EPI == EPI_DGELU) {
-            g.outb[o] = __float2bfloat16(v * gelu_d(g.zin[o]));
-          } else {
-            g.outf[(int64_t)blockIdx.z * g.split_stride + o] = v;
-          }
+      for (int e = 0; e < 2; e++) {
+        const int row = i0 + wm * 16 + gq + h * 8, col = j0 + wn * 32 + nt * 8 + tq * 2 + e;
+        if (row >= g.M || col >= g.N) continue;
+        const float v = acc[nt][h * 2 + e];
+        const int64_t o = (int64_t)row * g.ldo + col;
+        if (EPI == EPI_GELU) {
+          const float z = v + g.bias[col];
+          g.outf[o] = z;
+          g.outb[o] = __float2bfloat16(gelu_f(z));
+        } else if (EPI == EPI_LINEAR) {
+          g.outf[o] = v + g.bias[col];
+        } else if (EPI == EPI_DGELU) {
+          g.outb[o] = __float2bfloat16(v * gelu_d(g.zin[o]));
+        } else {
+          g.outf[(int64_t)blockIdx.z * g.split_stride + o] = v;
         }
+      }
   if (EPI == EPI_PARTIAL && g.bias_part && blockIdx.x == 0 && tid < kGemmTM && i0 + tid < g.M)
     g.bias_part[(int64_t)blockIdx.z * g.split_stride + i0 + tid] = bsum;
 }
@@ -441,7 +455,7 @@ static int gemm(cudaStream_t st, GemmArgs g, int splits = 1) {
   const size_t smem = (size_t)(kGemmTM + kGemmTN) * (g.kstage + kGemmPad) * sizeof(bf16);
   const dim3 grid((unsigned)((g.N + kGemmTN - 1) / kGemmTN), (unsigned)((g.M + kGemmTM - 1) / kGemmTM),
                   (unsigned)splits);
-  k_prop_gemm<EPI><<<grid, 128, smem, st>>>(g);
+  k_prop_gemm<EPI><<<grid, kGemmThreads, smem, st>>>(g);
   PD_CUDA(cudaGetLastError());
   return PD_OK;
 }
