@@ -64,9 +64,9 @@ def args_():
                    help="1: candidate columns ordered by first-probe offset (default), 0: index order")
     a.add_argument("--learned", type=int, default=1, help="1: time the learned-proposal forest beside the plain one")
     a.add_argument("--autotune", type=int, default=1, help="1: launch shapes from pd_autotune before timing")
-    a.add_argument("--fit-steps", type=int, default=200)
-    a.add_argument("--fit-batch", type=int, default=2048)
-    a.add_argument("--fit-lr", type=float, default=2e-3)
+    a.add_argument("--fit-steps", type=int, default=100)
+    a.add_argument("--fit-batch", type=int, default=4096)
+    a.add_argument("--fit-lr", type=float, default=3e-3)
     a.add_argument("--only", default=None,
                    choices=["sampler_uniform", "sampler_class_weighted", "labels", "learned"],
                    help="run one kernel family alone on --images synthetic images already in device memory "
