@@ -64,11 +64,13 @@ def args_():
                    help="1: candidate columns ordered by first-probe offset (default), 0: index order")
     a.add_argument("--learned", type=int, default=1, help="1: time the learned-proposal forest beside the plain one")
     a.add_argument("--autotune", type=int, default=1, help="1: launch shapes from pd_autotune before timing")
+    a.add_argument("--mixed", type=int, default=1,
+                   help="1: time the mixed-size configuration (5000 images of three sizes, depth 20)")
     a.add_argument("--fit-steps", type=int, default=100)
     a.add_argument("--fit-batch", type=int, default=4096)
     a.add_argument("--fit-lr", type=float, default=3e-3)
     a.add_argument("--only", default=None,
-                   choices=["sampler_uniform", "sampler_class_weighted", "labels", "learned"],
+                   choices=["sampler_uniform", "sampler_class_weighted", "labels", "learned", "mixed"],
                    help="run one kernel family alone on --images synthetic images already in device memory "
                         "(--reps times) and print its times: the workload of the sampler and label profiles")
     a.add_argument("--reps", type=int, default=3)
@@ -505,6 +507,74 @@ def rgb_bench(a, pg, device: int):
     return out
 
 
+def mixed_bench(a, pg, device):
+    """The mixed-size frontier-batched configuration: 5000 synthetic depth maps, a third each of
+    160x120, 320x240 and 640x480 (made like the headline's: 2-5 bodies, 9 classes, 2000 samples
+    per image), F=2000 x T=50, one tree of depth 20 (min 20 per leaf).  Every depth's frontier
+    nodes, whatever their sizes, go through one histogram launch per slice (the whole frontier
+    at these sizes), with launch shapes from the autotuner.  Beside it, the per-node-launch form
+    (a histogram budget of one node per slice: candidates, histogram and split launched per
+    frontier node, as the reference launches per node batch and image) on the first 12 levels,
+    where both forms must give the same tree."""
+    import tempfile
+
+    import torch
+    from padenti_gb300 import _native as N
+
+    sizes = [(160, 120), (320, 240), (640, 480)]
+    images = []
+    for k, (w, h) in enumerate(sizes):
+        cnt = 5000 // 3 + (1 if k < 5000 % 3 else 0)
+        px, lb, sm = pg.synth_depth(a.seed, cnt, w, h, first_image=10_000_000 + 100_000 * k, parts=1,
+                                    min_ellipses=2, max_ellipses=5, samples_per_image=a.samples, bg_permille=100)
+        images += [pg.TrainingSetImage(px[i], lb[i], 9, sm[i]) for i in range(cnt)]
+    cfg = pg.ForestConfig("depth_diff2", 9)
+    ts = pg.TrainingSet(9, images)
+    tp = pg.TreeTrainerParameters(a.features, a.thresholds, [-60000] * 4, [60000] * 4, -500, 500, a.min_leaf)
+    tr = pg.TreeTrainer(cfg, device=device)
+    tr.upload(ts)
+    stream = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(tr.h))
+    cache = os.path.join(tempfile.mkdtemp(), "tune.txt")
+    tune = tr.autotune(ts, tp, 20, cache=cache, max_trials=6) if a.autotune else None
+
+    def timed_tree(trainer, tid, depth):
+        tree = pg.Tree(cfg, tid, depth)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s = torch.cuda.ExternalStream(N.lib().pd_ctx_stream(trainer.h))
+        e0.record(s)
+        trainer.train(tree, ts, tp)
+        e1.record(s)
+        e1.synchronize()
+        return tree, e0.elapsed_time(e1), trainer.stats()
+
+    timed_tree(tr, 90, 20)  # warm-up
+    tree, ms, st = timed_tree(tr, 0, 20)
+    out = dict(workload="mixed-size depth maps: 5000 images (a third each of 160x120, 320x240, 640x480), 9 classes, "
+                        "2000 samples/image, F=2000, T=50, depth 20, min 20",
+               metric=METRIC, value=st["evals"] / (ms / 1000), unit=UNIT, ms_per_tree=ms, samples=ts.n_samples,
+               nodes_trained=st["nodes_trained"], nodes_split=st["nodes_split"], hist_launches=st["hist_launches"],
+               kernel_launches=st["kernel_launches"],
+               launch_shape={k: tune[k] for k in ("chunk", "hist_spi", "fuse_max", "cand_order", "persist")}
+               if tune else "fixed")
+    # per-node launches against the batched form on the first 12 levels
+    depth_cmp = 12
+    b_tree, b_ms, b_st = timed_tree(tr, 1, depth_cmp)
+    per_slot = 9 * tp.n_thresholds * tp.n_features * 4 + tp.n_thresholds * tp.n_features * 9 + 4 * tp.n_features * 5
+    pn = pg.TreeTrainer(cfg, device=device, hist_budget=max(1 << 20, per_slot))
+    pn.upload(ts)
+    timed_tree(pn, 91, 4)  # warm-up
+    p_tree, p_ms, p_st = timed_tree(pn, 1, depth_cmp)
+    same = all(np.array_equal(getattr(b_tree, f), getattr(p_tree, f)) for f in
+               ("left_child", "features", "thresholds")) and np.array_equal(
+        b_tree.posteriors.view(np.uint32), p_tree.posteriors.view(np.uint32))
+    out["per_node_launch"] = dict(depth=depth_cmp, batched_ms=b_ms, batched_hist_launches=b_st["hist_launches"],
+                                  per_node_ms=p_ms, per_node_hist_launches=p_st["hist_launches"],
+                                  per_node_kernel_launches=p_st["kernel_launches"],
+                                  speedup=p_ms / b_ms, identical_trees=bool(same))
+    del pn
+    return out
+
+
 def forest_accuracy(pg, cfg, trees, device, hx, hl):
     """Held-out per-pixel accuracy of a forest (argmax of the posterior against the labels):
     over all pixels, and over the object (non-background) pixels."""
@@ -886,6 +956,7 @@ def run_ours(a):
     learned = learned_bench(a, pg, cfg, ts, tp, local) if a.learned and world == 1 else None
     samp = sampler_bench(a, pg, N, px, lb) if a.sampler_images > 0 else None
     rgb = rgb_bench(a, pg, local) if a.rgb_images > 0 else None
+    mixed = mixed_bench(a, pg, local) if a.mixed and world == 1 else None
     if samp is not None:
         samp["label_images"] = loader_bench(a, pg, N)
 
@@ -947,14 +1018,18 @@ def run_ours(a):
                             parallelism=f"replicas x{world} (one tree per GPU per step)",
                             l2="inputs 1.23 GB > L2 (129 MB), no flush"),
                 roofline=roof, roofline_issue=issue_roof, roofline_atomic=atomic_roof, cpu_baseline=base,
-                gpu_on_cpu_sample=same, rgb_config=rgb, learned_proposals=learned, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
+                gpu_on_cpu_sample=same, rgb_config=rgb, learned_proposals=learned, mixed_sizes=mixed, e2e=e2e, gpu_launches=launches, clocks=clk.summary(),
                 predict=pred, sampler=samp, phases_per_step={k: v / a.steps for k, v in phases.items()}, impl="ours")
     print(json.dumps(line), flush=True)
 
 
 def main():
     a = args_()
-    if a.only == "learned":
+    if a.only == "mixed":
+        import padenti_gb300 as pg
+
+        print(json.dumps(mixed_bench(a, pg, 0)), flush=True)
+    elif a.only == "learned":
         import padenti_gb300 as pg
 
         pg_, cfg, ts, tp, _ = make_workload(a, 0)
