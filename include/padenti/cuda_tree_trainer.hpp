@@ -38,9 +38,13 @@ inline void check(int rc) {
 template <typename ImgType>
 constexpr int32_t img_type_code() {
   if constexpr (std::is_same_v<ImgType, unsigned char>) return PD_IMG_U8;
+  else if constexpr (std::is_same_v<ImgType, unsigned short>) return PD_IMG_U16;
+  else if constexpr (std::is_same_v<ImgType, short>) return PD_IMG_I16;
+  else if constexpr (std::is_same_v<ImgType, int>) return PD_IMG_I32;
   else {
-    static_assert(std::is_same_v<ImgType, unsigned short>, "padenti_gb300: ImgType must be unsigned char or unsigned short");
-    return PD_IMG_U16;
+    static_assert(std::is_same_v<ImgType, float>,
+                  "padenti_gb300: ImgType must be unsigned char, unsigned short, short, int or float");
+    return PD_IMG_F32;
   }
 }
 template <typename FeatType>
