@@ -70,7 +70,7 @@ def args_():
     a.add_argument("--fit-batch", type=int, default=4096)
     a.add_argument("--fit-lr", type=float, default=3e-3)
     a.add_argument("--only", default=None,
-                   choices=["sampler_uniform", "sampler_class_weighted", "labels", "learned", "mixed"],
+                   choices=["sampler_uniform", "sampler_class_weighted", "labels", "learned", "mixed", "fit"],
                    help="run one kernel family alone on --images synthetic images already in device memory "
                         "(--reps times) and print its times: the workload of the sampler and label profiles")
     a.add_argument("--reps", type=int, default=3)
@@ -505,6 +505,32 @@ def rgb_bench(a, pg, device: int):
                                    kind="port", sample=f"root histogram of the first {m} images ({ds.n_samples} "
                                    f"samples x 1000 candidates x 30 thresholds), reference-cost oracle; {dt:.1f} s")
     return out
+
+
+def fit_only(a):
+    """The proposal network's fit alone, on 18 000 seeded synthetic records of the depth
+    configuration's shape (9 classes, FeatDim 4), --fit-steps steps of --fit-batch records,
+    twice on one network (the second run replays the captured step): the workload of the
+    network's kernel profiles."""
+    import padenti_gb300 as pg
+
+    cfg = pg.ForestConfig("depth_diff2", 9)
+    tr = pg.TreeTrainer(cfg)
+    tp = pg.TreeTrainerParameters(300, a.thresholds, [-60000] * 4, [60000] * 4, -500, 500, a.min_leaf)
+    rng = np.random.default_rng(a.seed)
+    n = 18000
+    rec = np.zeros(n, pg.RECORD_DTYPE)
+    rec["depth"] = rng.integers(1, 16, n)
+    cc = rng.integers(0, 1000, (n, 9)).astype(np.uint32)
+    rec["class_count"][:, :9] = cc
+    rec["count"] = cc.sum(1)
+    rec["feat"][:, :4] = rng.integers(-60000, 60000, (n, 4))
+    rec["thr"] = rng.integers(-500, 500, n)
+    net = pg.ProposalNetwork(tr, tp, seed=a.seed)
+    r1 = net.fit(rec, steps=a.fit_steps, batch=a.fit_batch, lr=a.fit_lr)
+    r2 = net.fit(rec, steps=a.fit_steps, batch=a.fit_batch, lr=a.fit_lr)
+    return dict(steps=a.fit_steps, batch=a.fit_batch, ms_first=r1["ms"], ms=r2["ms"],
+                us_per_step=1000 * r2["ms"] / a.fit_steps, last_loss=float(r2["loss"][-1]))
 
 
 def mixed_bench(a, pg, device):
@@ -1025,7 +1051,9 @@ def run_ours(a):
 
 def main():
     a = args_()
-    if a.only == "mixed":
+    if a.only == "fit":
+        print(json.dumps(fit_only(a)), flush=True)
+    elif a.only == "mixed":
         import padenti_gb300 as pg
 
         print(json.dumps(mixed_bench(a, pg, 0)), flush=True)
