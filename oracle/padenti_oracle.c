@@ -172,6 +172,52 @@ int32_t or_feature(int32_t plugin, int32_t feat_type, const void *img, uint32_t 
   return 0;
 }
 
+/* The tree a feature that reads it sees: this image's node map (NULL: none),
+ * the tree's left children and posteriors, the class count, the map's level
+ * (root 0) and the tree's node count.  The feature reads the splits of nodes
+ * above the level (-1 at and below it) and the posteriors of nodes down to it
+ * (0 below): the part of the tree that is the same in training and prediction. */
+typedef struct {
+  const int32_t *nodes;
+  const int32_t *lc;
+  const float *post;
+  uint32_t K;
+  int32_t level, n_nodes;
+} tree_view;
+
+static inline int32_t node_level(int32_t n) {
+  int32_t l = 0;
+  for (uint32_t v = (uint32_t)n + 1u; v > 1u; v >>= 1) l++;
+  return l;
+}
+static inline int32_t view_left_child(const tree_view *tv, int32_t n) {
+  if (!tv || !tv->lc || n < 0 || n >= tv->n_nodes || node_level(n) >= tv->level) return -1;
+  return tv->lc[n];
+}
+static inline float view_posterior(const tree_view *tv, int32_t n, int32_t k) {
+  if (!tv || !tv->post || n < 0 || n >= tv->n_nodes || node_level(n) > tv->level || k < 0 || (uint32_t)k >= tv->K)
+    return 0.0f;
+  return tv->post[(size_t)n * tv->K + (uint32_t)k];
+}
+
+static int32_t feature_at(int32_t plugin, int32_t feat_type, const void *img, uint32_t w, uint32_t h,
+                          uint32_t n_channels, int32_t x, int32_t y, const int32_t *feat, const tree_view *tv) {
+  if (plugin != OR_PLUGIN_AUTO_CONTEXT) return or_feature(plugin, feat_type, img, w, h, n_channels, x, y, feat);
+  const uint16_t *im = (const uint16_t *)img;
+  const int32_t x1 = x + feat[0], y1 = y + feat[1];
+  int32_t n1 = 0;
+  if (tv && tv->nodes && x1 >= 0 && y1 >= 0 && (uint32_t)x1 < w && (uint32_t)y1 < h)
+    n1 = tv->nodes[(size_t)y1 * w + (size_t)x1];
+  const int32_t K = tv && tv->K ? (int32_t)tv->K : 1;
+  const int32_t k = ((feat[2] % K) + K) % K;
+  const float pv = view_posterior(tv, n1, k);
+  const int32_t inner = view_left_child(tv, n1) >= 0 ? 2000 : 0;
+  const int32_t x3 = x + feat[3];
+  const int32_t a = x3 >= 0 && (uint32_t)x3 < w ? (int32_t)im[(size_t)y * w + (size_t)x3] : 0;
+  const int32_t b = (int32_t)im[(size_t)y * w + (size_t)x];
+  return (int32_t)(pv * 1000.0f) + inner + (a - b) / 16 + n1 % 5;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Exact log2 of integers in double-double arithmetic (Dekker 1971 products,  */
 /* Knuth two-sum, Hida-Li-Bailey double-double add/mul/div), evaluated with   */
@@ -316,9 +362,42 @@ static int64_t find_slot(const node_slot_t *m, uint32_t n, int32_t node) {
   return -1;
 }
 
+/* Node maps of a training set for features that read the tree: map of image i
+ * from moff[i], the tree as the histograms of a depth see it. */
+typedef struct {
+  const int32_t *map;
+  const uint64_t *moff;
+  const int32_t *lc;
+  const float *post;
+  uint32_t K;
+  int32_t level, n_nodes;
+} set_view;
+
+static int hist_impl(const or_params *p, const or_dataset *ds, uint32_t tree_id, const int32_t *sample_node,
+                     const int32_t *nodes, uint32_t n_nodes, uint32_t *hist, int reference_cost, int n_threads,
+                     const set_view *sv);
+
 int or_hist(const or_params *p, const or_dataset *ds, uint32_t tree_id,
             const int32_t *sample_node, const int32_t *nodes, uint32_t n_nodes,
             uint32_t *hist, int reference_cost, int n_threads) {
+  return hist_impl(p, ds, tree_id, sample_node, nodes, n_nodes, hist, reference_cost, n_threads, NULL);
+}
+
+int or_hist_tree(const or_params *p, const or_dataset *ds, uint32_t tree_id, const int32_t *sample_node,
+                 const int32_t *nodes, uint32_t n_nodes, uint32_t *hist, const int32_t *maps, const int32_t *lc,
+                 const float *post, int32_t level, int32_t tree_nodes, int n_threads) {
+  uint64_t *moff = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)ds->n_images + 1));
+  moff[0] = 0;
+  for (uint32_t i = 0; i < ds->n_images; i++) moff[i + 1] = moff[i] + (uint64_t)ds->width[i] * ds->height[i];
+  set_view sv = {maps, moff, lc, post, (uint32_t)p->n_classes, level, tree_nodes};
+  const int rc = hist_impl(p, ds, tree_id, sample_node, nodes, n_nodes, hist, 0, n_threads, &sv);
+  free(moff);
+  return rc;
+}
+
+static int hist_impl(const or_params *p, const or_dataset *ds, uint32_t tree_id, const int32_t *sample_node,
+                     const int32_t *nodes, uint32_t n_nodes, uint32_t *hist, int reference_cost, int n_threads,
+                     const set_view *sv) {
   const uint32_t F = p->n_features, T = p->n_thresholds, K = (uint32_t)p->n_classes;
   const int D = p->feat_dim;
   uint64_t S;
@@ -384,8 +463,10 @@ int or_hist(const or_params *p, const or_dataset *ds, uint32_t tree_id,
           or_candidate(p, tree_id, (uint32_t)nodes[slot], f, feat, thr);
           fv = feat; tv = thr;
         }
-        int32_t r = or_feature(p->plugin, p->feat_type, image_ptr(ds, sm->img), ds->width[sm->img],
-                               ds->height[sm->img], ds->n_channels, sm->x, sm->y, fv);
+        tree_view view = {sv ? sv->map + sv->moff[sm->img] : NULL, sv ? sv->lc : NULL, sv ? sv->post : NULL,
+                          sv ? sv->K : 0, sv ? sv->level : 0, sv ? sv->n_nodes : 0};
+        int32_t r = feature_at(p->plugin, p->feat_type, image_ptr(ds, sm->img), ds->width[sm->img],
+                               ds->height[sm->img], ds->n_channels, sm->x, sm->y, fv, &view);
         uint32_t *lp = loc + (size_t)sm->label * T;
         for (uint32_t t = 0; t < T; t++) lp[t] += (uint32_t)(r <= tv[t]);
       }
@@ -593,8 +674,23 @@ static int train_tree_impl(const or_params *p, const or_dataset *ds, uint32_t tr
 
   int32_t *frontier = (int32_t *)malloc(sizeof(int32_t) * ((n_nodes + 1) / 2 + 1));
   uint8_t *split_now = (uint8_t *)calloc(n_nodes, 1);
+  /* a feature that reads the tree: every pixel's node (traverse_ts.hpp:140-244),
+   * starting at the root, and the tree as a depth's histograms see it */
+  const int actx = p->plugin == OR_PLUGIN_AUTO_CONTEXT;
+  uint64_t *moff = NULL;
+  int32_t *map = NULL, *map2 = NULL;
+  if (actx) {
+    moff = (uint64_t *)malloc(sizeof(uint64_t) * ((size_t)ds->n_images + 1));
+    moff[0] = 0;
+    for (uint32_t i = 0; i < ds->n_images; i++) moff[i + 1] = moff[i] + (uint64_t)ds->width[i] * ds->height[i];
+    map = (int32_t *)calloc(moff[ds->n_images] + 1, sizeof(int32_t));
+    map2 = (int32_t *)calloc(moff[ds->n_images] + 1, sizeof(int32_t));
+  }
+  set_view sv = {map, moff, lc, posts, K, 0, (int32_t)n_nodes};
   for (uint32_t depth = 1; depth < end_depth; depth++) {
     uint32_t nf = 0;
+    sv.map = map;
+    sv.level = (int32_t)depth - 1; /* the node map's level: the frontier's */
     if (depth == 1) {
       frontier[nf++] = 0;
       for (uint64_t s = 0; s < S; s++) class_tot[smp[s].label]++;
@@ -610,7 +706,7 @@ static int train_tree_impl(const or_params *p, const or_dataset *ds, uint32_t tr
       const int32_t *sl = frontier + s0;
       uint32_t *hist = (uint32_t *)malloc(sizeof(uint32_t) * per_node * ns);
       double t0 = now_s();
-      or_hist(p, ds, tree_id, snode, sl, ns, hist, reference_cost, n_threads);
+      hist_impl(p, ds, tree_id, snode, sl, ns, hist, reference_cost, n_threads, actx ? &sv : NULL);
       double t1 = now_s();
       uint32_t *ctot = (uint32_t *)malloc(sizeof(uint32_t) * K * ns);
       for (uint32_t i = 0; i < ns; i++) memcpy(ctot + (size_t)i * K, class_tot + (size_t)sl[i] * K, sizeof(uint32_t) * K);
@@ -643,6 +739,7 @@ static int train_tree_impl(const or_params *p, const or_dataset *ds, uint32_t tr
         if (xr != 0) {
           free(xcl); free(hist); free(ctot); free(bt); free(bf); free(bg);
           free(frontier); free(split_now); free(L); free(class_tot); free(node_tot); free(snode); free(smp);
+          free(moff); free(map); free(map2);
           return -2;
         }
       } else {
@@ -687,15 +784,42 @@ static int train_tree_impl(const or_params *p, const or_dataset *ds, uint32_t tr
       int32_t n = snode[s];
       if (!split_now[n]) continue;
       const sample_t *sm = &smp[s];
-      int32_t r = or_feature(p->plugin, p->feat_type, image_ptr(ds, sm->img), ds->width[sm->img],
-                             ds->height[sm->img], ds->n_channels, sm->x, sm->y, feats + (size_t)n * D);
+      tree_view tv = {actx ? map + moff[sm->img] : NULL, lc, posts, K, (int32_t)depth - 1, (int32_t)n_nodes};
+      int32_t r = feature_at(p->plugin, p->feat_type, image_ptr(ds, sm->img), ds->width[sm->img],
+                             ds->height[sm->img], ds->n_channels, sm->x, sm->y, feats + (size_t)n * D, &tv);
       snode[s] = lc[n] + (r <= thrs[n] ? 0 : 1);
     }
     for (uint32_t i = 0; i < nf; i++) split_now[frontier[i]] = 0;
+    if (actx && depth + 1 < end_depth) {
+      /* the next depth's node map: labelled pixels at split nodes move on
+       * (predict.cl:36-85 over the label image as mask) */
+#pragma omp parallel for schedule(dynamic, 1) NT(n_threads)
+      for (int64_t i = 0; i < (int64_t)ds->n_images; i++) {
+        const uint32_t w = ds->width[i], h = ds->height[i];
+        const int32_t *mi = map + moff[i];
+        int32_t *mo = map2 + moff[i];
+        const uint8_t *lab = ds->labels + ds->lab_off[i];
+        tree_view tv = {mi, lc, posts, K, (int32_t)depth - 1, (int32_t)n_nodes};
+        for (uint64_t q = 0; q < (uint64_t)w * h; q++) {
+          const int32_t n = mi[q], c = lab[q] ? lc[n] : -1;
+          if (c < 0) {
+            mo[q] = n;
+            continue;
+          }
+          int32_t r = feature_at(p->plugin, p->feat_type, image_ptr(ds, (uint32_t)i), w, h, ds->n_channels,
+                                 (int32_t)(q % w), (int32_t)(q / w), feats + (size_t)n * D, &tv);
+          mo[q] = c + (r <= thrs[n] ? 0 : 1);
+        }
+      }
+      int32_t *sw = map;
+      map = map2;
+      map2 = sw;
+    }
   }
   if (sample_leaf) memcpy(sample_leaf, snode, sizeof(int32_t) * S);
   if (stats) *stats = st;
   free(frontier); free(split_now); free(L); free(class_tot); free(node_tot); free(snode); free(smp);
+  free(moff); free(map); free(map2);
   return 0;
 }
 
@@ -716,6 +840,32 @@ static inline int32_t traverse(const or_params *p, const void *img, uint32_t w, 
   return node;
 }
 
+/* The node map of one tree over an image for a feature that reads the tree:
+ * all pixels at the root, then depth-1 synchronous steps of the pixels inside
+ * the mask (cl_classifier_impl.hpp:478-520, predict.cl:36-85); out[q] = the
+ * pixel's leaf (0 outside the mask). */
+static void tree_node_map(const or_params *p, const void *img, uint32_t w, uint32_t h, uint32_t nch,
+                          const uint8_t *mask, uint32_t depth, const int32_t *lc, const int32_t *feats,
+                          const int32_t *thrs, const float *posts, int32_t *out, int32_t *tmp, int n_threads) {
+  const size_t P = (size_t)w * h;
+  memset(out, 0, sizeof(int32_t) * P);
+  for (uint32_t d = 1; d < depth; d++) {
+    tree_view tv = {out, lc, posts, (uint32_t)p->n_classes, (int32_t)d - 1, (int32_t)((1u << depth) - 1u)};
+#pragma omp parallel for schedule(static) NT(n_threads)
+    for (int64_t q = 0; q < (int64_t)P; q++) {
+      const int32_t n = out[q], c = (mask && !mask[q]) ? -1 : lc[n];
+      if (c < 0) {
+        tmp[q] = n;
+        continue;
+      }
+      int32_t r = feature_at(p->plugin, p->feat_type, img, w, h, nch, (int32_t)(q % w), (int32_t)(q / w),
+                             feats + (size_t)n * p->feat_dim, &tv);
+      tmp[q] = c + (r <= thrs[n] ? 0 : 1);
+    }
+    memcpy(out, tmp, sizeof(int32_t) * P);
+  }
+}
+
 int or_predict_posterior(const or_params *p, const void *img, uint32_t w, uint32_t h,
                          uint32_t nch, const uint8_t *mask, uint32_t n_trees,
                          const uint32_t *depth, const uint64_t *node_off,
@@ -724,6 +874,22 @@ int or_predict_posterior(const or_params *p, const void *img, uint32_t w, uint32
   const uint32_t K = (uint32_t)p->n_classes;
   const size_t P = (size_t)w * h;
   memset(out, 0, sizeof(float) * P * K);
+  if (p->plugin == OR_PLUGIN_AUTO_CONTEXT) {
+    int32_t *m = (int32_t *)malloc(sizeof(int32_t) * (P + 1)), *tmp = (int32_t *)malloc(sizeof(int32_t) * (P + 1));
+    for (uint32_t t = 0; t < n_trees; t++) {
+      const uint64_t o = node_off[t];
+      tree_node_map(p, img, w, h, nch, mask, depth[t], lc + o, feats + o * p->feat_dim, thrs + o, posts + o * K, m,
+                    tmp, n_threads);
+      for (size_t q = 0; q < P; q++) {
+        if (mask && !mask[q]) continue;
+        for (uint32_t l = 0; l < K; l++) out[(size_t)l * P + q] += posts[(o + (uint64_t)m[q]) * K + l];
+      }
+    }
+    free(m);
+    free(tmp);
+    for (size_t i = 0; i < P * K; i++) out[i] /= (float)n_trees;
+    return 0;
+  }
 #pragma omp parallel for schedule(static) NT(n_threads)
   for (int64_t q = 0; q < (int64_t)P; q++) {
     if (mask && !mask[q]) continue;
@@ -743,10 +909,22 @@ int or_predict_leaf(const or_params *p, const void *img, uint32_t w, uint32_t h,
                     const int32_t *lc, const int32_t *feats, const int32_t *thrs,
                     int32_t *out, int n_threads) {
   const size_t P = (size_t)w * h;
+  if (p->plugin == OR_PLUGIN_AUTO_CONTEXT) return -1; /* needs the posteriors: or_predict_leaf_tree */
 #pragma omp parallel for schedule(static) NT(n_threads)
   for (int64_t q = 0; q < (int64_t)P; q++) {
     if (mask && !mask[q]) { out[q] = 0; continue; }
     out[q] = traverse(p, img, w, h, nch, (int32_t)(q % w), (int32_t)(q / w), depth, lc, feats, thrs);
   }
+  return 0;
+}
+
+int or_predict_leaf_tree(const or_params *p, const void *img, uint32_t w, uint32_t h, uint32_t nch,
+                         const uint8_t *mask, uint32_t depth, const int32_t *lc, const int32_t *feats,
+                         const int32_t *thrs, const float *posts, int32_t *out, int n_threads) {
+  if (p->plugin != OR_PLUGIN_AUTO_CONTEXT)
+    return or_predict_leaf(p, img, w, h, nch, mask, depth, lc, feats, thrs, out, n_threads);
+  int32_t *tmp = (int32_t *)malloc(sizeof(int32_t) * ((size_t)w * h + 1));
+  tree_node_map(p, img, w, h, nch, mask, depth, lc, feats, thrs, posts, out, tmp, n_threads);
+  free(tmp);
   return 0;
 }

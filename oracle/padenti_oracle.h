@@ -43,7 +43,18 @@ enum { OR_IMG_U8 = 1, OR_IMG_U16 = 2 };
 enum {
   OR_PLUGIN_DEPTH_DIFF2 = 1,   /* I(x+u/d) - I(x+v/d), int32, D=4 */
   OR_PLUGIN_DEPTH_DIFF1 = 2,   /* test/feature.cl: D(x) - D(x+round(u*500/D(x))), int16, D=2 */
-  OR_PLUGIN_CHANNEL_DIFF = 3   /* I_c1(x+u) - I_c2(x+v), RGB u8, int32, D=6 */
+  OR_PLUGIN_CHANNEL_DIFF = 3,  /* I_c1(x+u) - I_c2(x+v), RGB u8, int32, D=6 */
+  /* A feature that reads the tree (auto-context), for the tests of the plugin
+   * arguments treeLeftChildren / treePosteriors / imageNodesID
+   * (padenti.hpp.in:169-177); uint16 images, int32, D=4:
+   *   n1 = node map at (x+f0, y+f1) (0 outside), k = f2 mod K,
+   *   (int)(posterior(n1, k) * 1000) + (left_child(n1) >= 0 ? 2000 : 0)
+   *     + (I(x+f3, y) - I(x, y)) / 16 + n1 % 5      (I = 0 outside),
+   * with the tree seen from the node map's level L (root 0): left_child(n) is
+   * -1 for nodes at level >= L, posterior(n, k) 0 for nodes below L.  Trees
+   * and predictions of this plugin keep a per-pixel node map, advanced one
+   * level at a time over the labelled (training) or masked-in pixels. */
+  OR_PLUGIN_AUTO_CONTEXT = 16
 };
 
 #define OR_MAX_FEAT_DIM 8
@@ -92,7 +103,8 @@ void or_md5(const uint32_t in[4], uint32_t out[4]);
 void or_candidate(const or_params *p, uint32_t tree_id, uint32_t node, uint32_t f,
                   int32_t *feat_out /*[D]*/, int32_t *thr_out /*[T]*/);
 
-/* a4: built-in plugin response at pixel (x,y) of one image. */
+/* a4: built-in plugin response at pixel (x,y) of one image (a feature that
+ * reads the tree sees node 0, no posteriors and no children here). */
 int32_t or_feature(int32_t plugin, int32_t feat_type, const void *img, uint32_t w, uint32_t h,
                    uint32_t n_channels, int32_t x, int32_t y, const int32_t *feat);
 
@@ -105,6 +117,13 @@ void or_log2_table(uint32_t n, double *out);
 int or_hist(const or_params *p, const or_dataset *ds, uint32_t tree_id,
             const int32_t *sample_node, const int32_t *nodes, uint32_t n_nodes,
             uint32_t *hist, int reference_cost, int n_threads);
+
+/* or_hist for a feature that reads the tree: maps holds every image's node
+ * map (concatenated in image order, [H][W] each) at `level`, lc / post the
+ * tree (tree_nodes nodes). */
+int or_hist_tree(const or_params *p, const or_dataset *ds, uint32_t tree_id, const int32_t *sample_node,
+                 const int32_t *nodes, uint32_t n_nodes, uint32_t *hist, const int32_t *maps, const int32_t *lc,
+                 const float *post, int32_t level, int32_t tree_nodes, int n_threads);
 
 /* a7: exact best split per node.  out_t/out_f/out_gain receive the winner. */
 int or_split(const or_params *p, const uint32_t *hist, const uint32_t *class_tot,
@@ -152,6 +171,12 @@ int or_predict_leaf(const or_params *p, const void *img, uint32_t w, uint32_t h,
                     uint32_t n_channels, const uint8_t *mask, uint32_t depth,
                     const int32_t *left_child, const int32_t *features,
                     const int32_t *thresholds, int32_t *out, int n_threads);
+
+/* Leaf-ID prediction of one tree with its posteriors, for every plugin
+ * (a feature that reads the tree needs them; or_predict_leaf refuses it). */
+int or_predict_leaf_tree(const or_params *p, const void *img, uint32_t w, uint32_t h, uint32_t nch,
+                         const uint8_t *mask, uint32_t depth, const int32_t *lc, const int32_t *feats,
+                         const int32_t *thrs, const float *posts, int32_t *out, int n_threads);
 
 /* Pixel samplers (image_sampler.c): UniformImageSampler and
  * ClassWeightedImageSampler with their Boost randomness restated. */

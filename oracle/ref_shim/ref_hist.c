@@ -42,6 +42,16 @@ static struct {
   feat_t *tmp, *buf;
 } A;
 
+/* The tree the kernel passes to computeFeature (treeLeftChildren,
+ * treePosteriors): null unless set by ref_hist_tree. */
+static int *rh_lc;
+static float *rh_post;
+
+void ref_hist_tree(const int32_t *lc, const float *post) {
+  rh_lc = (int *)lc;
+  rh_post = (float *)post;
+}
+
 static int rh_done[RH_GROUP];
 static int rh_barriers[RH_GROUP];
 
@@ -97,8 +107,8 @@ int ref_per_image_hist(int img_type, uint n_channels, const void *pixels, uint w
   A.tree = tree;
   A.start_node = start_node;
   A.end_node = end_node;
-  A.lc = NULL;
-  A.post = NULL;
+  A.lc = rh_lc;
+  A.post = rh_post;
   A.tmp = tmp;
   A.buf = buf;
   cl_shim_lsize[0] = 1;

@@ -98,7 +98,9 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
                     &ctx->cand_feat, &ctx->cand_thr, &ctx->cand_perm, &ctx->cand_ord, &ctx->parent, &ctx->xlog2_tab, &ctx->split_par, &ctx->hist, &ctx->g32, &ctx->items, &ctx->hist_queue,
                     &ctx->zero_slots, &ctx->split_out, &ctx->split_cl, &ctx->recheck, &ctx->split_scratch, &ctx->fused_scratch, &ctx->t_lc,
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
-                    &ctx->f_post, &ctx->f_meta, &ctx->f_cand, &ctx->p_img, &ctx->p_mask, &ctx->p_out};
+                    &ctx->f_post, &ctx->f_meta, &ctx->f_cand, &ctx->p_img, &ctx->p_mask, &ctx->p_out,
+                    &ctx->nm_map[0], &ctx->nm_map[1], &ctx->nm_off, &ctx->nm_label, &ctx->np_map[0],
+                    &ctx->np_map[1], &ctx->np_desc};
   for (DevBuf *b : bufs) b->release();
   if (ctx->batch_graph) cudaGraphExecDestroy(ctx->batch_graph);
   ctx->b_img.release();
@@ -274,6 +276,23 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   }
   PD_TRY(build_sample_records(ctx, S));
   ctx->h_label.assign(lab, lab + S);
+  if (ctx->tree_feature) {
+    // the node map's layout and every pixel's label: the map advances on labelled pixels
+    // (cl_tree_trainer_impl_traverse_ts.hpp:215-232 passes the label image as the mask)
+    std::vector<uint64_t> moff(n + 1, 0);
+    for (uint32_t i = 0; i < n; i++) moff[i + 1] = moff[i] + (uint64_t)ds->width[i] * ds->height[i];
+    const uint64_t np = moff[n];
+    PD_TRY(ctx->nm_off.ensure((n + 1) * 8));
+    PD_TRY(ctx->nm_label.ensure(np));
+    PD_TRY(ctx->nm_map[0].ensure(np * 4));
+    PD_TRY(ctx->nm_map[1].ensure(np * 4));
+    PD_CUDA(h2d(ctx, ctx->nm_off.ptr, moff.data(), (n + 1) * 8));
+    for (uint32_t i = 0; i < n; i++)
+      PD_CUDA(h2d(ctx, ctx->nm_label.as<uint8_t>() + moff[i], ds->labels + ds->lab_off[i], moff[i + 1] - moff[i]));
+    ctx->nm_pixels = np;
+  } else {
+    ctx->nm_pixels = 0;
+  }
   PD_CUDA(cudaStreamSynchronize(st));
   ctx->pixels_bytes = bytes;
   ctx->n_images = n;

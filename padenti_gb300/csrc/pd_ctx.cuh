@@ -17,6 +17,7 @@ struct pd_ctx {
   pd_config cfg{};
   int device = 0;
   pd::RtcPlugin *rtc = nullptr;  // the compiled user feature plugin (PD_PLUGIN_USER)
+  bool tree_feature = false;     // its computeFeature reads the tree: the node map is kept
   cudaStream_t stream = nullptr;
   uint64_t hist_budget = 8ull << 30;
   uint32_t chunk = 16384;  // samples per histogram work item (at most 65535)
@@ -66,6 +67,14 @@ struct pd_ctx {
   pd::DevBuf items, zero_slots, hist_queue;
   pd::DevBuf split_out, split_cl, recheck, split_scratch, fused_scratch;
   pd::DevBuf t_lc, t_feat, t_thr, t_post;  // device copy of the tree being trained
+  // ---- node map of features that read the tree (tree_feature) ----
+  pd::DevBuf nm_map[2];   // int32 node per pixel of every training image, this depth's and the next
+  pd::DevBuf nm_off;      // uint64 [n_images + 1] first pixel of each image in the map
+  pd::DevBuf nm_label;    // uint8 label of every pixel (nonzero: the map advances there)
+  uint64_t nm_pixels = 0;
+  int nm_cur = 0;
+  int32_t nm_level = 0, nm_nodes = 0;  // the map's level (the depth being trained), the tree's node count
+  pd::DevBuf np_map[2], np_desc;  // prediction: the map of the images predicted, their descriptors
   pd_train_stats stats{};
 
   // ---- forest (CLClassifier) ----

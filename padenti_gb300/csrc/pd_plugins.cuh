@@ -26,6 +26,14 @@ struct ImageRef {
   const ImgT *data;        // interleaved [H][W][C]
   int32_t w, h;
   const uint32_t *magic;   // RoundDiv multipliers by depth (65536 entries)
+  // for features that read the tree (kUsesTree plugins): this image's per-pixel
+  // node map (null when none is kept), the tree being trained or evaluated, the
+  // map's level and the tree's node count
+  const int32_t *nodes = nullptr;
+  const int32_t *tree_lc = nullptr;
+  const float *tree_post = nullptr;
+  uint32_t n_classes = 0;
+  int32_t tree_level = 0, tree_nodes = 0;
 };
 
 template <typename T>
@@ -125,6 +133,7 @@ struct DepthDiff2 {
   static constexpr int kOrderDim = 0;  // feature dims (0, 1): the first probe offset
   static constexpr bool kTrainMapsZero = true;  // 0 and 10000 read alike everywhere
   static constexpr bool kRtcOnly = false;     // kernels compiled into the library
+  static constexpr bool kUsesTree = false;    // reads neither the tree nor a node map
   struct Prep {
     const uint16_t *im;
     uint32_t w, h;
@@ -206,6 +215,7 @@ struct DepthDiff1 {
   static constexpr int kOrderDim = 0;  // feature dims (0, 1): the probe offset
   static constexpr bool kTrainMapsZero = false;  // the centre depth is used as read
   static constexpr bool kRtcOnly = false;     // kernels compiled into the library
+  static constexpr bool kUsesTree = false;    // reads neither the tree nor a node map
   struct Prep {
     const uint16_t *im;
     uint32_t w, h;
@@ -283,6 +293,7 @@ struct ChannelDiff {
   static constexpr int kOrderDim = 2;  // feature dims (2, 3): the first probe offset
   static constexpr bool kTrainMapsZero = false;
   static constexpr bool kRtcOnly = false;     // kernels compiled into the library
+  static constexpr bool kUsesTree = false;    // reads neither the tree nor a node map
   struct Prep {
     const uint8_t *im;
     uint32_t w, h;
@@ -355,6 +366,7 @@ struct UserHost {
   static constexpr int kId = PD_PLUGIN_USER;
   static constexpr bool kTrainMapsZero = false;
   static constexpr bool kRtcOnly = true;
+  static constexpr bool kUsesTree = false;  // known at run time: pd_ctx::tree_feature
   struct __align__(16) Cand {
     FeatT f[D];
   };

@@ -4,7 +4,9 @@
 // sums on the host (cl_classifier_impl.hpp:478-552).  Here one kernel walks the
 // whole forest per pixel, keeps the leaf ids of all trees, sums the leaf
 // posteriors in tree order and divides by the tree count, writing the planar
-// posterior once, coalesced.
+// posterior once, coalesced.  A user feature that reads the tree and the node
+// map (auto-context) needs every pixel's node of the level before it, so its
+// prediction keeps the reference's level-synchronous steps (node_map_predict).
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -113,6 +115,103 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
   return PD_OK;
 }
 
+// The forest posterior of features that read the tree, one tree at a time
+// (computePosterior, kernels/predict.cl:88-117): each pixel adds its node's
+// posterior to the planes in tree order and the last tree divides by the tree
+// count -- the sums and the division of k_predict_posterior; masked-out pixels 0.
+static __global__ void __launch_bounds__(256) k_node_map_posterior(const int32_t *__restrict__ map,
+                                                                   const uint8_t *__restrict__ masks,
+                                                                   const float *__restrict__ post, uint32_t K,
+                                                                   float *__restrict__ out, uint64_t plane,
+                                                                   uint64_t n_pix, int first, int last, float nt) {
+  const uint64_t q = (uint64_t)blockIdx.x * 256u + threadIdx.x;
+  if (q >= n_pix) return;
+  float *o = out + (q / plane) * K * plane + q % plane;
+  if (masks && !masks[q]) {
+    if (first)
+      for (uint32_t l = 0; l < K; l++) o[l * plane] = 0.0f;
+    return;
+  }
+  const float *pn = post + (size_t)map[q] * K;
+  for (uint32_t l = 0; l < K; l++) {
+    float acc = (first ? 0.0f : o[l * plane]) + pn[l];
+    if (last) acc = fdiv(acc, nt);
+    o[l * plane] = acc;
+  }
+}
+
+// Prediction of n same-size images (device buffers) for a feature that reads
+// the tree: per tree, the node map from the root (all pixels at node 0) through
+// depth - 1 synchronous steps (cl_classifier_impl.hpp:478-520), then either the
+// posterior accumulation (leaf_tree < 0) or the map itself as the leaf ids of
+// tree leaf_tree.
+static int node_map_predict(pd_ctx *ctx, uint32_t n, const void *images, uint32_t W, uint32_t H, const uint8_t *masks,
+                            float *post_out, int64_t leaf_tree, int32_t *leaf_out) {
+  PD_CHECK(W < 65536 && H < 65536, PD_ERR_UNSUPPORTED, "image %ux%u: a feature that reads the tree needs sides < 65536",
+           W, H);
+  const RtcKernels *rk = nullptr;
+  PD_TRY(rtc_kernels(ctx, &rk));
+  const uint64_t P_ = (uint64_t)W * H, NP = P_ * n;
+  const uint64_t img_bytes = P_ * ctx->cfg.n_channels * img_size(ctx->cfg.img_type);
+  const uint32_t K = (uint32_t)ctx->cfg.n_classes, D = (uint32_t)ctx->cfg.feat_dim;
+  const size_t fs = feat_size(ctx->cfg.feat_type);
+  cudaStream_t st = ctx->stream;
+  PD_TRY(ctx->np_map[0].ensure(NP * 4));
+  PD_TRY(ctx->np_map[1].ensure(NP * 4));
+  // descriptors: map offsets [n + 1], image byte offsets [n], sizes [n]
+  std::vector<uint64_t> desc(2 * (size_t)n + 1 + ((size_t)n + 1) / 2, 0);
+  uint32_t *wh = reinterpret_cast<uint32_t *>(desc.data() + 2 * (size_t)n + 1);
+  for (uint32_t z = 0; z <= n; z++) desc[z] = (uint64_t)z * P_;
+  for (uint32_t z = 0; z < n; z++) {
+    desc[n + 1 + z] = (uint64_t)z * img_bytes;
+    wh[z] = W | (H << 16);
+  }
+  PD_TRY(ctx->np_desc.ensure(desc.size() * 8));
+  PD_CUDA(h2d(ctx, ctx->np_desc.ptr, desc.data(), desc.size() * 8));
+  const uint64_t *dd = ctx->np_desc.as<uint64_t>();
+  const uint32_t nt = (uint32_t)ctx->tree_depth.size();
+  const uint32_t t0 = leaf_tree < 0 ? 0u : (uint32_t)leaf_tree, t1 = leaf_tree < 0 ? nt : t0 + 1;
+  const dim3 grid((unsigned)((NP + 255) / 256));
+  for (uint32_t t = t0; t < t1; t++) {
+    const uint64_t off = ctx->tree_off[t];
+    int cur = 0;
+    PD_CUDA(cudaMemsetAsync(ctx->np_map[0].ptr, 0, NP * 4, st));
+    for (uint32_t d = 1; d < ctx->tree_depth[t]; d++) {
+      NodeMapStep a;
+      a.pixels = static_cast<const uint8_t *>(images);
+      a.img_off = dd + n + 1;
+      a.img_wh = reinterpret_cast<const uint32_t *>(dd + 2 * (size_t)n + 1);
+      a.map_off = dd;
+      a.n_images = n;
+      a.n_pix = NP;
+      a.mask = masks;
+      a.map_in = ctx->np_map[cur].as<int32_t>();
+      a.map_out = ctx->np_map[1 - cur].as<int32_t>();
+      a.lc = ctx->f_lc.as<int32_t>() + off;
+      a.feat = ctx->f_feat.as<uint8_t>() + off * D * fs;
+      a.thr = ctx->f_thr.as<uint8_t>() + off * fs;
+      a.post = ctx->f_post.as<float>() + off * K;
+      a.n_classes = K;
+      a.level = (int32_t)d - 1;
+      a.n_nodes = (int32_t)((1u << ctx->tree_depth[t]) - 1u);
+      a.magic = ctx->magic_tab.as<uint32_t>();
+      void *args[] = {&a};
+      PD_TRY(rtc_launch(ctx, rk->node_map_step, grid, dim3(256), 0, args));
+      cur = 1 - cur;
+    }
+    if (leaf_tree >= 0) {
+      PD_CUDA(cudaMemcpyAsync(leaf_out, ctx->np_map[cur].ptr, NP * 4, cudaMemcpyDeviceToDevice, st));
+    } else {
+      k_node_map_posterior<<<grid, 256, 0, st>>>(ctx->np_map[cur].as<int32_t>(), masks,
+                                                 ctx->f_post.as<float>() + off * K, K, post_out, P_, NP, t == 0,
+                                                 t + 1 == nt, (float)nt);
+      PD_CUDA(cudaGetLastError());
+      ctx->launches++;
+    }
+  }
+  return PD_OK;
+}
+
 }  // namespace pd
 
 using namespace pd;
@@ -166,6 +265,8 @@ extern "C" int pd_predict_posterior_device(pd_ctx *ctx, uint32_t n_images, const
   PD_CHECK(width >= 1 && height >= 1 && n_images >= 1 && n_images <= 65535, PD_ERR_INVALID, "bad image batch");
   PD_CUDA(cudaSetDevice(ctx->device));
   PD_TRY(upload_forest(ctx));
+  if (ctx->tree_feature)
+    return node_map_predict(ctx, n_images, images_device, width, height, masks_device, out_device, -1, nullptr);
   return dispatch_config(ctx->cfg, [&]<class P>() {
     return launch_posterior<P>(ctx, n_images, images_device, width, height, masks_device, out_device);
   });
@@ -204,6 +305,14 @@ extern "C" int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *c
   PD_CHECK(n >= 1, PD_ERR_INVALID, "empty batch");
   PD_CHECK(!ctx->tree_depth.empty(), PD_ERR_STATE, "empty forest");
   PD_CUDA(cudaSetDevice(ctx->device));
+  if (ctx->tree_feature) {
+    // a feature that reads the tree: the node-map steps of each image in turn
+    for (uint32_t i = 0; i < n; i++) {
+      PD_CHECK(images[i] && outs[i], PD_ERR_INVALID, "batch image %u: null buffer", i);
+      PD_TRY(pd_predict_posterior(ctx, images[i], widths[i], heights[i], masks ? masks[i] : nullptr, outs[i]));
+    }
+    return PD_OK;
+  }
   PD_TRY(upload_forest(ctx));
   const uint32_t K = (uint32_t)ctx->cfg.n_classes, nt = (uint32_t)ctx->tree_depth.size();
   const size_t px = (size_t)ctx->cfg.n_channels * img_size(ctx->cfg.img_type);
@@ -316,6 +425,13 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
   if (mask) PD_CUDA(h2d(ctx, ctx->p_mask.ptr, mask, P_));
   const size_t off = ctx->tree_off[tree];
   const uint32_t depth = ctx->tree_depth[tree];
+  if (ctx->tree_feature) {
+    PD_TRY(node_map_predict(ctx, 1, ctx->p_img.ptr, width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr, nullptr,
+                            tree, ctx->p_out.as<int32_t>()));
+    PD_CUDA(d2h(ctx, out, ctx->p_out.ptr, P_ * 4));
+    PD_CUDA(cudaStreamSynchronize(st));
+    return PD_OK;
+  }
   PD_TRY(dispatch_config(ctx->cfg, [&]<class P>() {
     using FeatT = typename P::feat_t;
     dim3 grid((width + kPredX - 1) / kPredX, (height + kPredY - 1) / kPredY, 1);

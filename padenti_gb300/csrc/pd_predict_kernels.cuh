@@ -203,4 +203,70 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__
   out[pix] = walk<P>(P::prepare(im, (int32_t)x, (int32_t)y), lc, cand, thr, depth);
 }
 
+// One step of the per-pixel node map of features that read the tree
+// (kernels/predict.cl:36-85, launched once per level by
+// cl_tree_trainer_impl_traverse_ts.hpp:215-232 and cl_classifier_impl.hpp:478-520):
+// a pixel inside the mask whose node has children moves to the child its
+// feature selects -- the feature reading the map before the step and the tree
+// as seen from that map's level -- and every other pixel keeps its node.  Pixel q of the concatenated images
+// (image i starts at map_off[i]; n_images + 1 offsets).
+struct NodeMapStep {
+  const uint8_t *pixels;
+  const uint64_t *img_off;   // byte offset of each image
+  const uint32_t *img_wh;    // w | h << 16
+  const uint64_t *map_off;
+  uint32_t n_images;
+  uint64_t n_pix;
+  const uint8_t *mask;       // per pixel (nonzero: inside); null: every pixel
+  const int32_t *map_in;
+  int32_t *map_out;
+  const int32_t *lc;
+  const void *feat, *thr;    // feat_t [node][D], [node]
+  const float *post;
+  uint32_t n_classes;
+  int32_t level, n_nodes;    // the level of map_in (root 0), the tree's node count
+  const uint32_t *magic;
+};
+
+template <class P>
+__global__ void __launch_bounds__(256) k_node_map_step(NodeMapStep a) {
+  using FeatT = typename P::feat_t;
+  using ImgT = typename P::img_t;
+  constexpr int D = P::kFeatDim;
+  const uint64_t q = (uint64_t)blockIdx.x * 256u + threadIdx.x;
+  if (q >= a.n_pix) return;
+  const int32_t n = a.map_in[q];
+  int32_t out = n;
+  const int32_t c = (a.mask && !a.mask[q]) ? -1 : a.lc[n];
+  if (c >= 0) {
+    uint32_t lo = 0, hi = a.n_images;  // the last image starting at or before q
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (a.map_off[mid] <= q) lo = mid;
+      else hi = mid;
+    }
+    const uint32_t wh = a.img_wh[lo], w = wh & 0xffffu;
+    const uint64_t pix = q - a.map_off[lo];
+    ImageRef<ImgT> im;
+    im.data = reinterpret_cast<const ImgT *>(a.pixels + a.img_off[lo]);
+    im.w = (int32_t)w;
+    im.h = (int32_t)(wh >> 16);
+    im.magic = a.magic;
+    im.nodes = a.map_in + a.map_off[lo];
+    im.tree_lc = a.lc;
+    im.tree_post = a.post;
+    im.n_classes = a.n_classes;
+    im.tree_level = a.level;
+    im.tree_nodes = a.n_nodes;
+    const FeatT *fp = static_cast<const FeatT *>(a.feat) + (size_t)n * D;
+    FeatT fv[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) fv[d] = fp[d];
+    const auto prep = P::prepare(im, (int32_t)(pix % w), (int32_t)(pix / w));
+    const FeatT resp = P::eval(prep, fv);
+    out = c + (resp > static_cast<const FeatT *>(a.thr)[n] ? 1 : 0);
+  }
+  a.map_out[q] = out;
+}
+
 }  // namespace pd

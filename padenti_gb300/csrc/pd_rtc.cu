@@ -209,7 +209,9 @@ extern "C" int pd_plugin_check(const pd_config *cfg, const char *source, char *l
   PD_CHECK(cfg->plugin == PD_PLUGIN_USER, PD_ERR_INVALID, "the configuration's plugin is not PD_PLUGIN_USER");
   std::string lg;
   const int rc = compile_unit(*cfg, source, "sm_103a",
-                              {"pd::k_reassign<pd::UserPlugin>", "pd::k_predict_leaf<pd::UserPlugin>"}, nullptr,
+                              {"pd::k_reassign<pd::UserPlugin>", "pd::k_predict_leaf<pd::UserPlugin>",
+                               "pd::k_node_map_step<pd::UserPlugin>", "pd::k_hist<pd::UserPlugin, 16, 8>"},
+                              nullptr,
                               nullptr, &lg);
   if (log && log_size) {
     const size_t n = std::min(log_size - 1, lg.size());
@@ -230,13 +232,24 @@ extern "C" int pd_plugin_compile(pd_ctx *ctx, const char *source) {
   const std::vector<std::string> exprs = {
       "pd::k_reassign<pd::UserPlugin>", "pd::k_build_rec<pd::UserPlugin>", "pd::k_cand_order<pd::UserPlugin>",
       "pd::k_predict_posterior<pd::UserPlugin>", "pd::k_predict_leaf<pd::UserPlugin>",
-      "pd::k_predict_batch<pd::UserPlugin>", "pd::k_forest_cands<pd::UserPlugin>"};
+      "pd::k_predict_batch<pd::UserPlugin>", "pd::k_forest_cands<pd::UserPlugin>",
+      "pd::k_node_map_step<pd::UserPlugin>"};
   std::string cubin;
   std::vector<std::string> low;
   int rc = compile_unit(ctx->cfg, p->source, p->arch, exprs, &cubin, &low, nullptr);
   cudaLibrary_t lib = nullptr;
   std::vector<cudaKernel_t> ks;
   if (rc == PD_OK) rc = load_kernels(cubin, low, &lib, &ks);
+  int reads_tree = 0;
+  if (rc == PD_OK) {
+    // the form of the user's computeFeature, as the compiler saw it
+    void *flag = nullptr;
+    size_t bytes = 0;
+    cudaError_t e = cudaLibraryGetGlobal(&flag, &bytes, lib, "pd_user_reads_tree");
+    if (e == cudaSuccess && bytes == sizeof(int)) e = cudaMemcpy(&reads_tree, flag, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess || bytes != sizeof(int))
+      rc = set_error(PD_ERR_CUDA, "reading the plugin's form flag: %s", cudaGetErrorString(e));
+  }
   if (rc != PD_OK) {
     if (lib) cudaLibraryUnload(lib);
     delete p;
@@ -250,8 +263,10 @@ extern "C" int pd_plugin_compile(pd_ctx *ctx, const char *source) {
   p->base.predict_leaf = ks[4];
   p->base.predict_batch = ks[5];
   p->base.forest_cands = ks[6];
+  p->base.node_map_step = ks[7];
   rtc_release(ctx);  // a previous plugin of this context
   ctx->rtc = p;
+  ctx->tree_feature = reads_tree != 0;
   ctx->have_dataset = false;  // the sample records depend on the plugin: upload again
   return PD_OK;
 }

@@ -13,6 +13,7 @@ struct RtcKernels {
   cudaKernel_t reassign = nullptr, build_rec = nullptr, cand_order = nullptr;
   cudaKernel_t predict_posterior = nullptr, predict_leaf = nullptr, predict_batch = nullptr;
   cudaKernel_t forest_cands = nullptr;
+  cudaKernel_t node_map_step = nullptr;  // k_node_map_step (features that read the tree)
 };
 
 // The compiled base kernels; PD_ERR_STATE when pd_plugin_compile has not run.

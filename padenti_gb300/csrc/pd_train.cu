@@ -12,6 +12,7 @@
 #include "pd_ctx.cuh"
 #include "pd_hist_grid.cuh"
 #include "pd_rtc.cuh"
+#include "pd_predict_kernels.cuh"
 #include "pd_train_kernels.cuh"
 
 namespace pd {
@@ -43,6 +44,14 @@ static DevSet devset(const pd_ctx *ctx) {
   d.s_xy = ctx->s_xy.as<uint32_t>();
   d.s_img = ctx->s_img.as<uint32_t>();
   d.s_label = ctx->s_label.as<uint8_t>();
+  const bool tf = ctx->tree_feature && ctx->nm_pixels;
+  d.nodes = tf ? ctx->nm_map[ctx->nm_cur].as<int32_t>() : nullptr;
+  d.map_off = tf ? ctx->nm_off.as<uint64_t>() : nullptr;
+  d.tree_lc = ctx->t_lc.as<int32_t>();
+  d.tree_post = ctx->t_post.as<float>();
+  d.n_classes = (uint32_t)ctx->cfg.n_classes;
+  d.tree_level = ctx->nm_level;
+  d.tree_nodes = ctx->nm_nodes;
   return d;
 }
 
@@ -445,6 +454,33 @@ static int64_t gain_key_host(double g) {
 // network (learned proposals); with ctx->collect_records, one pd_record per
 // split node is kept; with `shard`, this rank's candidates are a range of the
 // node's and each slice's winners are exchanged with the other ranks.
+// One level of the training images' node map (k_node_map_step over every
+// pixel, labelled pixels advancing) with the device tree being trained.
+static int launch_node_map_step(pd_ctx *ctx, const int32_t *in, int32_t *out) {
+  const RtcKernels *rk = nullptr;
+  PD_TRY(rtc_kernels(ctx, &rk));
+  NodeMapStep a;
+  a.pixels = ctx->pixels.as<uint8_t>();
+  a.img_off = ctx->img_off.as<uint64_t>();
+  a.img_wh = ctx->img_wh.as<uint32_t>();
+  a.map_off = ctx->nm_off.as<uint64_t>();
+  a.n_images = ctx->n_images;
+  a.n_pix = ctx->nm_pixels;
+  a.mask = ctx->nm_label.as<uint8_t>();
+  a.map_in = in;
+  a.map_out = out;
+  a.lc = ctx->t_lc.as<int32_t>();
+  a.feat = ctx->t_feat.ptr;
+  a.thr = ctx->t_thr.ptr;
+  a.post = ctx->t_post.as<float>();
+  a.n_classes = (uint32_t)ctx->cfg.n_classes;
+  a.level = ctx->nm_level;
+  a.n_nodes = ctx->nm_nodes;
+  a.magic = ctx->magic_tab.as<uint32_t>();
+  void *args[] = {&a};
+  return rtc_launch(ctx, rk->node_map_step, dim3((unsigned)((a.n_pix + 255) / 256)), dim3(256), 0, args);
+}
+
 template <class P>
 static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_id, uint32_t end_depth,
                            const float *root_prior, int32_t *lc, typename P::feat_t *feats,
@@ -485,6 +521,13 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
   PD_TRY(ctx->scan_blocks.ensure((S / kScanItems + 2) * 8 + 16));
   PD_TRY(ctx->scatter_err.ensure(16));
   PD_CUDA(cudaMemsetAsync(ctx->snode.ptr, 0, S * 4, st));
+  if (ctx->tree_feature) {
+    // every pixel starts at the root (traverse_ts.hpp:146-163 fills the node image with 0)
+    PD_CHECK(ctx->nm_pixels, PD_ERR_STATE, "the training set was uploaded before the plugin was compiled");
+    ctx->nm_cur = 0;
+    ctx->nm_nodes = (int32_t)n_nodes;
+    PD_CUDA(cudaMemsetAsync(ctx->nm_map[0].ptr, 0, ctx->nm_pixels * 4, st));
+  }
   if (S) {
     k_iota<<<(unsigned)((S + 255) / 256), 256, 0, st>>>(ctx->act[0].as<uint32_t>(), ctx->act_slot[0].as<uint32_t>(), (uint32_t)S);
     k_gather_rec<<<(unsigned)((S + 255) / 256), 256, 0, st>>>(ctx->act[0].as<uint32_t>(), (uint32_t)S,
@@ -515,6 +558,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
     if (depth == 1) {
       for (uint64_t s = 0; s < S; s++) class_tot[ctx->h_label[s]]++;
     }
+    ctx->nm_level = (int32_t)depth - 1;  // the node map's level: the frontier's
     const uint32_t nf = (uint32_t)frontier.size();
     if (nf == 0) break;
     for (uint32_t i = 0; i < nf; i++) stats.evals += (uint64_t)node_tot[frontier[i]] * F;
@@ -723,6 +767,12 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
         ctx->launches++;
       }
     }
+    if (ctx->tree_feature && !next.empty()) {
+      // the node map of the next depth, from this depth's map and the tree as it now stands
+      PD_TRY(launch_node_map_step(ctx, ctx->nm_map[ctx->nm_cur].as<int32_t>(),
+                                  ctx->nm_map[1 - ctx->nm_cur].as<int32_t>()));
+      ctx->nm_cur = 1 - ctx->nm_cur;
+    }
     const uint64_t n_next = next_off.back();
     if (!next.empty() && n_act) {
       const uint32_t nb = (uint32_t)((n_act + kScanItems - 1) / kScanItems);
@@ -892,6 +942,8 @@ extern "C" int pd_hist(pd_ctx *ctx, const pd_train_params *params, uint32_t tree
                        const int32_t *nodes, uint32_t n_nodes, uint32_t *hist_out) {
   PD_CHECK(ctx && sample_node && nodes && hist_out, PD_ERR_INVALID, "null argument");
   PD_CHECK(ctx->have_dataset, PD_ERR_STATE, "no dataset uploaded");
+  PD_CHECK(!ctx->tree_feature, PD_ERR_UNSUPPORTED,
+           "the feature reads the tree and the node map, which only pd_train_tree keeps: no stage call");
   PD_TRY(check_params(ctx, params));
   PD_CUDA(cudaSetDevice(ctx->device));
   const uint64_t S = ctx->n_samples;

@@ -68,7 +68,30 @@ struct DevSet {
   const uint32_t *s_xy;
   const uint32_t *s_img;
   const uint8_t *s_label;
+  // for features that read the tree (P::kUsesTree): the node map of the depth
+  // being trained (int32 per pixel, image i from map_off[i]; null when none is
+  // kept), the device tree, its class count, the map's level (the depth being
+  // trained, root 0) and the tree's node count
+  const int32_t *nodes;
+  const uint64_t *map_off;
+  const int32_t *tree_lc;
+  const float *tree_post;
+  uint32_t n_classes;
+  int32_t tree_level, tree_nodes;
 };
+
+// The tree-reading fields of an image reference (a no-op for other plugins).
+template <class P, class ImgT>
+PD_D void attach_tree(ImageRef<ImgT> &im, const DevSet &ds, uint64_t map_off) {
+  if constexpr (P::kUsesTree) {
+    im.nodes = ds.nodes ? ds.nodes + map_off : nullptr;
+    im.tree_lc = ds.tree_lc;
+    im.tree_post = ds.tree_post;
+    im.n_classes = ds.n_classes;
+    im.tree_level = ds.tree_level;
+    im.tree_nodes = ds.tree_nodes;
+  }
+}
 
 // What the kernels need of a sample, in one 16-byte word: its position, image
 // and class, and the plugin's preload words of its pixel (static per sample).
@@ -401,7 +424,7 @@ PD_D void hist_samples(const DevSet &ds, const SampleRec *__restrict__ rec, cons
     const uint32_t n_here = min(32u, w.end - base);
     // lane-parallel preload of 32 samples: position, class, image, pixel words
     uint32_t my_xy = 0, my_wh = 0, my_row = 0, my_pre[PW];
-    uint64_t my_off = 0;
+    uint64_t my_off = 0, my_moff = 0;
 #pragma unroll
     for (int k = 0; k < PW; k++) my_pre[k] = 0u;
     if ((uint32_t)lane < n_here) {
@@ -413,6 +436,7 @@ PD_D void hist_samples(const DevSet &ds, const SampleRec *__restrict__ rec, cons
       if (PW > 1) my_pre[PW - 1] = r.w;
       my_off = ds.img_off[imi];
       my_wh = ds.img_wh[imi];
+      if constexpr (P::kUsesTree) my_moff = ds.map_off ? ds.map_off[imi] : 0ull;
     }
     auto eval_at = [&](uint32_t i) -> Eval {
       const uint32_t xy = __shfl_sync(full, my_xy, i);
@@ -426,6 +450,7 @@ PD_D void hist_samples(const DevSet &ds, const SampleRec *__restrict__ rec, cons
       im.w = (int32_t)(wh & 0xffffu);
       im.h = (int32_t)(wh >> 16);
       im.magic = ds.magic;
+      if constexpr (P::kUsesTree) attach_tree<P>(im, ds, __shfl_sync(full, my_moff, i));
       const auto prep = P::prepare(im, (int32_t)(xy & 0xffffu), (int32_t)(xy >> 16), pre);
       Eval e;
       e.ra = P::template eval_train<FAST>(prep, ca);
@@ -1205,6 +1230,7 @@ __global__ void k_reassign(DevSet ds, const uint32_t *__restrict__ act, const Sa
     im.w = (int32_t)(wh & 0xffffu);
     im.h = (int32_t)(wh >> 16);
     im.magic = ds.magic;
+    if constexpr (P::kUsesTree) attach_tree<P>(im, ds, ds.map_off ? ds.map_off[im_i] : 0ull);
     FeatT fv[D];
 #pragma unroll
     for (int d = 0; d < D; d++) fv[d] = feat[(size_t)n * D + d];

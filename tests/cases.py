@@ -40,6 +40,34 @@ def rgb_case(n_images=8, width=80, height=60, n_features=40, n_thresholds=12, se
     return cfg, ts, tp, (px, lb, sm)
 
 
+# A feature that reads the tree (auto-context): the oracle's OR_PLUGIN_AUTO_CONTEXT
+# (and oracle/ref_shim/cl/actx/feature.cl) written as a user feature.
+AUTO_CONTEXT_SOURCE = r"""
+__device__ feat_t computeFeature(const pd::ImageView &img, int2 c, const pd::TreeView &tree, const feat_t *f,
+                                 unsigned featDim) {
+  const int n1 = img.nodeID(c.x + f[0], c.y + f[1]);
+  const int K = (int)tree.nClasses;
+  const int k = ((f[2] % K) + K) % K;
+  const float pv = tree.posterior(n1, k);
+  const int inner = tree.leftChild(n1) >= 0 ? 2000 : 0;
+  const int a = img.read(c.x + f[3], c.y, 0), b = img.read(c.x, c.y, 0);
+  return (int)__fmul_rn(pv, 1000.0f) + inner + (a - b) / 16 + n1 % 5;
+}
+"""
+
+
+def actx_case(n_images=6, width=64, height=48, n_features=64, n_thresholds=8, seed=11, samples=300, min_leaf=10):
+    """Depth maps (3 classes) with the auto-context feature: offsets +-12 px, class selector
+    in [0, 3], thresholds over [-400, 3400] (the posterior term spans 0..1000, the
+    children term 0 or 2000)."""
+    px, lb, sm = pg.synth_depth(seed, n_images, width, height, samples_per_image=samples)
+    cfg = pg.ForestConfig("user", 3, source=AUTO_CONTEXT_SOURCE, shape="u16x1_i32x4")
+    ts = pg.training_set(3, px, lb, sm)
+    tp = pg.TreeTrainerParameters(n_features, n_thresholds, [-12, -12, 0, -12], [12, 12, 3, 12], -400, 3400,
+                                  min_leaf)
+    return cfg, ts, tp, (px, lb, sm)
+
+
 def tree_tuple(tree):
     return (tree.depth, tree.left_child, np.asarray(tree.features, np.int32), np.asarray(tree.thresholds, np.int32),
             tree.posteriors)

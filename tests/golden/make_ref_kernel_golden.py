@@ -9,7 +9,8 @@ them.
     make -C oracle ref REF=<Padenti source tree> && python tests/golden/make_ref_kernel_golden.py
 
 Per workload (the reference's test/feature.cl, the depth-difference feature,
-the RGB channel-difference feature): an oracle-trained tree (tree 3, depth 5)
+the RGB channel-difference feature, and a feature that reads the tree and the
+node map, oracle/ref_shim/cl/actx/feature.cl): an oracle-trained tree (tree 3, depth 5)
 that tests/test_reference_kernels.py checks depth by depth against the
 reference kernels; for every depth, the frontier, each sample's node given by
 the reference's traversal kernel and the sha256 of the frontier's histograms
@@ -49,8 +50,9 @@ def masks_of(im):
 def compute(plugin: str) -> dict:
     rk = ob.ref_kernels(plugin)
     assert rk is not None, "build the reference kernels first (make -C oracle ref REF=...)"
-    cfg, ts, tp, (px, lb, sm) = rkt.CASES[plugin]()
-    p = ob.params(cfg, tp)
+    actx = plugin == "auto_context"
+    cfg, ts, tp, (px, lb, sm) = rkt._actx() if actx else rkt.CASES[plugin]()
+    p = ob.params(cfg, tp, plugin)
     ds = ob.OracleSet(ts, cfg)
     K, T, F = cfg.n_classes, tp.n_thresholds, tp.n_features
     out = {"inputs_sha256": sha(np.concatenate([px.reshape(-1).view(np.uint8), lb.reshape(-1),
@@ -85,7 +87,8 @@ def compute(plugin: str) -> dict:
         idx = {int(n): i for i, n in enumerate(frontier)}
         href = np.zeros((len(frontier), K, T, F), np.uint32)
         for i, (im, m) in enumerate(zip(ts.images, maps)):
-            ind = rkt._ref_indicators(rk, cfg, tp, im, m, TREE_ID, start, end)
+            ind = rkt._ref_indicators(rk, cfg, tp, im, m, TREE_ID, start, end,
+                                      tree=(lc, o["posteriors"]) if actx else None)
             sel = img_of == i
             for s, (n, lab) in enumerate(zip(node[sel], labels[sel])):
                 if start <= n <= end and tot[n] > thr:
@@ -116,7 +119,7 @@ def compute(plugin: str) -> dict:
 
 def main() -> None:
     data = {}
-    for plugin in sorted(rkt.CASES):
+    for plugin in sorted(rkt.CASES) + ["auto_context"]:
         for k, v in compute(plugin).items():
             data[f"{plugin}/{k}"] = v
     np.savez_compressed(HERE / "ref_kernels.npz", **data)

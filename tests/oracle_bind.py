@@ -16,7 +16,7 @@ REPO = pathlib.Path(__file__).resolve().parent.parent
 ORACLE_SO = REPO / "oracle" / "_build" / "libpadenti_oracle.so"
 REF_DIR = REPO / "oracle" / "_ref"
 
-PLUGIN_IDS = {"depth_diff2": 1, "depth_diff1": 2, "channel_diff": 3}
+PLUGIN_IDS = {"depth_diff2": 1, "depth_diff1": 2, "channel_diff": 3, "auto_context": 16}
 FEAT_IDS = {np.dtype(np.int16): 1, np.dtype(np.int32): 2}
 
 
@@ -65,10 +65,11 @@ def P(a):
     return None if a is None else C.c_void_p(a.ctypes.data)
 
 
-def params(config, tp) -> Params:
-    """Oracle parameters from a ForestConfig and TreeTrainerParameters."""
+def params(config, tp, plugin=None) -> Params:
+    """Oracle parameters from a ForestConfig and TreeTrainerParameters (plugin: the
+    oracle's feature when the config's is a user feature)."""
     p = Params()
-    p.plugin = PLUGIN_IDS[config.plugin]
+    p.plugin = PLUGIN_IDS[plugin or config.plugin]
     p.feat_type = FEAT_IDS[np.dtype(config.feat_dtype)]
     p.feat_dim = config.feat_dim
     p.n_classes = config.n_classes
@@ -125,6 +126,19 @@ def hist(p: Params, ds: OracleSet, tree: int, sample_node, nodes, reference_cost
     out = np.zeros((len(nodes), p.n_classes, p.n_thresholds, p.n_features), np.uint32)
     rc = lib().or_hist(C.byref(p), C.byref(ds.c), tree, P(sample_node), P(nodes), len(nodes), P(out),
                        int(reference_cost), threads)
+    assert rc == 0
+    return out
+
+
+def hist_tree(p: Params, ds: OracleSet, tree: int, sample_node, nodes, maps, lc, post, level, threads=0):
+    """hist for a feature that reads the tree: maps = every image's node map at `level`, lc / post the tree."""
+    nodes = np.ascontiguousarray(nodes, np.int32)
+    sample_node = np.ascontiguousarray(sample_node, np.int32)
+    m = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int32).reshape(-1) for x in maps]))
+    out = np.zeros((len(nodes), p.n_classes, p.n_thresholds, p.n_features), np.uint32)
+    rc = lib().or_hist_tree(C.byref(p), C.byref(ds.c), tree, P(sample_node), P(nodes), len(nodes), P(out), P(m),
+                            P(np.ascontiguousarray(lc, np.int32)), P(np.ascontiguousarray(post, np.float32)),
+                            C.c_int32(level), C.c_int32(len(lc)), threads)
     assert rc == 0
     return out
 
@@ -190,15 +204,17 @@ def predict_posterior(p: Params, image, mask, trees, n_channels=1, threads=0):
     return out
 
 
-def predict_leaf(p: Params, image, mask, depth, lc, feats, thrs, n_channels=1, threads=0):
+def predict_leaf(p: Params, image, mask, depth, lc, feats, thrs, n_channels=1, threads=0, posts=None):
+    """Leaf ids of one tree; posts (the tree's posteriors) for a feature that reads the tree."""
     H, W = image.shape[:2]
     img = np.ascontiguousarray(image)
     m = None if mask is None else np.ascontiguousarray(mask, np.uint8)
     out = np.zeros((H, W), np.int32)
-    rc = lib().or_predict_leaf(C.byref(p), P(img), W, H, n_channels, P(m), depth,
-                               P(np.ascontiguousarray(lc, np.int32)),
-                               P(np.ascontiguousarray(np.asarray(feats, np.int32).reshape(-1))),
-                               P(np.ascontiguousarray(np.asarray(thrs, np.int32))), P(out), threads)
+    po = np.zeros((len(lc), p.n_classes), np.float32) if posts is None else np.ascontiguousarray(posts, np.float32)
+    rc = lib().or_predict_leaf_tree(C.byref(p), P(img), W, H, n_channels, P(m), depth,
+                                    P(np.ascontiguousarray(lc, np.int32)),
+                                    P(np.ascontiguousarray(np.asarray(feats, np.int32).reshape(-1))),
+                                    P(np.ascontiguousarray(np.asarray(thrs, np.int32))), P(po), P(out), threads)
     assert rc == 0
     return out
 
@@ -312,7 +328,8 @@ def rgb_to_labels(image, colours) -> np.ndarray:
 
 
 # ------------------------------------------------- reference kernels as C ----
-REF_KERNEL_LIBS = {"depth_diff1": "kernels_dd1", "depth_diff2": "kernels_dd2", "channel_diff": "kernels_chd"}
+REF_KERNEL_LIBS = {"depth_diff1": "kernels_dd1", "depth_diff2": "kernels_dd2", "channel_diff": "kernels_chd",
+                   "auto_context": "kernels_actx"}
 
 
 def ref_kernels(plugin: str):
@@ -322,6 +339,7 @@ def ref_kernels(plugin: str):
     if r is not None:
         r.ref_per_image_hist.restype = C.c_int
         r.ref_predict_step.restype = C.c_int
+        r.ref_hist_tree.restype = None
     return r
 
 

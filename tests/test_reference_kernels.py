@@ -34,7 +34,7 @@ import numpy as np
 import pytest
 
 import oracle_bind as ob
-from cases import depth1_case, depth_case, rgb_case
+from cases import actx_case, depth1_case, depth_case, rgb_case
 
 _U = C.c_uint
 _I = C.c_int
@@ -73,8 +73,13 @@ def _ref_node_map(rk, cfg, im, tree, steps, mask):
     return nodes
 
 
-def _ref_indicators(rk, cfg, tp, im, nodes_img, tree_id, start, end):
-    """computePerImageHistogram over (nSamples, nFeatures), local (1, 256): uint8 [s][t][f]."""
+def _ref_indicators(rk, cfg, tp, im, nodes_img, tree_id, start, end, tree=None):
+    """computePerImageHistogram over (nSamples, nFeatures), local (1, 256): uint8 [s][t][f];
+    tree = (left children, posteriors) passed to the feature (null when None)."""
+    keep = None
+    if tree is not None:
+        keep = (np.ascontiguousarray(tree[0], np.int32), np.ascontiguousarray(tree[1], np.float32))
+        rk.ref_hist_tree(ob.P(keep[0]), ob.P(keep[1]))
     H, W = im.labels.shape[:2]
     S = len(im.samples)
     out = np.zeros((S, tp.n_thresholds, tp.n_features), np.uint8)
@@ -86,6 +91,8 @@ def _ref_indicators(rk, cfg, tp, im, nodes_img, tree_id, start, end):
                                ob.P(smp), _U(S), _U(tp.n_features), _U(cfg.feat_dim), ob.P(lo), ob.P(up),
                                _U(tp.n_thresholds), _I(int(tp.thr_low_bound)), _I(int(tp.thr_up_bound)),
                                _U(tree_id), _I(int(start)), _I(int(end)), ob.P(out))
+    if keep is not None:
+        rk.ref_hist_tree(None, None)
     assert rc == 0
     return out
 
@@ -270,3 +277,165 @@ def test_oracle_reproduces_reference_kernel_fixture(plugin):
             continue
         h = ob.hist(p, ds, 3, gold[f"{plugin}/d{d}_sample_node"], gold[f"{plugin}/d{d}_frontier"])
         assert hashlib.sha256(np.ascontiguousarray(h).tobytes()).hexdigest() == str(gold[key]), d
+
+
+# A feature that reads the tree (auto-context): oracle/ref_shim/cl/actx/feature.cl is
+# the oracle's OR_PLUGIN_AUTO_CONTEXT as a Padenti feature.cl; the reference's kernels
+# pass it their treeLeftChildren, treePosteriors and imageNodesID.
+def _actx():
+    return actx_case(n_images=4, width=64, height=48, n_features=256, n_thresholds=8, samples=200, min_leaf=10)
+
+
+def test_auto_context_tree_depths_match_reference_kernels():
+    """Every depth of an oracle-trained auto-context tree: the reference's traversal
+    (with the tree passed to the feature) puts each sample on the oracle's node, and its
+    per-image indicators over the node maps, summed as its host does, equal the oracle's
+    histograms; the split and the stored candidate follow as for the other features."""
+    rk = _kernels("auto_context")
+    cfg, ts, tp, _ = _actx()
+    depth, tree_id = 5, 3
+    p = ob.params(cfg, tp, "auto_context")
+    ds = ob.OracleSet(ts, cfg)
+    o = ob.train_tree(p, ds, tree_id, depth, ts.priors)
+    lc, posts = o["left_child"], o["posteriors"]
+    tree = (lc, o["features"], o["thresholds"], posts)
+    K, T, F = cfg.n_classes, tp.n_thresholds, tp.n_features
+    thr = tp.per_leaf_samples_thr
+    labels = np.concatenate([im.labels.reshape(-1)[im.samples] for im in ts.images]).astype(np.int64)
+    img_of = np.concatenate([np.full(len(im.samples), i) for i, im in enumerate(ts.images)])
+    assert o["nodes_split"] >= 3
+    checked = 0
+    for d in range(1, depth):
+        node_d = _ancestor_at(o["sample_leaf"], d)
+        maps = [_ref_node_map(rk, cfg, im, tree, d - 1, im.labels != 0) for im in ts.images]
+        ref_node = np.concatenate([m.reshape(-1)[im.samples] for m, im in zip(maps, ts.images)])
+        assert np.array_equal(ref_node, node_d), d
+        tot = np.bincount(node_d, minlength=len(lc))
+        level = np.arange((1 << (d - 1)) - 1, (1 << d) - 1)
+        frontier = [int(n) for n in level if lc[n] != -2 and tot[n] > thr]
+        if not frontier:
+            break
+        start, end = frontier[0], frontier[-1]
+        idx = {n: i for i, n in enumerate(frontier)}
+        href = np.zeros((len(frontier), K, T, F), np.uint32)
+        for i, (im, m) in enumerate(zip(ts.images, maps)):
+            ind = _ref_indicators(rk, cfg, tp, im, m, tree_id, start, end, tree=(lc, posts))
+            sel = img_of == i
+            for s, (n, lab) in enumerate(zip(ref_node[sel], labels[sel])):
+                if start <= n <= end and tot[n] > thr:
+                    href[idx[int(n)], lab - 1] += ind[s]
+        horc = ob.hist_tree(p, ds, tree_id, node_d, frontier, maps, lc, posts, d - 1)
+        assert np.array_equal(href, horc), d
+        ctot = np.stack([np.bincount(labels[node_d == n] - 1, minlength=K) for n in frontier]).astype(np.uint32)
+        t, f, g, _, _ = ob.split(p, href, ctot)
+        for i, n in enumerate(frontier):
+            if lc[n] < 0:
+                continue
+            feat, thr_t = ob.candidate(p, tree_id, n, int(f[i]))
+            assert np.array_equal(np.asarray(o["features"][n], np.int32), feat), (d, n)
+            assert int(o["thresholds"][n]) == int(thr_t[t[i]]), (d, n)
+            checked += 1
+    assert checked >= 3
+
+
+def test_auto_context_forest_matches_reference_kernels():
+    """Forest posterior and leaf maps of two auto-context trees: the reference's predict
+    launches (the tree and the node image passed to the feature) and computePosterior,
+    summed in tree order, equal the oracle's level-synchronous prediction."""
+    rk = _kernels("auto_context")
+    cfg, ts, tp, _ = _actx()
+    p = ob.params(cfg, tp, "auto_context")
+    ds = ob.OracleSet(ts, cfg)
+    depth = 5
+    trees = []
+    for tid in (0, 1):
+        o = ob.train_tree(p, ds, tid, depth, ts.priors)
+        trees.append((depth, o["left_child"], o["features"], o["thresholds"], o["posteriors"]))
+    K = cfg.n_classes
+    rng = np.random.default_rng(2)
+    for im in ts.images[:2]:
+        H, W = im.labels.shape[:2]
+        for mask in (np.ones((H, W), np.uint8), (rng.random((H, W)) < 0.6).astype(np.uint8)):
+            post = np.zeros((K, H, W), np.float32)
+            buf = np.zeros((K, H, W), np.float32)
+            for (dep, lc, ft, th, po) in trees:
+                nodes = _ref_node_map(rk, cfg, im, (lc, ft, th, po), dep - 1, mask)
+                pp = np.ascontiguousarray(po, np.float32)
+                rk.ref_compute_posterior(ob.P(nodes), _U(W), _U(H), _U(K), ob.P(pp), ob.P(mask), ob.P(buf))
+                m = mask != 0
+                for c in range(K):
+                    post[c][m] = post[c][m] + buf[c][m]
+                leaf = ob.predict_leaf(p, im.data, mask, dep, lc, ft, th, posts=po)
+                assert np.array_equal(leaf[m], nodes[m])
+            post = (post / np.float32(len(trees))).astype(np.float32)
+            o = ob.predict_posterior(p, im.data, mask, trees)
+            assert np.array_equal(o.view(np.uint32), post.view(np.uint32))
+
+
+def test_auto_context_feature_reads_the_tree():
+    """The auto-context oracle's training is self-consistent (every sample's node is the
+    leaf its pixel reaches in level-synchronous prediction over the labels as mask), and
+    the tree term matters: the same splits read without the tree route pixels differently."""
+    cfg, ts, tp, _ = actx_case()
+    p = ob.params(cfg, tp, "auto_context")
+    ds = ob.OracleSet(ts, cfg)
+    o = ob.train_tree(p, ds, 3, 6, ts.priors)
+    lc = o["left_child"]
+    assert (lc >= 0).sum() >= 8
+    leaf, off, moved = o["sample_leaf"], 0, 0
+    for im in ts.images:
+        m = (im.labels != 0).astype(np.uint8)
+        pl = ob.predict_leaf(p, im.data, m, 6, lc, o["features"], o["thresholds"], posts=o["posteriors"])
+        s = im.samples
+        assert np.array_equal(pl.reshape(-1)[s], leaf[off:off + len(s)])
+        off += len(s)
+        # the same tree with the posteriors zeroed: the context term changes, and so do leaves
+        pz = ob.predict_leaf(p, im.data, m, 6, lc, o["features"], o["thresholds"],
+                             posts=np.zeros_like(o["posteriors"]))
+        moved += int((pz != pl).sum())
+    assert moved > 0
+
+
+def test_oracle_reproduces_auto_context_fixture():
+    """The auto-context oracle gives the fixture's numbers from the reference's kernels
+    (tests/golden/make_ref_kernel_golden.py): both trees, every depth's histograms given
+    the reference's sample nodes and node maps (the oracle's own maps, labels as mask),
+    the leaf maps and the two-tree forest posterior.  Runs without the Padenti sources."""
+    import hashlib
+    import pathlib
+
+    def sha(a):
+        return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+    gold = dict(np.load(pathlib.Path(__file__).resolve().parent / "golden" / "ref_kernels.npz"))
+    g = {k.split("/", 1)[1]: v for k, v in gold.items() if k.startswith("auto_context/")}
+    cfg, ts, tp, _ = _actx()
+    p = ob.params(cfg, tp, "auto_context")
+    ds = ob.OracleSet(ts, cfg)
+    trees = {}
+    for tid in (3, 0):
+        o = ob.train_tree(p, ds, tid, 5, ts.priors)
+        trees[tid] = o
+        for k in ("left_child", "features", "thresholds", "posteriors"):
+            assert np.array_equal(o[k], g[f"tree{tid}_{k}"]), (tid, k)
+    o = trees[3]
+    for d in range(1, 5):
+        if f"d{d}_hist_sha256" not in g:
+            continue
+        maps = [ob.predict_leaf(p, im.data, (im.labels != 0).astype(np.uint8), d, o["left_child"], o["features"],
+                                o["thresholds"], posts=o["posteriors"]) for im in ts.images]
+        node = np.concatenate([m.reshape(-1)[im.samples] for m, im in zip(maps, ts.images)])
+        assert np.array_equal(node, g[f"d{d}_sample_node"]), d
+        h = ob.hist_tree(p, ds, 3, node, g[f"d{d}_frontier"], maps, o["left_child"], o["posteriors"], d - 1)
+        assert sha(h) == str(g[f"d{d}_hist_sha256"]), d
+    forest = [(5, trees[t]["left_child"], trees[t]["features"], trees[t]["thresholds"], trees[t]["posteriors"])
+              for t in (3, 0)]
+    for i, im in enumerate(ts.images[:2]):
+        H, W = im.labels.shape[:2]
+        rng = np.random.default_rng(2)  # the generator's masks: the same draw for every image
+        for mi, mask in enumerate([np.ones((H, W), np.uint8), (rng.random((H, W)) < 0.6).astype(np.uint8)]):
+            for k, (dep, lc, ft, th, po) in enumerate(forest):
+                leaf = ob.predict_leaf(p, im.data, mask, dep, lc, ft, th, posts=po)
+                assert sha(leaf) == str(g[f"img{i}_mask{mi}_tree{k}_leaf_sha256"]), (i, mi, k)
+            post = ob.predict_posterior(p, im.data, mask, forest)
+            assert sha(post) == str(g[f"img{i}_mask{mi}_posterior_sha256"]), (i, mi)

@@ -8,8 +8,9 @@ pin to the oracle).  Compilation itself needs no GPU.
 import numpy as np
 import pytest
 
+import oracle_bind as ob
 import padenti_gb300 as pg
-from cases import depth1_case, depth_case, rgb_case
+from cases import AUTO_CONTEXT_SOURCE, actx_case, depth1_case, depth_case, rgb_case
 
 # kernels/feature.cl-style features written against pd::ImageView (read() is 0 outside)
 SOURCES = {
@@ -195,3 +196,60 @@ def test_generic_user_plugin_equals_the_builtin(shape):
     cb << b
     assert np.array_equal(ca.predict(px[0]).view(np.uint32), cb.predict(upx[0]).view(np.uint32))
     assert np.array_equal(ca.predict_leaf(0, px[0]), cb.predict_leaf(0, upx[0]))
+
+
+# A feature that reads the tree (auto-context): computeFeature takes a pd::TreeView and
+# reads the node map through ImageView::nodeID; the library keeps a per-pixel node map.
+def test_auto_context_plugin_compiles_without_a_gpu():
+    assert isinstance(pg.check_plugin(pg.ForestConfig("user", 3, source=AUTO_CONTEXT_SOURCE, shape="u16x1_i32x4")),
+                      str)
+
+
+@pytest.mark.gpu
+def test_auto_context_feature_matches_the_oracle():
+    """Trees, forest posteriors (with and without a mask), leaf maps and the mixed batch of
+    the auto-context feature, bit-identical to the oracle's OR_PLUGIN_AUTO_CONTEXT (which
+    tests/test_reference_kernels.py pins to the reference's kernels)."""
+    cfg, ts, tp, (px, lb, sm) = actx_case()
+    p = ob.params(cfg, tp, "auto_context")
+    ds = ob.OracleSet(ts, cfg)
+    trainer = pg.TreeTrainer(cfg)
+    clf = pg.Classifier(cfg)
+    forest = []
+    for tid in (3, 0):
+        o = ob.train_tree(p, ds, tid, 6, ts.priors)
+        t = pg.Tree(cfg, tid, 6)
+        trainer.train(t, ts, tp)
+        assert (o["left_child"] >= 0).sum() >= 8
+        assert np.array_equal(t.left_child, o["left_child"]), tid
+        assert np.array_equal(np.asarray(t.features, np.int32), o["features"]), tid
+        assert np.array_equal(np.asarray(t.thresholds, np.int32), o["thresholds"]), tid
+        assert np.array_equal(t.posteriors.view(np.uint32), o["posteriors"].view(np.uint32)), tid
+        clf << t
+        forest.append((6, o["left_child"], o["features"], o["thresholds"], o["posteriors"]))
+    rng = np.random.default_rng(4)
+    for image in px[:2]:
+        mask = (rng.random(image.shape[:2]) < 0.7).astype(np.uint8)
+        for m in (None, mask):
+            want = ob.predict_posterior(p, image, m, forest)
+            assert np.array_equal(clf.predict(image, m).view(np.uint32), want.view(np.uint32))
+            for k, (dep, lc, ft, th, po) in enumerate(forest):
+                assert np.array_equal(clf.predict_leaf(k, image, m), ob.predict_leaf(p, image, m, dep, lc, ft, th,
+                                                                                     posts=po))
+    batch = clf.predict_batch([px[0], px[1][:40, :50]])
+    assert np.array_equal(batch[0].view(np.uint32), ob.predict_posterior(p, px[0], None, forest).view(np.uint32))
+    assert np.array_equal(batch[1].view(np.uint32),
+                          ob.predict_posterior(p, np.ascontiguousarray(px[1][:40, :50]), None, forest).view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_auto_context_refuses_the_histogram_stage_call():
+    from padenti_gb300 import _native as N
+    import ctypes as C
+
+    cfg, ts, tp, _ = actx_case(n_images=2)
+    trainer = pg.TreeTrainer(cfg)
+    t = pg.Tree(cfg, 0, 3)
+    trainer.train(t, ts, tp)  # uploads the set and compiles the plugin
+    with pytest.raises(pg.PadentiError, match="node map"):
+        trainer.hist(tp, 0, np.zeros(len(ts.flat()["samples"]), np.int32), np.array([0], np.int32))
