@@ -420,8 +420,13 @@ PD_D void hist_samples(const DevSet &ds, const SampleRec *__restrict__ rec, cons
     FeatT ra, rb;
     uint32_t row;  // class * (T + 1) * 32: the class block of the histogram
   };
-  for (uint32_t base = w.begin + warp * 32; base < w.end; base += kHistThreads) {
-    const uint32_t n_here = min(32u, w.end - base);
+  // samples per warp batch: 32, or for an item of fewer than 256 samples an equal
+  // share (rounded up to SPI) so that every warp of the CTA has samples
+  const uint32_t n_item = w.end - w.begin;
+  const uint32_t share = (n_item + kHistThreads / 32 - 1) / (kHistThreads / 32);
+  const uint32_t bs = n_item >= kHistThreads ? 32u : min(32u, (share + SPI - 1) / SPI * SPI);
+  for (uint32_t base = w.begin + warp * bs; base < w.end; base += bs * (kHistThreads / 32)) {
+    const uint32_t n_here = min(bs, w.end - base);
     // lane-parallel preload of 32 samples: position, class, image, pixel words
     uint32_t my_xy = 0, my_wh = 0, my_row = 0, my_pre[PW];
     uint64_t my_off = 0, my_moff = 0;
@@ -552,17 +557,29 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   __shared__ uint16_t s_list[kRecheckList];
   __shared__ unsigned long long s_pmin;
   __shared__ int s_j0;
+  __shared__ uint8_t s_cls[PD_MAX_CLASSES];  // the classes present in the node, in class order
+  __shared__ uint32_t s_nc;
   const uint32_t slot = w.slot, f0 = w.tile * kTileF;
   const uint32_t TS = T + 1;  // histogram rows per class
   for (uint32_t l = threadIdx.x; l < K; l += blockDim.x) s_tot[l] = fs.class_tot[(size_t)slot * K + l];
+  __syncthreads();
   if (threadIdx.x == 0) {
     s_nlist = 0u;
     s_pmin = ~0ull;
     s_j0 = 0;
+    uint32_t nc = 0;
+    for (uint32_t l = 0; l < K; l++)
+      if (s_tot[l]) s_cls[nc++] = (uint8_t)l;
+    s_nc = nc;
   }
-  // in-place prefix over the ranks of each (class, packed column)
-  for (uint32_t q = threadIdx.x; q < K * 32; q += blockDim.x) {
-    const uint32_t l = q >> 5, col = q & 31;
+  __syncthreads();
+  // Only the classes present in the node: the item holds all of the node's
+  // samples, so an absent class's rows were never counted (nor zeroed, hist_item)
+  // and every term they would add is c log2 c of 0, or skipped as c = 0.
+  const uint32_t nc = s_nc;
+  // in-place prefix over the ranks of each (present class, packed column)
+  for (uint32_t q = threadIdx.x; q < nc * 32; q += blockDim.x) {
+    const uint32_t l = s_cls[q >> 5], col = q & 31;
     uint32_t run = 0;
     for (uint32_t j = 0; j < T; j++) {
       run += sh_hist[(l * TS + j) * 32 + col];
@@ -603,7 +620,7 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     for (uint32_t q = threadIdx.x; q < T * 32; q += blockDim.x) {
       const uint32_t j = q >> 5, col = q & 31;
       uint32_t n = 0;
-      for (uint32_t l = 0; l < K; l++) n += sh_hist[(l * TS + j) * 32 + col];
+      for (uint32_t i = 0; i < nc; i++) n += sh_hist[(s_cls[i] * TS + j) * 32 + col];
       sh_nl[q] = n;
     }
     __syncthreads();
@@ -620,7 +637,8 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
           // counts are monotone in j: an equal total means equal counts
           if (j == 0 || half16(sh_nl[(j - 1) * 32 + (c & 31)], c) != nL) {
             float sl = __ldg(X + nL), sr = __ldg(X + (N - nL));
-            for (uint32_t l = 0; l < K; l++) {
+            for (uint32_t i = 0; i < nc; i++) {
+              const uint32_t l = s_cls[i];
               const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
               sl -= __ldg(X + cl);
               sr -= __ldg(X + (s_tot[l] - cl));
@@ -651,7 +669,8 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
         const double Ll = L[nL], Lr = L[nR];
         double sl = 0.0, sr = 0.0;
 #pragma unroll 3
-        for (uint32_t l = 0; l < K; l++) {
+        for (uint32_t i = 0; i < nc; i++) {
+          const uint32_t l = s_cls[i];
           const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c), cr = s_tot[l] - cl;
           if (cl != 0u && (uint64_t)cl * 1000000ull > nL) sl = dadd(sl, dmul((double)cl, dsub(Ll, L[cl])));
           if (cr != 0u && (uint64_t)cr * 1000000ull > nR) sr = dadd(sr, dmul((double)cr, dsub(Lr, L[cr])));
@@ -737,7 +756,8 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     fs.part_best[pi] = pb;
     if (pb.idx != LLONG_MAX) {
       const uint32_t c = (uint32_t)pb.col - f0;
-      for (uint32_t l = 0; l < K; l++) fs.part_cl[pi * K + l] = half16(sh_hist[(l * TS + pb.j) * 32 + (c & 31)], c);
+      for (uint32_t l = 0; l < K; l++)
+        fs.part_cl[pi * K + l] = s_tot[l] ? half16(sh_hist[(l * TS + pb.j) * 32 + (c & 31)], c) : 0u;
     }
     __threadfence();
     s_last = atomicAdd(fs.done + slot, 1u) == fs.tiles - 1;
@@ -798,7 +818,14 @@ __device__ __forceinline__ void hist_item(const DevSet &ds, const SampleRec *__r
     sh_thr[(c >> 5) * (TP * 32) + t * 32 + (c & 31)] =
         (t < T && ff < F) ? cand_thr[((size_t)w.slot * T + t) * F + ff] : max_of<FeatT>();
   }
-  for (uint32_t j = threadIdx.x; j < K * (T + 1) * 32; j += blockDim.x) sh_hist[j] = 0u;
+  if (w.multi == 2) {
+    // a fused item: only the rows of the classes present in the node are counted and read
+    for (uint32_t l = 0; l < K; l++)
+      if (fs.class_tot[(size_t)w.slot * K + l])
+        for (uint32_t j = threadIdx.x; j < (T + 1) * 32; j += blockDim.x) sh_hist[l * (T + 1) * 32 + j] = 0u;
+  } else {
+    for (uint32_t j = threadIdx.x; j < K * (T + 1) * 32; j += blockDim.x) sh_hist[j] = 0u;
+  }
   if (w.multi == 2) {
     // the fused split reads the tile's threshold permutation and column order
     // at the end; bring them to L2 now

@@ -196,6 +196,16 @@ def test_generic_user_plugin_equals_the_builtin(shape):
     cb << b
     assert np.array_equal(ca.predict(px[0]).view(np.uint32), cb.predict(upx[0]).view(np.uint32))
     assert np.array_equal(ca.predict_leaf(0, px[0]), cb.predict_leaf(0, upx[0]))
+    # and directly against the oracle (the built-in feature on the original pixels)
+    p = ob.params(cfg, tp)
+    o = ob.train_tree(p, ob.OracleSet(ts, cfg), 3, 7, ts.priors)
+    assert np.array_equal(b.left_child, o["left_child"])
+    assert np.array_equal(np.asarray(b.features, np.int32)[:, :D], o["features"])
+    assert np.array_equal(np.asarray(b.thresholds, np.int32), o["thresholds"])
+    assert np.array_equal(b.posteriors.view(np.uint32), o["posteriors"].view(np.uint32))
+    want = ob.predict_posterior(p, px[0], None, [(7, o["left_child"], o["features"], o["thresholds"],
+                                                  o["posteriors"])], n_channels=cfg.n_channels)
+    assert np.array_equal(cb.predict(upx[0]).view(np.uint32), want.view(np.uint32))
 
 
 # A feature that reads the tree (auto-context): computeFeature takes a pd::TreeView and
