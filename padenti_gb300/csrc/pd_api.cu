@@ -210,8 +210,10 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
     bytes = std::max<uint64_t>(bytes, ds->pix_off[i] + (uint64_t)ds->width[i] * ds->height[i] * px);
   }
   // per-sample position, image and class: host threads over interleaved images,
-  // into pinned staging; each thread keeps its first bad sample and the lowest
-  // one is reported (the one a sequential pass meets first)
+  // into pinned staging, with per-thread class totals; each thread keeps its
+  // first bad sample and the lowest one is reported (the one a sequential pass
+  // meets first).  Nothing reaches the device before every sample is checked, so
+  // a failed upload keeps the training set uploaded before.
   PD_TRY(ctx->h_stage.ensure(S * 9 + 16));
   uint32_t *xy = ctx->h_stage.as<uint32_t>(), *im = xy + S;
   uint8_t *lab = reinterpret_cast<uint8_t *>(im + S);
@@ -222,7 +224,9 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
     int label = -1;  // -1: the sample lies outside the image
   };
   std::vector<Bad> bad(nt);
+  std::vector<std::vector<uint32_t>> cls(nt, std::vector<uint32_t>(ctx->cfg.n_classes, 0u));
   auto work = [&](unsigned t) {
+    uint32_t *ct = cls[t].data();
     for (uint32_t i = t; i < n; i += nt) {
       const uint32_t w = ds->width[i], h = ds->height[i];
       for (uint64_t k = ds->samp_off[i]; k < ds->samp_off[i + 1]; k++) {
@@ -239,6 +243,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
         xy[k] = (p % w) | ((p / w) << 16);
         im[k] = i;
         lab[k] = (uint8_t)(l - 1);
+        ct[l - 1]++;
       }
     }
   };
@@ -259,6 +264,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
                      (unsigned long long)first.k, first.image, first.label, ctx->cfg.n_classes);
   }
   cudaStream_t st = ctx->stream;
+  ctx->have_dataset = false;  // until the new set is in place
   PD_TRY(ctx->pixels.ensure(bytes));
   PD_TRY(ctx->img_off.ensure(n * 8));
   PD_TRY(ctx->img_wh.ensure(n * 4));
@@ -275,7 +281,9 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
     PD_CUDA(h2d(ctx, ctx->s_label.ptr, lab, S));
   }
   PD_TRY(build_sample_records(ctx, S));
-  ctx->h_label.assign(lab, lab + S);
+  ctx->root_class_tot.assign(ctx->cfg.n_classes, 0u);
+  for (const auto &c : cls)
+    for (int l = 0; l < ctx->cfg.n_classes; l++) ctx->root_class_tot[l] += c[l];
   if (ctx->tree_feature) {
     // the node map's layout and every pixel's label: the map advances on labelled pixels
     // (cl_tree_trainer_impl_traverse_ts.hpp:215-232 passes the label image as the mask)

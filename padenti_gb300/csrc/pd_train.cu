@@ -556,7 +556,7 @@ static int train_tree_impl(pd_ctx *ctx, const pd_train_params *p, uint32_t tree_
 
   for (uint32_t depth = 1; depth < end_depth; depth++) {
     if (depth == 1) {
-      for (uint64_t s = 0; s < S; s++) class_tot[ctx->h_label[s]]++;
+      for (uint32_t l = 0; l < K; l++) class_tot[l] = ctx->root_class_tot[l];
     }
     ctx->nm_level = (int32_t)depth - 1;  // the node map's level: the frontier's
     const uint32_t nf = (uint32_t)frontier.size();
