@@ -880,8 +880,11 @@ def run_ours(a):
     barrier()
     t0 = time.perf_counter()
     e2e_evals = 0
+    upload_s = 0.0
     for s in range(e2e_steps):
+        tu = time.perf_counter()
         N.check(N.lib().pd_dataset_upload(tr.h, C.byref(desc)))
+        upload_s += time.perf_counter() - tu
         tr._uploaded = None
         tree = pg.Tree(cfg, 500 + rank * 1000 + s, a.depth)
         prior = np.ascontiguousarray(ts.priors, np.float32)
@@ -897,6 +900,8 @@ def run_ours(a):
     e2e = dict(value=allsum(e2e_evals) / e2e_s, unit=UNIT,
                h2d_bytes_per_step=int((h1.value - h0.value) / max(1, e2e_steps)),
                d2h_bytes_per_step=int((d1.value - d0.value) / max(1, e2e_steps)),
+               upload_ms_per_step=1000 * upload_s / max(1, e2e_steps),
+               ms_per_step=1000 * e2e_s / max(1, e2e_steps),
                note="per step: pd_dataset_upload of the whole training set from pinned host memory + "
                     "pd_train_tree with the tree arrays in host memory; wall clock")
 

@@ -203,10 +203,22 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
   // value and index sort as one word
   const int64_t span = (int64_t)p->thr_up - p->thr_low;
   const bool packed = span >= 0 && span < (1 << 24) && (sizeof(FeatT) == 4 || span <= 32767);
+  const unsigned grid = (unsigned)((total + kCandThreads - 1) / kCandThreads);
+  const uint32_t T = p->n_thresholds;
+  if (!prop && packed && T <= 64) {
+    // MD5 candidates, keys sorted in registers
+    auto rk = T <= 16 ? k_candidates_reg<FeatT, 16> : (T <= 32 ? k_candidates_reg<FeatT, 32> : k_candidates_reg<FeatT, 64>);
+    rk<<<grid, kCandThreads, 0, ctx->stream>>>(d_nodes, n, tree, F, T, P::kFeatDim, b, ord, ctx->cand_feat.as<FeatT>(),
+                                               ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>());
+    PD_CUDA(cudaGetLastError());
+    ctx->launches++;
+    if (ord_out) *ord_out = ord;
+    return PD_OK;
+  }
   const size_t smem = (size_t)p->n_thresholds * kCandThreads * (packed ? 4 : sizeof(FeatT) + 1);
   auto kern = packed ? k_candidates<FeatT, true> : k_candidates<FeatT, false>;
   PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)((total + kCandThreads - 1) / kCandThreads), kCandThreads, smem, ctx->stream>>>(
+  kern<<<grid, kCandThreads, smem, ctx->stream>>>(
       d_nodes, n, tree, F, p->n_thresholds, P::kFeatDim, b, ord, ctx->cand_feat.as<FeatT>(),
       ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>(), prop ? *prop : PropSrc{});
   PD_CUDA(cudaGetLastError());

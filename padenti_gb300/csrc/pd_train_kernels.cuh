@@ -207,6 +207,83 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
   }
 }
 
+// The same table for MD5 candidates with packed keys and at most TP thresholds
+// (TP = 16, 32 or 64): the keys of a candidate live in registers (padded with
+// 0xffffffff, above every key since t < TP) and are sorted by a bitonic network
+// with compile-time indices -- branch-free min/max pairs in place of the
+// insertion sort, whose data-dependent shifts diverge across a warp.  Same
+// output as k_candidates<FeatT, true> without a proposal source.
+template <int N>
+PD_D void bitonic_sort_regs(uint32_t (&k)[N]) {
+#pragma unroll
+  for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+      for (int i = 0; i < N; i++) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const uint32_t a = k[i], c = k[j];
+          const uint32_t lo = min(a, c), hi = max(a, c);
+          if ((i & size) == 0) {
+            k[i] = lo;
+            k[j] = hi;
+          } else {
+            k[i] = hi;
+            k[j] = lo;
+          }
+        }
+      }
+    }
+  }
+}
+
+template <typename FeatT, int TP>
+__global__ void __launch_bounds__(kCandThreads) k_candidates_reg(const int32_t *__restrict__ nodes, uint32_t n_nodes,
+                                                                 uint32_t tree, uint32_t F, uint32_t T, int D,
+                                                                 CandBounds b, const uint32_t *__restrict__ ord,
+                                                                 FeatT *__restrict__ feat,
+                                                                 FeatT *__restrict__ thr_sorted,
+                                                                 uint8_t *__restrict__ perm) {
+  const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (uint64_t)n_nodes * F) return;
+  const uint32_t n = (uint32_t)(idx / F), c = (uint32_t)(idx % F);
+  const uint32_t node = (uint32_t)nodes[n];
+  const uint32_t f = ord ? ord[(size_t)n * F + c] : c;
+  const uint32_t fg = b.f_base + f;
+  {
+    FeatT fv[PD_MAX_FEAT_DIM];
+    candidate_feature<FeatT>(tree, node, fg, D, b.low, b.up, fv);
+    for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + c] = fv[d];
+  }
+  uint32_t key[TP];
+  uint32_t seed[4] = {tree, node, fg, 1u}, st[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int t = 0; t < TP; t++) {
+    if ((uint32_t)t < T) {
+      if ((t & 3) == 0) {
+        md5_block(seed, st);
+        seed[0] = st[0];
+        seed[1] = st[1];
+        seed[2] = st[2];
+        seed[3] = st[3];
+      }
+      const FeatT x = draw<FeatT>(st[t & 3], b.thr_lo, b.thr_hi);
+      key[t] = ((uint32_t)((int32_t)x - b.thr_lo) << 8) | (uint32_t)t;
+    } else {
+      key[t] = 0xffffffffu;
+    }
+  }
+  bitonic_sort_regs<TP>(key);
+#pragma unroll
+  for (int j = 0; j < TP; j++) {
+    if ((uint32_t)j < T) {
+      thr_sorted[((size_t)n * T + j) * F + c] = (FeatT)((int32_t)(key[j] >> 8) + b.thr_lo);
+      perm[((size_t)n * T + j) * F + c] = (uint8_t)(key[j] & 0xffu);
+    }
+  }
+}
+
 // ------------------------------------------------------ candidate order ----
 // Column order of a node's candidate table: the candidates sorted row-major by
 // their first probe offset (feature dims kOrderDim + 1 = y, then kOrderDim = x,

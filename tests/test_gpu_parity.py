@@ -30,12 +30,16 @@ def test_log2_table_bit_identical():
     assert np.array_equal(g.view(np.uint64), o.view(np.uint64))
 
 
-@pytest.mark.parametrize("thr_bounds", [(-500, 500), (-(1 << 30), 1 << 30)])
-def test_candidates_match_oracle(thr_bounds):
-    """Narrow threshold bounds sort (value, index) packed in one word; wide bounds
-    (a range of 2^24 or more) sort them as two columns."""
+@pytest.mark.parametrize("thr_bounds,T", [((-500, 500), 50), ((-(1 << 30), 1 << 30), 50), ((-500, 500), 3),
+                                          ((-500, 500), 17), ((-500, 500), 64), ((-500, 500), 100),
+                                          ((-20, 20), 64)])
+def test_candidates_match_oracle(thr_bounds, T):
+    """Narrow threshold bounds sort (value, index) packed in one word -- in registers by
+    a bitonic network for T <= 64 (16, 32 or 64 keys with padding), by insertion in
+    shared memory above; wide bounds (a range of 2^24 or more) sort them as two columns.
+    Bounds of +-20 with 64 thresholds give equal values, ordered by index."""
     cfg, ts, tp, _ = depth_case(n_images=2, n_features=100, n_thresholds=50)
-    tp = pg.TreeTrainerParameters(100, 50, [-60000] * 4, [60000] * 4, thr_bounds[0], thr_bounds[1], 20)
+    tp = pg.TreeTrainerParameters(100, T, [-60000] * 4, [60000] * 4, thr_bounds[0], thr_bounds[1], 20)
     tr = pg.TreeTrainer(cfg)
     nodes = np.array([0, 1, 2, 77, 4095, 123456], np.int32)
     feat, thr = tr.candidates(tp, 7, nodes)
