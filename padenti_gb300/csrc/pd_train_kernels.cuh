@@ -654,13 +654,24 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
   // samples, so an absent class's rows were never counted (nor zeroed, hist_item)
   // and every term they would add is c log2 c of 0, or skipped as c = 0.
   const uint32_t nc = s_nc;
-  // in-place prefix over the ranks of each (present class, packed column)
+  // in-place prefix over the ranks of each (present class, packed column), eight
+  // rows loaded together
   for (uint32_t q = threadIdx.x; q < nc * 32; q += blockDim.x) {
-    const uint32_t l = s_cls[q >> 5], col = q & 31;
-    uint32_t run = 0;
-    for (uint32_t j = 0; j < T; j++) {
-      run += sh_hist[(l * TS + j) * 32 + col];
-      sh_hist[(l * TS + j) * 32 + col] = run;
+    uint32_t *h = sh_hist + (s_cls[q >> 5] * TS) * 32 + (q & 31);
+    uint32_t run = 0, j = 0;
+    for (; j + 8 <= T; j += 8) {
+      uint32_t v[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) v[k] = h[(j + k) * 32];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        run += v[k];
+        h[(j + k) * 32] = run;
+      }
+    }
+    for (; j < T; j++) {
+      run += h[j * 32];
+      h[j * 32] = run;
     }
   }
   __syncthreads();
@@ -702,28 +713,35 @@ PD_D void fused_split(const FusedSplit &fs, const WorkItem &w, uint32_t *sh_hist
     }
     __syncthreads();
     const uint32_t pairs = T * kTileF;
-    // FP32 filter -(S_L + S_R) from the c log2 c table (fused_window) and the tile maximum
+    // FP32 filter -(S_L + S_R) from the c log2 c table (fused_window) and the tile
+    // maximum.  Thread (column c, quarter) walks a run of consecutive positions j of
+    // its column, so the previous position's left total stays in a register; the
+    // 32 lanes of a warp share j and read 32 consecutive words.
+    static_assert(kHistThreads == 4 * kTileF, "four threads per candidate column");
     float lmax = -FLT_MAX;
     if (ok) {
       const float *X = fs.xlog2;
-      for (uint32_t q = threadIdx.x; q < pairs; q += blockDim.x) {
-        const uint32_t j = q / kTileF, c = q % kTileF;
+      const uint32_t c = threadIdx.x & (kTileF - 1), col = c & 31, hs = (c >> 5) * 16;
+      const uint32_t per = (T + 3) / 4, jb = (threadIdx.x / kTileF) * per, je = min(T, jb + per);
+      const bool valid = f0 + c < F;
+      uint32_t prev = jb > 0 && jb < je ? (sh_nl[(jb - 1) * 32 + col] >> hs) & 0xffffu : 0xffffffffu;
+      for (uint32_t j = jb; j < je; j++) {
+        const uint32_t nL = (sh_nl[j * 32 + col] >> hs) & 0xffffu;
         float g = -FLT_MAX;  // duplicates of the previous position stay -max
-        if (f0 + c < F) {
-          const uint32_t nL = half16(sh_nl[j * 32 + (c & 31)], c);
-          // counts are monotone in j: an equal total means equal counts
-          if (j == 0 || half16(sh_nl[(j - 1) * 32 + (c & 31)], c) != nL) {
-            float sl = __ldg(X + nL), sr = __ldg(X + (N - nL));
-            for (uint32_t i = 0; i < nc; i++) {
-              const uint32_t l = s_cls[i];
-              const uint32_t cl = half16(sh_hist[(l * TS + j) * 32 + (c & 31)], c);
-              sl -= __ldg(X + cl);
-              sr -= __ldg(X + (s_tot[l] - cl));
-            }
-            g = -(sl + sr);
+        // counts are monotone in j: an equal total means equal counts
+        if (valid && nL != prev) {
+          float sl = __ldg(X + nL), sr = __ldg(X + (N - nL));
+          const uint32_t *hj = sh_hist + j * 32 + col;
+          for (uint32_t i = 0; i < nc; i++) {
+            const uint32_t l = s_cls[i];
+            const uint32_t cl = (hj[l * TS * 32] >> hs) & 0xffffu;
+            sl -= __ldg(X + cl);
+            sr -= __ldg(X + (s_tot[l] - cl));
           }
+          g = -(sl + sr);
         }
-        sh_g[q] = g;
+        prev = nL;
+        sh_g[j * kTileF + c] = g;
         lmax = fmaxf(lmax, g);
       }
     }
