@@ -881,10 +881,15 @@ def run_ours(a):
     t0 = time.perf_counter()
     e2e_evals = 0
     upload_s = 0.0
+    up_samples = up_device = 0.0
     for s in range(e2e_steps):
         tu = time.perf_counter()
         N.check(N.lib().pd_dataset_upload(tr.h, C.byref(desc)))
         upload_s += time.perf_counter() - tu
+        us = N.UploadStats()
+        N.check(N.lib().pd_dataset_upload_stats(tr.h, C.byref(us)))
+        up_samples += us.ms_samples
+        up_device += us.ms_device
         tr._uploaded = None
         tree = pg.Tree(cfg, 500 + rank * 1000 + s, a.depth)
         prior = np.ascontiguousarray(ts.priors, np.float32)
@@ -901,6 +906,8 @@ def run_ours(a):
                h2d_bytes_per_step=int((h1.value - h0.value) / max(1, e2e_steps)),
                d2h_bytes_per_step=int((d1.value - d0.value) / max(1, e2e_steps)),
                upload_ms_per_step=1000 * upload_s / max(1, e2e_steps),
+               upload_host_samples_ms=up_samples / max(1, e2e_steps),
+               upload_device_ms=up_device / max(1, e2e_steps),
                ms_per_step=1000 * e2e_s / max(1, e2e_steps),
                note="per step: pd_dataset_upload of the whole training set from pinned host memory + "
                     "pd_train_tree with the tree arrays in host memory; wall clock")

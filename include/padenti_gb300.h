@@ -205,6 +205,14 @@ int pd_ctx_transfer_bytes(pd_ctx *ctx, uint64_t *h2d, uint64_t *d2h);
  * cl_tree_trainer_impl_traverse_ts.hpp:127-358): the whole set is kept in HBM. */
 int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds);
 int pd_dataset_info(pd_ctx *ctx, uint64_t *n_samples, uint32_t *n_images);
+/* Wall times of the last pd_dataset_upload: the host pass over the samples
+ * (checks, positions, classes), then the copies, kernels and synchronisation. */
+typedef struct {
+  double ms_samples;
+  double ms_device;
+  double ms_total;
+} pd_upload_stats;
+int pd_dataset_upload_stats(pd_ctx *ctx, pd_upload_stats *out);
 
 /* Training: CLTreeTrainer::train (cl_tree_trainer_impl.hpp:203-255).
  * Levels start_depth..end_depth-1 are split (start_depth must be 1, as in the

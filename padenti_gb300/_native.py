@@ -119,6 +119,10 @@ PD_SAMPLER_CLASS_WEIGHTED = 2
 
 # name -> (restype, argtypes)
 _P = C.c_void_p
+class UploadStats(C.Structure):
+    _fields_ = [("ms_samples", C.c_double), ("ms_device", C.c_double), ("ms_total", C.c_double)]
+
+
 _SIGS = {
     "pd_last_error": (C.c_char_p, []),
     "pd_version": (C.c_int, []),
@@ -133,6 +137,7 @@ _SIGS = {
     "pd_ctx_transfer_bytes": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "pd_dataset_upload": (C.c_int, [_P, C.POINTER(DatasetDesc)]),
     "pd_dataset_info": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
+    "pd_dataset_upload_stats": (C.c_int, [_P, C.POINTER(UploadStats)]),
     "pd_train_tree": (C.c_int, [_P, C.POINTER(TrainParams), C.c_uint32, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P]),
     "pd_train_get_stats": (C.c_int, [_P, C.POINTER(TrainStats)]),
     "pd_train_sample_nodes": (C.c_int, [_P, _P]),

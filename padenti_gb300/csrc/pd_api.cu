@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <chrono>
 #include <thread>
 #include <vector>
 
@@ -180,6 +181,7 @@ extern "C" int pd_ctx_transfer_bytes(pd_ctx *ctx, uint64_t *h2d_bytes, uint64_t 
 }
 
 extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
+  const auto t_start = std::chrono::steady_clock::now();
   PD_CHECK(ctx && ds, PD_ERR_INVALID, "null argument");
   PD_CHECK(ds->n_images >= 1, PD_ERR_INVALID, "empty training set");
   PD_CHECK(ds->pixels && ds->pix_off && ds->width && ds->height && ds->labels && ds->lab_off && ds->samples &&
@@ -224,9 +226,12 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
     int label = -1;  // -1: the sample lies outside the image
   };
   std::vector<Bad> bad(nt);
-  std::vector<std::vector<uint32_t>> cls(nt, std::vector<uint32_t>(ctx->cfg.n_classes, 0u));
+  struct alignas(64) ClassCount {  // one cache line set per thread
+    uint32_t c[PD_MAX_CLASSES];
+  };
+  std::vector<ClassCount> cls(nt);
   auto work = [&](unsigned t) {
-    uint32_t *ct = cls[t].data();
+    uint32_t ct[PD_MAX_CLASSES] = {};
     for (uint32_t i = t; i < n; i += nt) {
       const uint32_t w = ds->width[i], h = ds->height[i];
       for (uint64_t k = ds->samp_off[i]; k < ds->samp_off[i + 1]; k++) {
@@ -246,6 +251,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
         ct[l - 1]++;
       }
     }
+    memcpy(cls[t].c, ct, sizeof(ct));
   };
   {
     std::vector<std::thread> th;
@@ -253,6 +259,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
     work(0);
     for (auto &x : th) x.join();
   }
+  const auto t_samples = std::chrono::steady_clock::now();
   Bad first;
   for (const Bad &b : bad)
     if (b.k < first.k) first = b;
@@ -283,7 +290,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   PD_TRY(build_sample_records(ctx, S));
   ctx->root_class_tot.assign(ctx->cfg.n_classes, 0u);
   for (const auto &c : cls)
-    for (int l = 0; l < ctx->cfg.n_classes; l++) ctx->root_class_tot[l] += c[l];
+    for (int l = 0; l < ctx->cfg.n_classes; l++) ctx->root_class_tot[l] += c.c[l];
   if (ctx->tree_feature) {
     // the node map's layout and every pixel's label: the map advances on labelled pixels
     // (cl_tree_trainer_impl_traverse_ts.hpp:215-232 passes the label image as the mask)
@@ -308,6 +315,16 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   ctx->have_dataset = true;
   PD_TRY(ensure_log2_table(ctx, S + 2));
   PD_CUDA(cudaStreamSynchronize(st));
+  const auto t_end = std::chrono::steady_clock::now();
+  ctx->upload_stats.ms_samples = std::chrono::duration<double, std::milli>(t_samples - t_start).count();
+  ctx->upload_stats.ms_device = std::chrono::duration<double, std::milli>(t_end - t_samples).count();
+  ctx->upload_stats.ms_total = std::chrono::duration<double, std::milli>(t_end - t_start).count();
+  return PD_OK;
+}
+
+extern "C" int pd_dataset_upload_stats(pd_ctx *ctx, pd_upload_stats *out) {
+  PD_CHECK(ctx && out, PD_ERR_INVALID, "null argument");
+  *out = ctx->upload_stats;
   return PD_OK;
 }
 

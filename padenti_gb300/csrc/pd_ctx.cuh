@@ -43,6 +43,7 @@ struct pd_ctx {
   pd::DevBuf s_img;     // uint32 image per sample
   pd::DevBuf s_label;   // uint8 class (0..K-1) per sample
   std::vector<uint32_t> root_class_tot;  // samples per class (the root's class totals)
+  pd_upload_stats upload_stats{};        // of the last pd_dataset_upload
   pd::HostBuf h_stage;           // pinned staging of the per-sample upload arrays
   pd::HostBuf h_items;           // pinned staging of a histogram launch's work list
   pd::DevBuf log2_tab;  // double log2(n), n < log2_len
