@@ -135,6 +135,53 @@ extern "C" int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes) {
   return PD_OK;
 }
 
+namespace pd {
+
+// Copy of n16 16-byte words from pinned, device-mapped host memory by the SMs
+// (each thread keeps four loads in flight over the host link) -- the
+// alternative to the copy engine for the training images.
+static __global__ void __launch_bounds__(256) k_copy_from_host(const uint4 *__restrict__ src, uint4 *__restrict__ dst,
+                                                               uint64_t n16) {
+  const uint64_t stride = (uint64_t)gridDim.x * 256u;
+  uint64_t i = (uint64_t)blockIdx.x * 256u + threadIdx.x;
+  for (; i + 3 * stride < n16; i += 4 * stride) {
+    const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+    dst[i] = a;
+    dst[i + stride] = b;
+    dst[i + 2 * stride] = c;
+    dst[i + 3 * stride] = d;
+  }
+  for (; i < n16; i += stride) dst[i] = src[i];
+}
+
+// Host -> device copy of the training images: by the SMs when the source is
+// pinned host memory the device can address and both ends are 16-byte aligned
+// (upload_copy = 1), else by the copy engine.
+static int upload_bytes(pd_ctx *ctx, void *dst, const void *src, size_t n) {
+  if (ctx->upload_copy == 1 && n >= 16) {
+    cudaPointerAttributes a;
+    memset(&a, 0, sizeof(a));
+    if (cudaPointerGetAttributes(&a, src) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer &&
+        ((uintptr_t)a.devicePointer % 16) == 0 && ((uintptr_t)dst % 16) == 0) {
+      const uint64_t n16 = n / 16;
+      const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n16 + 255) / 256, (uint64_t)ctx->n_sms * 8));
+      k_copy_from_host<<<grid, 256, 0, ctx->stream>>>(static_cast<const uint4 *>(a.devicePointer),
+                                                      static_cast<uint4 *>(dst), n16);
+      PD_CUDA(cudaGetLastError());
+      ctx->launches++;
+      ctx->bytes_h2d += n16 * 16;
+      if (n % 16)
+        PD_CUDA(h2d(ctx, static_cast<uint8_t *>(dst) + n16 * 16, static_cast<const uint8_t *>(src) + n16 * 16, n % 16));
+      return PD_OK;
+    }
+    cudaGetLastError();  // a pointer the runtime does not know reports an error: clear it
+  }
+  PD_CUDA(h2d(ctx, dst, src, n));
+  return PD_OK;
+}
+
+}  // namespace pd
+
 extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
   PD_CHECK(ctx && name, PD_ERR_INVALID, "null argument");
   const std::string n(name);
@@ -159,6 +206,9 @@ extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
   } else if (n == "records") {
     PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "records must be 0 or 1");
     ctx->collect_records = value != 0;
+  } else if (n == "upload_copy") {
+    PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "upload_copy must be 0 (copy engine) or 1 (SM copy)");
+    ctx->upload_copy = (int)value;
   } else {
     return set_error(PD_ERR_INVALID, "unknown tuning knob '%s'", name);
   }
@@ -278,7 +328,7 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   PD_TRY(ctx->s_xy.ensure(S * 4 + 4));
   PD_TRY(ctx->s_img.ensure(S * 4 + 4));
   PD_TRY(ctx->s_label.ensure(S + 4));
-  PD_CUDA(h2d(ctx, ctx->pixels.ptr, ds->pixels, bytes));
+  PD_TRY(upload_bytes(ctx, ctx->pixels.ptr, ds->pixels, bytes));
   PD_TRY(map_training_pixels(ctx, bytes));
   PD_CUDA(h2d(ctx, ctx->img_off.ptr, off.data(), n * 8));
   PD_CUDA(h2d(ctx, ctx->img_wh.ptr, wh.data(), n * 4));

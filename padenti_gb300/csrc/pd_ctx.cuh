@@ -25,6 +25,7 @@ struct pd_ctx {
   uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
   bool cand_order = true;    // order each node's candidate columns by first-probe offset
   bool persist = false;      // one persistent histogram grid per launch, items pulled largest first
+  int upload_copy = 0;       // training images from pinned host memory: 0 copy engine, 1 SM copy kernel
   int n_sms = 0;             // multiprocessors of the context's GPU
   uint64_t sample_group = 512ull << 20;  // bytes of images + labels pd_sample stages per round trip
   bool collect_records = false;          // keep a pd_record per split node (learned proposals)
