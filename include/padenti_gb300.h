@@ -172,7 +172,10 @@ int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
  *               >= 4096 (default 512 MiB);
  *   "persist"   1: one persistent histogram grid per launch (a few CTAs per SM) pulling the work
  *               items from a device counter, largest first; 0 (default): one CTA per work item;
- *   "records"   1: training calls keep one pd_record per split node (pd_train_records); 0 (default): none. */
+ *   "records"   1: training calls keep one pd_record per split node (pd_train_records); 0 (default): none;
+ *   "upload_copy" 1 (default): training images in pinned host memory, and pd_sample's staged
+ *               batches, are copied to the device by an SM kernel reading over the host link;
+ *               0: by the copy engine (pageable memory always is). */
 int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value);
 /* The launch shape chosen by pd_autotune. */
 typedef struct {

@@ -154,10 +154,15 @@ static __global__ void __launch_bounds__(256) k_copy_from_host(const uint4 *__re
   for (; i < n16; i += stride) dst[i] = src[i];
 }
 
-// Host -> device copy of the training images: by the SMs when the source is
-// pinned host memory the device can address and both ends are 16-byte aligned
-// (upload_copy = 1), else by the copy engine.
-static int upload_bytes(pd_ctx *ctx, void *dst, const void *src, size_t n) {
+}  // namespace pd
+
+// Host -> device copy of bulk inputs (training images, staged sampler batches):
+// by the SMs when the source is pinned host memory the device can address and
+// both ends are 16-byte aligned (upload_copy = 1), else by the copy engine.  On
+// GB300 the copy engine's first large copy after the host link has been idle
+// for a few hundred milliseconds runs at ~30 GB/s instead of ~210 GB/s; the SM
+// copy does not slow down.
+int pd::upload_bytes(pd_ctx *ctx, void *dst, const void *src, size_t n) {
   if (ctx->upload_copy == 1 && n >= 16) {
     cudaPointerAttributes a;
     memset(&a, 0, sizeof(a));
@@ -179,8 +184,6 @@ static int upload_bytes(pd_ctx *ctx, void *dst, const void *src, size_t n) {
   PD_CUDA(h2d(ctx, dst, src, n));
   return PD_OK;
 }
-
-}  // namespace pd
 
 extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
   PD_CHECK(ctx && name, PD_ERR_INVALID, "null argument");

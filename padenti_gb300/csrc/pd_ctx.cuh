@@ -25,7 +25,7 @@ struct pd_ctx {
   uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
   bool cand_order = true;    // order each node's candidate columns by first-probe offset
   bool persist = false;      // one persistent histogram grid per launch, items pulled largest first
-  int upload_copy = 0;       // training images from pinned host memory: 0 copy engine, 1 SM copy kernel
+  int upload_copy = 1;       // bulk inputs from pinned host memory: 0 copy engine, 1 SM copy kernel
   int n_sms = 0;             // multiprocessors of the context's GPU
   uint64_t sample_group = 512ull << 20;  // bytes of images + labels pd_sample stages per round trip
   bool collect_records = false;          // keep a pd_record per split node (learned proposals)
@@ -129,6 +129,8 @@ struct PropSrc;
 // totals d_ctot [n][K] on the device), on the context's stream (pd_propose.cu).
 int proposer_infer(pd_proposer *p, const uint32_t *d_ctot, uint32_t n, uint32_t depth, uint32_t n_prop, PropSrc *src);
 int ensure_log2_table(pd_ctx *ctx, uint64_t n);
+// Host -> device copy of bulk inputs on the context's stream (pd_api.cu).
+int upload_bytes(pd_ctx *ctx, void *dst, const void *src, size_t n);
 int init_tables(pd_ctx *ctx);
 // Prepares the uploaded images for the plugin's eval_train (zero depths).
 int map_training_pixels(pd_ctx *ctx, uint64_t bytes);

@@ -853,7 +853,7 @@ extern "C" int pd_sample(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, co
     PD_TRY(ctx->sm_desc.ensure(lay.bytes));
     PD_TRY(ctx->sm_out.ensure(((uint64_t)n * stride + n) * 4 + 16));
     uint8_t *dd = ctx->sm_data.as<uint8_t>(), *dl = dd + data_cur;
-    PD_CUDA(h2d(ctx, dd, hd, data_cur + lab_cur));
+    PD_TRY(upload_bytes(ctx, dd, hd, data_cur + lab_cur));
     uint32_t *dout = ctx->sm_out.as<uint32_t>(), *dcnt = dout + (uint64_t)n * stride;
     PD_TRY(launch_batch(ctx, s, pl, n, dd, dl, dout, dcnt, lay, ctx->sm_desc.as<uint8_t>()));
     uint32_t err[2];

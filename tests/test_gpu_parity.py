@@ -338,3 +338,30 @@ def test_predict_rgb_bit_exact():
     g = clf.predict(px[0])
     o = ob.predict_posterior(ob.params(cfg, tp), px[0], None, [tree_tuple(tree)], n_channels=3)
     assert np.array_equal(g.view(np.uint32), o.view(np.uint32))
+
+
+def test_upload_from_pinned_memory_by_sm_copy():
+    """A training set in pinned host memory goes up through the SM copy kernel (the
+    default, upload_copy = 1) or the copy engine (0); both train the oracle's tree."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    from padenti_gb300 import _native as N
+
+    cfg, ts, tp, _ = depth_case(n_images=10, n_features=32, n_thresholds=10)
+    flat = ts.flat()
+    pinned = {k: torch.empty(max(1, v.nbytes), dtype=torch.uint8, pin_memory=True) for k, v in flat.items()}
+    for k, v in flat.items():
+        pinned[k].numpy()[: v.nbytes] = v.view(np.uint8).reshape(-1)
+    pf = {k: pinned[k].numpy()[: v.nbytes].view(v.dtype) for k, v in flat.items()}
+    o = ob.train_tree(ob.params(cfg, tp), ob.OracleSet(ts, cfg), 4, 6, ts.priors)
+    prior = np.ascontiguousarray(ts.priors, np.float32)
+    for mode in (1, 0):
+        tr = pg.TreeTrainer(cfg)
+        N.check(N.lib().pd_ctx_set_tuning(tr.h, b"upload_copy", mode))
+        N.check(N.lib().pd_dataset_upload(tr.h, C.byref(pg.TrainingSet.desc(pf))))
+        t = pg.Tree(cfg, 4, 6)
+        N.check(N.lib().pd_train_tree(tr.h, C.byref(tp.c()), 4, 1, 6, prior.ctypes.data, t.left_child.ctypes.data,
+                                      t.features.ctypes.data, t.thresholds.ctypes.data, t.posteriors.ctypes.data))
+        assert np.array_equal(t.left_child, o["left_child"]), mode
+        assert np.array_equal(np.asarray(t.features, np.int32), o["features"]), mode
+        assert np.array_equal(t.posteriors.view(np.uint32), o["posteriors"].view(np.uint32)), mode
