@@ -115,6 +115,16 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
   ctx->sm_out.release();
   ctx->h_sm.release();
   ctx->h_sm_desc.release();
+  for (auto &sl : ctx->samp) {
+    sl.h_data.release();
+    sl.h_desc.release();
+    sl.h_out.release();
+    sl.d_data.release();
+    sl.d_desc.release();
+    sl.d_out.release();
+    for (cudaEvent_t &e : sl.ev)
+      if (e) cudaEventDestroy(e);
+  }
   ctx->lab_tab.release();
   ctx->lab_src.release();
   ctx->lab_dst.release();

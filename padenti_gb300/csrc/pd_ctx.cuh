@@ -102,6 +102,14 @@ struct pd_ctx {
   pd::DevBuf sm_desc;            // SampImage per image, item -> image map, checksums, counts, error
   pd::DevBuf sm_out;             // samples and counts of a host batch
   pd::HostBuf h_sm, h_sm_desc;   // pinned staging of a host batch and of its descriptors
+  // pd_sample's two pipeline slots: a group is staged into one while the device
+  // works on the other's (pinned data, descriptors, results; device copies; events
+  // around the scan, the draws and the results)
+  struct SampSlot {
+    pd::HostBuf h_data, h_desc, h_out;
+    pd::DevBuf d_data, d_desc, d_out;
+    cudaEvent_t ev[4] = {};
+  } samp[2];
   pd_sample_stats sample_stats{};
   // ---- label images (pd_rgb_to_labels*) ----
   pd::DevBuf lab_tab, lab_src, lab_dst;

@@ -670,9 +670,9 @@ const uint32_t *shift_constants() {
 // Uploads the descriptor block and launches the two kernels on a batch that is
 // in device memory.  counts/err stay on the device.
 int launch_batch(pd_ctx *ctx, const pd_sampler *s, const SamplerPlan &pl, uint32_t n, const uint8_t *data, const uint8_t *labels, uint32_t *out, uint32_t *counts, const DescLayout &lay,
-                 uint8_t *dev_desc) {
+                 uint8_t *dev_desc, const void *host_desc, cudaEvent_t *ev) {
   cudaStream_t st = ctx->stream;
-  PD_CUDA(h2d(ctx, dev_desc, ctx->h_sm_desc.ptr, lay.bytes));
+  PD_CUDA(h2d(ctx, dev_desc, host_desc, lay.bytes));
   const SampImage *imgs = reinterpret_cast<const SampImage *>(dev_desc + lay.imgs);
   const uint32_t *item_img = reinterpret_cast<const uint32_t *>(dev_desc + lay.items);
   uint32_t *crc = reinterpret_cast<uint32_t *>(dev_desc + lay.crc);
@@ -682,12 +682,12 @@ int launch_batch(pd_ctx *ctx, const pd_sampler *s, const SamplerPlan &pl, uint32
   PD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
   PD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sample_scan, kSmThreads, 0));
   const uint32_t grid = std::max(1u, std::min<uint32_t>(lay.n_items, (uint32_t)(sms * std::max(per_sm, 1))));
-  PD_CUDA(cudaEventRecord(ctx->ev[0], st));
+  PD_CUDA(cudaEventRecord(ev[0], st));
   k_sample_scan<<<grid, kSmThreads, 0, st>>>(data, labels, imgs, item_img, lay.n_items, lay.n_crc_items,
                                              reinterpret_cast<const uint32_t *>(dev_desc + lay.shifts), crc, cnt,
                                              err + 2);
   PD_CUDA(cudaGetLastError());
-  PD_CUDA(cudaEventRecord(ctx->ev[1], st));
+  PD_CUDA(cudaEventRecord(ev[1], st));
   if (s->kind == PD_SAMPLER_UNIFORM) {
     const size_t smem = (size_t)pl.sort_n * 4;
     PD_CUDA(cudaFuncSetAttribute(k_sample_uniform, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -701,7 +701,7 @@ int launch_batch(pd_ctx *ctx, const pd_sampler *s, const SamplerPlan &pl, uint32
                                                          s->n_classes, pl.stride, s->seed, pl.sort_n, out, counts, err);
   }
   PD_CUDA(cudaGetLastError());
-  PD_CUDA(cudaEventRecord(ctx->ev[2], st));
+  PD_CUDA(cudaEventRecord(ev[2], st));
   ctx->launches += 2;
   ctx->sample_stats.kernel_launches += 2;
   return PD_OK;
@@ -715,7 +715,7 @@ struct ImagePlace {
   uint32_t n_pix;
 };
 
-int fill_desc(pd_ctx *ctx, const SamplerPlan &pl, const std::vector<ImagePlace> &place, DescLayout *lay_out) {
+int fill_desc(HostBuf &hb, const SamplerPlan &pl, const std::vector<ImagePlace> &place, DescLayout *lay_out) {
   const uint32_t n = (uint32_t)place.size();
   uint64_t n_crc = 0, n_lab = 0;
   std::vector<uint32_t> slices(n), chunks(n);
@@ -728,8 +728,8 @@ int fill_desc(pd_ctx *ctx, const SamplerPlan &pl, const std::vector<ImagePlace> 
   PD_CHECK(n_crc + n_lab < (1ull << 31), PD_ERR_UNSUPPORTED, "batch too large");
   DescLayout lay(n, (uint32_t)(n_crc + n_lab), (uint32_t)pl.bucket.size());
   lay.n_crc_items = (uint32_t)n_crc;
-  PD_TRY(ctx->h_sm_desc.ensure(lay.bytes));
-  uint8_t *h = ctx->h_sm_desc.as<uint8_t>();
+  PD_TRY(hb.ensure(lay.bytes));
+  uint8_t *h = hb.as<uint8_t>();
   SampImage *im = reinterpret_cast<SampImage *>(h + lay.imgs);
   uint32_t *item_img = reinterpret_cast<uint32_t *>(h + lay.items);
   uint32_t *crc = reinterpret_cast<uint32_t *>(h + lay.crc);
@@ -804,11 +804,17 @@ extern "C" int pd_sample(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, co
   PD_CUDA(cudaSetDevice(ctx->device));
   const uint64_t h2d0 = ctx->bytes_h2d, d2h0 = ctx->bytes_d2h;
   // groups of images whose staged bytes stay below a bound
-  const uint64_t kGroupBytes = ctx->sample_group;
-  uint32_t first = 0;
-  while (first < n_images) {
+  struct Group {
+    uint32_t first, n;
+    uint64_t data_cur, lab_cur;
     std::vector<ImagePlace> place;
-    uint64_t data_cur = 0, lab_cur = 0;
+  };
+  std::vector<Group> groups;
+  const uint64_t kGroupBytes = ctx->sample_group;
+  for (uint32_t first = 0; first < n_images;) {
+    Group g;
+    g.first = first;
+    g.data_cur = g.lab_cur = 0;
     uint32_t last = first;
     for (; last < n_images; last++) {
       PD_CHECK(images[last] && labels[last], PD_ERR_INVALID, "image %u has a null buffer", last);
@@ -821,19 +827,63 @@ extern "C" int pd_sample(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, co
       // checksum reads 256-byte blocks counted from the end)
       const uint64_t pad = (256 - db % 256) % 256;
       const uint64_t dsz = pad + db, lsz = (np + 15) / 16 * 16;
-      if (last > first && data_cur + dsz + lab_cur + lsz > kGroupBytes) break;
-      place.push_back(ImagePlace{data_cur, data_cur + dsz, lab_cur, (uint64_t)(last - first) * stride, db, (uint32_t)np});
-      data_cur += dsz;
-      lab_cur += lsz;
+      if (last > first && g.data_cur + dsz + g.lab_cur + lsz > kGroupBytes) break;
+      g.place.push_back(
+          ImagePlace{g.data_cur, g.data_cur + dsz, g.lab_cur, (uint64_t)(last - first) * stride, db, (uint32_t)np});
+      g.data_cur += dsz;
+      g.lab_cur += lsz;
     }
-    const uint32_t n = last - first;
+    g.n = last - first;
+    groups.push_back(std::move(g));
+    first = last;
+  }
+  // Two slots: the host stages group k into one while the device copies, scans
+  // and draws group k - 1 from the other; a slot's results come back to its
+  // pinned buffer and reach the caller when the slot is reused or at the end.
+  PD_CUDA(cudaStreamSynchronize(ctx->stream));  // no earlier call still reads a slot
+  for (auto &sl : ctx->samp)
+    for (cudaEvent_t &e : sl.ev)
+      if (!e) PD_CUDA(cudaEventCreate(&e));
+  int busy[2] = {-1, -1};
+  DescLayout lays[2];
+  auto finish = [&](int si) -> int {
+    pd_ctx::SampSlot &sl = ctx->samp[si];
+    const Group &g = groups[busy[si]];
+    busy[si] = -1;
+    PD_CUDA(cudaEventSynchronize(sl.ev[3]));
+    const uint32_t *ho = sl.h_out.as<uint32_t>();
+    const uint32_t *err = ho + (uint64_t)g.n * stride + g.n;
+    PD_TRY(check_errors(err, g.first, s));
+    std::memcpy(samples + (uint64_t)g.first * stride, ho, (uint64_t)g.n * stride * 4);
+    std::memcpy(counts + g.first, ho + (uint64_t)g.n * stride, (uint64_t)g.n * 4);
+    ctx->sample_stats.ms_scan += event_ms(sl.ev[0], sl.ev[1]);
+    ctx->sample_stats.ms_draw += event_ms(sl.ev[1], sl.ev[2]);
+    for (const ImagePlace &p : g.place) {
+      ctx->sample_stats.data_bytes += p.data_bytes;
+      ctx->sample_stats.label_bytes += p.n_pix;
+    }
+    return PD_OK;
+  };
+  auto fail = [&](int rc) {  // nothing of a failed call stays in flight
+    cudaStreamSynchronize(ctx->stream);
+    return rc;
+  };
+  for (size_t k = 0; k < groups.size(); k++) {
+    const int si = (int)(k % 2);
+    pd_ctx::SampSlot &sl = ctx->samp[si];
+    if (busy[si] >= 0) {
+      const int rc = finish(si);
+      if (rc != PD_OK) return fail(rc);
+    }
+    const Group &g = groups[k];
+    const uint32_t n = g.n, first = g.first;
     // staging: data then labels, each image's zero padding included
-    PD_TRY(ctx->h_sm.ensure(data_cur + lab_cur + 16));
-    uint8_t *hd = ctx->h_sm.as<uint8_t>(), *hl = hd + data_cur;
+    PD_TRY(sl.h_data.ensure(g.data_cur + g.lab_cur + 16));
+    uint8_t *hd = sl.h_data.as<uint8_t>(), *hl = hd + g.data_cur;
     const unsigned nt = std::max(1u, std::min({16u, std::thread::hardware_concurrency(), n}));
     auto work = [&](unsigned th) {
       for (uint32_t i = th; i < n; i += nt) {
-        const ImagePlace &p = place[i];
+        const ImagePlace &p = g.place[i];
         const uint64_t pad = p.data_end - p.data_lo - p.data_bytes;
         std::memset(hd + p.data_lo, 0, pad);
         std::memcpy(hd + p.data_lo + pad, images[first + i], p.data_bytes);
@@ -843,32 +893,37 @@ extern "C" int pd_sample(pd_ctx *ctx, const pd_sampler *s, uint32_t n_images, co
     };
     {
       std::vector<std::thread> th;
-      for (unsigned k = 1; k < nt; k++) th.emplace_back(work, k);
+      for (unsigned q = 1; q < nt; q++) th.emplace_back(work, q);
       work(0);
       for (auto &x : th) x.join();
     }
-    DescLayout lay;
-    PD_TRY(fill_desc(ctx, pl, place, &lay));
-    PD_TRY(ctx->sm_data.ensure(data_cur + lab_cur + 16));
-    PD_TRY(ctx->sm_desc.ensure(lay.bytes));
-    PD_TRY(ctx->sm_out.ensure(((uint64_t)n * stride + n) * 4 + 16));
-    uint8_t *dd = ctx->sm_data.as<uint8_t>(), *dl = dd + data_cur;
-    PD_TRY(upload_bytes(ctx, dd, hd, data_cur + lab_cur));
-    uint32_t *dout = ctx->sm_out.as<uint32_t>(), *dcnt = dout + (uint64_t)n * stride;
-    PD_TRY(launch_batch(ctx, s, pl, n, dd, dl, dout, dcnt, lay, ctx->sm_desc.as<uint8_t>()));
-    uint32_t err[2];
-    PD_CUDA(d2h(ctx, samples + (uint64_t)first * stride, dout, (uint64_t)n * stride * 4));
-    PD_CUDA(d2h(ctx, counts + first, dcnt, (uint64_t)n * 4));
-    PD_CUDA(d2h(ctx, err, ctx->sm_desc.as<uint8_t>() + lay.err, 8));
-    PD_CUDA(cudaStreamSynchronize(ctx->stream));
-    PD_TRY(check_errors(err, first, s));
-    ctx->sample_stats.ms_scan += event_ms(ctx->ev[0], ctx->ev[1]);
-    ctx->sample_stats.ms_draw += event_ms(ctx->ev[1], ctx->ev[2]);
-    for (const ImagePlace &p : place) {
-      ctx->sample_stats.data_bytes += p.data_bytes;
-      ctx->sample_stats.label_bytes += p.n_pix;
+    DescLayout &lay = lays[si];
+    PD_TRY(fill_desc(sl.h_desc, pl, g.place, &lay));
+    PD_TRY(sl.d_data.ensure(g.data_cur + g.lab_cur + 16));
+    PD_TRY(sl.d_desc.ensure(lay.bytes));
+    const uint64_t out_words = (uint64_t)n * stride + n;
+    PD_TRY(sl.d_out.ensure(out_words * 4 + 16));
+    PD_TRY(sl.h_out.ensure(out_words * 4 + 16));
+    uint8_t *dd = sl.d_data.as<uint8_t>(), *dl = dd + g.data_cur;
+    int rc = upload_bytes(ctx, dd, hd, g.data_cur + g.lab_cur);
+    uint32_t *dout = sl.d_out.as<uint32_t>(), *dcnt = dout + (uint64_t)n * stride;
+    if (rc == PD_OK) rc = launch_batch(ctx, s, pl, n, dd, dl, dout, dcnt, lay, sl.d_desc.as<uint8_t>(),
+                                       sl.h_desc.ptr, sl.ev);
+    if (rc != PD_OK) return fail(rc);
+    // samples, counts and the two error words into the slot's pinned buffer
+    uint32_t *ho = sl.h_out.as<uint32_t>();
+    PD_CUDA(d2h(ctx, ho, dout, out_words * 4));
+    PD_CUDA(d2h(ctx, ho + out_words, sl.d_desc.as<uint8_t>() + lay.err, 8));
+    PD_CUDA(cudaEventRecord(sl.ev[3], ctx->stream));
+    busy[si] = (int)k;
+  }
+  // the last two groups, in order
+  for (size_t k = groups.size() >= 2 ? groups.size() - 2 : 0; k < groups.size(); k++) {
+    const int si = (int)(k % 2);
+    if (busy[si] == (int)k) {
+      const int rc = finish(si);
+      if (rc != PD_OK) return fail(rc);
     }
-    first = last;
   }
   ctx->sample_stats.images = n_images;
   ctx->sample_stats.h2d_bytes = ctx->bytes_h2d - h2d0;
@@ -902,10 +957,10 @@ extern "C" int pd_sample_device(pd_ctx *ctx, const pd_sampler *s, uint32_t n_ima
   for (uint32_t i = 0; i < n_images; i++)
     place[i] = ImagePlace{i * db, (i + 1) * db, i * np, (uint64_t)i * stride, db, (uint32_t)np};
   DescLayout lay;
-  PD_TRY(fill_desc(ctx, pl, place, &lay));
+  PD_TRY(fill_desc(ctx->h_sm_desc, pl, place, &lay));
   PD_TRY(ctx->sm_desc.ensure(lay.bytes));
   PD_TRY(launch_batch(ctx, s, pl, n_images, static_cast<const uint8_t *>(images_device), labels_device,
-                      samples_device, counts_device, lay, ctx->sm_desc.as<uint8_t>()));
+                      samples_device, counts_device, lay, ctx->sm_desc.as<uint8_t>(), ctx->h_sm_desc.ptr, ctx->ev));
   uint32_t err[2];
   PD_CUDA(d2h(ctx, err, ctx->sm_desc.as<uint8_t>() + lay.err, 8));
   PD_CUDA(cudaStreamSynchronize(ctx->stream));
