@@ -288,7 +288,7 @@ def sampler_bench(a, pg, N, px, lb):
         ms_scan, ms_draw = float(np.median(scan)), float(np.median(draw))
         scan_bytes = n * a.width * a.height * 3  # image bytes (2 per pixel) + label bytes (1 per pixel)
         # host buffers in, samples out
-        imgs, lbs = [px[i] for i in range(n)], [lb[i] for i in range(n)]
+        imgs, lbs = px[:n], lb[:n]  # the stacked-array form of sample_batch
         sm.sample_batch(imgs, lbs)
         t0 = time.perf_counter()
         e_reps = 2

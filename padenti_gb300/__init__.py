@@ -619,31 +619,51 @@ class ImageSampler:
     def sample(self, data: np.ndarray, labels: np.ndarray) -> np.ndarray:
         return self.sample_batch([data], [labels])[0]
 
-    def sample_batch(self, images: list, labels: list) -> list:
+    def sample_batch(self, images, labels) -> list:
+        """Samples of many images: lists of images and label images of any sizes, or one
+        array of N same-size images ([N][H][W] or [N][H][W][C]) and one [N][H][W] label
+        array.  Returns one index array per image (views into one result buffer)."""
         n = len(images)
         if n != len(labels):
             raise ValueError("one label image per image")
-        imgs = [np.ascontiguousarray(a) for a in images]
-        lbs = [np.ascontiguousarray(a, np.uint8) for a in labels]
         if n == 0:
             return []
-        pb = {a.nbytes // max(a.shape[0] * a.shape[1], 1) for a in imgs}
-        if len(pb) != 1:
-            raise ValueError("all images of a batch need the same pixel type and channel count")
-        for a, lb in zip(imgs, lbs):
-            if a.shape[:2] != lb.shape:
-                raise ValueError(f"image {a.shape[:2]} and labels {lb.shape} differ in size")
         stride = self.stride
+        if isinstance(images, np.ndarray) and isinstance(labels, np.ndarray) and images.ndim >= 3:
+            # stacked same-size images: pointers by arithmetic, no per-image Python work
+            imgs = np.ascontiguousarray(images)
+            lbs = np.ascontiguousarray(labels, np.uint8)
+            if lbs.ndim != 3 or imgs.shape[:3] != lbs.shape:
+                raise ValueError(f"images {imgs.shape} and labels {lbs.shape} differ in size")
+            H, W = lbs.shape[1], lbs.shape[2]
+            pixel_bytes = imgs[0].nbytes // max(H * W, 1)
+            iptr = imgs.ctypes.data + np.arange(n, dtype=np.uint64) * np.uint64(imgs[0].nbytes)
+            lptr = lbs.ctypes.data + np.arange(n, dtype=np.uint64) * np.uint64(H * W)
+            w = np.full(n, W, np.uint32)
+            h = np.full(n, H, np.uint32)
+            keep = (imgs, lbs)
+        else:
+            imgs = [np.ascontiguousarray(a) for a in images]
+            lbs = [np.ascontiguousarray(a, np.uint8) for a in labels]
+            pb = {a.nbytes // max(a.shape[0] * a.shape[1], 1) for a in imgs}
+            if len(pb) != 1:
+                raise ValueError("all images of a batch need the same pixel type and channel count")
+            pixel_bytes = pb.pop()
+            for a, lb in zip(imgs, lbs):
+                if a.shape[:2] != lb.shape:
+                    raise ValueError(f"image {a.shape[:2]} and labels {lb.shape} differ in size")
+            iptr = np.array([a.ctypes.data for a in imgs], np.uint64)
+            lptr = np.array([a.ctypes.data for a in lbs], np.uint64)
+            w = np.array([a.shape[1] for a in lbs], np.uint32)
+            h = np.array([a.shape[0] for a in lbs], np.uint32)
+            keep = (imgs, lbs)
         out = np.zeros((n, max(stride, 1)), np.uint32)
         counts = np.zeros(n, np.uint32)
-        iptr = (C.c_void_p * n)(*[a.ctypes.data for a in imgs])
-        lptr = (C.c_void_p * n)(*[a.ctypes.data for a in lbs])
-        w = np.array([a.shape[1] for a in lbs], np.uint32)
-        h = np.array([a.shape[0] for a in lbs], np.uint32)
         with _SAMPLER_LOCK:
-            check(lib().pd_sample(_sampler_ctx(self.device), C.byref(self._c(pb.pop())), n, iptr, lptr, _ptr(w),
-                                  _ptr(h), max(stride, 1), _ptr(out), _ptr(counts)))
-        return [out[i, :counts[i]].copy() for i in range(n)]
+            check(lib().pd_sample(_sampler_ctx(self.device), C.byref(self._c(pixel_bytes)), n, _ptr(iptr), _ptr(lptr),
+                                  _ptr(w), _ptr(h), max(stride, 1), _ptr(out), _ptr(counts)))
+        del keep
+        return [row[:c] for row, c in zip(out, counts.tolist())]
 
     def _read_stats(self) -> dict:
         st = N.SampleStats()

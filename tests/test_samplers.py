@@ -124,6 +124,8 @@ def test_gpu_sampler_groups_and_device_entry():
     N.check(N.lib().pd_ctx_set_tuning(h, b"sample_group", 200000))  # two images per group
     try:
         assert all(np.array_equal(a, b) for a, b in zip(ref, s.sample_batch(list(px), list(lb))))
+        # the stacked-array form, through the two pipeline slots
+        assert all(np.array_equal(a, b) for a, b in zip(ref, s.sample_batch(px, lb)))
     finally:
         N.check(N.lib().pd_ctx_set_tuning(h, b"sample_group", 512 << 20))
     dpx = torch.from_numpy(px.view(np.int16)).cuda()
