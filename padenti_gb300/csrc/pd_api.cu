@@ -101,7 +101,7 @@ extern "C" int pd_ctx_destroy(pd_ctx *ctx) {
                     &ctx->t_feat, &ctx->t_thr, &ctx->t_post, &ctx->f_lc, &ctx->f_feat, &ctx->f_thr,
                     &ctx->f_post, &ctx->f_meta, &ctx->f_cand, &ctx->p_img, &ctx->p_mask, &ctx->p_out,
                     &ctx->nm_map[0], &ctx->nm_map[1], &ctx->nm_off, &ctx->nm_label, &ctx->np_map[0],
-                    &ctx->np_map[1], &ctx->np_desc};
+                    &ctx->np_map[1], &ctx->np_desc, &ctx->f_fast};
   for (DevBuf *b : bufs) b->release();
   if (ctx->batch_graph) cudaGraphExecDestroy(ctx->batch_graph);
   ctx->b_img.release();

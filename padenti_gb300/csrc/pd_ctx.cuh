@@ -89,6 +89,8 @@ struct pd_ctx {
   pd::DevBuf f_lc, f_feat, f_thr, f_post, f_meta;
   pd::DevBuf f_cand;                   // P::Cand of every forest node (k_forest_cands)
   uint64_t cand_version = ~0ull;       // forest_version f_cand was built for
+  bool forest_fast = false;            // every node takes the plugin's fast path (built-in plugins)
+  pd::DevBuf f_fast;                   // its device flag
   pd::DevBuf p_img, p_mask, p_out;     // staging for host-buffer prediction
   uint64_t forest_version = 0;         // bumped when the forest arrays are uploaded again
   // mixed-size prediction batches: buffers, the layout they were built for and

@@ -72,7 +72,16 @@ static int ensure_forest_cands(pd_ctx *ctx) {
   } else if constexpr (!P::kRtcOnly) {
     k_forest_cands<P><<<grid, 256, 0, ctx->stream>>>(ft, nodes, ctx->f_cand.as<typename P::Cand>());
     PD_CUDA(cudaGetLastError());
-    ctx->launches++;
+    // whether every node takes the fast path: the prediction kernels then carry no slow path
+    PD_TRY(ctx->f_fast.ensure(16));
+    int all = 1;
+    PD_CUDA(h2d(ctx, ctx->f_fast.ptr, &all, 4));
+    k_forest_fast<P><<<grid, 256, 0, ctx->stream>>>(ctx->f_cand.as<typename P::Cand>(), nodes, ctx->f_fast.as<int>());
+    PD_CUDA(cudaGetLastError());
+    PD_CUDA(d2h(ctx, &all, ctx->f_fast.ptr, 4));
+    PD_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->forest_fast = all != 0;
+    ctx->launches += 2;
   }
   ctx->cand_version = ctx->forest_version;
   return PD_OK;
@@ -104,8 +113,9 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
     return rtc_launch(ctx, rk->predict_posterior, grid, dim3(kPredX, kPredY), smem, args);
   }
   if constexpr (!P::kRtcOnly) {
-    PD_CUDA(cudaFuncSetAttribute(k_predict_posterior<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_predict_posterior<P><<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
+    auto kern = ctx->forest_fast ? k_predict_posterior<P, true> : k_predict_posterior<P, false>;
+    PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
         static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_lc.as<int32_t>(),
         ctx->f_cand.as<typename P::Cand>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(),
         ctx->f_meta.as<TreeMeta>(), nt, (uint32_t)ctx->cfg.n_classes, ctx->magic_tab.as<uint32_t>());
@@ -376,8 +386,9 @@ extern "C" int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *c
         PD_TRY(rtc_set_smem(ctx, rk->predict_batch, smem));
         fn = (const void *)rk->predict_batch;
       } else if constexpr (!P::kRtcOnly) {
-        fn = (const void *)k_predict_batch<P>;
-        PD_CUDA(cudaFuncSetAttribute(k_predict_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        auto kern = ctx->forest_fast ? k_predict_batch<P, true> : k_predict_batch<P, false>;
+        fn = (const void *)kern;
+        PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       }
       cudaGraph_t g = nullptr;
       PD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -450,7 +461,8 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
       return rtc_launch(ctx, rk->predict_leaf, grid, dim3(kPredX, kPredY), 0, args);
     }
     if constexpr (!P::kRtcOnly) {
-      k_predict_leaf<P><<<grid, dim3(kPredX, kPredY), 0, st>>>(
+      auto kern = ctx->forest_fast ? k_predict_leaf<P, true> : k_predict_leaf<P, false>;
+      kern<<<grid, dim3(kPredX, kPredY), 0, st>>>(
           ctx->p_img.as<uint8_t>(), width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
           ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_cand.as<typename P::Cand>() + off,
           ctx->f_thr.as<FeatT>() + off, depth, ctx->magic_tab.as<uint32_t>());

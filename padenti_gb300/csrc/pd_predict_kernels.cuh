@@ -24,7 +24,9 @@ constexpr int kPredGroup = PD_PRED_GROUP;
 // Leaf reached by one tree from the root; cand holds P::candidate of every
 // node's features (k_forest_cands), so a visit loads the node's constants
 // instead of deriving them.
-template <class P>
+// AF: every node of the forest takes the plugin's fast path (P::fast, checked
+// once per forest upload), so the walk carries no per-visit test or slow path.
+template <class P, bool AF = false>
 PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
                   const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
                   uint32_t depth) {
@@ -34,7 +36,7 @@ PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
     const int32_t c = ldg(lc + node);
     if (c < 0) break;  // leaf (-1); an untrained root (-2) also stops
     const typename P::Cand cd = cand[node];
-    const FeatT r = P::fast(cd) ? P::template eval<true>(prep, cd) : P::template eval<false>(prep, cd);
+    const FeatT r = (AF || P::fast(cd)) ? P::template eval<true>(prep, cd) : P::template eval<false>(prep, cd);
     node = c + (r <= ldg(thr + node) ? 0 : 1);
   }
   return node;
@@ -48,10 +50,18 @@ __global__ void k_forest_cands(const typename P::feat_t *__restrict__ feat, unsi
   if (i < n_nodes) cand[i] = P::candidate(feat + i * P::kFeatDim);
 }
 
+// Clears *all_fast when a node of the forest needs the plugin's slow path.
+template <class P>
+__global__ void k_forest_fast(const typename P::Cand *__restrict__ cand, unsigned long long n_nodes,
+                              int *__restrict__ all_fast) {
+  const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+  if (i < n_nodes && !P::fast(cand[i])) *all_fast = 0;
+}
+
 // The leaves of trees t0 .. t0+G-1 (those below n_trees) for one pixel, the G
 // walks interleaved level by level so that their loads overlap; each walk is
 // the one walk() does.
-template <class P, int G>
+template <class P, int G, bool AF = false>
 PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ lc,
                      const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
                      const TreeMeta *__restrict__ meta, uint32_t t0, uint32_t n_trees, int32_t *leaf_s,
@@ -80,7 +90,7 @@ PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ l
         continue;
       }
       const typename P::Cand cd = cand[off[g] + node[g]];
-      const FeatT r = P::fast(cd) ? P::template eval<true>(prep, cd) : P::template eval<false>(prep, cd);
+      const FeatT r = (AF || P::fast(cd)) ? P::template eval<true>(prep, cd) : P::template eval<false>(prep, cd);
       node[g] = c + (r <= ldg(thr + off[g] + node[g]) ? 0 : 1);
       if (d + 1 >= depth[g]) live &= ~(1u << g);
     }
@@ -93,7 +103,7 @@ PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ l
 // The forest posterior of pixel (x, y): the leaf of every tree (kept in the
 // CTA's leaf_s, [tree][thread]), then the leaf posteriors summed in tree order
 // and divided by the tree count, written planar with stride plane.
-template <class P>
+template <class P, bool AF = false>
 PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint32_t y, bool masked_out, float *o,
                         size_t plane, const int32_t *__restrict__ lc, const typename P::Cand *__restrict__ cand,
                         const typename P::feat_t *__restrict__ thr, const float *__restrict__ post,
@@ -105,7 +115,7 @@ PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint3
   }
   const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
   for (uint32_t t = 0; t < n_trees; t += kPredGroup)
-    walk_group<P, kPredGroup>(prep, lc, cand, thr, meta, t, n_trees, leaf_s, tid);
+    walk_group<P, kPredGroup, AF>(prep, lc, cand, thr, meta, t, n_trees, leaf_s, tid);
   const float nt = (float)n_trees;
   for (uint32_t l = 0; l < K; l++) {
     float acc = 0.0f;
@@ -116,7 +126,7 @@ PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint3
 }
 
 // grid (ceil(W/32), ceil(H/8), n_images); dynamic smem n_trees*256 int32.
-template <class P>
+template <class P, bool AF = false>
 __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
     const uint8_t *__restrict__ images, uint64_t img_bytes, uint32_t W, uint32_t H,
     const uint8_t *__restrict__ masks, float *__restrict__ out, const int32_t *__restrict__ lc,
@@ -134,7 +144,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
   im.w = (int32_t)W;
   im.h = (int32_t)H;
   im.magic = magic;
-  predict_pixel<P>(im, x, y, masks && !masks[(size_t)z * P_ + pix], out + (size_t)z * K * P_ + pix, P_, lc, cand,
+  predict_pixel<P, AF>(im, x, y, masks && !masks[(size_t)z * P_ + pix], out + (size_t)z * K * P_ + pix, P_, lc, cand,
                    thr, post, meta, n_trees, K, leaf_s, tid);
 }
 
@@ -148,7 +158,7 @@ struct BatchImage {
 
 // A mixed-size batch in one launch: CTA b serves tile b of the concatenated
 // tile lists (32x8 pixels; its image found by binary search over tile0).
-template <class P>
+template <class P, bool AF = false>
 __global__ void __launch_bounds__(kPredThreads) k_predict_batch(
     const uint8_t *__restrict__ images, const uint8_t *__restrict__ masks, uint8_t *__restrict__ out,
     const BatchImage *__restrict__ batch, uint32_t n, const int32_t *__restrict__ lc,
@@ -175,11 +185,11 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_batch(
   im.h = (int32_t)b.h;
   im.magic = magic;
   const bool masked_out = b.has_mask && !masks[b.mask_off + pix];
-  predict_pixel<P>(im, x, y, masked_out, reinterpret_cast<float *>(out + b.out_off) + pix, P_, lc, cand, thr, post,
+  predict_pixel<P, AF>(im, x, y, masked_out, reinterpret_cast<float *>(out + b.out_off) + pix, P_, lc, cand, thr, post,
                    meta, n_trees, K, leaf_s, tid);
 }
 
-template <class P>
+template <class P, bool AF = false>
 __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__restrict__ image, uint32_t W,
                                                                uint32_t H, const uint8_t *__restrict__ mask,
                                                                int32_t *__restrict__ out,
@@ -200,7 +210,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__
   im.w = (int32_t)W;
   im.h = (int32_t)H;
   im.magic = magic;
-  out[pix] = walk<P>(P::prepare(im, (int32_t)x, (int32_t)y), lc, cand, thr, depth);
+  out[pix] = walk<P, AF>(P::prepare(im, (int32_t)x, (int32_t)y), lc, cand, thr, depth);
 }
 
 // One step of the per-pixel node map of features that read the tree
