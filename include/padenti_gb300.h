@@ -173,6 +173,8 @@ int pd_ctx_set_hist_budget(pd_ctx *ctx, uint64_t bytes);
  *   "persist"   1: one persistent histogram grid per launch (a few CTAs per SM) pulling the work
  *               items from a device counter, largest first; 0 (default): one CTA per work item;
  *   "records"   1: training calls keep one pd_record per split node (pd_train_records); 0 (default): none;
+ *   "cand_regs" 1 (default): each candidate's thresholds are sorted in registers (at most 64
+ *               thresholds, ranges below 2^24); 0: by insertion in shared memory (same tables);
  *   "upload_copy" 1 (default): training images in pinned host memory, and pd_sample's staged
  *               batches, are copied to the device by an SM kernel reading over the host link;
  *               0: by the copy engine (pageable memory always is). */

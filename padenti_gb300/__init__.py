@@ -323,7 +323,8 @@ class TreeTrainer(_Ctx):
             check(lib().pd_ctx_set_hist_budget(self.h, hist_budget))
 
     def set_tuning(self, name: str, value: int) -> None:
-        """Launch-shape knob of the histogram kernel ("chunk", "hist_spi", "fuse_max", "cand_order"); results do not change."""
+        """A knob of pd_ctx_set_tuning: launch shapes ("chunk", "hist_spi", "fuse_max", "cand_order", "persist",
+        "cand_regs", "upload_copy"; results do not change) or "records" (keep split records)."""
         check(lib().pd_ctx_set_tuning(self.h, name.encode(), int(value)))
 
     def autotune(self, ts: TrainingSet, params: TreeTrainerParameters, end_depth: int, cache: str | None = None,

@@ -219,6 +219,9 @@ extern "C" int pd_ctx_set_tuning(pd_ctx *ctx, const char *name, int64_t value) {
   } else if (n == "records") {
     PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "records must be 0 or 1");
     ctx->collect_records = value != 0;
+  } else if (n == "cand_regs") {
+    PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "cand_regs must be 0 or 1");
+    ctx->cand_regs = value != 0;
   } else if (n == "upload_copy") {
     PD_CHECK(value == 0 || value == 1, PD_ERR_INVALID, "upload_copy must be 0 (copy engine) or 1 (SM copy)");
     ctx->upload_copy = (int)value;

@@ -24,6 +24,7 @@ struct pd_ctx {
   uint32_t hist_spi = 8;  // samples per iteration of the histogram kernel (2, 4 or 8)
   uint32_t fuse_max = 4096;  // nodes with at most this many samples get the fused split
   bool cand_order = true;    // order each node's candidate columns by first-probe offset
+  bool cand_regs = true;     // candidate keys sorted in registers (T <= 64), else in shared memory
   bool persist = false;      // one persistent histogram grid per launch, items pulled largest first
   int upload_copy = 1;       // bulk inputs from pinned host memory: 0 copy engine, 1 SM copy kernel
   int n_sms = 0;             // multiprocessors of the context's GPU

@@ -205,11 +205,12 @@ static int launch_candidates(pd_ctx *ctx, const pd_train_params *p, uint32_t tre
   const bool packed = span >= 0 && span < (1 << 24) && (sizeof(FeatT) == 4 || span <= 32767);
   const unsigned grid = (unsigned)((total + kCandThreads - 1) / kCandThreads);
   const uint32_t T = p->n_thresholds;
-  if (!prop && packed && T <= 64) {
-    // MD5 candidates, keys sorted in registers
+  if (packed && T <= 64 && ctx->cand_regs) {
+    // keys sorted in registers
     auto rk = T <= 16 ? k_candidates_reg<FeatT, 16> : (T <= 32 ? k_candidates_reg<FeatT, 32> : k_candidates_reg<FeatT, 64>);
     rk<<<grid, kCandThreads, 0, ctx->stream>>>(d_nodes, n, tree, F, T, P::kFeatDim, b, ord, ctx->cand_feat.as<FeatT>(),
-                                               ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>());
+                                               ctx->cand_thr.as<FeatT>(), ctx->cand_perm.as<uint8_t>(),
+                                               prop ? *prop : PropSrc{});
     PD_CUDA(cudaGetLastError());
     ctx->launches++;
     if (ord_out) *ord_out = ord;

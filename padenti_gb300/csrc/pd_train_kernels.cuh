@@ -207,12 +207,12 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates(const int32_t *__re
   }
 }
 
-// The same table for MD5 candidates with packed keys and at most TP thresholds
-// (TP = 16, 32 or 64): the keys of a candidate live in registers (padded with
-// 0xffffffff, above every key since t < TP) and are sorted by a bitonic network
-// with compile-time indices -- branch-free min/max pairs in place of the
-// insertion sort, whose data-dependent shifts diverge across a warp.  Same
-// output as k_candidates<FeatT, true> without a proposal source.
+// The same table with packed keys and at most TP thresholds (TP = 16, 32 or 64):
+// the keys of a candidate live in registers (padded with 0xffffffff, above every
+// key since t < TP) and are sorted by a bitonic network with compile-time
+// indices -- branch-free min/max pairs in place of the insertion sort, whose
+// data-dependent shifts diverge across a warp.  Same output as
+// k_candidates<FeatT, true>, proposal source included.
 template <int N>
 PD_D void bitonic_sort_regs(uint32_t (&k)[N]) {
 #pragma unroll
@@ -244,16 +244,25 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates_reg(const int32_t *
                                                                  CandBounds b, const uint32_t *__restrict__ ord,
                                                                  FeatT *__restrict__ feat,
                                                                  FeatT *__restrict__ thr_sorted,
-                                                                 uint8_t *__restrict__ perm) {
+                                                                 uint8_t *__restrict__ perm, PropSrc prop) {
   const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (uint64_t)n_nodes * F) return;
   const uint32_t n = (uint32_t)(idx / F), c = (uint32_t)(idx % F);
   const uint32_t node = (uint32_t)nodes[n];
   const uint32_t f = ord ? ord[(size_t)n * F + c] : c;
   const uint32_t fg = b.f_base + f;
+  const bool net = prop.out != nullptr && f < prop.n_prop;
+  uint64_t stream = 0;
+  uint32_t g = 0;
   {
     FeatT fv[PD_MAX_FEAT_DIM];
-    candidate_feature<FeatT>(tree, node, fg, D, b.low, b.up, fv);
+    if (net) {
+      stream = prop_stream(prop.seed, tree, node, f);
+      g = prop_component(prop, n, stream);
+      for (int d = 0; d < D; d++) fv[d] = (FeatT)prop_draw(prop, n, g, (uint32_t)d, stream, (uint32_t)d);
+    } else {
+      candidate_feature<FeatT>(tree, node, fg, D, b.low, b.up, fv);
+    }
     for (int d = 0; d < D; d++) feat[((size_t)n * D + d) * F + c] = fv[d];
   }
   uint32_t key[TP];
@@ -261,14 +270,19 @@ __global__ void __launch_bounds__(kCandThreads) k_candidates_reg(const int32_t *
 #pragma unroll
   for (int t = 0; t < TP; t++) {
     if ((uint32_t)t < T) {
-      if ((t & 3) == 0) {
-        md5_block(seed, st);
-        seed[0] = st[0];
-        seed[1] = st[1];
-        seed[2] = st[2];
-        seed[3] = st[3];
+      FeatT x;
+      if (net) {
+        x = (FeatT)prop_draw(prop, n, g, (uint32_t)D, stream, (uint32_t)D + 1u + (uint32_t)t);
+      } else {
+        if ((t & 3) == 0) {
+          md5_block(seed, st);
+          seed[0] = st[0];
+          seed[1] = st[1];
+          seed[2] = st[2];
+          seed[3] = st[3];
+        }
+        x = draw<FeatT>(st[t & 3], b.thr_lo, b.thr_hi);
       }
-      const FeatT x = draw<FeatT>(st[t & 3], b.thr_lo, b.thr_hi);
       key[t] = ((uint32_t)((int32_t)x - b.thr_lo) << 8) | (uint32_t)t;
     } else {
       key[t] = 0xffffffffu;

@@ -181,6 +181,13 @@ def test_proposed_tree_is_valid_deterministic_and_records_match():
     tr.train_proposed(t2, ts, tp, net, 48)
     for f in ("left_child", "features", "thresholds", "posteriors"):
         assert np.array_equal(getattr(t1, f), getattr(t2, f)), f
+    # the candidate tables sorted in shared memory instead of registers: the same tree
+    tr.set_tuning("cand_regs", 0)
+    t3 = pg.Tree(cfg, 1, 9)
+    tr.train_proposed(t3, ts, tp, net, 48)
+    tr.set_tuning("cand_regs", 1)
+    for f in ("left_child", "features", "thresholds", "posteriors"):
+        assert np.array_equal(getattr(t1, f), getattr(t3, f)), f
     s = t1.left_child >= 0
     assert s.sum() >= 10
     assert np.all(t1.features[s] >= -60000) and np.all(t1.features[s] <= 60000)
