@@ -365,3 +365,27 @@ def test_upload_from_pinned_memory_by_sm_copy():
         assert np.array_equal(t.left_child, o["left_child"]), mode
         assert np.array_equal(np.asarray(t.features, np.int32), o["features"]), mode
         assert np.array_equal(t.posteriors.view(np.uint32), o["posteriors"].view(np.uint32)), mode
+
+
+def test_offsets_beyond_the_exact_division_range():
+    """Offsets above 2^21 px*mm take the plugin's float path (roundf of the float quotient)
+    in training and in prediction (the forest is then not all-fast: the prediction kernels
+    with the per-visit test run); trees and posteriors equal the oracle's."""
+    cfg, ts, tp, (px, lb, sm) = depth_case(n_images=8, n_features=64, n_thresholds=12)
+    tp = pg.TreeTrainerParameters(64, 12, [-(1 << 23)] * 4, [1 << 23] * 4, -3000, 3000, 20)
+    p = ob.params(cfg, tp)
+    o = ob.train_tree(p, ob.OracleSet(ts, cfg), 2, 6, ts.priors)
+    t = pg.Tree(cfg, 2, 6)
+    pg.TreeTrainer(cfg).train(t, ts, tp)
+    assert (t.left_child >= 0).sum() >= 4
+    assert np.array_equal(t.left_child, o["left_child"])
+    assert np.array_equal(np.asarray(t.features, np.int32), o["features"])
+    assert np.array_equal(t.posteriors.view(np.uint32), o["posteriors"].view(np.uint32))
+    big = np.abs(np.asarray(t.features)[t.left_child >= 0]).max()
+    assert big > (1 << 21), "the tree should split on a float-path offset"
+    clf = pg.Classifier(cfg)
+    clf << t
+    want = ob.predict_posterior(p, px[0], None, [tree_tuple(t)])
+    assert np.array_equal(clf.predict(px[0]).view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(clf.predict_leaf(0, px[0]), ob.predict_leaf(p, px[0], None, 6, t.left_child, t.features,
+                                                                      t.thresholds))
