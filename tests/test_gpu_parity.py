@@ -372,7 +372,9 @@ def test_offsets_beyond_the_exact_division_range():
     in training and in prediction (the forest is then not all-fast: the prediction kernels
     with the per-visit test run); trees and posteriors equal the oracle's."""
     cfg, ts, tp, (px, lb, sm) = depth_case(n_images=8, n_features=64, n_thresholds=12)
-    tp = pg.TreeTrainerParameters(64, 12, [-(1 << 23)] * 4, [1 << 23] * 4, -3000, 3000, 20)
+    # the first probe's offsets reach 2^22 (it reads the background), the second's stay small
+    big, small = 1 << 22, 60000
+    tp = pg.TreeTrainerParameters(64, 12, [-big, -big, -small, -small], [big, big, small, small], -500, 9500, 20)
     p = ob.params(cfg, tp)
     o = ob.train_tree(p, ob.OracleSet(ts, cfg), 2, 6, ts.priors)
     t = pg.Tree(cfg, 2, 6)
@@ -381,8 +383,7 @@ def test_offsets_beyond_the_exact_division_range():
     assert np.array_equal(t.left_child, o["left_child"])
     assert np.array_equal(np.asarray(t.features, np.int32), o["features"])
     assert np.array_equal(t.posteriors.view(np.uint32), o["posteriors"].view(np.uint32))
-    big = np.abs(np.asarray(t.features)[t.left_child >= 0]).max()
-    assert big > (1 << 21), "the tree should split on a float-path offset"
+    assert np.abs(np.asarray(t.features)[t.left_child >= 0]).max() > (1 << 21), "splits on float-path offsets"
     clf = pg.Classifier(cfg)
     clf << t
     want = ob.predict_posterior(p, px[0], None, [tree_tuple(t)])
