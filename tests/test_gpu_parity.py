@@ -390,3 +390,28 @@ def test_offsets_beyond_the_exact_division_range():
     assert np.array_equal(clf.predict(px[0]).view(np.uint32), want.view(np.uint32))
     assert np.array_equal(clf.predict_leaf(0, px[0]), ob.predict_leaf(p, px[0], None, 6, t.left_child, t.features,
                                                                       t.thresholds))
+
+
+def test_device_batch_prediction_matches_per_image():
+    """pd_predict_posterior_device on three same-size images in device memory, with masks,
+    gives each image's host-buffer posterior (which the other tests pin to the oracle)."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    from padenti_gb300 import _native as N
+
+    cfg, ts, tp, (px, lb, sm) = depth_case(n_images=6, n_features=48, n_thresholds=12)
+    t = pg.Tree(cfg, 1, 7)
+    pg.TreeTrainer(cfg).train(t, ts, tp)
+    clf = pg.Classifier(cfg)
+    clf << t
+    imgs = np.ascontiguousarray(px[:3])
+    rng = np.random.default_rng(9)
+    masks = (rng.random(imgs.shape) < 0.8).astype(np.uint8)
+    H, W = imgs.shape[1:3]
+    dimg = torch.from_numpy(imgs.view(np.int16)).cuda()
+    dmask = torch.from_numpy(masks).cuda()
+    dout = torch.zeros((3, cfg.n_classes, H, W), dtype=torch.float32, device="cuda")
+    N.check(N.lib().pd_predict_posterior_device(clf.h, 3, dimg.data_ptr(), W, H, dmask.data_ptr(), dout.data_ptr()))
+    got = dout.cpu().numpy()
+    for i in range(3):
+        assert np.array_equal(got[i].view(np.uint32), clf.predict(imgs[i], masks[i]).view(np.uint32)), i

@@ -246,6 +246,18 @@ def test_auto_context_feature_matches_the_oracle():
             for k, (dep, lc, ft, th, po) in enumerate(forest):
                 assert np.array_equal(clf.predict_leaf(k, image, m), ob.predict_leaf(p, image, m, dep, lc, ft, th,
                                                                                      posts=po))
+    # three same-size images in device memory: the node maps of all three in one set of steps
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    from padenti_gb300 import _native as N
+    imgs = np.ascontiguousarray(px[:3])
+    H, W = imgs.shape[1:3]
+    dimg = torch.from_numpy(imgs.view(np.int16)).cuda()
+    dout = torch.zeros((3, cfg.n_classes, H, W), dtype=torch.float32, device="cuda")
+    N.check(N.lib().pd_predict_posterior_device(clf.h, 3, dimg.data_ptr(), W, H, None, dout.data_ptr()))
+    got = dout.cpu().numpy()
+    for i in range(3):
+        assert np.array_equal(got[i].view(np.uint32), ob.predict_posterior(p, imgs[i], None, forest).view(np.uint32)), i
     batch = clf.predict_batch([px[0], px[1][:40, :50]])
     assert np.array_equal(batch[0].view(np.uint32), ob.predict_posterior(p, px[0], None, forest).view(np.uint32))
     assert np.array_equal(batch[1].view(np.uint32),
