@@ -10,7 +10,7 @@ import pytest
 
 import oracle_bind as ob
 import padenti_gb300 as pg
-from cases import depth_case, rgb_case
+from cases import actx_case, depth_case, rgb_case
 from padenti_gb300 import dist as pdist
 
 pytestmark = pytest.mark.gpu
@@ -60,6 +60,17 @@ def test_sharded_rgb_tree_equals_unsharded():
         for f in ("left_child", "features", "thresholds"):
             assert np.array_equal(getattr(t, f), getattr(ref, f)), f
         assert np.array_equal(t.posteriors.view(np.uint32), ref.posteriors.view(np.uint32))
+
+
+def test_sharded_auto_context_tree_equals_the_oracle():
+    """A feature that reads the tree: every rank keeps its own node maps and trains the
+    oracle's tree."""
+    cfg, ts, tp, _ = actx_case(n_features=96)
+    o = ob.train_tree(ob.params(cfg, tp, "auto_context"), ob.OracleSet(ts, cfg), 3, 7, ts.priors)
+    for t in _run_ranks(cfg, ts, tp, 2, 3, 7):
+        assert np.array_equal(t.left_child, o["left_child"])
+        assert np.array_equal(np.asarray(t.features, np.int32), o["features"])
+        assert np.array_equal(t.posteriors.view(np.uint32), o["posteriors"].view(np.uint32))
 
 
 def test_failed_exchange_is_an_error():
