@@ -348,10 +348,10 @@ extern "C" int pd_dataset_upload(pd_ctx *ctx, const pd_dataset_desc *ds) {
   PD_TRY(map_training_pixels(ctx, bytes));
   PD_CUDA(h2d(ctx, ctx->img_off.ptr, off.data(), n * 8));
   PD_CUDA(h2d(ctx, ctx->img_wh.ptr, wh.data(), n * 4));
-  if (S) {  // from the pinned staging
-    PD_TRY(upload_bytes(ctx, ctx->s_xy.ptr, xy, S * 4));
-    PD_TRY(upload_bytes(ctx, ctx->s_img.ptr, im, S * 4));
-    PD_TRY(upload_bytes(ctx, ctx->s_label.ptr, lab, S));
+  if (S) {
+    PD_CUDA(h2d(ctx, ctx->s_xy.ptr, xy, S * 4));
+    PD_CUDA(h2d(ctx, ctx->s_img.ptr, im, S * 4));
+    PD_CUDA(h2d(ctx, ctx->s_label.ptr, lab, S));
   }
   PD_TRY(build_sample_records(ctx, S));
   ctx->root_class_tot.assign(ctx->cfg.n_classes, 0u);
