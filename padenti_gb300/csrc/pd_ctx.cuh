@@ -88,7 +88,7 @@ struct pd_ctx {
   std::vector<float> h_post;
   bool forest_dirty = true;
   pd::DevBuf f_lc, f_feat, f_thr, f_post, f_meta;
-  pd::DevBuf f_cand;                   // P::Cand of every forest node (k_forest_cands)
+  pd::DevBuf f_cand;                   // NodeRec of every forest node (k_forest_nodes)
   uint64_t cand_version = ~0ull;       // forest_version f_cand was built for
   bool forest_fast = false;            // every node takes the plugin's fast path (built-in plugins)
   pd::DevBuf f_fast;                   // its device flag

@@ -45,38 +45,48 @@ static int upload_forest(pd_ctx *ctx) {
   return PD_OK;
 }
 
-// Bytes of one node's candidate record: P::Cand, or for a user feature the
-// UserPlugin::Cand compiled at run time (its feature values, 16-byte aligned).
+// Bytes of one node's record: NodeRec<P>, or for a user feature the
+// NodeRec<UserPlugin> compiled at run time (its size read from the module).
 template <class P>
-static size_t cand_record(const pd_ctx *ctx) {
-  if (is_user_plugin(ctx)) return ((size_t)ctx->cfg.feat_dim * feat_size(ctx->cfg.feat_type) + 15) / 16 * 16;
-  return sizeof(typename P::Cand);
+static int node_record(pd_ctx *ctx, size_t *bytes) {
+  if (is_user_plugin(ctx)) {
+    const RtcKernels *rk = nullptr;
+    PD_TRY(rtc_kernels(ctx, &rk));
+    *bytes = (size_t)rk->node_rec_bytes;
+    return PD_OK;
+  }
+  if constexpr (!P::kRtcOnly) *bytes = sizeof(NodeRec<P>);
+  return PD_OK;
 }
 
-// The candidate record of every forest node (k_forest_cands), rebuilt when the
-// forest changes, so that a tree walk loads each node's constants.
+// The record of every forest node (k_forest_nodes), rebuilt when the forest
+// changes, so that a tree walk loads each node in one record.
 template <class P>
-static int ensure_forest_cands(pd_ctx *ctx) {
+static int ensure_forest_nodes(pd_ctx *ctx) {
   if (ctx->cand_version == ctx->forest_version) return PD_OK;
   using FeatT = typename P::feat_t;
   unsigned long long nodes = ctx->h_lc.size();
-  PD_TRY(ctx->f_cand.ensure(nodes * cand_record<P>(ctx) + 16));
-  const FeatT *ft = ctx->f_feat.as<FeatT>();
+  size_t rec = 0;
+  PD_TRY(node_record<P>(ctx, &rec));
+  PD_CHECK(rec >= 16 && rec % 16 == 0, PD_ERR_STATE, "node record of %zu bytes", rec);
+  PD_TRY(ctx->f_cand.ensure(nodes * rec + 16));
+  const FeatT *ft = ctx->f_feat.as<FeatT>(), *th = ctx->f_thr.as<FeatT>();
+  const int32_t *lc = ctx->f_lc.as<int32_t>();
   const dim3 grid((unsigned)((nodes + 255) / 256 + (nodes == 0)));
   if (is_user_plugin(ctx)) {
     const RtcKernels *rk = nullptr;
     PD_TRY(rtc_kernels(ctx, &rk));
     void *out = ctx->f_cand.ptr;
-    void *args[] = {&ft, &nodes, &out};
-    PD_TRY(rtc_launch(ctx, rk->forest_cands, grid, dim3(256), 0, args));
+    void *args[] = {&ft, &th, &lc, &nodes, &out};
+    PD_TRY(rtc_launch(ctx, rk->forest_nodes, grid, dim3(256), 0, args));
   } else if constexpr (!P::kRtcOnly) {
-    k_forest_cands<P><<<grid, 256, 0, ctx->stream>>>(ft, nodes, ctx->f_cand.as<typename P::Cand>());
+    k_forest_nodes<P><<<grid, 256, 0, ctx->stream>>>(ft, th, lc, nodes, ctx->f_cand.as<NodeRec<P>>());
     PD_CUDA(cudaGetLastError());
     // whether every node takes the fast path: the prediction kernels then carry no slow path
     PD_TRY(ctx->f_fast.ensure(16));
     int all = 1;
     PD_CUDA(h2d(ctx, ctx->f_fast.ptr, &all, 4));
-    k_forest_fast<P><<<grid, 256, 0, ctx->stream>>>(ctx->f_cand.as<typename P::Cand>(), nodes, ctx->f_fast.as<int>());
+    k_forest_fast<P><<<grid, 256, 0, ctx->stream>>>(ctx->f_cand.as<NodeRec<P>>(), nodes, ctx->f_fast.as<int>());
     PD_CUDA(cudaGetLastError());
     PD_CUDA(d2h(ctx, &all, ctx->f_fast.ptr, 4));
     PD_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -95,7 +105,7 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
   const size_t smem = (size_t)nt * kPredThreads * 4;
   dim3 grid((W + kPredX - 1) / kPredX, (H + kPredY - 1) / kPredY, n);
   const uint64_t img_bytes = (uint64_t)W * H * ctx->cfg.n_channels * img_size(ctx->cfg.img_type);
-  PD_TRY(ensure_forest_cands<P>(ctx));
+  PD_TRY(ensure_forest_nodes<P>(ctx));
   if (is_user_plugin(ctx)) {
     const RtcKernels *rk = nullptr;
     PD_TRY(rtc_kernels(ctx, &rk));
@@ -103,22 +113,20 @@ static int launch_posterior(pd_ctx *ctx, uint32_t n, const void *images, uint32_
     const uint8_t *im = static_cast<const uint8_t *>(images);
     uint64_t ib = img_bytes;
     uint32_t w_ = W, h_ = H, nt_ = nt, k_ = (uint32_t)ctx->cfg.n_classes;
-    const int32_t *lc = ctx->f_lc.as<int32_t>();
-    const void *cd = ctx->f_cand.ptr;
-    const FeatT *th = ctx->f_thr.as<FeatT>();
+    const void *nd = ctx->f_cand.ptr;
     const float *po = ctx->f_post.as<float>();
     const TreeMeta *me = ctx->f_meta.as<TreeMeta>();
     const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
-    void *args[] = {&im, &ib, &w_, &h_, &masks, &out, &lc, &cd, &th, &po, &me, &nt_, &k_, &mg};
+    void *args[] = {&im, &ib, &w_, &h_, &masks, &out, &nd, &po, &me, &nt_, &k_, &mg};
     return rtc_launch(ctx, rk->predict_posterior, grid, dim3(kPredX, kPredY), smem, args);
   }
   if constexpr (!P::kRtcOnly) {
     auto kern = ctx->forest_fast ? k_predict_posterior<P, true> : k_predict_posterior<P, false>;
     PD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<grid, dim3(kPredX, kPredY), smem, ctx->stream>>>(
-        static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_lc.as<int32_t>(),
-        ctx->f_cand.as<typename P::Cand>(), ctx->f_thr.as<FeatT>(), ctx->f_post.as<float>(),
-        ctx->f_meta.as<TreeMeta>(), nt, (uint32_t)ctx->cfg.n_classes, ctx->magic_tab.as<uint32_t>());
+        static_cast<const uint8_t *>(images), img_bytes, W, H, masks, out, ctx->f_cand.as<NodeRec<P>>(),
+        ctx->f_post.as<float>(), ctx->f_meta.as<TreeMeta>(), nt, (uint32_t)ctx->cfg.n_classes,
+        ctx->magic_tab.as<uint32_t>());
     PD_CUDA(cudaGetLastError());
     ctx->launches++;
   }
@@ -365,20 +373,17 @@ extern "C" int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *c
     PD_CUDA(cudaStreamSynchronize(st));
     const size_t smem = (size_t)nt * kPredThreads * 4;
     const int rc = dispatch_config(ctx->cfg, [&]<class P>() -> int {
-      using FeatT = typename P::feat_t;
-      PD_TRY(ensure_forest_cands<P>(ctx));
+      PD_TRY(ensure_forest_nodes<P>(ctx));
       PD_CUDA(cudaStreamSynchronize(st));
       const uint8_t *im = ctx->b_img.as<uint8_t>(), *mk = ctx->b_mask.as<uint8_t>();
       uint8_t *o = ctx->b_out.as<uint8_t>();
       const BatchImage *bd = ctx->b_desc.as<BatchImage>();
       uint32_t n_ = n, nt_ = nt, k_ = K;
-      const int32_t *lc = ctx->f_lc.as<int32_t>();
-      const void *cd = ctx->f_cand.ptr;
-      const FeatT *th = ctx->f_thr.as<FeatT>();
+      const void *nd = ctx->f_cand.ptr;
       const float *po = ctx->f_post.as<float>();
       const TreeMeta *me = ctx->f_meta.as<TreeMeta>();
       const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
-      void *args[] = {&im, &mk, &o, &bd, &n_, &lc, &cd, &th, &po, &me, &nt_, &k_, &mg};
+      void *args[] = {&im, &mk, &o, &bd, &n_, &nd, &po, &me, &nt_, &k_, &mg};
       const void *fn = nullptr;
       if (is_user_plugin(ctx)) {
         const RtcKernels *rk = nullptr;
@@ -444,28 +449,26 @@ extern "C" int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, ui
     return PD_OK;
   }
   PD_TRY(dispatch_config(ctx->cfg, [&]<class P>() {
-    using FeatT = typename P::feat_t;
     dim3 grid((width + kPredX - 1) / kPredX, (height + kPredY - 1) / kPredY, 1);
-    PD_TRY(ensure_forest_cands<P>(ctx));
+    PD_TRY(ensure_forest_nodes<P>(ctx));
+    size_t rec = 0;
+    PD_TRY(node_record<P>(ctx, &rec));
     if (is_user_plugin(ctx)) {
       const RtcKernels *rk = nullptr;
       PD_TRY(rtc_kernels(ctx, &rk));
       const uint8_t *im = ctx->p_img.as<uint8_t>(), *mk = mask ? ctx->p_mask.as<uint8_t>() : nullptr;
       uint32_t w_ = width, h_ = height, dp = depth;
       int32_t *o = ctx->p_out.as<int32_t>();
-      const int32_t *lc = ctx->f_lc.as<int32_t>() + off;
-      const void *cd = ctx->f_cand.as<uint8_t>() + off * cand_record<P>(ctx);
-      const FeatT *th = ctx->f_thr.as<FeatT>() + off;
+      const void *nd = ctx->f_cand.as<uint8_t>() + off * rec;
       const uint32_t *mg = ctx->magic_tab.as<uint32_t>();
-      void *args[] = {&im, &w_, &h_, &mk, &o, &lc, &cd, &th, &dp, &mg};
+      void *args[] = {&im, &w_, &h_, &mk, &o, &nd, &dp, &mg};
       return rtc_launch(ctx, rk->predict_leaf, grid, dim3(kPredX, kPredY), 0, args);
     }
     if constexpr (!P::kRtcOnly) {
       auto kern = ctx->forest_fast ? k_predict_leaf<P, true> : k_predict_leaf<P, false>;
       kern<<<grid, dim3(kPredX, kPredY), 0, st>>>(
           ctx->p_img.as<uint8_t>(), width, height, mask ? ctx->p_mask.as<uint8_t>() : nullptr,
-          ctx->p_out.as<int32_t>(), ctx->f_lc.as<int32_t>() + off, ctx->f_cand.as<typename P::Cand>() + off,
-          ctx->f_thr.as<FeatT>() + off, depth, ctx->magic_tab.as<uint32_t>());
+          ctx->p_out.as<int32_t>(), ctx->f_cand.as<NodeRec<P>>() + off, depth, ctx->magic_tab.as<uint32_t>());
       PD_CUDA(cudaGetLastError());
     }
     return PD_OK;

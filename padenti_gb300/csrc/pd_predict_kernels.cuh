@@ -12,6 +12,17 @@ struct TreeMeta {
   uint32_t depth, pad;
 };
 
+// One forest node as the prediction kernels read it: the plugin's candidate
+// record (P::candidate of its features, built once per forest upload), its
+// threshold and its left child, together in one 16-byte-aligned record -- one
+// visit fetches one or two 32-byte sectors instead of three arrays.
+template <class P>
+struct __align__(16) NodeRec {
+  typename P::Cand c;
+  typename P::feat_t thr;
+  int32_t lc;
+};
+
 constexpr int kPredX = 32, kPredY = 8, kPredThreads = kPredX * kPredY;
 // Tree walks interleaved per pixel.  On the 3-tree, depth-16 forest of 640x480
 // depth maps, 1 measures fastest (7.07e9 pixels/s; 2: 6.91e9, 3: 7.08e9): the
@@ -21,49 +32,50 @@ constexpr int kPredX = 32, kPredY = 8, kPredThreads = kPredX * kPredY;
 #endif
 constexpr int kPredGroup = PD_PRED_GROUP;
 
-// Leaf reached by one tree from the root; cand holds P::candidate of every
-// node's features (k_forest_cands), so a visit loads the node's constants
-// instead of deriving them.
+// Leaf reached by one tree from the root (nodes: the tree's records).
 // AF: every node of the forest takes the plugin's fast path (P::fast, checked
 // once per forest upload), so the walk carries no per-visit test or slow path.
 template <class P, bool AF = false>
-PD_D int32_t walk(const typename P::Prep &prep, const int32_t *__restrict__ lc,
-                  const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
-                  uint32_t depth) {
+PD_D int32_t walk(const typename P::Prep &prep, const NodeRec<P> *__restrict__ nodes, uint32_t depth) {
   using FeatT = typename P::feat_t;
   int32_t node = 0;
   for (uint32_t d = 1; d < depth; d++) {
-    const int32_t c = ldg(lc + node);
-    if (c < 0) break;  // leaf (-1); an untrained root (-2) also stops
-    const typename P::Cand cd = cand[node];
-    const FeatT r = (AF || P::fast(cd)) ? P::template eval<true>(prep, cd) : P::template eval<false>(prep, cd);
-    node = c + (r <= ldg(thr + node) ? 0 : 1);
+    const NodeRec<P> nr = nodes[node];
+    if (nr.lc < 0) break;  // leaf (-1); an untrained root (-2) also stops
+    const FeatT r = (AF || P::fast(nr.c)) ? P::template eval<true>(prep, nr.c) : P::template eval<false>(prep, nr.c);
+    node = nr.lc + (r <= nr.thr ? 0 : 1);
   }
   return node;
 }
 
-// P::candidate of every node's features, for the prediction kernels.
+// The record of every forest node, for the prediction kernels.
 template <class P>
-__global__ void k_forest_cands(const typename P::feat_t *__restrict__ feat, unsigned long long n_nodes,
-                               typename P::Cand *__restrict__ cand) {
+__global__ void k_forest_nodes(const typename P::feat_t *__restrict__ feat, const typename P::feat_t *__restrict__ thr,
+                               const int32_t *__restrict__ lc, unsigned long long n_nodes,
+                               NodeRec<P> *__restrict__ out) {
   const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-  if (i < n_nodes) cand[i] = P::candidate(feat + i * P::kFeatDim);
+  if (i < n_nodes) {
+    NodeRec<P> r;
+    r.c = P::candidate(feat + i * P::kFeatDim);
+    r.thr = thr[i];
+    r.lc = lc[i];
+    out[i] = r;
+  }
 }
 
 // Clears *all_fast when a node of the forest needs the plugin's slow path.
 template <class P>
-__global__ void k_forest_fast(const typename P::Cand *__restrict__ cand, unsigned long long n_nodes,
+__global__ void k_forest_fast(const NodeRec<P> *__restrict__ nodes, unsigned long long n_nodes,
                               int *__restrict__ all_fast) {
   const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-  if (i < n_nodes && !P::fast(cand[i])) *all_fast = 0;
+  if (i < n_nodes && !P::fast(nodes[i].c)) *all_fast = 0;
 }
 
 // The leaves of trees t0 .. t0+G-1 (those below n_trees) for one pixel, the G
 // walks interleaved level by level so that their loads overlap; each walk is
 // the one walk() does.
 template <class P, int G, bool AF = false>
-PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ lc,
-                     const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
+PD_D void walk_group(const typename P::Prep &prep, const NodeRec<P> *__restrict__ nodes,
                      const TreeMeta *__restrict__ meta, uint32_t t0, uint32_t n_trees, int32_t *leaf_s,
                      uint32_t tid) {
   using FeatT = typename P::feat_t;
@@ -84,14 +96,13 @@ PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ l
 #pragma unroll
     for (int g = 0; g < G; g++) {
       if (!((live >> g) & 1u)) continue;
-      const int32_t c = ldg(lc + off[g] + node[g]);
-      if (c < 0) {  // leaf (-1); an untrained root (-2) also stops
+      const NodeRec<P> nr = nodes[off[g] + node[g]];
+      if (nr.lc < 0) {  // leaf (-1); an untrained root (-2) also stops
         live &= ~(1u << g);
         continue;
       }
-      const typename P::Cand cd = cand[off[g] + node[g]];
-      const FeatT r = (AF || P::fast(cd)) ? P::template eval<true>(prep, cd) : P::template eval<false>(prep, cd);
-      node[g] = c + (r <= ldg(thr + off[g] + node[g]) ? 0 : 1);
+      const FeatT r = (AF || P::fast(nr.c)) ? P::template eval<true>(prep, nr.c) : P::template eval<false>(prep, nr.c);
+      node[g] = nr.lc + (r <= nr.thr ? 0 : 1);
       if (d + 1 >= depth[g]) live &= ~(1u << g);
     }
   }
@@ -105,8 +116,7 @@ PD_D void walk_group(const typename P::Prep &prep, const int32_t *__restrict__ l
 // and divided by the tree count, written planar with stride plane.
 template <class P, bool AF = false>
 PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint32_t y, bool masked_out, float *o,
-                        size_t plane, const int32_t *__restrict__ lc, const typename P::Cand *__restrict__ cand,
-                        const typename P::feat_t *__restrict__ thr, const float *__restrict__ post,
+                        size_t plane, const NodeRec<P> *__restrict__ nodes, const float *__restrict__ post,
                         const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K, int32_t *leaf_s,
                         uint32_t tid) {
   if (masked_out) {
@@ -115,7 +125,7 @@ PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint3
   }
   const auto prep = P::prepare(im, (int32_t)x, (int32_t)y);
   for (uint32_t t = 0; t < n_trees; t += kPredGroup)
-    walk_group<P, kPredGroup, AF>(prep, lc, cand, thr, meta, t, n_trees, leaf_s, tid);
+    walk_group<P, kPredGroup, AF>(prep, nodes, meta, t, n_trees, leaf_s, tid);
   const float nt = (float)n_trees;
   for (uint32_t l = 0; l < K; l++) {
     float acc = 0.0f;
@@ -129,8 +139,7 @@ PD_D void predict_pixel(const ImageRef<typename P::img_t> &im, uint32_t x, uint3
 template <class P, bool AF = false>
 __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
     const uint8_t *__restrict__ images, uint64_t img_bytes, uint32_t W, uint32_t H,
-    const uint8_t *__restrict__ masks, float *__restrict__ out, const int32_t *__restrict__ lc,
-    const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
+    const uint8_t *__restrict__ masks, float *__restrict__ out, const NodeRec<P> *__restrict__ nodes,
     const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
     const uint32_t *__restrict__ magic) {
   using ImgT = typename P::img_t;
@@ -144,8 +153,8 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_posterior(
   im.w = (int32_t)W;
   im.h = (int32_t)H;
   im.magic = magic;
-  predict_pixel<P, AF>(im, x, y, masks && !masks[(size_t)z * P_ + pix], out + (size_t)z * K * P_ + pix, P_, lc, cand,
-                   thr, post, meta, n_trees, K, leaf_s, tid);
+  predict_pixel<P, AF>(im, x, y, masks && !masks[(size_t)z * P_ + pix], out + (size_t)z * K * P_ + pix, P_, nodes,
+                       post, meta, n_trees, K, leaf_s, tid);
 }
 
 // One image of a mixed-size batch: byte offsets of its pixels, mask and
@@ -161,8 +170,7 @@ struct BatchImage {
 template <class P, bool AF = false>
 __global__ void __launch_bounds__(kPredThreads) k_predict_batch(
     const uint8_t *__restrict__ images, const uint8_t *__restrict__ masks, uint8_t *__restrict__ out,
-    const BatchImage *__restrict__ batch, uint32_t n, const int32_t *__restrict__ lc,
-    const typename P::Cand *__restrict__ cand, const typename P::feat_t *__restrict__ thr,
+    const BatchImage *__restrict__ batch, uint32_t n, const NodeRec<P> *__restrict__ nodes,
     const float *__restrict__ post, const TreeMeta *__restrict__ meta, uint32_t n_trees, uint32_t K,
     const uint32_t *__restrict__ magic) {
   using ImgT = typename P::img_t;
@@ -185,17 +193,15 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_batch(
   im.h = (int32_t)b.h;
   im.magic = magic;
   const bool masked_out = b.has_mask && !masks[b.mask_off + pix];
-  predict_pixel<P, AF>(im, x, y, masked_out, reinterpret_cast<float *>(out + b.out_off) + pix, P_, lc, cand, thr, post,
-                   meta, n_trees, K, leaf_s, tid);
+  predict_pixel<P, AF>(im, x, y, masked_out, reinterpret_cast<float *>(out + b.out_off) + pix, P_, nodes, post, meta,
+                       n_trees, K, leaf_s, tid);
 }
 
 template <class P, bool AF = false>
 __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__restrict__ image, uint32_t W,
                                                                uint32_t H, const uint8_t *__restrict__ mask,
                                                                int32_t *__restrict__ out,
-                                                               const int32_t *__restrict__ lc,
-                                                               const typename P::Cand *__restrict__ cand,
-                                                               const typename P::feat_t *__restrict__ thr,
+                                                               const NodeRec<P> *__restrict__ nodes,
                                                                uint32_t depth, const uint32_t *__restrict__ magic) {
   using ImgT = typename P::img_t;
   const uint32_t x = blockIdx.x * kPredX + threadIdx.x, y = blockIdx.y * kPredY + threadIdx.y;
@@ -210,7 +216,7 @@ __global__ void __launch_bounds__(kPredThreads) k_predict_leaf(const uint8_t *__
   im.w = (int32_t)W;
   im.h = (int32_t)H;
   im.magic = magic;
-  out[pix] = walk<P, AF>(P::prepare(im, (int32_t)x, (int32_t)y), lc, cand, thr, depth);
+  out[pix] = walk<P, AF>(P::prepare(im, (int32_t)x, (int32_t)y), nodes, depth);
 }
 
 // One step of the per-pixel node map of features that read the tree

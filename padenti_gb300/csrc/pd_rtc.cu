@@ -232,7 +232,7 @@ extern "C" int pd_plugin_compile(pd_ctx *ctx, const char *source) {
   const std::vector<std::string> exprs = {
       "pd::k_reassign<pd::UserPlugin>", "pd::k_build_rec<pd::UserPlugin>", "pd::k_cand_order<pd::UserPlugin>",
       "pd::k_predict_posterior<pd::UserPlugin>", "pd::k_predict_leaf<pd::UserPlugin>",
-      "pd::k_predict_batch<pd::UserPlugin>", "pd::k_forest_cands<pd::UserPlugin>",
+      "pd::k_predict_batch<pd::UserPlugin>", "pd::k_forest_nodes<pd::UserPlugin>",
       "pd::k_node_map_step<pd::UserPlugin>"};
   std::string cubin;
   std::vector<std::string> low;
@@ -240,15 +240,17 @@ extern "C" int pd_plugin_compile(pd_ctx *ctx, const char *source) {
   cudaLibrary_t lib = nullptr;
   std::vector<cudaKernel_t> ks;
   if (rc == PD_OK) rc = load_kernels(cubin, low, &lib, &ks);
-  int reads_tree = 0;
-  if (rc == PD_OK) {
-    // the form of the user's computeFeature, as the compiler saw it
-    void *flag = nullptr;
+  int reads_tree = 0, rec_bytes = 0;
+  // the form of the user's computeFeature and the size of its node records, as the compiler saw them
+  for (auto [name, dst] : {std::pair<const char *, int *>{"pd_user_reads_tree", &reads_tree},
+                           std::pair<const char *, int *>{"pd_node_rec_bytes", &rec_bytes}}) {
+    if (rc != PD_OK) break;
+    void *g = nullptr;
     size_t bytes = 0;
-    cudaError_t e = cudaLibraryGetGlobal(&flag, &bytes, lib, "pd_user_reads_tree");
-    if (e == cudaSuccess && bytes == sizeof(int)) e = cudaMemcpy(&reads_tree, flag, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaLibraryGetGlobal(&g, &bytes, lib, name);
+    if (e == cudaSuccess && bytes == sizeof(int)) e = cudaMemcpy(dst, g, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess || bytes != sizeof(int))
-      rc = set_error(PD_ERR_CUDA, "reading the plugin's form flag: %s", cudaGetErrorString(e));
+      rc = set_error(PD_ERR_CUDA, "reading %s from the plugin module: %s", name, cudaGetErrorString(e));
   }
   if (rc != PD_OK) {
     if (lib) cudaLibraryUnload(lib);
@@ -262,8 +264,9 @@ extern "C" int pd_plugin_compile(pd_ctx *ctx, const char *source) {
   p->base.predict_posterior = ks[3];
   p->base.predict_leaf = ks[4];
   p->base.predict_batch = ks[5];
-  p->base.forest_cands = ks[6];
+  p->base.forest_nodes = ks[6];
   p->base.node_map_step = ks[7];
+  p->base.node_rec_bytes = rec_bytes;
   rtc_release(ctx);  // a previous plugin of this context
   ctx->rtc = p;
   ctx->tree_feature = reads_tree != 0;

@@ -12,8 +12,9 @@ namespace pd {
 struct RtcKernels {
   cudaKernel_t reassign = nullptr, build_rec = nullptr, cand_order = nullptr;
   cudaKernel_t predict_posterior = nullptr, predict_leaf = nullptr, predict_batch = nullptr;
-  cudaKernel_t forest_cands = nullptr;
+  cudaKernel_t forest_nodes = nullptr;
   cudaKernel_t node_map_step = nullptr;  // k_node_map_step (features that read the tree)
+  int node_rec_bytes = 0;                // sizeof(NodeRec<UserPlugin>) as compiled
 };
 
 // The compiled base kernels; PD_ERR_STATE when pd_plugin_compile has not run.

@@ -78,3 +78,4 @@ struct UserPlugin {
 
 // Read by the host after loading the module (pd_plugin_compile).
 extern "C" __device__ const int pd_user_reads_tree = pd::kUserReadsTree ? 1 : 0;
+extern "C" __device__ const int pd_node_rec_bytes = (int)sizeof(pd::NodeRec<pd::UserPlugin>);
