@@ -411,7 +411,9 @@ def test_device_batch_prediction_matches_per_image():
     dimg = torch.from_numpy(imgs.view(np.int16)).cuda()
     dmask = torch.from_numpy(masks).cuda()
     dout = torch.zeros((3, cfg.n_classes, H, W), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the buffers are ready before the context's stream uses them
     N.check(N.lib().pd_predict_posterior_device(clf.h, 3, dimg.data_ptr(), W, H, dmask.data_ptr(), dout.data_ptr()))
+    N.check(N.lib().pd_ctx_sync(clf.h))
     got = dout.cpu().numpy()
     for i in range(3):
         assert np.array_equal(got[i].view(np.uint32), clf.predict(imgs[i], masks[i]).view(np.uint32)), i

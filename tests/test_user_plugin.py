@@ -254,7 +254,9 @@ def test_auto_context_feature_matches_the_oracle():
     H, W = imgs.shape[1:3]
     dimg = torch.from_numpy(imgs.view(np.int16)).cuda()
     dout = torch.zeros((3, cfg.n_classes, H, W), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()  # the buffers are ready before the context's stream uses them
     N.check(N.lib().pd_predict_posterior_device(clf.h, 3, dimg.data_ptr(), W, H, None, dout.data_ptr()))
+    N.check(N.lib().pd_ctx_sync(clf.h))
     got = dout.cpu().numpy()
     for i in range(3):
         assert np.array_equal(got[i].view(np.uint32), ob.predict_posterior(p, imgs[i], None, forest).view(np.uint32)), i
