@@ -377,7 +377,9 @@ int pd_predict_leaf(pd_ctx *ctx, uint32_t tree, const void *image, uint32_t widt
 int pd_predict_posterior_batch(pd_ctx *ctx, uint32_t n, const void *const *images, const uint32_t *widths,
                                const uint32_t *heights, const uint8_t *const *masks, float *const *outs);
 /* Batched posterior prediction of n same-size images already in device
- * memory: images n*H*W*C, masks n*H*W (or NULL), out n*K*H*W. */
+ * memory: images n*H*W*C, masks n*H*W (or NULL), out n*K*H*W.  Asynchronous on
+ * the context's stream (pd_ctx_stream): order the caller's own work on these
+ * buffers with pd_ctx_sync or stream events. */
 int pd_predict_posterior_device(pd_ctx *ctx, uint32_t n_images, const void *images_device,
                                 uint32_t width, uint32_t height, const uint8_t *masks_device,
                                 float *out_device);
